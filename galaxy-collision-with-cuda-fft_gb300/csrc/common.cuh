@@ -1,0 +1,210 @@
+// Internal definitions shared by the gcpm translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdarg.h>
+#include <string.h>
+
+#include "../../include/gcpm.h"
+
+#define GC_MAX_LEVELS 24
+// Levels with at most this many nodes per axis are relaxed together by one CTA.
+#define GC_TAIL_MAX_N 17
+
+struct LevelGeom {
+  int n;        // nodes per axis (array extent)
+  int J;        // last interior index; interior is 1..J on every axis
+  float a;      // Shortley-Weller weight of the west neighbour at i == J
+  float dB;     // Shortley-Weller diagonal contribution of the boundary axis at i == J
+  float p;      // far face position in this level's node units, (G-1)/2^l
+};
+
+// Slots of ctx->dsmall.
+enum {
+  GC_S_BNORM2 = 0,   // ||b0||^2 (h^2-scaled rhs, all nodes)
+  GC_S_RNORM2 = 1,   // ||r0||^2 (interior) of the last residual evaluation
+  GC_S_MASS = 2,     // total deposited density-mass used for the fixed-point quantum
+  GC_S_QEXP = 3,     // quantum exponent E: quantum = 2^E (density units)
+  GC_S_RHO_BAD = 4,  // count of non-finite density values (as double)
+  GC_S_RNORM64 = 5,  // FP64 residual norm^2 (verification kernel)
+  GC_S_GRIDPE = 6,   // Sum b0*phi (engine grid energy, h^2 4 pi G units)
+  GC_S_MASS_PM = 7,  // engine: total density-mass of its particles
+  GC_S_QEXP_PM = 8,  // engine: quantum exponent
+  GC_S_NSLOTS = 64
+};
+
+struct gc_ctx {
+  int G;
+  double dx;
+  double grav;
+  cudaStream_t stream;
+  int device;
+
+  int nlev;             // multigrid levels (0 = finest)
+  int tail;             // first level handled by the single-CTA tail kernel (== nlev if none)
+  LevelGeom lev[GC_MAX_LEVELS];
+
+  // finest level: double-float potential, h^2-scaled right-hand side, residual scratch
+  float *hi, *lo, *b0, *r0;
+  // coarse levels (index >= 1): correction e and h^2-scaled right-hand side b
+  float *e[GC_MAX_LEVELS];
+  float *b[GC_MAX_LEVELS];
+  float *rc;            // residual scratch for coarse levels (sized for level 1)
+
+  long long *q;         // int64 fixed-point mass grid (G^3)
+  double *red;          // reduction scratch (block partials)
+  size_t red_cap;       // doubles in red
+  double *dmom;         // 10 moments
+  double *dsmall;       // 64 device scalars, see GC_S_* below
+  double *hsmall;       // pinned host mirror of dsmall
+  unsigned *dstatus;    // device status word
+  double *ddiag;        // 16 doubles for diagnostics
+
+  // particle scratch (grown on demand)
+  uint32_t *keys, *keys2, *vals, *vals2;
+  unsigned *hist;       // radix histogram (digits x blocks)
+  unsigned *hist_aux;   // scan auxiliaries
+  size_t pcap;          // capacity of the particle scratch (elements)
+  size_t hist_cap;
+
+  double mass_sum_cache; // sum of masses for the engine's fixed-point quantum
+  int last_step_valid;
+  int solved_once;
+  gc_mg_stats last_stats;
+
+  char err[512];
+};
+
+// ---- error helpers -----------------------------------------------------------
+void gc_set_error(gc_ctx *ctx, const char *fmt, ...);
+int gc_check_launch(gc_ctx *ctx, const char *what);
+
+#define GC_CUDA(ctx, call)                                                              \
+  do {                                                                                  \
+    cudaError_t _e = (call);                                                            \
+    if (_e != cudaSuccess) {                                                            \
+      gc_set_error((ctx), "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e),       \
+                   __FILE__, __LINE__);                                                 \
+      return GC_ERR_CUDA;                                                               \
+    }                                                                                   \
+  } while (0)
+
+#define GC_LAUNCH_CHECK(ctx, what)                                                      \
+  do {                                                                                  \
+    int _s = gc_check_launch((ctx), (what));                                            \
+    if (_s != GC_OK) return _s;                                                         \
+  } while (0)
+
+#define GC_REQUIRE(ctx, cond, ...)                                                      \
+  do {                                                                                  \
+    if (!(cond)) {                                                                      \
+      gc_set_error((ctx), __VA_ARGS__);                                                 \
+      return GC_ERR_ARG;                                                                \
+    }                                                                                   \
+  } while (0)
+
+int gc_ensure_red(gc_ctx *ctx, size_t ndoubles);
+int gc_ensure_particle_scratch(gc_ctx *ctx, size_t n);
+
+static inline unsigned gc_blocks(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+// ---- double-float (FP32 pair) arithmetic ---------------------------------------
+// Error-free transforms with explicit round-to-nearest intrinsics so that no
+// contraction or reassociation can break them.
+__device__ __forceinline__ void df_two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void df_fast_two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+// ---- reference CIC geometry (deposit.py:62-70) ---------------------------------
+// gx = x/dx (IEEE f32 division), ix = floor(gx), fx = gx - ix. Non-finite or
+// far-outside coordinates are reported as "no deposit" before any cast.
+struct CellPos {
+  int ix, iy, iz;
+  float fx, fy, fz;
+};
+
+__device__ __forceinline__ bool gc_cell_of(float x, float y, float z, float dx, int G, CellPos &c) {
+  float gx = __fdiv_rn(x, dx), gy = __fdiv_rn(y, dx), gz = __fdiv_rn(z, dx);
+  // Every node the particle could touch is in [ix, ix+1]; keep -1 <= ix <= G-1.
+  const float lo = -1.0f, hi = (float)G;  // gx < G  <=>  floor(gx) <= G-1
+  if (!(gx >= lo && gx < hi && gy >= lo && gy < hi && gz >= lo && gz < hi)) return false;
+  float flx = floorf(gx), fly = floorf(gy), flz = floorf(gz);
+  c.ix = (int)flx; c.iy = (int)fly; c.iz = (int)flz;
+  c.fx = __fsub_rn(gx, flx); c.fy = __fsub_rn(gy, fly); c.fz = __fsub_rn(gz, flz);
+  return true;
+}
+
+// Is (x,y,z) finite? Used to raise GC_FLAG_NONFINITE_POS.
+__device__ __forceinline__ bool gc_finite3(float x, float y, float z) {
+  return isfinite(x) && isfinite(y) && isfinite(z);
+}
+
+// Block reduction: every thread passes NV values; thread 0 of the block writes
+// their block sums to out[0..NV). Deterministic (fixed shuffle tree).
+template <int NV>
+__device__ __forceinline__ void block_partials(double (&v)[NV], double *out) {
+  __shared__ double sh[32][NV];
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    double x = v[i];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    v[i] = x;
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) sh[wid][i] = v[i];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      double x = lane < nw ? sh[lane][i] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0) out[i] = x;
+    }
+  }
+}
+
+// Internals shared between translation units
+int gc_mg_build_levels(gc_ctx *ctx);
+int gc_mg_alloc(gc_ctx *ctx);
+void gc_mg_free(gc_ctx *ctx);
+int gc_mg_run(gc_ctx *ctx, const gc_mg_params *p, gc_mg_stats *st);
+int gc_faces_from_moments(gc_ctx *ctx);
+int gc_finalize(gc_ctx *ctx, const double *parts, int nparts, int nv, double *dst);
+// Sum of m/dx^3 (FP64, deterministic) into dsmall[mass_slot] and the fixed-point
+// exponent E (quantum 2^E, total <= 2^bits quanta) into dsmall[exp_slot].
+int gc_fixed_point_setup(gc_ctx *ctx, const float *m, int64_t n, int bits, int mass_slot, int exp_slot);
+// int64 fixed-point CIC deposit into ctx->q (which must be zero on entry).
+// sorted_runs != 0 selects the run-aggregated kernel meant for cell-sorted particles.
+int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, const float *m, int64_t n,
+                 const double *qexp, int sorted_runs);
+// Read ctx->q, write rho (may be NULL) and b = f32(q 2^E 4 pi G h^2) (may be NULL),
+// zero q, and reduce the ten moments into ctx->dmom and ||b||^2 into dsmall[GC_S_BNORM2].
+int gc_convert_q(gc_ctx *ctx, const double *qexp, float *rho_out, float *b_out);
+int gc_mg_check_params(gc_ctx *ctx, const gc_mg_params *p);
+// Fused gather(-grad phi of ctx->hi) + kicks + drift over p (mode: gc_step_mode).
+// With diag, writes nparts rows of 11 FP64 partials into ctx->red.
+int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode, int diag, float *axo, float *ayo,
+                         float *azo, int *nparts_out);
+// dst = sum a*b in FP64 (async).
+int gc_dot_async(gc_ctx *ctx, const float *a, const float *b, size_t n, double *dst);
+// Stable LSD radix sort of (keys, vals) pairs on the low `bits` bits; results in
+// ctx->keys/ctx->vals after the call (inputs may alias them).
+int gc_radix_sort_pairs(gc_ctx *ctx, const uint32_t *keys_in, const uint32_t *vals_in, int64_t n, int bits,
+                        uint32_t **keys_out, uint32_t **vals_out);

@@ -1,0 +1,79 @@
+// Fused PM step: the force chain of accel_fn (sim.py:320-325) and the KDK kicks
+// and drift of kdk_step (integrator.py:100-131) in four device passes:
+//   1. int64 fixed-point CIC deposit (run-aggregated for cell-sorted particles)
+//   2. q -> b = 4 pi G h^2 rho, exact integer moments, ||b||, q cleared
+//   3. FP64 multipole faces + adaptive multigrid on the double-float potential
+//   4. one particle pass: gather of -grad(phi) computed on the fly, the closing
+//      half-kick, FP64 diagnostics at the synchronised time, the opening
+//      half-kick and the drift.
+// The state between ADVANCE calls is (x_n, v_{n-1/2}); PRIME and CLOSE enter and
+// leave the synchronised state, so PRIME + (K-1) ADVANCE + CLOSE reproduce K
+// calls of kdk_step after the priming force evaluation.
+#include "common.cuh"
+
+#include <math.h>
+
+extern "C" int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp, gc_step_stats *st) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, p && sp, "gc_pm_step: NULL argument");
+  GC_REQUIRE(ctx, p->n >= 0 && p->n < (1LL << 31), "particle count out of range");
+  GC_REQUIRE(ctx, p->n == 0 || (p->x && p->y && p->z && p->vx && p->vy && p->vz && p->m),
+             "gc_pm_step: particle arrays required");
+  GC_REQUIRE(ctx, sp->mode >= GC_STEP_PRIME && sp->mode <= GC_STEP_CLOSE, "gc_pm_step: bad mode %d", sp->mode);
+  GC_REQUIRE(ctx, sp->dt == sp->dt, "gc_pm_step: dt must be finite");
+  GC_REQUIRE(ctx, sp->fixed_point_bits >= 24 && sp->fixed_point_bits <= 60, "fixed_point_bits must be in [24, 60]");
+  if (sp->mode != GC_STEP_PRIME && !ctx->last_step_valid) {
+    gc_set_error(ctx, "gc_pm_step: ADVANCE/CLOSE before PRIME");
+    return GC_ERR_STATE;
+  }
+  int s = gc_mg_check_params(ctx, &sp->mg);
+  if (s) return s;
+  const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
+
+  // 1. deposit (the quantum is fixed at PRIME: the masses do not change)
+  if (sp->mode == GC_STEP_PRIME) {
+    if ((s = gc_fixed_point_setup(ctx, p->m, p->n, sp->fixed_point_bits, GC_S_MASS_PM, GC_S_QEXP_PM))) return s;
+  }
+  if ((s = gc_deposit_q(ctx, p->x, p->y, p->z, p->m, p->n, ctx->dsmall + GC_S_QEXP_PM, 1))) return s;
+  // 2. b0, moments, ||b0||
+  if ((s = gc_convert_q(ctx, ctx->dsmall + GC_S_QEXP_PM, nullptr, ctx->b0))) return s;
+  // 3. initial guess and faces, then V-cycles
+  if (!sp->warm_start || !ctx->solved_once) {
+    GC_CUDA(ctx, cudaMemsetAsync(ctx->hi, 0, g3 * sizeof(float), ctx->stream));
+    GC_CUDA(ctx, cudaMemsetAsync(ctx->lo, 0, g3 * sizeof(float), ctx->stream));
+  }
+  if ((s = gc_faces_from_moments(ctx))) return s;
+  gc_mg_stats mst;
+  if ((s = gc_mg_run(ctx, &sp->mg, &mst))) return s;
+  // 4. particle pass
+  int nparts = 0;
+  if ((s = gc_gather_kick_drift(ctx, p, sp->dt, sp->mode, sp->diagnostics, nullptr, nullptr, nullptr, &nparts)))
+    return s;
+  if (sp->diagnostics) {
+    if ((s = gc_finalize(ctx, ctx->red, nparts, 11, ctx->ddiag))) return s;
+    if ((s = gc_dot_async(ctx, ctx->b0, ctx->hi, g3, ctx->ddiag + 11))) return s;
+  }
+  ctx->last_step_valid = (sp->mode != GC_STEP_CLOSE);
+  if (st) {
+    memset(st, 0, sizeof(*st));
+    st->mg = mst;
+    if (sp->diagnostics) {
+      double h[12];
+      GC_CUDA(ctx, cudaMemcpyAsync(h, ctx->ddiag, 12 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      for (int i = 0; i < 11; ++i) st->diag[i] = h[i];
+      // sum rho phi = sum b0 phi / (4 pi G h^2)
+      const double bfac = 4.0 * M_PI * ctx->grav * ctx->dx * ctx->dx;
+      st->grid_pe_raw = bfac != 0.0 ? h[11] / bfac : 0.0;
+    }
+  }
+  return GC_OK;
+}
+
+extern "C" int gc_pm_copy_potential(gc_ctx *ctx, float *phi) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, phi, "gc_pm_copy_potential: NULL phi");
+  const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
+  GC_CUDA(ctx, cudaMemcpyAsync(phi, ctx->hi, g3 * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+  return GC_OK;
+}

@@ -1,0 +1,975 @@
+// Open-boundary multigrid Poisson solver for laplacian(phi) = 4 pi G rho.
+//
+// The discrete problem is the reference's (src/galaxy_collision/solver/multigrid.py):
+// 7-point Laplacian on the finest node grid, Dirichlet faces from the monopole +
+// quadrupole of rho about its centre of mass (multigrid.py:261-295), residual
+// ||rhs - L phi||_2 against ||rhs||_2 (multigrid.py:473-485). Only the finest
+// level defines the answer (multigrid.py:8-15), so the hierarchy is free:
+//
+//  * Level l has its far face at p_l = (G-1)/2^l (in level-l node units). Coarse
+//    node J <-> fine node 2J. When p_l is fractional the last interior node J_l
+//    uses a Shortley-Weller stencil with the Dirichlet face at distance
+//    delta = p_l - J_l, and the transfer operators interpolate to that face. The
+//    reference instead cuts the coarse grid at fine node 2(n/2)-2 and converges
+//    at ~0.6-0.7 per V-cycle; this hierarchy converges at ~0.1.
+//  * The finest level relaxes the potential itself as a double-float pair
+//    (hi + lo, both FP32): each red-black Gauss-Seidel update is computed from
+//    an accurate local residual (exact neighbour differences summed with
+//    error-free transforms), so the residual can be driven below the FP32 floor
+//    (~6e-5 relative in the reference) with FP32 arithmetic only. This is the
+//    defect-correction loop: coarse levels relax FP32 corrections of that
+//    residual, the coarsest level is solved in FP64.
+//  * All arrays are C-order [i][j][k], k fastest. Right-hand sides are stored
+//    h^2-scaled (b = h^2 * rhs) so stencils need no division by h^2.
+#include "common.cuh"
+
+#include <math.h>
+#include <stdlib.h>
+
+#define RB_TX 32
+#define RB_TY 8
+
+// ------------------------------------------------------------------------------
+// level geometry
+// ------------------------------------------------------------------------------
+int gc_mg_build_levels(gc_ctx *ctx) {
+  const int G = ctx->G;
+  ctx->nlev = 0;
+  ctx->tail = 0;
+  if (G - 2 < 1) return GC_OK;  // no interior node: the solve is the boundary alone
+  LevelGeom g0;
+  g0.n = G;
+  g0.J = G - 2;
+  g0.a = 1.0f;
+  g0.dB = 2.0f;
+  g0.p = (float)(G - 1);
+  ctx->lev[0] = g0;
+  int nl = 1;
+  for (int l = 1; l < GC_MAX_LEVELS; ++l) {
+    double p = (double)(G - 1) / (double)(1 << l);
+    int J = (int)ceil(p) - 1;
+    if (J < 1) break;
+    double delta = p - (double)J;
+    LevelGeom g;
+    g.n = J + 2;
+    g.J = J;
+    g.a = (float)(2.0 / (1.0 + delta));
+    g.dB = (float)(2.0 / delta);
+    g.p = (float)p;
+    ctx->lev[nl++] = g;
+  }
+  ctx->nlev = nl;
+  int tail = nl;
+  for (int l = 1; l < nl; ++l) {
+    if (ctx->lev[l].n <= GC_TAIL_MAX_N) {
+      tail = l;
+      break;
+    }
+  }
+  ctx->tail = tail;
+  return GC_OK;
+}
+
+static size_t tail_smem_bytes(const gc_ctx *ctx) {
+  size_t bytes = 0;
+  for (int l = ctx->tail; l < ctx->nlev; ++l) {
+    size_t n3 = (size_t)ctx->lev[l].n * ctx->lev[l].n * ctx->lev[l].n;
+    if (l == ctx->nlev - 1)
+      bytes += 2 * n3 * sizeof(double);
+    else
+      bytes += 3 * n3 * sizeof(float);
+    bytes = (bytes + 15) & ~(size_t)15;
+  }
+  return bytes;
+}
+
+int gc_mg_alloc(gc_ctx *ctx) {
+  const size_t G = ctx->G;
+  const size_t g3 = G * G * G;
+  GC_CUDA(ctx, cudaMalloc(&ctx->hi, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMalloc(&ctx->lo, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMalloc(&ctx->b0, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMalloc(&ctx->r0, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMemset(ctx->hi, 0, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMemset(ctx->lo, 0, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMemset(ctx->b0, 0, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMemset(ctx->r0, 0, g3 * sizeof(float)));
+  size_t rc_n = 0;
+  for (int l = 1; l < ctx->nlev; ++l) {
+    size_t n3 = (size_t)ctx->lev[l].n * ctx->lev[l].n * ctx->lev[l].n;
+    GC_CUDA(ctx, cudaMalloc(&ctx->e[l], n3 * sizeof(float)));
+    GC_CUDA(ctx, cudaMalloc(&ctx->b[l], n3 * sizeof(float)));
+    GC_CUDA(ctx, cudaMemset(ctx->e[l], 0, n3 * sizeof(float)));
+    GC_CUDA(ctx, cudaMemset(ctx->b[l], 0, n3 * sizeof(float)));
+    if (l < ctx->tail && n3 > rc_n) rc_n = n3;
+  }
+  if (rc_n) {
+    GC_CUDA(ctx, cudaMalloc(&ctx->rc, rc_n * sizeof(float)));
+    GC_CUDA(ctx, cudaMemset(ctx->rc, 0, rc_n * sizeof(float)));
+  }
+  return GC_OK;
+}
+
+void gc_mg_free(gc_ctx *ctx) {
+  cudaFree(ctx->hi); cudaFree(ctx->lo); cudaFree(ctx->b0); cudaFree(ctx->r0);
+  for (int l = 1; l < GC_MAX_LEVELS; ++l) {
+    cudaFree(ctx->e[l]); cudaFree(ctx->b[l]);
+    ctx->e[l] = ctx->b[l] = nullptr;
+  }
+  cudaFree(ctx->rc);
+  ctx->hi = ctx->lo = ctx->b0 = ctx->r0 = ctx->rc = nullptr;
+}
+
+// ------------------------------------------------------------------------------
+// reductions: per-block partials written in a fixed order, then one block sums them
+// ------------------------------------------------------------------------------
+// Flattened thread id for the 1D-launched reductions below.
+__device__ __forceinline__ int flat_tid() { return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); }
+
+// Sum nparts rows of NV partials into dst[0..NV) (single block, fixed order).
+__global__ void k_finalize(const double *__restrict__ parts, int nparts, int nv, double *__restrict__ dst,
+                           int accumulate) {
+  __shared__ double sh[32];
+  for (int v = 0; v < nv; ++v) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += parts[(size_t)i * nv + v];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double x = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (threadIdx.x == 0) dst[v] = accumulate ? dst[v] + x : x;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------------
+// finest level: double-float red-black Gauss-Seidel, residual, prolongation
+// ------------------------------------------------------------------------------
+// Accurate residual r = b - L_h2(hi + lo) at interior node c (h^2 units).
+__device__ __forceinline__ float df_residual(const float *__restrict__ hi, const float *__restrict__ lo,
+                                             float bc, size_t c, size_t sj, size_t si, float &hc_out,
+                                             float &lc_out) {
+  const float hc = hi[c];
+  const float d0 = __fsub_rn(hi[c + si], hc);
+  const float d1 = __fsub_rn(hi[c - si], hc);
+  const float d2 = __fsub_rn(hi[c + sj], hc);
+  const float d3 = __fsub_rn(hi[c - sj], hc);
+  const float d4 = __fsub_rn(hi[c + 1], hc);
+  const float d5 = __fsub_rn(hi[c - 1], hc);
+  float s, e, t;
+  df_two_sum(d0, d1, s, e);
+  df_two_sum(s, d2, s, t); e = __fadd_rn(e, t);
+  df_two_sum(s, d3, s, t); e = __fadd_rn(e, t);
+  df_two_sum(s, d4, s, t); e = __fadd_rn(e, t);
+  df_two_sum(s, d5, s, t); e = __fadd_rn(e, t);
+  const float lc = lo[c];
+  const float ln = ((((lo[c + si] + lo[c - si]) + lo[c + sj]) + lo[c - sj]) + lo[c + 1]) + lo[c - 1];
+  const float ll = __fsub_rn(ln, __fmul_rn(6.0f, lc));
+  float r1, r1e;
+  df_two_sum(bc, -s, r1, r1e);
+  hc_out = hc;
+  lc_out = lc;
+  return __fadd_rn(r1, __fsub_rn(r1e, __fadd_rn(e, ll)));
+}
+
+__global__ void __launch_bounds__(RB_TX *RB_TY)
+    k_smooth0(float *__restrict__ hi, float *__restrict__ lo, const float *__restrict__ b, int G, int color) {
+  const int kk = blockIdx.x * RB_TX + threadIdx.x;
+  const int j = blockIdx.y * RB_TY + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  if (j > G - 2) return;
+  const int k = 2 * kk + ((color + i + j) & 1);
+  if (k < 1 || k > G - 2) return;
+  const size_t sj = (size_t)G, si = (size_t)G * G;
+  const size_t c = (size_t)i * si + (size_t)j * sj + k;
+  float hc, lc;
+  const float r = df_residual(hi, lo, b[c], c, sj, si, hc, lc);
+  // Gauss-Seidel: phi_new = (sum6 - h^2 rhs)/6 = phi - r/6
+  const float delta = __fmul_rn(r, -0.16666667f);
+  float s2, e2, h3, l3;
+  df_two_sum(hc, delta, s2, e2);
+  const float ln = __fadd_rn(lc, e2);
+  df_fast_two_sum(s2, ln, h3, l3);
+  hi[c] = h3;
+  lo[c] = l3;
+}
+
+// Residual on the finest interior (r may be NULL) and per-block partial of sum r^2.
+__global__ void __launch_bounds__(256)
+    k_resid0(const float *__restrict__ hi, const float *__restrict__ lo, const float *__restrict__ b,
+             float *__restrict__ r, double *__restrict__ parts, int G) {
+  const int k = blockIdx.x * 32 + threadIdx.x + 1;
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  double acc[1] = {0.0};
+  if (k <= G - 2 && j <= G - 2) {
+    const size_t sj = (size_t)G, si = (size_t)G * G;
+    const size_t c = (size_t)i * si + (size_t)j * sj + k;
+    float hc, lc;
+    const float rv = df_residual(hi, lo, b[c], c, sj, si, hc, lc);
+    if (r) r[c] = rv;
+    acc[0] = (double)rv * (double)rv;
+  }
+  if (parts) {
+    const size_t bid = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    block_partials<1>(acc, parts + bid);
+  }
+}
+
+// FP64 verification residual: phi = (double)hi + (double)lo, or hi alone when lo is NULL.
+__global__ void __launch_bounds__(256)
+    k_resid64(const float *__restrict__ hi, const float *__restrict__ lo, const float *__restrict__ b,
+              double *__restrict__ parts, int G) {
+  const int k = blockIdx.x * 32 + threadIdx.x + 1;
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  double acc[1] = {0.0};
+  if (k <= G - 2 && j <= G - 2) {
+    const size_t sj = (size_t)G, si = (size_t)G * G;
+    const size_t c = (size_t)i * si + (size_t)j * sj + k;
+    auto P = [&](size_t q) { return lo ? (double)hi[q] + (double)lo[q] : (double)hi[q]; };
+    const double pc = P(c);
+    const double lap = (P(c + si) - pc) + (P(c - si) - pc) + (P(c + sj) - pc) + (P(c - sj) - pc) +
+                       (P(c + 1) - pc) + (P(c - 1) - pc);
+    const double rv = (double)b[c] - lap;
+    acc[0] = rv * rv;
+  }
+  const size_t bid = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+  block_partials<1>(acc, parts + bid);
+}
+
+// ------------------------------------------------------------------------------
+// coarse levels (FP32 corrections, Shortley-Weller far faces)
+// ------------------------------------------------------------------------------
+struct AxisTerm {
+  float s;  // weighted neighbour sum along the axis
+  float d;  // diagonal contribution
+};
+
+__device__ __forceinline__ AxisTerm sw_axis(const float *__restrict__ e, size_t c, size_t stride, int idx,
+                                            const LevelGeom &g) {
+  AxisTerm t;
+  if (idx == g.J) {
+    t.s = g.a * e[c - stride];
+    t.d = g.dB;
+  } else {
+    t.s = e[c + stride] + e[c - stride];
+    t.d = 2.0f;
+  }
+  return t;
+}
+
+__device__ __forceinline__ void sw_stencil(const float *__restrict__ e, size_t c, int i, int j, int k,
+                                           const LevelGeom &g, float &sum, float &diag) {
+  const size_t n = (size_t)g.n;
+  const AxisTerm ax = sw_axis(e, c, n * n, i, g);
+  const AxisTerm ay = sw_axis(e, c, n, j, g);
+  const AxisTerm az = sw_axis(e, c, 1, k, g);
+  sum = (ax.s + ay.s) + az.s;
+  diag = (ax.d + ay.d) + az.d;
+}
+
+__global__ void __launch_bounds__(RB_TX *RB_TY)
+    k_smooth(float *__restrict__ e, const float *__restrict__ b, LevelGeom g, int color) {
+  const int kk = blockIdx.x * RB_TX + threadIdx.x;
+  const int j = blockIdx.y * RB_TY + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  if (j > g.J) return;
+  const int k = 2 * kk + ((color + i + j) & 1);
+  if (k < 1 || k > g.J) return;
+  const size_t n = g.n;
+  const size_t c = ((size_t)i * n + j) * n + k;
+  float sum, diag;
+  sw_stencil(e, c, i, j, k, g, sum, diag);
+  e[c] = (sum - b[c]) / diag;
+}
+
+__global__ void __launch_bounds__(256)
+    k_resid(const float *__restrict__ e, const float *__restrict__ b, float *__restrict__ r, LevelGeom g) {
+  const int k = blockIdx.x * 32 + threadIdx.x + 1;
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  if (k > g.J || j > g.J) return;
+  const size_t n = g.n;
+  const size_t c = ((size_t)i * n + j) * n + k;
+  float sum, diag;
+  sw_stencil(e, c, i, j, k, g, sum, diag);
+  r[c] = b[c] - (sum - diag * e[c]);
+}
+
+// 1-D restriction weight of fine node 2J'+o into coarse node J' (transpose of the prolongation / 2).
+__device__ __forceinline__ float restrict_w(int Jc, int o, const LevelGeom &f, const LevelGeom &cg) {
+  const int i = 2 * Jc + o;
+  if (i < 1 || i > f.J) return 0.0f;
+  if (o == 0) return 0.5f;
+  if (o < 0) return 0.25f;
+  if (Jc < cg.J) return 0.25f;
+  return 0.5f * (f.p - (float)i) / (f.p - (float)(2 * Jc));
+}
+
+// b_c = 4 * R(r_f): full weighting (transpose of trilinear prolongation).
+__global__ void __launch_bounds__(256)
+    k_restrict(const float *__restrict__ rf, LevelGeom f, float *__restrict__ bc, LevelGeom cg) {
+  const int K = blockIdx.x * 32 + threadIdx.x + 1;
+  const int Jj = blockIdx.y * 8 + threadIdx.y + 1;
+  const int I = blockIdx.z + 1;
+  if (K > cg.J || Jj > cg.J) return;
+  float wi[3], wj[3], wk[3];
+#pragma unroll
+  for (int o = -1; o <= 1; ++o) {
+    wi[o + 1] = restrict_w(I, o, f, cg);
+    wj[o + 1] = restrict_w(Jj, o, f, cg);
+    wk[o + 1] = restrict_w(K, o, f, cg);
+  }
+  const size_t n = f.n;
+  float acc = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (wi[a] == 0.0f) continue;
+    const size_t fi = (size_t)(2 * I + a - 1);
+#pragma unroll
+    for (int bb = 0; bb < 3; ++bb) {
+      if (wj[bb] == 0.0f) continue;
+      const size_t fj = (size_t)(2 * Jj + bb - 1);
+      const float wij = wi[a] * wj[bb];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (wk[c] == 0.0f) continue;
+        const size_t fk = (size_t)(2 * K + c - 1);
+        acc += wij * wk[c] * rf[(fi * n + fj) * n + fk];
+      }
+    }
+  }
+  const size_t m = cg.n;
+  bc[((size_t)I * m + Jj) * m + K] = 4.0f * acc;
+}
+
+// 1-D prolongation weights of fine node i from the coarse level.
+__device__ __forceinline__ int prolong_w(int i, const LevelGeom &f, const LevelGeom &cg, int &c0, float &w0,
+                                         float &w1) {
+  c0 = i >> 1;
+  if ((i & 1) == 0) {
+    w0 = 1.0f;
+    w1 = 0.0f;
+    return 1;
+  }
+  if (c0 + 1 <= cg.J) {
+    w0 = 0.5f;
+    w1 = 0.5f;
+    return 2;
+  }
+  w0 = (f.p - (float)i) / (f.p - (float)(2 * c0));
+  w1 = 0.0f;
+  return 1;
+}
+
+__device__ __forceinline__ float prolong_value(const float *__restrict__ ec, int i, int j, int k,
+                                               const LevelGeom &f, const LevelGeom &cg) {
+  int ci, cj, ck;
+  float wi0, wi1, wj0, wj1, wk0, wk1;
+  const int ni = prolong_w(i, f, cg, ci, wi0, wi1);
+  const int nj = prolong_w(j, f, cg, cj, wj0, wj1);
+  const int nk = prolong_w(k, f, cg, ck, wk0, wk1);
+  const size_t m = cg.n;
+  float val = 0.0f;
+  for (int a = 0; a < ni; ++a) {
+    const float wa = a ? wi1 : wi0;
+    for (int bb = 0; bb < nj; ++bb) {
+      const float wb = bb ? wj1 : wj0;
+      const size_t row = ((size_t)(ci + a) * m + (cj + bb)) * m + ck;
+      const float wab = wa * wb;
+      val += wab * wk0 * ec[row];
+      if (nk == 2) val += wab * wk1 * ec[row + 1];
+    }
+  }
+  return val;
+}
+
+__global__ void __launch_bounds__(256)
+    k_prolong(const float *__restrict__ ec, LevelGeom cg, float *__restrict__ ef, LevelGeom f) {
+  const int k = blockIdx.x * 32 + threadIdx.x + 1;
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  if (k > f.J || j > f.J) return;
+  const size_t n = f.n;
+  ef[((size_t)i * n + j) * n + k] += prolong_value(ec, i, j, k, f, cg);
+}
+
+// Finest level: add the coarse correction into the double-float pair.
+__global__ void __launch_bounds__(256)
+    k_prolong0(const float *__restrict__ ec, LevelGeom cg, float *__restrict__ hi, float *__restrict__ lo,
+               LevelGeom f) {
+  const int k = blockIdx.x * 32 + threadIdx.x + 1;
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  if (k > f.J || j > f.J) return;
+  const size_t n = f.n;
+  const size_t c = ((size_t)i * n + j) * n + k;
+  const float v = prolong_value(ec, i, j, k, f, cg);
+  float s, e, h, l;
+  df_two_sum(hi[c], v, s, e);
+  const float ln = __fadd_rn(lo[c], e);
+  df_fast_two_sum(s, ln, h, l);
+  hi[c] = h;
+  lo[c] = l;
+}
+
+// ------------------------------------------------------------------------------
+// tail: all levels with n <= GC_TAIL_MAX_N relaxed by one CTA in shared memory
+// ------------------------------------------------------------------------------
+struct TailDesc {
+  int nl;                       // number of tail levels
+  int pre, post, coarse;
+  LevelGeom g[GC_MAX_LEVELS];   // g[0] = first tail level
+  LevelGeom gf;                 // level above the tail (for nothing but completeness)
+};
+
+template <typename T>
+__device__ void t_zero(T *a, int n3) {
+  for (int i = threadIdx.x; i < n3; i += blockDim.x) a[i] = (T)0;
+}
+
+template <typename T>
+__device__ void t_smooth(T *e, const T *b, const LevelGeom &g, int sweeps) {
+  const int n = g.n, J = g.J;
+  const int m = J * J * J;
+  for (int s = 0; s < sweeps; ++s) {
+    for (int color = 0; color < 2; ++color) {
+      for (int t = threadIdx.x; t < m; t += blockDim.x) {
+        const int k = t % J + 1, j = (t / J) % J + 1, i = t / (J * J) + 1;
+        if (((i + j + k) & 1) != color) continue;
+        const int c = (i * n + j) * n + k;
+        T sx, sy, sz, dx_, dy_, dz_;
+        if (i == J) { sx = (T)g.a * e[c - n * n]; dx_ = (T)g.dB; } else { sx = e[c + n * n] + e[c - n * n]; dx_ = 2; }
+        if (j == J) { sy = (T)g.a * e[c - n]; dy_ = (T)g.dB; } else { sy = e[c + n] + e[c - n]; dy_ = 2; }
+        if (k == J) { sz = (T)g.a * e[c - 1]; dz_ = (T)g.dB; } else { sz = e[c + 1] + e[c - 1]; dz_ = 2; }
+        e[c] = ((sx + sy + sz) - b[c]) / (dx_ + dy_ + dz_);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__device__ void t_resid(const float *e, const float *b, float *r, const LevelGeom &g) {
+  const int n = g.n, J = g.J;
+  const int m = J * J * J;
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    const int k = t % J + 1, j = (t / J) % J + 1, i = t / (J * J) + 1;
+    const int c = (i * n + j) * n + k;
+    float sum, diag;
+    sw_stencil(e, (size_t)c, i, j, k, g, sum, diag);
+    r[c] = b[c] - (sum - diag * e[c]);
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ void t_restrict(const float *rf, const LevelGeom &f, T *bc, const LevelGeom &cg) {
+  const int J = cg.J, m = cg.n, n = f.n;
+  const int tot = J * J * J;
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int K = t % J + 1, Jj = (t / J) % J + 1, I = t / (J * J) + 1;
+    float acc = 0.0f;
+    for (int a = -1; a <= 1; ++a) {
+      const float wa = restrict_w(I, a, f, cg);
+      if (wa == 0.0f) continue;
+      for (int bb = -1; bb <= 1; ++bb) {
+        const float wb = restrict_w(Jj, bb, f, cg);
+        if (wb == 0.0f) continue;
+        for (int c = -1; c <= 1; ++c) {
+          const float wc = restrict_w(K, c, f, cg);
+          if (wc == 0.0f) continue;
+          acc += wa * wb * wc * rf[((2 * I + a) * n + (2 * Jj + bb)) * n + (2 * K + c)];
+        }
+      }
+    }
+    bc[(I * m + Jj) * m + K] = (T)(4.0f * acc);
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ void t_prolong(const T *ec, const LevelGeom &cg, float *ef, const LevelGeom &f) {
+  const int J = f.J, n = f.n, m = cg.n;
+  const int tot = J * J * J;
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int k = t % J + 1, j = (t / J) % J + 1, i = t / (J * J) + 1;
+    int ci, cj, ck;
+    float wi0, wi1, wj0, wj1, wk0, wk1;
+    const int ni = prolong_w(i, f, cg, ci, wi0, wi1);
+    const int nj = prolong_w(j, f, cg, cj, wj0, wj1);
+    const int nk = prolong_w(k, f, cg, ck, wk0, wk1);
+    float val = 0.0f;
+    for (int a = 0; a < ni; ++a)
+      for (int bb = 0; bb < nj; ++bb)
+        for (int c = 0; c < nk; ++c) {
+          const float w = (a ? wi1 : wi0) * (bb ? wj1 : wj0) * (c ? wk1 : wk0);
+          val += w * (float)ec[((ci + a) * m + (cj + bb)) * m + (ck + c)];
+        }
+    ef[(i * n + j) * n + k] += val;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(512) k_tail(const float *__restrict__ b_in, float *__restrict__ e_out, TailDesc d) {
+  extern __shared__ __align__(16) unsigned char tsm[];
+  float *E[GC_MAX_LEVELS], *B[GC_MAX_LEVELS], *R[GC_MAX_LEVELS];
+  double *E64 = nullptr, *B64 = nullptr;
+  size_t off = 0;
+  for (int l = 0; l < d.nl; ++l) {
+    const int n3 = d.g[l].n * d.g[l].n * d.g[l].n;
+    if (l == d.nl - 1) {
+      E64 = (double *)(tsm + off);
+      B64 = E64 + n3;
+      off += 2 * (size_t)n3 * sizeof(double);
+    } else {
+      E[l] = (float *)(tsm + off);
+      B[l] = E[l] + n3;
+      R[l] = B[l] + n3;
+      off += 3 * (size_t)n3 * sizeof(float);
+    }
+    off = (off + 15) & ~(size_t)15;
+  }
+  const int n0 = d.g[0].n * d.g[0].n * d.g[0].n;
+  if (d.nl == 1) {
+    for (int i = threadIdx.x; i < n0; i += blockDim.x) {
+      B64[i] = (double)b_in[i];
+      E64[i] = 0.0;
+    }
+    __syncthreads();
+    t_smooth<double>(E64, B64, d.g[0], d.coarse);
+    for (int i = threadIdx.x; i < n0; i += blockDim.x) e_out[i] = (float)E64[i];
+    return;
+  }
+  for (int i = threadIdx.x; i < n0; i += blockDim.x) {
+    B[0][i] = b_in[i];
+    E[0][i] = 0.0f;
+    R[0][i] = 0.0f;
+  }
+  for (int l = 1; l < d.nl - 1; ++l) {
+    const int n3 = d.g[l].n * d.g[l].n * d.g[l].n;
+    t_zero<float>(R[l], n3);
+    t_zero<float>(B[l], n3);
+  }
+  {
+    const int n3 = d.g[d.nl - 1].n * d.g[d.nl - 1].n * d.g[d.nl - 1].n;
+    t_zero<double>(B64, n3);
+  }
+  __syncthreads();
+  for (int l = 0; l < d.nl - 1; ++l) {
+    if (l > 0) {
+      t_zero<float>(E[l], d.g[l].n * d.g[l].n * d.g[l].n);
+      __syncthreads();
+    }
+    t_smooth<float>(E[l], B[l], d.g[l], d.pre);
+    t_resid(E[l], B[l], R[l], d.g[l]);
+    if (l + 1 == d.nl - 1)
+      t_restrict<double>(R[l], d.g[l], B64, d.g[l + 1]);
+    else
+      t_restrict<float>(R[l], d.g[l], B[l + 1], d.g[l + 1]);
+  }
+  {
+    const LevelGeom &gc = d.g[d.nl - 1];
+    t_zero<double>(E64, gc.n * gc.n * gc.n);
+    __syncthreads();
+    t_smooth<double>(E64, B64, gc, d.coarse);
+  }
+  for (int l = d.nl - 2; l >= 0; --l) {
+    if (l + 1 == d.nl - 1)
+      t_prolong<double>(E64, d.g[l + 1], E[l], d.g[l]);
+    else
+      t_prolong<float>(E[l + 1], d.g[l + 1], E[l], d.g[l]);
+    t_smooth<float>(E[l], B[l], d.g[l], d.post);
+  }
+  for (int i = threadIdx.x; i < n0; i += blockDim.x) e_out[i] = E[0][i];
+}
+
+// ------------------------------------------------------------------------------
+// boundary faces, moments, scaling
+// ------------------------------------------------------------------------------
+// Multipole Dirichlet faces (multigrid.py:261-295) evaluated in FP64 from the raw
+// moments (multigrid.py:378-389), written as double-float pairs.
+__global__ void k_faces(float *__restrict__ hi, float *__restrict__ lo, int G, double dx, double grav,
+                        const double *__restrict__ mom) {
+  const long long tot = 6LL * G * G;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= tot) return;
+  const int face = (int)(t / ((long long)G * G));
+  const int rem = (int)(t % ((long long)G * G));
+  const int u = rem / G, v = rem % G;
+  int i, j, k;
+  switch (face) {
+    case 0: i = 0; j = u; k = v; break;
+    case 1: i = G - 1; j = u; k = v; break;
+    case 2: j = 0; i = u; k = v; break;
+    case 3: j = G - 1; i = u; k = v; break;
+    case 4: k = 0; i = u; j = v; break;
+    default: k = G - 1; i = u; j = v; break;
+  }
+  const double M = mom[0];
+  double phi = 0.0;
+  if (M > 0.0) {
+    const double cx = mom[1] / M, cy = mom[2] / M, cz = mom[3] / M;
+    const double sxx = mom[4] - M * cx * cx, syy = mom[5] - M * cy * cy, szz = mom[6] - M * cz * cz;
+    const double sxy = mom[7] - M * cx * cy, sxz = mom[8] - M * cx * cz, syz = mom[9] - M * cy * cz;
+    const double trs = sxx + syy + szz;
+    const double rx = i * dx - cx, ry = j * dx - cy, rz = k * dx - cz;
+    const double d2 = rx * rx + ry * ry + rz * rz + 1e-12;
+    const double dd = sqrt(d2);
+    const double nx = rx / dd, ny = ry / dd, nz = rz / dd;
+    const double nsn = nx * nx * sxx + ny * ny * syy + nz * nz * szz + 2.0 * (nx * ny * sxy + nx * nz * sxz + ny * nz * syz);
+    const double quad = 3.0 * nsn - trs;
+    phi = -grav * (M / dd + quad / (2.0 * d2 * dd));
+  }
+  const size_t c = ((size_t)i * G + j) * G + k;
+  const float h = (float)phi;
+  hi[c] = h;
+  lo[c] = (float)(phi - (double)h);
+}
+
+// Column moments of an f32 density: one warp per (i,j) column, Kahan-compensated
+// FP32 sums along k, FP64 across columns (the reference's column scheme,
+// multigrid.py:192-221, finished in FP64). Block partials of the ten raw moments.
+__global__ void __launch_bounds__(256)
+    k_moments_rho(const float *__restrict__ rho, int G, double dx, double *__restrict__ parts, unsigned *status) {
+  const int lane = threadIdx.x & 31;
+  const long long col = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+  double v[10];
+#pragma unroll
+  for (int q = 0; q < 10; ++q) v[q] = 0.0;
+  if (col < (long long)G * G) {
+    const int i = (int)(col / G), j = (int)(col % G);
+    const float *p = rho + (size_t)col * G;
+    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
+    bool bad = false;
+    for (int k = lane; k < G; k += 32) {
+      const float r = p[k];
+      if (!isfinite(r)) { bad = true; continue; }
+      const float fk = (float)k;
+      float y, t;
+      y = r - c0; t = s0 + y; c0 = (t - s0) - y; s0 = t;
+      const float r1 = r * fk;
+      y = r1 - c1; t = s1 + y; c1 = (t - s1) - y; s1 = t;
+      const float r2 = r1 * fk;
+      y = r2 - c2; t = s2 + y; c2 = (t - s2) - y; s2 = t;
+    }
+    if (bad) atomicOr(status, GC_FLAG_NONFINITE_RHO);
+    double S0 = (double)s0 - (double)c0, S1 = (double)s1 - (double)c1, S2 = (double)s2 - (double)c2;
+    for (int o = 16; o > 0; o >>= 1) {
+      S0 += __shfl_down_sync(0xffffffffu, S0, o);
+      S1 += __shfl_down_sync(0xffffffffu, S1, o);
+      S2 += __shfl_down_sync(0xffffffffu, S2, o);
+    }
+    if (lane == 0) {
+      const double vol = dx * dx * dx;
+      const double x = i * dx, y = j * dx;
+      const double m0 = S0 * vol, m1 = S1 * vol * dx, m2 = S2 * vol * dx * dx;
+      v[0] = m0; v[1] = m0 * x; v[2] = m0 * y; v[3] = m1;
+      v[4] = m0 * x * x; v[5] = m0 * y * y; v[6] = m2;
+      v[7] = m0 * x * y; v[8] = m1 * x; v[9] = m1 * y;
+    }
+  }
+  block_partials<10>(v, parts + (size_t)blockIdx.x * 10);
+}
+
+// b0 = h^2 * f32(f32(4 pi G) * rho); partial sums of b0^2 over all nodes.
+__global__ void __launch_bounds__(256)
+    k_rhs_from_rho(const float *__restrict__ rho, float *__restrict__ b0, size_t n, float fpg, float h2,
+                   double *__restrict__ parts) {
+  double acc[1] = {0.0};
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const float rhs = __fmul_rn(fpg, rho[t]);
+    const float bv = __fmul_rn(rhs, h2);
+    b0[t] = bv;
+    acc[0] += (double)bv * (double)bv;
+  }
+  block_partials<1>(acc, parts + blockIdx.x);
+}
+
+__global__ void __launch_bounds__(256) k_sumsq(const float *__restrict__ a, size_t n, double *__restrict__ parts) {
+  double acc[1] = {0.0};
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const double v = a[t];
+    acc[0] += v * v;
+  }
+  block_partials<1>(acc, parts + blockIdx.x);
+}
+
+__global__ void k_copy_hi_to(const float *__restrict__ hi, float *__restrict__ out, size_t n) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    out[t] = hi[t];
+}
+
+// ------------------------------------------------------------------------------
+// host orchestration
+// ------------------------------------------------------------------------------
+static dim3 rb_grid(const LevelGeom &g) {
+  const int nkk = g.n / 2 + 1;
+  return dim3(gc_blocks(nkk, RB_TX), gc_blocks(g.J, RB_TY), (unsigned)g.J);
+}
+static dim3 node_grid(const LevelGeom &g) { return dim3(gc_blocks(g.J, 32), gc_blocks(g.J, 8), (unsigned)g.J); }
+
+static int launch_smooth0(gc_ctx *ctx, int sweeps) {
+  const LevelGeom &g = ctx->lev[0];
+  for (int s = 0; s < sweeps; ++s)
+    for (int color = 0; color < 2; ++color)
+      k_smooth0<<<rb_grid(g), dim3(RB_TX, RB_TY), 0, ctx->stream>>>(ctx->hi, ctx->lo, ctx->b0, ctx->G, color);
+  GC_LAUNCH_CHECK(ctx, "smooth0");
+  return GC_OK;
+}
+
+static int launch_smooth(gc_ctx *ctx, int l, int sweeps) {
+  const LevelGeom &g = ctx->lev[l];
+  for (int s = 0; s < sweeps; ++s)
+    for (int color = 0; color < 2; ++color)
+      k_smooth<<<rb_grid(g), dim3(RB_TX, RB_TY), 0, ctx->stream>>>(ctx->e[l], ctx->b[l], g, color);
+  GC_LAUNCH_CHECK(ctx, "smooth");
+  return GC_OK;
+}
+
+static int launch_tail(gc_ctx *ctx, const gc_mg_params *p) {
+  TailDesc d;
+  memset(&d, 0, sizeof(d));
+  d.nl = ctx->nlev - ctx->tail;
+  d.pre = p->pre_sweeps;
+  d.post = p->post_sweeps;
+  d.coarse = p->coarse_sweeps;
+  for (int l = 0; l < d.nl; ++l) d.g[l] = ctx->lev[ctx->tail + l];
+  const size_t smem = tail_smem_bytes(ctx);
+  static int attr_set_for = -1;
+  if (smem > 48 * 1024 && attr_set_for != (int)smem) {
+    GC_CUDA(ctx, cudaFuncSetAttribute(k_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set_for = (int)smem;
+  }
+  k_tail<<<1, 512, smem, ctx->stream>>>(ctx->b[ctx->tail], ctx->e[ctx->tail], d);
+  GC_LAUNCH_CHECK(ctx, "tail");
+  return GC_OK;
+}
+
+static int vcycle(gc_ctx *ctx, const gc_mg_params *p) {
+  const int L = ctx->nlev;
+  if (L == 0) return GC_OK;
+  if (L == 1) return launch_smooth0(ctx, p->coarse_sweeps);
+  int st;
+  if ((st = launch_smooth0(ctx, p->pre_sweeps))) return st;
+  const LevelGeom &g0 = ctx->lev[0];
+  k_resid0<<<node_grid(g0), dim3(32, 8), 0, ctx->stream>>>(ctx->hi, ctx->lo, ctx->b0, ctx->r0, nullptr, ctx->G);
+  k_restrict<<<node_grid(ctx->lev[1]), dim3(32, 8), 0, ctx->stream>>>(ctx->r0, g0, ctx->b[1], ctx->lev[1]);
+  GC_LAUNCH_CHECK(ctx, "resid0/restrict");
+  for (int l = 1; l < ctx->tail; ++l) {
+    const LevelGeom &g = ctx->lev[l];
+    const size_t n3 = (size_t)g.n * g.n * g.n;
+    GC_CUDA(ctx, cudaMemsetAsync(ctx->e[l], 0, n3 * sizeof(float), ctx->stream));
+    if ((st = launch_smooth(ctx, l, p->pre_sweeps))) return st;
+    k_resid<<<node_grid(g), dim3(32, 8), 0, ctx->stream>>>(ctx->e[l], ctx->b[l], ctx->rc, g);
+    k_restrict<<<node_grid(ctx->lev[l + 1]), dim3(32, 8), 0, ctx->stream>>>(ctx->rc, g, ctx->b[l + 1], ctx->lev[l + 1]);
+    GC_LAUNCH_CHECK(ctx, "resid/restrict");
+  }
+  if (ctx->tail < L) {
+    if ((st = launch_tail(ctx, p))) return st;
+  }
+  for (int l = ctx->tail - 1; l >= 1; --l) {
+    k_prolong<<<node_grid(ctx->lev[l]), dim3(32, 8), 0, ctx->stream>>>(ctx->e[l + 1], ctx->lev[l + 1], ctx->e[l], ctx->lev[l]);
+    GC_LAUNCH_CHECK(ctx, "prolong");
+    if ((st = launch_smooth(ctx, l, p->post_sweeps))) return st;
+  }
+  k_prolong0<<<node_grid(g0), dim3(32, 8), 0, ctx->stream>>>(ctx->e[1], ctx->lev[1], ctx->hi, ctx->lo, g0);
+  GC_LAUNCH_CHECK(ctx, "prolong0");
+  return launch_smooth0(ctx, p->post_sweeps);
+}
+
+int gc_finalize(gc_ctx *ctx, const double *parts, int nparts, int nv, double *dst) {
+  k_finalize<<<1, 1024, 0, ctx->stream>>>(parts, nparts, nv, dst, 0);
+  GC_LAUNCH_CHECK(ctx, "finalize");
+  return GC_OK;
+}
+
+static int finalize_to(gc_ctx *ctx, int nparts, int nv, int slot) {
+  return gc_finalize(ctx, ctx->red, nparts, nv, ctx->dsmall + slot);
+}
+
+// ||r0||^2 into dsmall[GC_S_RNORM2] (async).
+static int resid_norm_async(gc_ctx *ctx) {
+  const LevelGeom &g0 = ctx->lev[0];
+  const dim3 grid = node_grid(g0);
+  const size_t nb = (size_t)grid.x * grid.y * grid.z;
+  int st = gc_ensure_red(ctx, nb);
+  if (st) return st;
+  k_resid0<<<grid, dim3(32, 8), 0, ctx->stream>>>(ctx->hi, ctx->lo, ctx->b0, nullptr, ctx->red, ctx->G);
+  GC_LAUNCH_CHECK(ctx, "resid0 norm");
+  return finalize_to(ctx, (int)nb, 1, GC_S_RNORM2);
+}
+
+static int read_small(gc_ctx *ctx, int slot, int count) {
+  GC_CUDA(ctx, cudaMemcpyAsync(ctx->hsmall + slot, ctx->dsmall + slot, count * sizeof(double), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return GC_OK;
+}
+
+// ||b0||^2 into dsmall[GC_S_BNORM2] (async).
+int gc_norm_b(gc_ctx *ctx) {
+  const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
+  const int nb = 1024;
+  int st = gc_ensure_red(ctx, nb);
+  if (st) return st;
+  k_sumsq<<<nb, 256, 0, ctx->stream>>>(ctx->b0, g3, ctx->red);
+  GC_LAUNCH_CHECK(ctx, "sumsq");
+  return finalize_to(ctx, nb, 1, GC_S_BNORM2);
+}
+
+int gc_faces_from_moments(gc_ctx *ctx) {
+  const long long tot = 6LL * ctx->G * ctx->G;
+  k_faces<<<gc_blocks(tot, 256), 256, 0, ctx->stream>>>(ctx->hi, ctx->lo, ctx->G, ctx->dx, ctx->grav, ctx->dmom);
+  GC_LAUNCH_CHECK(ctx, "faces");
+  return GC_OK;
+}
+
+// Adaptive V-cycling (multigrid.py:473-485). Expects b0, faces and the initial
+// interior guess in place and ||b0||^2 in dsmall.
+int gc_mg_run(gc_ctx *ctx, const gc_mg_params *p, gc_mg_stats *stats) {
+  gc_mg_stats st;
+  memset(&st, 0, sizeof(st));
+  int s = read_small(ctx, GC_S_BNORM2, 1);
+  if (s) return s;
+  const double bnorm = sqrt(ctx->hsmall[GC_S_BNORM2]);
+  const double h2 = ctx->dx * ctx->dx;
+  st.rhs_norm = bnorm / h2;
+  st.cycles = p->max_cycles;
+  st.converged = 0;
+  double rnorm = NAN;
+  if (ctx->nlev == 0) {
+    st.cycles = 0;
+    st.converged = 1;
+    st.res_norm = 0.0;
+  } else {
+    for (int c = 0; c < p->max_cycles; ++c) {
+      if ((s = vcycle(ctx, p))) return s;
+      if (c + 1 >= p->min_cycles && bnorm > 0.0) {
+        if ((s = resid_norm_async(ctx))) return s;
+        if ((s = read_small(ctx, GC_S_RNORM2, 1))) return s;
+        rnorm = sqrt(ctx->hsmall[GC_S_RNORM2]);
+        if (rnorm < p->tol * bnorm) {
+          st.cycles = c + 1;
+          st.converged = 1;
+          break;
+        }
+      }
+    }
+    if (!(rnorm == rnorm)) {
+      if ((s = resid_norm_async(ctx))) return s;
+      if ((s = read_small(ctx, GC_S_RNORM2, 1))) return s;
+      rnorm = sqrt(ctx->hsmall[GC_S_RNORM2]);
+    }
+    st.res_norm = rnorm / h2;
+  }
+  ctx->last_stats = st;
+  ctx->solved_once = 1;
+  if (stats) *stats = st;
+  return GC_OK;
+}
+
+int gc_mg_check_params(gc_ctx *ctx, const gc_mg_params *p) {
+  GC_REQUIRE(ctx, p->pre_sweeps >= 0 && p->post_sweeps >= 0 && p->pre_sweeps + p->post_sweeps >= 1,
+             "sweep counts must be >= 0 with at least one smoothing sweep");
+  GC_REQUIRE(ctx, p->coarse_sweeps >= 1, "coarse_sweeps must be >= 1");
+  GC_REQUIRE(ctx, p->max_cycles >= 0 && p->max_cycles <= 100000, "max_cycles out of range");
+  GC_REQUIRE(ctx, p->tol >= 0.0, "tol must be >= 0");
+  return GC_OK;
+}
+
+// Moments of an f32 density into ctx->dmom (async). Raises GC_FLAG_NONFINITE_RHO.
+static int moments_rho_async(gc_ctx *ctx, const float *rho) {
+  const long long cols = (long long)ctx->G * ctx->G;
+  const unsigned nb = gc_blocks(cols, 8);
+  int s = gc_ensure_red(ctx, (size_t)nb * 10);
+  if (s) return s;
+  k_moments_rho<<<nb, 256, 0, ctx->stream>>>(rho, ctx->G, ctx->dx, ctx->red, ctx->dstatus);
+  GC_LAUNCH_CHECK(ctx, "moments");
+  k_finalize<<<1, 1024, 0, ctx->stream>>>(ctx->red, (int)nb, 10, ctx->dmom, 0);
+  GC_LAUNCH_CHECK(ctx, "moments finalize");
+  return GC_OK;
+}
+
+extern "C" int gc_moments(gc_ctx *ctx, const float *rho, double out[10]) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, rho && out, "gc_moments: NULL pointer");
+  int s = moments_rho_async(ctx, rho);
+  if (s) return s;
+  GC_CUDA(ctx, cudaMemcpyAsync(out, ctx->dmom, 10 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return GC_OK;
+}
+
+extern "C" int gc_mg_solve(gc_ctx *ctx, const float *rho, float *phi, int warm_start, const gc_mg_params *params,
+                           gc_mg_stats *stats) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, rho && phi, "gc_mg_solve: NULL rho or phi");
+  gc_mg_params p;
+  if (params)
+    p = *params;
+  else
+    gc_mg_default_params(&p);
+  int s = gc_mg_check_params(ctx, &p);
+  if (s) return s;
+  const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
+  // moments (multigrid.py:364-389), on the device, no host round trip
+  if ((s = moments_rho_async(ctx, rho))) return s;
+  // b0 = h^2 * 4 pi G rho (multigrid.py:463) and ||b0||^2 (multigrid.py:477)
+  {
+    const int nb = 1024;
+    if ((s = gc_ensure_red(ctx, nb))) return s;
+    const float fpg = (float)(4.0 * M_PI * ctx->grav);
+    const float h2 = (float)(ctx->dx * ctx->dx);
+    k_rhs_from_rho<<<nb, 256, 0, ctx->stream>>>(rho, ctx->b0, g3, fpg, h2, ctx->red);
+    GC_LAUNCH_CHECK(ctx, "rhs");
+    if ((s = finalize_to(ctx, nb, 1, GC_S_BNORM2))) return s;
+  }
+  // initial guess (multigrid.py:464-467): previous phi or zero; the lo part starts at zero
+  if (warm_start) {
+    GC_CUDA(ctx, cudaMemcpyAsync(ctx->hi, phi, g3 * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+  } else {
+    GC_CUDA(ctx, cudaMemsetAsync(ctx->hi, 0, g3 * sizeof(float), ctx->stream));
+  }
+  GC_CUDA(ctx, cudaMemsetAsync(ctx->lo, 0, g3 * sizeof(float), ctx->stream));
+  if ((s = gc_faces_from_moments(ctx))) return s;
+  if ((s = gc_mg_run(ctx, &p, stats))) return s;
+  // phi = f32(hi + lo) == hi (the pair is normalised)
+  k_copy_hi_to<<<1024, 256, 0, ctx->stream>>>(ctx->hi, phi, g3);
+  GC_LAUNCH_CHECK(ctx, "copy phi");
+  uint32_t flags = 0;
+  if ((s = gc_status(ctx, &flags, 0))) return s;
+  if (flags & GC_FLAG_NONFINITE_RHO) {
+    gc_set_error(ctx, "rho contains non-finite values");
+    return GC_ERR_NONFINITE;
+  }
+  return GC_OK;
+}
+
+extern "C" int gc_mg_residual_norm(gc_ctx *ctx, const float *phi_f32, double *out) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, out, "gc_mg_residual_norm: NULL out");
+  if (ctx->nlev == 0) {
+    *out = 0.0;
+    return GC_OK;
+  }
+  const LevelGeom &g0 = ctx->lev[0];
+  const dim3 grid = node_grid(g0);
+  const size_t nb = (size_t)grid.x * grid.y * grid.z;
+  int s = gc_ensure_red(ctx, nb);
+  if (s) return s;
+  if (phi_f32)
+    k_resid64<<<grid, dim3(32, 8), 0, ctx->stream>>>(phi_f32, nullptr, ctx->b0, ctx->red, ctx->G);
+  else
+    k_resid64<<<grid, dim3(32, 8), 0, ctx->stream>>>(ctx->hi, ctx->lo, ctx->b0, ctx->red, ctx->G);
+  GC_LAUNCH_CHECK(ctx, "resid64");
+  if ((s = finalize_to(ctx, (int)nb, 1, GC_S_RNORM64))) return s;
+  if ((s = read_small(ctx, GC_S_RNORM64, 1))) return s;
+  *out = sqrt(ctx->hsmall[GC_S_RNORM64]) / (ctx->dx * ctx->dx);
+  return GC_OK;
+}
+
+extern "C" const float *gc_pm_potential(const gc_ctx *ctx) { return ctx ? ctx->hi : nullptr; }

@@ -1,0 +1,712 @@
+// Particle <-> grid kernels of the PM force chain.
+//
+// Arithmetic follows the reference kernels in src/galaxy_collision/deposit.py
+// and integrator.py operation by operation in f32 with explicit
+// round-to-nearest intrinsics (no FMA contraction), so the CPU restatement can
+// reproduce them bit for bit. The deposit accumulates the reference's per-corner
+// f32 contributions m*wx*wy*wz into an int64 fixed-point grid: integer addition
+// is associative, so the density is bit-identical whatever the particle order or
+// atomic interleaving.
+#include "common.cuh"
+
+#include <math.h>
+
+// ------------------------------------------------------------------------------
+// fixed-point set-up: total density-mass and quantum exponent
+// ------------------------------------------------------------------------------
+// The quantum must not depend on the particle order (sorting permutes the
+// particles), so the total S = sum m/dx^3 is formed exactly: every positive
+// finite term is truncated to an integer multiple of 2^-s, with s chosen from
+// the largest term (an order-independent maximum) so that the integer sum of
+// all n terms stays below 2^62, and the integers are summed exactly.
+__global__ void __launch_bounds__(256) k_mass_max(const float *__restrict__ m, long long n, float inv_vol,
+                                                  unsigned *__restrict__ maxbits) {
+  unsigned best = 0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const float mm = __fmul_rn(m[p], inv_vol);
+    if (isfinite(mm) && mm > 0.0f) best = max(best, __float_as_uint(mm));
+  }
+  best = __reduce_max_sync(0xffffffffu, best);
+  if ((threadIdx.x & 31) == 0 && best) atomicMax(maxbits, best);
+}
+
+__device__ __forceinline__ int mass_shift(unsigned maxbits, int log2n) {
+  const int emax = (int)((maxbits >> 23) & 0xffu) - 127;  // max term < 2^(emax+1)
+  return 62 - log2n - (emax + 1);
+}
+
+__global__ void __launch_bounds__(256) k_mass_isum(const float *__restrict__ m, long long n, float inv_vol,
+                                                   const unsigned *__restrict__ maxbits, int log2n,
+                                                   unsigned long long *__restrict__ isum) {
+  const int s = mass_shift(*maxbits, log2n);
+  const double scale = ldexp(1.0, s);
+  unsigned long long acc = 0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const float mm = __fmul_rn(m[p], inv_vol);
+    if (isfinite(mm) && mm > 0.0f) acc += __double2ull_rz((double)mm * scale);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(isum, acc);
+}
+
+// E = exponent(S) - bits so that the whole mass is at most 2^bits quanta.
+__global__ void k_qexp(const unsigned *__restrict__ maxbits, const unsigned long long *__restrict__ isum, int log2n,
+                       double *__restrict__ small, int mass_slot, int exp_slot, int bits) {
+  if (threadIdx.x != 0) return;
+  double S = 0.0;
+  if (*maxbits) S = ldexp((double)(*isum), -mass_shift(*maxbits, log2n));
+  int ex = 0;
+  if (S > 0.0) frexp(S, &ex);  // S = f * 2^ex, f in [0.5, 1)
+  int E = ex - bits;
+  if (E < -120) E = -120;      // keep 2^-E a normal f32
+  if (E > 120) E = 120;
+  small[mass_slot] = S;
+  small[exp_slot] = (double)E;
+}
+
+static int ceil_log2(long long n) {
+  int L = 0;
+  while ((1LL << L) < n) ++L;
+  return L;
+}
+
+int gc_fixed_point_setup(gc_ctx *ctx, const float *m, int64_t n, int bits, int mass_slot, int exp_slot) {
+  const float dxf = (float)ctx->dx;
+  const float inv_vol = 1.0f / ((dxf * dxf) * dxf);
+  // two integer scratch words live in the reduction buffer
+  int s = gc_ensure_red(ctx, 4);
+  if (s) return s;
+  unsigned *maxbits = (unsigned *)ctx->red;
+  unsigned long long *isum = (unsigned long long *)(ctx->red + 1);
+  GC_CUDA(ctx, cudaMemsetAsync(ctx->red, 0, 2 * sizeof(double), ctx->stream));
+  unsigned nb = gc_blocks(n, 256);
+  if (nb > 152u * 8u) nb = 152u * 8u;
+  const int L = ceil_log2((long long)n);
+  k_mass_max<<<nb, 256, 0, ctx->stream>>>(m, (long long)n, inv_vol, maxbits);
+  k_mass_isum<<<nb, 256, 0, ctx->stream>>>(m, (long long)n, inv_vol, maxbits, L, isum);
+  k_qexp<<<1, 32, 0, ctx->stream>>>(maxbits, isum, L, ctx->dsmall, mass_slot, exp_slot, bits);
+  GC_LAUNCH_CHECK(ctx, "fixed-point set-up");
+  return GC_OK;
+}
+
+// ------------------------------------------------------------------------------
+// deposit (deposit.py:47-82)
+// ------------------------------------------------------------------------------
+struct DepCtx {
+  float dx;
+  float inv_vol;  // 1/(dx*dx*dx) in f32, as the reference (deposit.py:58)
+  int G;
+};
+
+// Per-corner int64 contributions of one particle; corners outside the box are 0.
+// Returns false when the particle deposits nothing.
+__device__ __forceinline__ bool cic_contrib(float x, float y, float z, float mass, const DepCtx &d, float qscale,
+                                            CellPos &c, long long (&q)[8]) {
+  if (!gc_cell_of(x, y, z, d.dx, d.G, c)) return false;
+  const float mm = __fmul_rn(mass, d.inv_vol);
+  const float wx[2] = {__fsub_rn(1.0f, c.fx), c.fx};
+  const float wy[2] = {__fsub_rn(1.0f, c.fy), c.fy};
+  const float wz[2] = {__fsub_rn(1.0f, c.fz), c.fz};
+#pragma unroll
+  for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+      for (int cz = 0; cz < 2; ++cz) {
+        const int jx = c.ix + cx, jy = c.iy + cy, jz = c.iz + cz;
+        const bool in = (unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G && (unsigned)jz < (unsigned)d.G;
+        const float w = __fmul_rn(__fmul_rn(__fmul_rn(mm, wx[cx]), wy[cy]), wz[cz]);
+        q[(cx * 2 + cy) * 2 + cz] = in ? __float2ll_rn(__fmul_rn(w, qscale)) : 0LL;
+      }
+  return true;
+}
+
+__device__ __forceinline__ void flush_corners(long long *__restrict__ qg, const CellPos &c, int G,
+                                              const long long (&q)[8]) {
+#pragma unroll
+  for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+      for (int cz = 0; cz < 2; ++cz) {
+        const long long v = q[(cx * 2 + cy) * 2 + cz];
+        if (v != 0) {
+          const size_t idx = ((size_t)(c.ix + cx) * G + (c.iy + cy)) * G + (c.iz + cz);
+          atomicAdd((unsigned long long *)(qg + idx), (unsigned long long)v);
+        }
+      }
+}
+
+// One particle per thread; when a whole warp shares one cell its 8 corner sums
+// are reduced in registers and flushed by one lane.
+__global__ void __launch_bounds__(256)
+    k_deposit(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
+              const float *__restrict__ m, long long n, DepCtx d, const double *__restrict__ qexp,
+              long long *__restrict__ qg, unsigned *__restrict__ status) {
+  const float qscale = ldexpf(1.0f, -(int)(*qexp));
+  const int lane = threadIdx.x & 31;
+  const long long warp0 = (blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31));
+  const long long wstride = (long long)gridDim.x * blockDim.x;
+  for (long long base = warp0; base < n; base += wstride) {
+    const long long p = base + lane;
+    CellPos c;
+    long long q[8];
+    bool ok = false;
+    if (p < n) {
+      const float px = x[p], py = y[p], pz = z[p];
+      if (!gc_finite3(px, py, pz)) atomicOr(status, GC_FLAG_NONFINITE_POS);
+      ok = cic_contrib(px, py, pz, m[p], d, qscale, c, q);
+    }
+    const unsigned key = ok ? (unsigned)(((c.ix + 1) * (d.G + 1) + (c.iy + 1)) * (d.G + 1) + (c.iz + 1))
+                            : (0x80000000u | (unsigned)lane);
+    int all_same = 0;
+    __match_all_sync(0xffffffffu, key, &all_same);
+    if (all_same) {
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        long long v = q[t];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        q[t] = v;
+      }
+      if (lane == 0) flush_corners(qg, c, d.G, q);
+    } else if (ok) {
+      flush_corners(qg, c, d.G, q);
+    }
+  }
+}
+
+// Cell-sorted particles: each thread walks RUN consecutive particles and keeps a
+// running 8-corner sum while the cell does not change; the warp then merges the
+// final runs when all lanes end in one cell.
+#define DEP_RUN 8
+__global__ void __launch_bounds__(256)
+    k_deposit_runs(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
+                   const float *__restrict__ m, long long n, DepCtx d, const double *__restrict__ qexp,
+                   long long *__restrict__ qg, unsigned *__restrict__ status) {
+  const float qscale = ldexpf(1.0f, -(int)(*qexp));
+  const int lane = threadIdx.x & 31;
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long nthreads = (long long)gridDim.x * blockDim.x;
+  const long long nchunks = (n + DEP_RUN - 1) / DEP_RUN;
+  const long long iters = (nchunks + nthreads - 1) / nthreads;
+  for (long long it = 0; it < iters; ++it) {
+    const long long chunk = it * nthreads + tid;
+    const long long p0 = chunk * DEP_RUN;
+    long long acc[8];
+    CellPos cur;
+    unsigned cur_key = 0xffffffffu;
+    bool have = false;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) acc[t] = 0;
+    if (p0 < n) {
+      const long long p1 = (p0 + DEP_RUN < n) ? p0 + DEP_RUN : n;
+      for (long long p = p0; p < p1; ++p) {
+        const float px = x[p], py = y[p], pz = z[p];
+        if (!gc_finite3(px, py, pz)) atomicOr(status, GC_FLAG_NONFINITE_POS);
+        CellPos c;
+        long long q[8];
+        if (!cic_contrib(px, py, pz, m[p], d, qscale, c, q)) continue;
+        const unsigned key = (unsigned)(((c.ix + 1) * (d.G + 1) + (c.iy + 1)) * (d.G + 1) + (c.iz + 1));
+        if (have && key == cur_key) {
+#pragma unroll
+          for (int t = 0; t < 8; ++t) acc[t] += q[t];
+        } else {
+          if (have) flush_corners(qg, cur, d.G, acc);
+          cur = c;
+          cur_key = key;
+          have = true;
+#pragma unroll
+          for (int t = 0; t < 8; ++t) acc[t] = q[t];
+        }
+      }
+    }
+    const unsigned mkey = have ? cur_key : (0x80000000u | (unsigned)lane);
+    int all_same = 0;
+    __match_all_sync(0xffffffffu, mkey, &all_same);
+    if (all_same) {
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        long long v = acc[t];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        acc[t] = v;
+      }
+      if (lane == 0) flush_corners(qg, cur, d.G, acc);
+    } else if (have) {
+      flush_corners(qg, cur, d.G, acc);
+    }
+  }
+}
+
+int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, const float *m, int64_t n,
+                 const double *qexp, int sorted_runs) {
+  if (n <= 0) return GC_OK;
+  DepCtx d;
+  d.dx = (float)ctx->dx;
+  d.inv_vol = 1.0f / ((d.dx * d.dx) * d.dx);
+  d.G = ctx->G;
+  if (sorted_runs) {
+    const long long nchunks = (n + DEP_RUN - 1) / DEP_RUN;
+    unsigned nb = gc_blocks(nchunks, 256);
+    if (nb > 152u * 16u) nb = 152u * 16u;
+    k_deposit_runs<<<nb, 256, 0, ctx->stream>>>(x, y, z, m, (long long)n, d, qexp, ctx->q, ctx->dstatus);
+  } else {
+    unsigned nb = gc_blocks(n, 256);
+    if (nb > 152u * 32u) nb = 152u * 32u;
+    k_deposit<<<nb, 256, 0, ctx->stream>>>(x, y, z, m, (long long)n, d, qexp, ctx->q, ctx->dstatus);
+  }
+  GC_LAUNCH_CHECK(ctx, "deposit");
+  return GC_OK;
+}
+
+// ------------------------------------------------------------------------------
+// q -> rho / b, zero q, exact integer column moments, ||b||^2
+// ------------------------------------------------------------------------------
+// One warp per (i,j) column. Column sums S0 = sum q, S1 = sum q k and
+// S2 = sum q k^2 are exact in integers (S2 split at bit 32), combined across
+// columns in FP64. Partials per block: 10 moments + ||b||^2.
+__global__ void __launch_bounds__(256)
+    k_convert_q(long long *__restrict__ qg, int G, double dx, const double *__restrict__ qexp, float *__restrict__ rho,
+                float *__restrict__ b, double bfac, double *__restrict__ parts) {
+  const int lane = threadIdx.x & 31;
+  const long long col = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int E = (int)(*qexp);
+  const float qinv = ldexpf(1.0f, E);
+  const float bscale = (float)(ldexp(1.0, E) * bfac);
+  double v[11];
+#pragma unroll
+  for (int t = 0; t < 11; ++t) v[t] = 0.0;
+  if (col < (long long)G * G) {
+    const int i = (int)(col / G), j = (int)(col % G);
+    long long *p = qg + (size_t)col * G;
+    long long S0 = 0, S1 = 0, S2h = 0;
+    unsigned long long S2l = 0;
+    float bb = 0.0f;
+    for (int k = lane; k < G; k += 32) {
+      const long long qv = p[k];
+      p[k] = 0;
+      const float qf = (float)qv;  // one rounding (cvt.rn)
+      if (rho) rho[(size_t)col * G + k] = __fmul_rn(qf, qinv);
+      const float bv = __fmul_rn(qf, bscale);
+      if (b) b[(size_t)col * G + k] = bv;
+      bb += bv * bv;
+      const long long kk = k;
+      S0 += qv;
+      S1 += qv * kk;
+      S2h += (qv >> 32) * (kk * kk);
+      S2l += (unsigned long long)(qv & 0xffffffffLL) * (unsigned long long)(kk * kk);
+    }
+    double d0 = (double)S0, d1 = (double)S1, d2 = (double)S2h * 4294967296.0 + (double)S2l;
+    double db = (double)bb;
+    for (int o = 16; o > 0; o >>= 1) {
+      d0 += __shfl_down_sync(0xffffffffu, d0, o);
+      d1 += __shfl_down_sync(0xffffffffu, d1, o);
+      d2 += __shfl_down_sync(0xffffffffu, d2, o);
+      db += __shfl_down_sync(0xffffffffu, db, o);
+    }
+    if (lane == 0) {
+      const double msc = ldexp(1.0, E) * dx * dx * dx;  // mass of one quantum
+      const double x = i * dx, y = j * dx;
+      const double m0 = d0 * msc, m1 = d1 * msc * dx, m2 = d2 * msc * dx * dx;
+      v[0] = m0; v[1] = m0 * x; v[2] = m0 * y; v[3] = m1;
+      v[4] = m0 * x * x; v[5] = m0 * y * y; v[6] = m2;
+      v[7] = m0 * x * y; v[8] = m1 * x; v[9] = m1 * y;
+      v[10] = db;
+    }
+  }
+  block_partials<11>(v, parts + (size_t)blockIdx.x * 11);
+}
+
+int gc_convert_q(gc_ctx *ctx, const double *qexp, float *rho_out, float *b_out) {
+  const long long cols = (long long)ctx->G * ctx->G;
+  const unsigned nb = gc_blocks(cols, 8);
+  int s = gc_ensure_red(ctx, (size_t)nb * 11);
+  if (s) return s;
+  const double bfac = 4.0 * M_PI * ctx->grav * ctx->dx * ctx->dx;
+  k_convert_q<<<nb, 256, 0, ctx->stream>>>(ctx->q, ctx->G, ctx->dx, qexp, rho_out, b_out, bfac, ctx->red);
+  GC_LAUNCH_CHECK(ctx, "convert q");
+  if ((s = gc_finalize(ctx, ctx->red, (int)nb, 11, ctx->dmom))) return s;
+  GC_CUDA(ctx, cudaMemcpyAsync(ctx->dsmall + GC_S_BNORM2, ctx->dmom + 10, sizeof(double), cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+  return GC_OK;
+}
+
+extern "C" int gc_deposit_cic(gc_ctx *ctx, const float *x, const float *y, const float *z, const float *m, int64_t n,
+                              int fixed_point_bits, float *rho) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, rho, "gc_deposit_cic: NULL rho");
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range: %lld", (long long)n);
+  GC_REQUIRE(ctx, n == 0 || (x && y && z && m), "gc_deposit_cic: NULL particle array");
+  GC_REQUIRE(ctx, fixed_point_bits >= 24 && fixed_point_bits <= 60, "fixed_point_bits must be in [24, 60]");
+  int s;
+  if (n > 0) {
+    if ((s = gc_fixed_point_setup(ctx, m, n, fixed_point_bits, GC_S_MASS, GC_S_QEXP))) return s;
+    if ((s = gc_deposit_q(ctx, x, y, z, m, n, ctx->dsmall + GC_S_QEXP, 0))) return s;
+  }
+  return gc_convert_q(ctx, ctx->dsmall + GC_S_QEXP, rho, nullptr);
+}
+
+// ------------------------------------------------------------------------------
+// gradient (deposit.py:132-174)
+// ------------------------------------------------------------------------------
+__device__ __forceinline__ float grad_comp(const float *__restrict__ phi, size_t c, size_t stride, int idx, int G,
+                                           float inv_dx, float inv_2dx) {
+  if (idx == 0) return -__fmul_rn(__fsub_rn(phi[c + stride], phi[c]), inv_dx);
+  if (idx == G - 1) return -__fmul_rn(__fsub_rn(phi[c], phi[c - stride]), inv_dx);
+  return -__fmul_rn(__fsub_rn(phi[c + stride], phi[c - stride]), inv_2dx);
+}
+
+struct GradCtx {
+  int G;
+  float inv_dx, inv_2dx;
+};
+
+__host__ static GradCtx make_grad(const gc_ctx *ctx) {
+  GradCtx g;
+  g.G = ctx->G;
+  const float dx = (float)ctx->dx;
+  g.inv_dx = 1.0f / dx;
+  g.inv_2dx = 1.0f / (2.0f * dx);
+  return g;
+}
+
+__global__ void __launch_bounds__(256)
+    k_grad(const float *__restrict__ phi, float *__restrict__ ax, float *__restrict__ ay, float *__restrict__ az,
+           GradCtx g) {
+  const int k = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y;
+  const int i = blockIdx.z;
+  if (k >= g.G || j >= g.G) return;
+  const size_t G = g.G;
+  const size_t c = ((size_t)i * G + j) * G + k;
+  ax[c] = grad_comp(phi, c, G * G, i, g.G, g.inv_dx, g.inv_2dx);
+  ay[c] = grad_comp(phi, c, G, j, g.G, g.inv_dx, g.inv_2dx);
+  az[c] = grad_comp(phi, c, 1, k, g.G, g.inv_dx, g.inv_2dx);
+}
+
+extern "C" int gc_potential_to_accel(gc_ctx *ctx, const float *phi, float *ax, float *ay, float *az) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, phi && ax && ay && az, "gc_potential_to_accel: NULL pointer");
+  const GradCtx g = make_grad(ctx);
+  k_grad<<<dim3(gc_blocks(g.G, 32), gc_blocks(g.G, 8), g.G), dim3(32, 8), 0, ctx->stream>>>(phi, ax, ay, az, g);
+  GC_LAUNCH_CHECK(ctx, "grad");
+  return GC_OK;
+}
+
+// ------------------------------------------------------------------------------
+// gather (deposit.py:85-129)
+// ------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+    k_gather(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z, long long n,
+             const float *__restrict__ axg, const float *__restrict__ ayg, const float *__restrict__ azg,
+             float *__restrict__ ax, float *__restrict__ ay, float *__restrict__ az, float dx, int G) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    CellPos c;
+    if (gc_cell_of(x[p], y[p], z[p], dx, G, c)) {
+      const float wx[2] = {__fsub_rn(1.0f, c.fx), c.fx};
+      const float wy[2] = {__fsub_rn(1.0f, c.fy), c.fy};
+      const float wz[2] = {__fsub_rn(1.0f, c.fz), c.fz};
+#pragma unroll
+      for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+        for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+          for (int cz = 0; cz < 2; ++cz) {
+            const int jx = c.ix + cx, jy = c.iy + cy, jz = c.iz + cz;
+            if ((unsigned)jx < (unsigned)G && (unsigned)jy < (unsigned)G && (unsigned)jz < (unsigned)G) {
+              const float w = __fmul_rn(__fmul_rn(wx[cx], wy[cy]), wz[cz]);
+              const size_t idx = ((size_t)jx * G + jy) * G + jz;
+              sx = __fadd_rn(sx, __fmul_rn(w, axg[idx]));
+              sy = __fadd_rn(sy, __fmul_rn(w, ayg[idx]));
+              sz = __fadd_rn(sz, __fmul_rn(w, azg[idx]));
+            }
+          }
+    }
+    ax[p] = sx;
+    ay[p] = sy;
+    az[p] = sz;
+  }
+}
+
+extern "C" int gc_gather_accel(gc_ctx *ctx, const float *x, const float *y, const float *z, int64_t n,
+                               const float *ax_g, const float *ay_g, const float *az_g, float *acc_x, float *acc_y,
+                               float *acc_z) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  if (n == 0) return GC_OK;
+  GC_REQUIRE(ctx, x && y && z && ax_g && ay_g && az_g && acc_x && acc_y && acc_z, "gc_gather_accel: NULL pointer");
+  unsigned nb = gc_blocks(n, 256);
+  if (nb > 152u * 32u) nb = 152u * 32u;
+  k_gather<<<nb, 256, 0, ctx->stream>>>(x, y, z, (long long)n, ax_g, ay_g, az_g, acc_x, acc_y, acc_z,
+                                        (float)ctx->dx, ctx->G);
+  GC_LAUNCH_CHECK(ctx, "gather");
+  return GC_OK;
+}
+
+// ------------------------------------------------------------------------------
+// kick / drift (integrator.py:27-59)
+// ------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_axpy3(float *__restrict__ u, float *__restrict__ v, float *__restrict__ w,
+                                               const float *__restrict__ a, const float *__restrict__ b,
+                                               const float *__restrict__ c, long long n, float dt) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    u[p] = __fadd_rn(u[p], __fmul_rn(a[p], dt));
+    v[p] = __fadd_rn(v[p], __fmul_rn(b[p], dt));
+    w[p] = __fadd_rn(w[p], __fmul_rn(c[p], dt));
+  }
+}
+
+static int axpy3(gc_ctx *ctx, float *u, float *v, float *w, const float *a, const float *b, const float *c,
+                 int64_t n, float dt, const char *what) {
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  if (n == 0) return GC_OK;
+  GC_REQUIRE(ctx, u && v && w && a && b && c, "%s: NULL pointer", what);
+  unsigned nb = gc_blocks(n, 256);
+  if (nb > 152u * 32u) nb = 152u * 32u;
+  k_axpy3<<<nb, 256, 0, ctx->stream>>>(u, v, w, a, b, c, (long long)n, dt);
+  GC_LAUNCH_CHECK(ctx, what);
+  return GC_OK;
+}
+
+extern "C" int gc_kick(gc_ctx *ctx, float *vx, float *vy, float *vz, const float *ax, const float *ay, const float *az,
+                       int64_t n, float dt) {
+  if (!ctx) return GC_ERR_ARG;
+  return axpy3(ctx, vx, vy, vz, ax, ay, az, n, dt, "kick");
+}
+
+extern "C" int gc_drift(gc_ctx *ctx, float *px, float *py, float *pz, const float *vx, const float *vy,
+                        const float *vz, int64_t n, float dt) {
+  if (!ctx) return GC_ERR_ARG;
+  return axpy3(ctx, px, py, pz, vx, vy, vz, n, dt, "drift");
+}
+
+// ------------------------------------------------------------------------------
+// fused: gather of -grad(phi) computed on the fly + KDK kicks + drift
+// ------------------------------------------------------------------------------
+struct FusedCtx {
+  float dx, inv_dx, inv_2dx;
+  int G;
+  float h, dt;
+  int mode;
+  int diag;
+};
+
+// Acceleration at a particle: the CIC gather of the node field g = -grad(phi),
+// each node's g formed exactly as _potential_to_accel does (deposit.py:148-174).
+__device__ __forceinline__ void gather_grad(const float *__restrict__ phi, float x, float y, float z,
+                                            const FusedCtx &f, float &ax, float &ay, float &az) {
+  ax = ay = az = 0.0f;
+  CellPos c;
+  if (!gc_cell_of(x, y, z, f.dx, f.G, c)) return;
+  const int G = f.G;
+  const size_t sG = (size_t)G;
+  const float wx[2] = {__fsub_rn(1.0f, c.fx), c.fx};
+  const float wy[2] = {__fsub_rn(1.0f, c.fy), c.fy};
+  const float wz[2] = {__fsub_rn(1.0f, c.fz), c.fz};
+#pragma unroll
+  for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+      for (int cz = 0; cz < 2; ++cz) {
+        const int jx = c.ix + cx, jy = c.iy + cy, jz = c.iz + cz;
+        if ((unsigned)jx < (unsigned)G && (unsigned)jy < (unsigned)G && (unsigned)jz < (unsigned)G) {
+          const size_t idx = ((size_t)jx * sG + jy) * sG + jz;
+          const float gx = grad_comp(phi, idx, sG * sG, jx, G, f.inv_dx, f.inv_2dx);
+          const float gy = grad_comp(phi, idx, sG, jy, G, f.inv_dx, f.inv_2dx);
+          const float gz = grad_comp(phi, idx, 1, jz, G, f.inv_dx, f.inv_2dx);
+          const float w = __fmul_rn(__fmul_rn(wx[cx], wy[cy]), wz[cz]);
+          ax = __fadd_rn(ax, __fmul_rn(w, gx));
+          ay = __fadd_rn(ay, __fmul_rn(w, gy));
+          az = __fadd_rn(az, __fmul_rn(w, gz));
+        }
+      }
+}
+
+__global__ void __launch_bounds__(256)
+    k_gather_kick_drift(float *__restrict__ x, float *__restrict__ y, float *__restrict__ z, float *__restrict__ vx,
+                        float *__restrict__ vy, float *__restrict__ vz, const float *__restrict__ m, long long n,
+                        const float *__restrict__ phi, FusedCtx f, float *__restrict__ axo, float *__restrict__ ayo,
+                        float *__restrict__ azo, double *__restrict__ parts) {
+  double dv[11];
+#pragma unroll
+  for (int t = 0; t < 11; ++t) dv[t] = 0.0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    float px = x[p], py = y[p], pz = z[p];
+    float ux = vx[p], uy = vy[p], uz = vz[p];
+    float ax, ay, az;
+    gather_grad(phi, px, py, pz, f, ax, ay, az);
+    if (axo) {
+      axo[p] = ax;
+      ayo[p] = ay;
+      azo[p] = az;
+    }
+    if (f.mode != GC_STEP_PRIME) {  // closing half-kick of the previous step (integrator.py:131)
+      ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
+      uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
+      uz = __fadd_rn(uz, __fmul_rn(az, f.h));
+    }
+    if (f.diag) {  // synchronised state (diagnostics_device.py:56-74)
+      const double mm = m[p];
+      const double X = px, Y = py, Z = pz, VX = ux, VY = uy, VZ = uz;
+      dv[0] += mm;
+      dv[1] += 0.5 * mm * (VX * VX + VY * VY + VZ * VZ);
+      dv[2] += mm * VX;
+      dv[3] += mm * VY;
+      dv[4] += mm * VZ;
+      dv[5] += mm * (Y * VZ - Z * VY);
+      dv[6] += mm * (Z * VX - X * VZ);
+      dv[7] += mm * (X * VY - Y * VX);
+      dv[8] += mm * X;
+      dv[9] += mm * Y;
+      dv[10] += mm * Z;
+    }
+    if (f.mode != GC_STEP_CLOSE) {  // opening half-kick + drift (integrator.py:128-129)
+      ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
+      uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
+      uz = __fadd_rn(uz, __fmul_rn(az, f.h));
+      x[p] = __fadd_rn(px, __fmul_rn(ux, f.dt));
+      y[p] = __fadd_rn(py, __fmul_rn(uy, f.dt));
+      z[p] = __fadd_rn(pz, __fmul_rn(uz, f.dt));
+    }
+    vx[p] = ux;
+    vy[p] = uy;
+    vz[p] = uz;
+  }
+  if (f.diag) block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
+}
+
+int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode, int diag, float *axo, float *ayo,
+                         float *azo, int *nparts_out) {
+  FusedCtx f;
+  f.dx = (float)ctx->dx;
+  f.inv_dx = 1.0f / f.dx;
+  f.inv_2dx = 1.0f / (2.0f * f.dx);
+  f.G = ctx->G;
+  f.dt = dt;
+  f.h = 0.5f * dt;
+  f.mode = mode;
+  f.diag = diag;
+  unsigned nb = gc_blocks(p->n, 256);
+  if (nb > 152u * 16u) nb = 152u * 16u;
+  int s = gc_ensure_red(ctx, (size_t)nb * 11);
+  if (s) return s;
+  k_gather_kick_drift<<<nb, 256, 0, ctx->stream>>>(p->x, p->y, p->z, p->vx, p->vy, p->vz, p->m, (long long)p->n,
+                                                   ctx->hi, f, axo, ayo, azo, ctx->red);
+  GC_LAUNCH_CHECK(ctx, "gather_kick_drift");
+  if (nparts_out) *nparts_out = (int)nb;
+  return GC_OK;
+}
+
+// ------------------------------------------------------------------------------
+// diagnostics (diagnostics_device.py)
+// ------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+    k_diag_particles(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
+                     const float *__restrict__ vx, const float *__restrict__ vy, const float *__restrict__ vz,
+                     const float *__restrict__ m, long long n, double *__restrict__ parts) {
+  double dv[11];
+#pragma unroll
+  for (int t = 0; t < 11; ++t) dv[t] = 0.0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const double mm = m[p];
+    const double X = x[p], Y = y[p], Z = z[p], VX = vx[p], VY = vy[p], VZ = vz[p];
+    dv[0] += mm;
+    dv[1] += 0.5 * mm * (VX * VX + VY * VY + VZ * VZ);
+    dv[2] += mm * VX;
+    dv[3] += mm * VY;
+    dv[4] += mm * VZ;
+    dv[5] += mm * (Y * VZ - Z * VY);
+    dv[6] += mm * (Z * VX - X * VZ);
+    dv[7] += mm * (X * VY - Y * VX);
+    dv[8] += mm * X;
+    dv[9] += mm * Y;
+    dv[10] += mm * Z;
+  }
+  block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
+}
+
+extern "C" int gc_diag_particles(gc_ctx *ctx, const float *x, const float *y, const float *z, const float *vx,
+                                 const float *vy, const float *vz, const float *m, int64_t n, double out[11]) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, out, "gc_diag_particles: NULL out");
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  GC_REQUIRE(ctx, n == 0 || (x && y && z && vx && vy && vz && m), "gc_diag_particles: NULL pointer");
+  const int nb = 512;
+  int s = gc_ensure_red(ctx, nb * 11);
+  if (s) return s;
+  k_diag_particles<<<nb, 256, 0, ctx->stream>>>(x, y, z, vx, vy, vz, m, (long long)n, ctx->red);
+  GC_LAUNCH_CHECK(ctx, "diag particles");
+  if ((s = gc_finalize(ctx, ctx->red, nb, 11, ctx->ddiag))) return s;
+  GC_CUDA(ctx, cudaMemcpyAsync(out, ctx->ddiag, 11 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return GC_OK;
+}
+
+__global__ void __launch_bounds__(256) k_dot(const float *__restrict__ a, const float *__restrict__ b, size_t n,
+                                             double *__restrict__ parts) {
+  double acc[1] = {0.0};
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    acc[0] += (double)a[t] * (double)b[t];
+  block_partials<1>(acc, parts + blockIdx.x);
+}
+
+int gc_dot_async(gc_ctx *ctx, const float *a, const float *b, size_t n, double *dst) {
+  const int nb = 1024;
+  int s = gc_ensure_red(ctx, nb);
+  if (s) return s;
+  k_dot<<<nb, 256, 0, ctx->stream>>>(a, b, n, ctx->red);
+  GC_LAUNCH_CHECK(ctx, "dot");
+  return gc_finalize(ctx, ctx->red, nb, 1, dst);
+}
+
+extern "C" int gc_diag_grid_pe(gc_ctx *ctx, const float *rho, const float *phi, double *out) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, rho && phi && out, "gc_diag_grid_pe: NULL pointer");
+  const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
+  int s = gc_dot_async(ctx, rho, phi, g3, ctx->ddiag + 12);
+  if (s) return s;
+  GC_CUDA(ctx, cudaMemcpyAsync(out, ctx->ddiag + 12, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return GC_OK;
+}
+
+__global__ void __launch_bounds__(256)
+    k_radial_hist(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
+                  const float *__restrict__ m, long long n, double cx, double cy, double cz, double inv_binw, int nbins,
+                  double *__restrict__ hist) {
+  extern __shared__ double sh[];
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) sh[b] = 0.0;
+  __syncthreads();
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const double rx = (double)x[p] - cx, ry = (double)y[p] - cy, rz = (double)z[p] - cz;
+    const double r = sqrt(rx * rx + ry * ry + rz * rz);
+    const double fb = r * inv_binw;
+    int b = fb >= (double)nbins ? nbins - 1 : (int)fb;
+    if (b < 0) b = 0;
+    atomicAdd(&sh[b], (double)m[p]);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+    if (sh[b] != 0.0) atomicAdd(&hist[b], sh[b]);
+}
+
+extern "C" int gc_radial_histogram(gc_ctx *ctx, const float *x, const float *y, const float *z, const float *m,
+                                   int64_t n, double cx, double cy, double cz, double inv_binw, int nbins,
+                                   double *hist) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, hist, "gc_radial_histogram: NULL hist");
+  GC_REQUIRE(ctx, nbins >= 1 && nbins <= 6144, "nbins must be in [1, 6144]");
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  GC_CUDA(ctx, cudaMemsetAsync(hist, 0, nbins * sizeof(double), ctx->stream));
+  if (n == 0) return GC_OK;
+  GC_REQUIRE(ctx, x && y && z && m, "gc_radial_histogram: NULL pointer");
+  const size_t smem = nbins * sizeof(double);
+  if (smem > 48 * 1024)
+    GC_CUDA(ctx, cudaFuncSetAttribute(k_radial_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  unsigned nb = gc_blocks(n, 256);
+  if (nb > 152u * 4u) nb = 152u * 4u;
+  k_radial_hist<<<nb, 256, smem, ctx->stream>>>(x, y, z, m, (long long)n, cx, cy, cz, inv_binw, nbins, hist);
+  GC_LAUNCH_CHECK(ctx, "radial hist");
+  return GC_OK;
+}

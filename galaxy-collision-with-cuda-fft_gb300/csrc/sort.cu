@@ -1,0 +1,312 @@
+// Cell keys and a stable LSD radix sort of (key, index) pairs.
+//
+// The key is the reference's cell index ix = floor(x/dx) (deposit.py:62-67),
+// linearised over the (G+1)^3 cells that can receive mass (-1 <= ix <= G-1).
+// Each radix pass is reduce-then-scan: per-tile digit histograms, one exclusive
+// scan of the digit-major histogram, then a stable scatter in which every warp
+// ranks its items round by round with match.any, so equal keys keep their input
+// order and the permutation is unique.
+#include "common.cuh"
+
+#define RS_BITS 8
+#define RS_RADIX 256
+#define RS_THREADS 256
+#define RS_WARPS (RS_THREADS / 32)
+#define RS_IPT 16                          // items per thread
+#define RS_TILE (RS_THREADS * RS_IPT)      // 4096 items per tile
+
+__global__ void __launch_bounds__(256)
+    k_cell_keys(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z, long long n,
+                float dx, int G, uint32_t *__restrict__ keys, uint32_t *__restrict__ iota) {
+  const uint32_t sentinel = (uint32_t)(G + 1) * (uint32_t)(G + 1) * (uint32_t)(G + 1);
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    CellPos c;
+    uint32_t key = sentinel;
+    if (gc_cell_of(x[p], y[p], z[p], dx, G, c))
+      key = ((uint32_t)(c.ix + 1) * (uint32_t)(G + 1) + (uint32_t)(c.iy + 1)) * (uint32_t)(G + 1) + (uint32_t)(c.iz + 1);
+    keys[p] = key;
+    if (iota) iota[p] = (uint32_t)p;
+  }
+}
+
+// Digit histogram of each tile: hist[d * ntiles + tile].
+__global__ void __launch_bounds__(RS_THREADS)
+    k_rs_hist(const uint32_t *__restrict__ keys, long long n, int shift, unsigned *__restrict__ hist, int ntiles) {
+  __shared__ unsigned cnt[RS_RADIX];
+  for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) cnt[d] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * RS_TILE;
+  for (int t = threadIdx.x; t < RS_TILE; t += RS_THREADS) {
+    const long long p = base + t;
+    if (p < n) atomicAdd(&cnt[(keys[p] >> shift) & (RS_RADIX - 1)], 1u);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) hist[(size_t)d * ntiles + blockIdx.x] = cnt[d];
+}
+
+// Exclusive scan of an unsigned array in three phases (tile sums, scan of sums, apply).
+#define SC_THREADS 1024
+#define SC_TILE 4096
+
+__device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned &total) {
+  __shared__ unsigned ws[SC_THREADS / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned w = lane < (int)(blockDim.x / 32) ? ws[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    ws[lane] = w;
+  }
+  __syncthreads();
+  const unsigned prefix = (wid > 0 ? ws[wid - 1] : 0u) + x - v;
+  total = ws[blockDim.x / 32 - 1];
+  __syncthreads();
+  return prefix;
+}
+
+__global__ void __launch_bounds__(SC_THREADS) k_scan_tile_sums(const unsigned *__restrict__ a, long long n,
+                                                               unsigned *__restrict__ sums) {
+  const long long base = (long long)blockIdx.x * SC_TILE;
+  unsigned s = 0;
+  for (int t = threadIdx.x; t < SC_TILE; t += SC_THREADS) {
+    const long long p = base + t;
+    if (p < n) s += a[p];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  __shared__ unsigned ws[SC_THREADS / 32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    unsigned w = ws[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+    if (threadIdx.x == 0) sums[blockIdx.x] = w;
+  }
+}
+
+// Single block: in-place exclusive scan of sums[0..m).
+__global__ void __launch_bounds__(SC_THREADS) k_scan_sums(unsigned *__restrict__ sums, int m) {
+  unsigned carry = 0;
+  for (int base = 0; base < m; base += SC_THREADS) {
+    const int p = base + threadIdx.x;
+    const unsigned v = p < m ? sums[p] : 0u;
+    unsigned total;
+    const unsigned ex = block_excl_scan(v, total);
+    if (p < m) sums[p] = carry + ex;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(SC_THREADS) k_scan_apply(unsigned *__restrict__ a, long long n,
+                                                           const unsigned *__restrict__ sums) {
+  const long long base = (long long)blockIdx.x * SC_TILE;
+  unsigned carry = sums[blockIdx.x];
+  for (int off = 0; off < SC_TILE; off += SC_THREADS) {
+    const long long p = base + off + threadIdx.x;
+    const unsigned v = p < n ? a[p] : 0u;
+    unsigned total;
+    const unsigned ex = block_excl_scan(v, total);
+    if (p < n) a[p] = carry + ex;
+    carry += total;
+  }
+}
+
+// Stable scatter. Warp w of a tile owns items [w*32*IPT, (w+1)*32*IPT) of the
+// tile; round r handles item r*32+lane of that range, so (round, lane) order is
+// input order.
+__global__ void __launch_bounds__(RS_THREADS)
+    k_rs_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, long long n, int shift,
+                 const unsigned *__restrict__ hist, int ntiles, uint32_t *__restrict__ kout,
+                 uint32_t *__restrict__ vout) {
+  __shared__ unsigned whist[RS_WARPS][RS_RADIX];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int t = threadIdx.x; t < RS_WARPS * RS_RADIX; t += RS_THREADS) (&whist[0][0])[t] = 0;
+  __syncthreads();
+  const long long seg = (long long)blockIdx.x * RS_TILE + (long long)w * 32 * RS_IPT;
+  uint32_t k[RS_IPT], v[RS_IPT];
+  unsigned rank[RS_IPT];
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int r = 0; r < RS_IPT; ++r) {
+    const long long p = seg + r * 32 + lane;
+    const bool ok = p < n;
+    k[r] = ok ? kin[p] : 0u;
+    v[r] = ok ? vin[p] : 0u;
+    const unsigned d = ok ? ((k[r] >> shift) & (RS_RADIX - 1)) : (unsigned)RS_RADIX + lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    unsigned old = 0;
+    if (ok) old = whist[w][d];
+    __syncwarp();
+    if (ok && (peers & lt) == 0) whist[w][d] = old + __popc(peers);
+    __syncwarp();
+    rank[r] = old + __popc(peers & lt);
+  }
+  __syncthreads();
+  // exclusive scan over warps per digit, plus the tile's global offset
+  for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) {
+    unsigned run = hist[(size_t)d * ntiles + blockIdx.x];
+    for (int ww = 0; ww < RS_WARPS; ++ww) {
+      const unsigned c = whist[ww][d];
+      whist[ww][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < RS_IPT; ++r) {
+    const long long p = seg + r * 32 + lane;
+    if (p < n) {
+      const unsigned d = (k[r] >> shift) & (RS_RADIX - 1);
+      const unsigned dst = whist[w][d] + rank[r];
+      kout[dst] = k[r];
+      vout[dst] = v[r];
+    }
+  }
+}
+
+static int exclusive_scan(gc_ctx *ctx, unsigned *a, long long n) {
+  const long long nt = (n + SC_TILE - 1) / SC_TILE;
+  unsigned *sums = ctx->hist_aux;
+  k_scan_tile_sums<<<(unsigned)nt, SC_THREADS, 0, ctx->stream>>>(a, n, sums);
+  k_scan_sums<<<1, SC_THREADS, 0, ctx->stream>>>(sums, (int)nt);
+  k_scan_apply<<<(unsigned)nt, SC_THREADS, 0, ctx->stream>>>(a, n, sums);
+  GC_LAUNCH_CHECK(ctx, "scan");
+  return GC_OK;
+}
+
+int gc_radix_sort_pairs(gc_ctx *ctx, const uint32_t *keys_in, const uint32_t *vals_in, int64_t n, int bits,
+                        uint32_t **keys_out, uint32_t **vals_out) {
+  int s = gc_ensure_particle_scratch(ctx, (size_t)n);
+  if (s) return s;
+  const int ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
+  const size_t hn = (size_t)ntiles * RS_RADIX;
+  if (ctx->hist_cap < hn) {
+    GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->hist);
+    cudaFree(ctx->hist_aux);
+    ctx->hist = ctx->hist_aux = nullptr;
+    ctx->hist_cap = 0;
+    GC_CUDA(ctx, cudaMalloc(&ctx->hist, hn * sizeof(unsigned)));
+    GC_CUDA(ctx, cudaMalloc(&ctx->hist_aux, ((hn + SC_TILE - 1) / SC_TILE + 32) * sizeof(unsigned)));
+    ctx->hist_cap = hn;
+  }
+  const uint32_t *kin = keys_in, *vin = vals_in;
+  // ping-pong between (keys, vals) and (keys2, vals2); never write into the caller's input
+  uint32_t *ka = ctx->keys, *va = ctx->vals, *kb = ctx->keys2, *vb = ctx->vals2;
+  int passes = (bits + RS_BITS - 1) / RS_BITS;
+  if (passes < 1) passes = 1;
+  for (int pss = 0; pss < passes; ++pss) {
+    const int shift = pss * RS_BITS;
+    uint32_t *ko = (pss & 1) ? kb : ka;
+    uint32_t *vo = (pss & 1) ? vb : va;
+    if (kin == ko) {  // input aliases this pass's output: use the other buffer
+      ko = (ko == ka) ? kb : ka;
+      vo = (vo == va) ? vb : va;
+    }
+    k_rs_hist<<<ntiles, RS_THREADS, 0, ctx->stream>>>(kin, (long long)n, shift, ctx->hist, ntiles);
+    GC_LAUNCH_CHECK(ctx, "radix hist");
+    if ((s = exclusive_scan(ctx, ctx->hist, (long long)hn))) return s;
+    k_rs_scatter<<<ntiles, RS_THREADS, 0, ctx->stream>>>(kin, vin, (long long)n, shift, ctx->hist, ntiles, ko, vo);
+    GC_LAUNCH_CHECK(ctx, "radix scatter");
+    kin = ko;
+    vin = vo;
+  }
+  *keys_out = (uint32_t *)kin;
+  *vals_out = (uint32_t *)vin;
+  return GC_OK;
+}
+
+static int key_bits(int G) {
+  const unsigned long long maxkey = (unsigned long long)(G + 1) * (G + 1) * (G + 1);
+  int b = 0;
+  while ((1ULL << b) <= maxkey) ++b;
+  return b;
+}
+
+extern "C" int gc_cell_keys(gc_ctx *ctx, const float *x, const float *y, const float *z, int64_t n, uint32_t *keys) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  if (n == 0) return GC_OK;
+  GC_REQUIRE(ctx, x && y && z && keys, "gc_cell_keys: NULL pointer");
+  GC_REQUIRE(ctx, (unsigned long long)(ctx->G + 1) * (ctx->G + 1) * (ctx->G + 1) < 0xffffffffULL,
+             "grid too large for 32-bit cell keys");
+  unsigned nb = gc_blocks(n, 256);
+  if (nb > 152u * 32u) nb = 152u * 32u;
+  k_cell_keys<<<nb, 256, 0, ctx->stream>>>(x, y, z, (long long)n, (float)ctx->dx, ctx->G, keys, nullptr);
+  GC_LAUNCH_CHECK(ctx, "cell keys");
+  return GC_OK;
+}
+
+__global__ void k_iota(uint32_t *__restrict__ a, long long n) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
+    a[p] = (uint32_t)p;
+}
+
+extern "C" int gc_sort_keys(gc_ctx *ctx, const uint32_t *keys, int64_t n, uint32_t *sorted_keys, uint32_t *perm) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  if (n == 0) return GC_OK;
+  GC_REQUIRE(ctx, keys && perm, "gc_sort_keys: NULL pointer");
+  int s = gc_ensure_particle_scratch(ctx, (size_t)n);
+  if (s) return s;
+  // values start as the identity in keys2's partner buffer
+  uint32_t *iota = ctx->vals2;
+  k_iota<<<gc_blocks(n, 256) > 4096 ? 4096 : gc_blocks(n, 256), 256, 0, ctx->stream>>>(iota, (long long)n);
+  GC_LAUNCH_CHECK(ctx, "iota");
+  uint32_t *ko, *vo;
+  // full 32-bit keys: any caller key is sorted stably
+  if ((s = gc_radix_sort_pairs(ctx, keys, iota, n, 32, &ko, &vo))) return s;
+  if (sorted_keys) GC_CUDA(ctx, cudaMemcpyAsync(sorted_keys, ko, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->stream));
+  GC_CUDA(ctx, cudaMemcpyAsync(perm, vo, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->stream));
+  return GC_OK;
+}
+
+template <typename T>
+__global__ void k_gather_perm(const T *__restrict__ in, T *__restrict__ out, const uint32_t *__restrict__ perm,
+                              long long n) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
+    out[p] = in[perm[p]];
+}
+
+extern "C" int gc_pm_sort(gc_ctx *ctx, const gc_particles *in, const gc_particles *out) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, in && out, "gc_pm_sort: NULL particle set");
+  const int64_t n = in->n;
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  GC_REQUIRE(ctx, out->n == n, "gc_pm_sort: in and out sizes differ");
+  if (n == 0) return GC_OK;
+  GC_REQUIRE(ctx, in->x && in->y && in->z, "gc_pm_sort: positions required");
+  int s = gc_ensure_particle_scratch(ctx, (size_t)n);
+  if (s) return s;
+  unsigned nb = gc_blocks(n, 256);
+  if (nb > 152u * 32u) nb = 152u * 32u;
+  k_cell_keys<<<nb, 256, 0, ctx->stream>>>(in->x, in->y, in->z, (long long)n, (float)ctx->dx, ctx->G, ctx->keys2,
+                                           ctx->vals2);
+  GC_LAUNCH_CHECK(ctx, "cell keys");
+  uint32_t *ko, *vo;
+  if ((s = gc_radix_sort_pairs(ctx, ctx->keys2, ctx->vals2, n, key_bits(ctx->G), &ko, &vo))) return s;
+  const float *fin[7] = {in->x, in->y, in->z, in->vx, in->vy, in->vz, in->m};
+  float *fout[7] = {out->x, out->y, out->z, out->vx, out->vy, out->vz, out->m};
+  for (int a = 0; a < 7; ++a) {
+    if (!fin[a]) continue;
+    GC_REQUIRE(ctx, fout[a] && fout[a] != fin[a], "gc_pm_sort: output array %d missing or aliases its input", a);
+    k_gather_perm<float><<<nb, 256, 0, ctx->stream>>>(fin[a], fout[a], vo, (long long)n);
+  }
+  const int32_t *iin[2] = {in->gid, in->pid};
+  int32_t *iout[2] = {out->gid, out->pid};
+  for (int a = 0; a < 2; ++a) {
+    if (!iin[a]) continue;
+    GC_REQUIRE(ctx, iout[a] && iout[a] != iin[a], "gc_pm_sort: id array %d missing or aliases its input", a);
+    k_gather_perm<int32_t><<<nb, 256, 0, ctx->stream>>>(iin[a], iout[a], vo, (long long)n);
+  }
+  GC_LAUNCH_CHECK(ctx, "permute");
+  return GC_OK;
+}

@@ -1,0 +1,115 @@
+"""Open-boundary multigrid Poisson solver on the GPU.
+
+Drop-in for ``MultigridPoissonSolver`` (src/galaxy_collision/solver/multigrid.py:298-494):
+same constructor keywords, the same adaptive stopping rule (stop once
+||rhs - L phi||_2 < tol * ||rhs||_2, never before ``min_cycles``, at most
+``n_cycles``), ``last_cycles`` and ``residual_norm()``. The discrete problem is
+the reference's: 7-point Laplacian on the finest grid, Dirichlet faces from the
+monopole + quadrupole of rho about its centre of mass. What differs is how it
+is solved (see ``csrc/multigrid.cu``): Shortley-Weller coarse levels that
+converge at ~0.1 per V-cycle instead of the reference's ~0.6, a double-float
+finest level so the residual can go below the FP32 floor, device-side moments
+and norms, and an FP64 coarsest solve.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+from galaxy_collision_gb300 import _native, units
+from galaxy_collision_gb300.data import as_tensor
+from galaxy_collision_gb300.solver.base import PoissonSolver
+
+
+class MultigridPoissonSolver(PoissonSolver):
+    """Open-BC Poisson solve by red-black Gauss-Seidel multigrid V-cycles (sm_103a)."""
+
+    def __init__(
+        self,
+        grid_size: int,
+        dx: float = 1.0,
+        grav_constant: float | None = None,
+        n_cycles: int = 20,
+        pre_sweeps: int = 2,
+        post_sweeps: int = 2,
+        coarse_sweeps: int = 40,
+        tol: float = 1e-3,
+        min_cycles: int = 1,
+    ):
+        self.grid_size = int(grid_size)
+        self.dx = float(dx)
+        self.G = units.G if grav_constant is None else float(grav_constant)
+        self.n_cycles = int(n_cycles)
+        self.nu1 = int(pre_sweeps)
+        self.nu2 = int(post_sweeps)
+        self.coarse_sweeps = int(coarse_sweeps)
+        self.tol = float(tol)
+        self.min_cycles = max(1, int(min_cycles))
+        self.last_cycles = 0
+        self.last_stats = None
+        self._ctx = _native.Context(self.grid_size, self.dx, self.G)
+        self.sizes = [n for (n, _J, _p) in self._ctx.levels()]
+
+    def _params(self) -> _native.MGParams:
+        p = _native.MGParams()
+        p.pre_sweeps = self.nu1
+        p.post_sweeps = self.nu2
+        p.coarse_sweeps = self.coarse_sweeps
+        p.max_cycles = self.n_cycles
+        p.min_cycles = self.min_cycles
+        p.tol = self.tol
+        return p
+
+    def solve(self, rho, phi, warm_start: bool = False) -> None:
+        G = self.grid_size
+        r = as_tensor(rho, shape=(G, G, G), name="rho")
+        f = as_tensor(phi, shape=(G, G, G), name="phi")
+        p = self._params()
+        st = _native.MGStats()
+        self._ctx.call("gc_mg_solve", r.data_ptr(), f.data_ptr(), int(bool(warm_start)), C.byref(p), C.byref(st),
+                       what="MultigridPoissonSolver.solve")
+        self.last_cycles = int(st.cycles)
+        self.last_stats = {
+            "cycles": int(st.cycles),
+            "converged": bool(st.converged),
+            "rhs_norm": float(st.rhs_norm),
+            "res_norm": float(st.res_norm),
+            "rel_residual": float(st.res_norm / st.rhs_norm) if st.rhs_norm > 0 else 0.0,
+        }
+
+    def residual_norm(self, phi=None) -> float:
+        """L2 norm (FP64) of the finest residual of the last solve.
+
+        With ``phi`` given, the residual of that f32 potential; otherwise that of
+        the solver's internal double-float iterate.
+        """
+        out = C.c_double()
+        ptr = None
+        if phi is not None:
+            G = self.grid_size
+            ptr = as_tensor(phi, shape=(G, G, G), name="phi").data_ptr()
+        self._ctx.call("gc_mg_residual_norm", ptr, C.byref(out), what="residual_norm")
+        return float(out.value)
+
+    def moments(self, rho):
+        """Raw FP64 moments [M, Smx, Smy, Smz, Smx2, Smy2, Smz2, Smxy, Smxz, Smyz] of rho."""
+        G = self.grid_size
+        r = as_tensor(rho, shape=(G, G, G), name="rho")
+        out = (C.c_double * 10)()
+        self._ctx.call("gc_moments", r.data_ptr(), out, what="moments")
+        return list(out)
+
+    def _moments_device(self, rho):
+        """(M, CM, S_ab) from the device moments, as multigrid.py:364-389 returns them."""
+        s = self.moments(rho)
+        total = s[0]
+        if total <= 0.0:
+            return 0.0, (0.0, 0.0, 0.0), (0.0,) * 6
+        cx, cy, cz = s[1] / total, s[2] / total, s[3] / total
+        return total, (cx, cy, cz), (
+            s[4] - total * cx * cx, s[5] - total * cy * cy, s[6] - total * cz * cz,
+            s[7] - total * cx * cy, s[8] - total * cx * cz, s[9] - total * cy * cz,
+        )
+
+
+__all__ = ["MultigridPoissonSolver"]

@@ -1,0 +1,231 @@
+/*
+ * gcpm.h — C ABI of the GB300 particle-mesh (PM) force chain.
+ *
+ * This is the drop-in boundary for the reference's PM hot path
+ * (pouyalj/Galaxy-Collision-with-CUDA-FFT, package src/galaxy_collision):
+ * CIC deposit -> open-boundary multigrid Poisson solve -> -grad(phi) -> CIC
+ * gather -> KDK kick/drift. Every entry point takes plain device pointers,
+ * element counts and an opaque context; no torch or CUDA types appear in the
+ * signatures (streams are passed as `void*` holding a cudaStream_t).
+ *
+ * Conventions shared with the reference (src/galaxy_collision/deposit.py:16-37):
+ *   - node-centred grid: node (i,j,k) sits at physical (i,j,k)*dx, the G nodes
+ *     per axis span [0, (G-1)*dx];
+ *   - grids are C-order [i][j][k] with k fastest (Taichi field to_numpy order);
+ *   - particles are SoA f32 arrays (src/galaxy_collision/data.py:84-113);
+ *   - out-of-box CIC weight is dropped, never wrapped (deposit.py:33-37).
+ *
+ * Error convention: every call returns GC_OK (0) or a negative status; the
+ * message of the last failure is returned by gc_last_error(ctx) (ctx may be
+ * NULL for failures of gc_ctx_create). Calls are stream-ordered and
+ * asynchronous unless their documentation says they return host scalars.
+ * No entry point allocates caller-visible memory or frees caller memory.
+ */
+#ifndef GCPM_H
+#define GCPM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GC_ABI_VERSION 1
+
+enum gc_status_code {
+  GC_OK = 0,
+  GC_ERR_ARG = -1,           /* bad argument: maps to ValueError, as the reference raises */
+  GC_ERR_CUDA = -2,          /* a CUDA runtime call failed */
+  GC_ERR_TIMEOUT = -3,       /* a bounded device wait gave up */
+  GC_ERR_NOT_CONVERGED = -4, /* reserved: the solvers report convergence in their stats */
+  GC_ERR_NONFINITE = -5,     /* non-finite particle or grid values were seen */
+  GC_ERR_STATE = -6          /* call made in the wrong state (e.g. step before prime) */
+};
+
+/* Device status bits, OR-ed by kernels into a per-context word (gc_status). */
+#define GC_FLAG_NONFINITE_POS 0x1u  /* a particle position was NaN/Inf: it deposited nothing */
+#define GC_FLAG_NONFINITE_RHO 0x2u  /* the density handed to the solver had NaN/Inf */
+
+typedef struct gc_ctx gc_ctx;
+
+/* Multigrid controls. Defaults follow MultigridPoissonSolver.__init__
+ * (src/galaxy_collision/solver/multigrid.py:301-312). */
+typedef struct gc_mg_params {
+  int pre_sweeps;     /* nu1 red-black sweeps before restriction (reference: 2) */
+  int post_sweeps;    /* nu2 sweeps after prolongation (reference: 2) */
+  int coarse_sweeps;  /* FP64 Gauss-Seidel sweeps on the coarsest level (reference: 40) */
+  int max_cycles;     /* V-cycle cap (reference n_cycles: 20) */
+  int min_cycles;     /* never fewer V-cycles than this (reference: 1) */
+  int reserved;
+  double tol;         /* stop when ||r||_2 < tol * ||4 pi G rho||_2 (reference: 1e-3) */
+} gc_mg_params;
+
+typedef struct gc_mg_stats {
+  int cycles;         /* V-cycles run by the last solve (reference last_cycles) */
+  int converged;      /* 1 if ||r|| < tol*||rhs|| was reached within max_cycles */
+  double rhs_norm;    /* ||4 pi G rho||_2 over all G^3 nodes */
+  double res_norm;    /* ||rhs - L phi||_2 over the interior after the last cycle */
+} gc_mg_stats;
+
+/* Particle set for the fused engine: SoA device arrays of length n. */
+typedef struct gc_particles {
+  float *x, *y, *z;      /* positions, grid-origin coordinates (node i at i*dx) */
+  float *vx, *vy, *vz;   /* velocities */
+  float *m;              /* masses */
+  int32_t *gid;          /* galaxy id (carried through sorts; may be NULL) */
+  int32_t *pid;          /* original particle index (carried through sorts; may be NULL) */
+  int64_t n;
+} gc_particles;
+
+/* Modes of gc_pm_step (the staggered KDK state machine of the fused engine). */
+enum gc_step_mode {
+  GC_STEP_PRIME = 0, /* a_0 = F(x_0); v += a h; x += v dt            (state -> open)   */
+  GC_STEP_ADVANCE = 1,/* a_n = F(x_n); v += a h; v += a h; x += v dt (open -> open)    */
+  GC_STEP_CLOSE = 2  /* a_n = F(x_n); v += a h                      (open -> synced)  */
+};
+
+typedef struct gc_step_params {
+  float dt;          /* full step; the kicks use dt/2 as in kdk_step */
+  int mode;          /* gc_step_mode */
+  int warm_start;    /* reuse the previous potential (hi+lo) as the initial guess */
+  int diagnostics;   /* 1: accumulate FP64 particle diagnostics at the synchronised time */
+  gc_mg_params mg;
+  int fixed_point_bits; /* deposit quantum = 2^-bits of the total deposited mass (40..56) */
+  int reserved;
+} gc_step_params;
+
+typedef struct gc_step_stats {
+  gc_mg_stats mg;
+  double diag[11];   /* M, KE, Px,Py,Pz, Lx,Ly,Lz, Sum m x, Sum m y, Sum m z (diagnostics_device.py:32-38) */
+  double grid_pe_raw;/* Sum rho*phi over the grid (diagnostics_device.py:78-88) */
+} gc_step_stats;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Create a context for a G^3 grid of node spacing dx and gravitational
+ * constant grav. Allocates the multigrid hierarchy, the int64 mass grid and
+ * reduction scratch on the current device. Replaces the per-solver state of
+ * MultigridPoissonSolver.__init__ (solver/multigrid.py:301-360) and the grid
+ * scratch of GridState (data.py:116-138). */
+int gc_ctx_create(gc_ctx **out, int grid_size, double dx, double grav_constant);
+int gc_ctx_destroy(gc_ctx *ctx);
+/* Message of the last failure on ctx (or of the last gc_ctx_create when ctx is NULL). */
+const char *gc_last_error(const gc_ctx *ctx);
+/* Stream (a cudaStream_t passed as void*) used by all later calls on ctx. NULL = legacy default. */
+int gc_set_stream(gc_ctx *ctx, void *stream);
+/* Read (and optionally clear) the device status word; synchronises the stream. */
+int gc_status(gc_ctx *ctx, uint32_t *flags_out, int clear);
+int gc_abi_version(void);
+int gc_num_levels(const gc_ctx *ctx);
+/* Level geometry of the multigrid hierarchy: nodes per axis and last interior index. */
+int gc_level_info(const gc_ctx *ctx, int level, int *n_nodes, int *last_interior, double *far_face);
+
+/* ---- particle <-> grid operators (reference deposit.py / integrator.py) -- */
+
+/* Zero rho, then CIC-deposit m*w/dx^3 onto the G^3 nodes, dropping out-of-box
+ * weight. Accumulates in int64 fixed point (quantum 2^-fixed_point_bits of the
+ * total), so rho is bit-identical run to run whatever the particle order.
+ * Replaces _deposit_cic / deposit_density (deposit.py:47-82, 177-182). */
+int gc_deposit_cic(gc_ctx *ctx, const float *x, const float *y, const float *z, const float *m,
+                   int64_t n, int fixed_point_bits, float *rho);
+
+/* g = -grad(phi) at every node: central differences inside, one-sided on faces.
+ * Replaces _potential_to_accel / potential_to_accel (deposit.py:132-174, 204-207). */
+int gc_potential_to_accel(gc_ctx *ctx, const float *phi, float *ax, float *ay, float *az);
+
+/* Trilinear gather of the node acceleration field to particles; out-of-box
+ * nodes contribute zero. Replaces _gather_accel / gather_acceleration
+ * (deposit.py:85-129, 185-201). */
+int gc_gather_accel(gc_ctx *ctx, const float *x, const float *y, const float *z, int64_t n,
+                    const float *ax_g, const float *ay_g, const float *az_g,
+                    float *acc_x, float *acc_y, float *acc_z);
+
+/* v += a*dt. Replaces integrator.kick (integrator.py:27-41). */
+int gc_kick(gc_ctx *ctx, float *vx, float *vy, float *vz, const float *ax, const float *ay,
+            const float *az, int64_t n, float dt);
+/* x += v*dt. Replaces integrator.drift (integrator.py:44-59). */
+int gc_drift(gc_ctx *ctx, float *px, float *py, float *pz, const float *vx, const float *vy,
+             const float *vz, int64_t n, float dt);
+
+/* Cell key of each particle from the reference's cell index ix=floor(x/dx)
+ * (deposit.py:62-67, f32 IEEE division and floor):
+ *   key = ((ix+1)*(G+1) + (iy+1))*(G+1) + (iz+1)   for -1 <= ix,iy,iz <= G-1,
+ *   key = (G+1)^3 (sentinel) for particles that deposit nothing or are non-finite. */
+int gc_cell_keys(gc_ctx *ctx, const float *x, const float *y, const float *z, int64_t n,
+                 uint32_t *keys);
+/* Stable LSD radix sort of the keys: sorted_keys (may be NULL) and the
+ * permutation perm (sorted position -> original index). Equal keys keep their
+ * original order, so the permutation is unique. No reference counterpart: it
+ * is the cell sort the reference benchmarked as a deposit variant
+ * (docs/performance.md:74-82), built here as the locality step of the deposit. */
+int gc_sort_keys(gc_ctx *ctx, const uint32_t *keys, int64_t n, uint32_t *sorted_keys,
+                 uint32_t *perm);
+
+/* ---- Poisson solve (reference solver/multigrid.py) ---------------------- */
+
+/* Default parameters of MultigridPoissonSolver (solver/multigrid.py:301-312). */
+void gc_mg_default_params(gc_mg_params *p);
+
+/* Solve laplacian(phi) = 4 pi G rho with the reference's open boundary:
+ * Dirichlet faces from the monopole+quadrupole of rho about its centre of mass
+ * (evaluated in FP64), then adaptive V-cycles until ||r|| < tol*||rhs||.
+ * Reads rho, overwrites phi; with warm_start the current phi is the initial
+ * guess. The finest level relaxes a double-float (hi+lo FP32 pair) potential so
+ * the residual can go below the FP32 floor; coarse levels relax FP32
+ * corrections; the coarsest level is solved in FP64. Synchronises the stream to
+ * read the residual norms. Replaces MultigridPoissonSolver.solve
+ * (solver/multigrid.py:455-487). stats may be NULL. */
+int gc_mg_solve(gc_ctx *ctx, const float *rho, float *phi, int warm_start,
+                const gc_mg_params *params, gc_mg_stats *stats);
+
+/* FP64 L2 norm of the finest residual rhs - L(phi) of the last solve, phi taken
+ * as the double-float pair (or as phi_f32 when it is non-NULL). Returns the norm
+ * in the reference's units. Replaces MultigridPoissonSolver.residual_norm
+ * (solver/multigrid.py:489-494). Synchronises. */
+int gc_mg_residual_norm(gc_ctx *ctx, const float *phi_f32, double *out);
+
+/* The ten raw mass moments [M, Smx, Smy, Smz, Smx2, Smy2, Smz2, Smxy, Smxz, Smyz]
+ * of rho (m = rho dx^3 at node (i,j,k)dx), FP64. Replaces _accumulate_moments
+ * (solver/multigrid.py:133-178). Synchronises. */
+int gc_moments(gc_ctx *ctx, const float *rho, double out[10]);
+
+/* ---- diagnostics (reference diagnostics_device.py) ---------------------- */
+
+/* FP64 sums [M, KE, P(3), L about the origin (3), Sum m r (3)].
+ * Replaces _reduce_particle_scalars (diagnostics_device.py:42-74). Synchronises. */
+int gc_diag_particles(gc_ctx *ctx, const float *x, const float *y, const float *z,
+                      const float *vx, const float *vy, const float *vz, const float *m,
+                      int64_t n, double out[11]);
+/* Raw Sum rho*phi in FP64. Replaces _reduce_grid_pe (diagnostics_device.py:78-88). Synchronises. */
+int gc_diag_grid_pe(gc_ctx *ctx, const float *rho, const float *phi, double *out);
+/* Mass-weighted histogram of radius about (cx,cy,cz), last bin catch-all, FP64
+ * (written to a device array of nbins doubles). Replaces _radial_mass_histogram
+ * (diagnostics_device.py:153-185). */
+int gc_radial_histogram(gc_ctx *ctx, const float *x, const float *y, const float *z,
+                        const float *m, int64_t n, double cx, double cy, double cz,
+                        double inv_binw, int nbins, double *hist);
+
+/* ---- fused engine (callers: bench.py:145-152, sim.py:320-325) ------------ */
+
+/* Stable-sort the particles by cell key and write the permuted set to out
+ * (every non-NULL array of in is permuted into the matching array of out). */
+int gc_pm_sort(gc_ctx *ctx, const gc_particles *in, const gc_particles *out);
+
+/* One force evaluation of the fused chain plus the kicks/drift of the mode:
+ * int64 fixed-point deposit, moments and 4 pi G h^2 rho in one pass, FP64
+ * boundary faces, adaptive multigrid to params->mg.tol, then one particle pass
+ * that gathers -grad(phi) on the fly and applies the kicks and drift.
+ * KDK arithmetic is that of kdk_step (integrator.py:100-131). Synchronises to
+ * fill stats (may be NULL). */
+int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp, gc_step_stats *st);
+
+/* Device pointer of the current finest-level potential (f32 hi part, G^3). */
+const float *gc_pm_potential(const gc_ctx *ctx);
+/* Stream-ordered copy of the current finest-level potential into phi (G^3 f32). */
+int gc_pm_copy_potential(gc_ctx *ctx, float *phi);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GCPM_H */

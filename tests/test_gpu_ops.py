@@ -1,0 +1,284 @@
+"""GPU parity of the particle<->grid operators against the CPU oracle.
+
+Integer and index work (cell keys, the sort permutation, the fixed-point
+density) must be bit-exact; the f32 operators (grad, gather, kick, drift) use
+the reference's operation order without contraction on both sides and must be
+bit-exact too.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+from oracle import pm
+
+pytestmark = pytest.mark.gpu
+
+
+def _parts(pos, mass=None, vel=None):
+    from galaxy_collision_gb300.data import ParticleState
+
+    pos = np.asarray(pos, np.float32)
+    n = pos.shape[0]
+    p = ParticleState(n)
+    p.pos_x.from_numpy(np.ascontiguousarray(pos[:, 0]))
+    p.pos_y.from_numpy(np.ascontiguousarray(pos[:, 1]))
+    p.pos_z.from_numpy(np.ascontiguousarray(pos[:, 2]))
+    p.mass.from_numpy(np.ones(n, np.float32) if mass is None else np.asarray(mass, np.float32))
+    if vel is not None:
+        vel = np.asarray(vel, np.float32)
+        p.vel_x.from_numpy(np.ascontiguousarray(vel[:, 0]))
+        p.vel_y.from_numpy(np.ascontiguousarray(vel[:, 1]))
+        p.vel_z.from_numpy(np.ascontiguousarray(vel[:, 2]))
+    return p
+
+
+def _edge_positions(G, dx, rng, n):
+    """Random positions plus the edge cases the reference tests touch: on nodes,
+    midpoints, the -1 cell, the top cell, just outside, far outside."""
+    pos = rng.uniform(-2.0 * dx, (G + 1) * dx, size=(n, 3)).astype(np.float32)
+    special = np.array([
+        [0.0, 0.0, 0.0], [(G - 1) * dx] * 3, [-0.5 * dx, 1.0, 1.0], [(G - 0.5) * dx, 2.0, 2.0],
+        [-dx, 3.0, 3.0], [-1.0001 * dx, 3.0, 3.0], [G * dx, 1.0, 1.0], [1e30, 0.0, 0.0], [-1e30, 0.0, 0.0],
+        [8.5 * dx, 8.5 * dx, 8.5 * dx], [np.nextafter(np.float32(G * dx), np.float32(0)), 1.0, 1.0],
+    ], dtype=np.float32)
+    return np.concatenate([pos, special[:, :3]], axis=0)
+
+
+@pytest.mark.parametrize("G,dx", [(16, 1.0), (33, 0.375), (64, 2.5)])
+def test_cell_keys_bit_exact(cuda, G, dx):
+    from galaxy_collision_gb300.deposit import cell_keys
+
+    rng = np.random.default_rng(G)
+    pos = _edge_positions(G, dx, rng, 20000)
+    keys = cell_keys(_parts(pos), G, dx).cpu().numpy().view(np.uint32)
+    np.testing.assert_array_equal(keys, pm.cell_keys(pos, dx, G))
+
+
+def test_cell_keys_nonfinite_are_sentinel(cuda):
+    from galaxy_collision_gb300.deposit import cell_keys
+
+    G = 16
+    pos = np.array([[np.nan, 1, 1], [1, np.inf, 1], [1, 1, -np.inf], [2, 2, 2]], np.float32)
+    keys = cell_keys(_parts(pos), G, 1.0).cpu().numpy().view(np.uint32)
+    assert list(keys[:3]) == [(G + 1) ** 3] * 3
+    assert keys[3] == ((3 * 17) + 3) * 17 + 3
+
+
+@pytest.mark.parametrize("n", [1, 31, 4096, 4097, 100003])
+def test_sort_permutation_bit_exact(cuda, n):
+    from galaxy_collision_gb300.deposit import sort_keys
+
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, 50, size=n).astype(np.uint32)  # many duplicates: stability matters
+    keys[::7] = rng.integers(0, 2**32 - 1, size=keys[::7].shape, dtype=np.uint64).astype(np.uint32)
+    kt = torch.from_numpy(keys.view(np.int32)).cuda()
+    sk, perm = sort_keys(kt, 16)
+    perm = perm.cpu().numpy().view(np.uint32)
+    ref = pm.stable_sort_perm(keys)
+    np.testing.assert_array_equal(perm, ref)
+    np.testing.assert_array_equal(sk.cpu().numpy().view(np.uint32), keys[ref])
+
+
+def test_pm_sort_permutes_all_arrays(cuda):
+    from galaxy_collision_gb300.engine import PMEngine
+
+    G, dx, n = 32, 1.0, 30001
+    rng = np.random.default_rng(7)
+    pos = rng.uniform(-1, G, size=(n, 3)).astype(np.float32)
+    vel = rng.normal(size=(n, 3)).astype(np.float32)
+    mass = rng.uniform(0.5, 1.5, size=n).astype(np.float32)
+    gid = rng.integers(0, 2, size=n).astype(np.int32)
+    eng = PMEngine(G, dx, sort_every=0)
+    eng.load(pos, vel, mass, gid, sort=True)
+    perm = pm.stable_sort_perm(pm.cell_keys(pos, dx, G))
+    cur = {k: v.cpu().numpy() for k, v in eng.cur.items()}
+    np.testing.assert_array_equal(cur["pid"], perm.astype(np.int32))
+    np.testing.assert_array_equal(cur["x"], pos[perm, 0])
+    np.testing.assert_array_equal(cur["vz"], vel[perm, 2])
+    np.testing.assert_array_equal(cur["m"], mass[perm])
+    np.testing.assert_array_equal(cur["gid"], gid[perm])
+
+
+@pytest.mark.parametrize("G,dx,bits", [(16, 1.0, 52), (48, 0.375, 52), (64, 2.5, 40), (33, 1.0, 60)])
+def test_deposit_bit_exact_vs_fixed_point_oracle(cuda, G, dx, bits):
+    from galaxy_collision_gb300.data import Field
+    from galaxy_collision_gb300.deposit import deposit_density
+
+    rng = np.random.default_rng(G + bits)
+    pos = _edge_positions(G, dx, rng, 50000)
+    mass = rng.uniform(0.1, 3.0, size=pos.shape[0]).astype(np.float32)
+    rho = Field((G, G, G))
+    deposit_density(_parts(pos, mass), rho, dx, fixed_point_bits=bits)
+    ref, _, _ = pm.deposit_fixed(pos, mass, dx, G, bits)
+    np.testing.assert_array_equal(rho.to_numpy(), ref)
+
+
+def test_deposit_vs_fp64_oracle(cuda):
+    from galaxy_collision_gb300.data import Field
+    from galaxy_collision_gb300.deposit import deposit_density
+
+    G, dx = 64, 0.375
+    rng = np.random.default_rng(11)
+    pos = (rng.normal(size=(200000, 3)) * 3.0 + 12.0).astype(np.float32)
+    mass = np.full(pos.shape[0], 1.0 / pos.shape[0], np.float32)
+    rho = Field((G, G, G))
+    deposit_density(_parts(pos, mass), rho, dx)
+    ref = pm.deposit_f64(pos, mass, dx, G)
+    assert rel_l2(rho.to_numpy(), ref) <= 1e-6
+    # mass conservation for the in-box particles
+    assert rho.to_numpy().astype(np.float64).sum() * dx**3 == pytest.approx(ref.sum() * dx**3, rel=1e-9)
+
+
+def test_deposit_reference_known_answers(cuda):  # tests/test_deposit.py:76-162
+    from galaxy_collision_gb300.data import GridState
+    from galaxy_collision_gb300.deposit import deposit_density
+
+    dx = 2.5
+    g = GridState(8)
+    deposit_density(_parts([[2 * dx, 3 * dx, 4 * dx]], [5.0]), g.rho, dx)
+    rho = g.rho.to_numpy()
+    assert rho[2, 3, 4] == pytest.approx(5.0 / dx**3) and rho.sum() == pytest.approx(5.0 / dx**3)
+    g = GridState(16)
+    deposit_density(_parts([[8.5, 8.5, 8.5]], [8.0]), g.rho, 1.0)
+    assert np.allclose(g.rho.to_numpy()[8:10, 8:10, 8:10], 1.0)
+    deposit_density(_parts([[-3.0, 8, 8], [40.0, 8, 8], [15.5, 8, 8]], [1, 1, 1]), g.rho, 1.0)
+    rho = g.rho.to_numpy()
+    assert rho.sum() <= 3.0 + 1e-5 and rho[15, 8, 8] == pytest.approx(0.5) and rho[0].sum() == 0.0
+
+
+def test_deposit_order_independent_and_reproducible(cuda):
+    from galaxy_collision_gb300.data import Field
+    from galaxy_collision_gb300.deposit import deposit_density
+
+    G = 32
+    rng = np.random.default_rng(3)
+    pos = (rng.normal(size=(300000, 3)) * 1.5 + 15.0).astype(np.float32)
+    mass = rng.uniform(0.5, 1.5, size=pos.shape[0]).astype(np.float32)
+    out = []
+    for order in (np.arange(pos.shape[0]), rng.permutation(pos.shape[0]), np.argsort(pos[:, 0])):
+        rho = Field((G, G, G))
+        deposit_density(_parts(pos[order], mass[order]), rho, 1.0)
+        out.append(rho.to_numpy())
+    np.testing.assert_array_equal(out[0], out[1])
+    np.testing.assert_array_equal(out[0], out[2])
+
+
+def test_nonfinite_position_flagged_and_skipped(cuda):
+    from galaxy_collision_gb300._ops import op_context
+    from galaxy_collision_gb300.data import Field
+    from galaxy_collision_gb300.deposit import deposit_density
+
+    G = 16
+    op_context(G, 1.0).status(clear=True)
+    rho = Field((G, G, G))
+    deposit_density(_parts([[np.nan, 4, 4], [4.0, 4.0, 4.0]], [1.0, 2.0]), rho, 1.0)
+    assert op_context(G, 1.0).status(clear=True) & 0x1
+    r = rho.to_numpy()
+    assert r[4, 4, 4] == pytest.approx(2.0) and r.sum() == pytest.approx(2.0)
+
+
+@pytest.mark.parametrize("G,dx", [(16, 1.0), (40, 0.375)])
+def test_grad_bit_exact(cuda, G, dx):
+    from galaxy_collision_gb300.data import Field, GridState
+    from galaxy_collision_gb300.deposit import potential_to_accel
+
+    rng = np.random.default_rng(G)
+    phi = rng.normal(size=(G, G, G)).astype(np.float32)
+    g = GridState(G)
+    g.phi.from_numpy(phi)
+    potential_to_accel(g.phi, g.ax, g.ay, g.az, dx)
+    ref = pm.grad(phi, dx)
+    for a, b in zip((g.ax, g.ay, g.az), ref):
+        np.testing.assert_array_equal(a.to_numpy(), b)
+    assert isinstance(g.ax, Field)
+
+
+def test_gather_bit_exact(cuda):
+    from galaxy_collision_gb300.data import Field, GridState
+    from galaxy_collision_gb300.deposit import gather_acceleration
+
+    G, dx = 24, 0.5
+    rng = np.random.default_rng(9)
+    pos = _edge_positions(G, dx, rng, 30000)
+    grids = [rng.normal(size=(G, G, G)).astype(np.float32) for _ in range(3)]
+    g = GridState(G)
+    for f, a in zip((g.ax, g.ay, g.az), grids):
+        f.from_numpy(a)
+    n = pos.shape[0]
+    acc = [Field(n) for _ in range(3)]
+    gather_acceleration(_parts(pos), g.ax, g.ay, g.az, *acc, dx)
+    ref = pm.gather(pos, *grids, dx)
+    for a, b in zip(acc, ref):
+        np.testing.assert_array_equal(a.to_numpy(), b)
+
+
+def test_kick_drift_bit_exact(cuda):
+    from galaxy_collision_gb300.data import Field
+    from galaxy_collision_gb300.integrator import drift, kick
+
+    n = 10007
+    rng = np.random.default_rng(1)
+    arrs = [rng.normal(size=n).astype(np.float32) for _ in range(9)]
+    f = [Field(n) for _ in range(9)]
+    for fi, a in zip(f, arrs):
+        fi.from_numpy(a)
+    kick(*f[3:6], *f[6:9], n, 0.013)
+    drift(*f[0:3], *f[3:6], n, 0.026)
+    ref = [a.copy() for a in arrs]
+    pm.axpy3(*ref[3:6], *ref[6:9], np.float32(0.013))
+    pm.axpy3(*ref[0:3], *ref[3:6], np.float32(0.026))
+    for fi, r in zip(f[:6], ref[:6]):
+        np.testing.assert_array_equal(fi.to_numpy(), r)
+
+
+def test_kdk_step_bit_identical_to_inline_loop(cuda):  # tests/test_integrator.py:189-257
+    from galaxy_collision_gb300.data import Field, GridState
+    from galaxy_collision_gb300.deposit import deposit_density, gather_acceleration, potential_to_accel
+    from galaxy_collision_gb300.integrator import drift, kdk_step, kick
+    from galaxy_collision_gb300.solver import make_solver
+
+    G, n, dt = 32, 2000, 0.05
+    rng = np.random.default_rng(2)
+    pos = (rng.normal(size=(n, 3)) * 2.0 + 15.5).astype(np.float32)
+    vel = (rng.normal(size=(n, 3)) * 0.2).astype(np.float32)
+    mass = np.full(n, 1.0 / n, np.float32)
+
+    def chain(parts):
+        grid = GridState(G)
+        acc = [Field(n) for _ in range(3)]
+        solver = make_solver("multigrid", G, grav_constant=1.0, tol=1e-6, n_cycles=30)
+
+        def accel_fn():
+            deposit_density(parts, grid.rho, 1.0)
+            solver.solve(grid.rho, grid.phi, warm_start=False)
+            potential_to_accel(grid.phi, grid.ax, grid.ay, grid.az, 1.0)
+            gather_acceleration(parts, grid.ax, grid.ay, grid.az, *acc, 1.0)
+
+        return acc, accel_fn
+
+    p1 = _parts(pos, mass, vel)
+    acc1, f1 = chain(p1)
+    calls = {"n": 0}
+
+    def counted():
+        calls["n"] += 1
+        f1()
+
+    counted()
+    for _ in range(5):
+        kdk_step(p1, *acc1, counted, dt)
+    assert calls["n"] == 6
+    p2 = _parts(pos, mass, vel)
+    acc2, f2 = chain(p2)
+    for _ in range(5):
+        f2()
+        kick(p2.vel_x, p2.vel_y, p2.vel_z, *acc2, n, dt / 2)
+        drift(p2.pos_x, p2.pos_y, p2.pos_z, p2.vel_x, p2.vel_y, p2.vel_z, n, dt)
+        f2()
+        kick(p2.vel_x, p2.vel_y, p2.vel_z, *acc2, n, dt / 2)
+    for a, b in zip(p1.fields()[:6], p2.fields()[:6]):
+        np.testing.assert_array_equal(a.to_numpy(), b.to_numpy())
