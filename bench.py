@@ -1,0 +1,435 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 PM force chain: particle-steps/s at 100M particles, 256^3.
+
+One *step* is one KDK step of the fused engine on the resident state: int64
+fixed-point CIC deposit, multigrid to a 1e-6 relative residual (FP64-class
+double-float finest level, FP64 faces and coarsest solve), and the fused
+gather(-grad phi) + kick + drift particle pass. Workload (default): the
+two-disk collision with 40M + 60M particles on a 256^3 grid over [-32, 32]^3,
+dt = 0.005, seed 2, mass quantum 2^-40 of the total.
+
+Printed: one JSON line (rank 0) with the value, per-step time, the roofline of
+the dominant kernel (CUDA-event time of its launches inside this run), the
+CPU baseline (the reference algorithm restated in C, on this host's cores),
+the end-to-end rate through the public API with host buffers, the SM clocks
+sampled during the timed region and the number of kernel launches.
+
+``--impl reference`` times the reference's algorithm instead: the C
+restatement of its Taichi kernels (the Taichi package itself cannot be
+installed here) with the reference's solver schedule, on all host threads.
+Multi-GPU: one process per GPU (torchrun); the simulation does not shard, so
+the ranks run independent replicas (weak scaling, no collective in the step).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for _p in (str(ROOT), str(ROOT / "galaxy-collision-with-cuda-fft_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s at 100M, 256^3"
+UNIT = "particle-steps/s"
+REFERENCE_PUBLISHED = 6.95e8  # reference, RTX 3070, 100M at 256^3 (its tol 1e-3): 6.95 steps/s x 1e8
+L2_BYTES = 126 * 1024**2
+
+# Algorithmic bytes per unit (per particle, or per finest cell) for each kernel.
+ALGO_BYTES = {
+    "gather_kick_drift": ("particle", 48.0),  # read x,y,z,vx,vy,vz; write them back
+    "deposit_runs": ("particle", 16.0),       # read x,y,z,m
+    "deposit": ("particle", 16.0),
+    "smooth0": ("cell", 10.0),                # one colour: half of (read hi,lo,b + write hi,lo)
+    "convert_q": ("cell", 20.0),              # read q, clear q, write b
+    "resid0": ("cell", 14.0),                 # read hi,lo,b; write r (restriction launches)
+    "prolong0": ("cell", 16.0),               # read/write hi,lo
+}
+
+
+def _parse(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--config", default="two_disk_100M")
+    ap.add_argument("--scale", type=float, default=1.0, help="particle-count scale of the configuration")
+    ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget-s", type=float, default=25.0)
+    ap.add_argument("--profile-steps", type=int, default=3)
+    ap.add_argument("--verbose", action="store_true")
+    return ap.parse_args(argv)
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _log(args, *msg):
+    if args.verbose:
+        print("[bench]", *msg, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+# ---------------------------------------------------------------------------- CPU arm
+def _reference_chain(pos_grid, vel, mass, G, dx, dt, steps, budget_s, threads=None):
+    """The reference's KDK step (bench.py:145-152 / sim.py:320-327) on the C restatement
+    of its kernels: kick, drift, deposit (parallel f32 atomics), multigrid with its
+    schedule (tol 1e-3, 20 cycles, warm start), grad, gather, kick.
+    Returns (seconds per step list, last solver cycles, residual ratio reached)."""
+    from oracle import pm
+
+    if threads:
+        pm.set_threads(threads)
+    x = [np.ascontiguousarray(pos_grid[:, i], dtype=np.float32) for i in range(3)]
+    v = [np.ascontiguousarray(vel[:, i], dtype=np.float32) for i in range(3)]
+    m = np.ascontiguousarray(mass, dtype=np.float32)
+    phi = np.zeros((G, G, G), np.float32)
+    mg = pm.ReferenceMultigrid(G, dx=dx, grav_constant=1.0)
+    warm = {"on": False}
+    acc = [None]
+
+    def accel():
+        rho = np.zeros((G, G, G), np.float32)
+        pm.lib().or_deposit_f32(x[0], x[1], x[2], m, m.shape[0], float(dx), int(G), rho, 1)
+        mg.solve(rho, phi, warm_start=warm["on"])
+        warm["on"] = True
+        acc[0] = pm.gather(np.stack(x, 1), *pm.grad(phi, dx), dx)
+
+    accel()
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        pm.axpy3(*v, *acc[0], np.float32(0.5 * dt))
+        pm.axpy3(*x, *v, np.float32(dt))
+        accel()
+        pm.axpy3(*v, *acc[0], np.float32(0.5 * dt))
+        times.append(time.perf_counter() - t0)
+        if sum(times) > budget_s:
+            break
+    ratio = mg.norms[1] / mg.norms[0] if mg.norms[0] > 0 else 0.0
+    return times, mg.last_cycles, float(ratio)
+
+
+def _cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:  # pragma: no cover
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------- GPU arm
+def aggregate(ms_local: float, n_local: int, steps: int, world: int, device="cpu"):
+    """Whole-job rate of `world` independent replicas: the slowest rank's time
+    (MAX over ranks) and the particles of all ranks. Returns (ms_max, value)."""
+    ms_max = float(ms_local)
+    total_n = int(n_local) * world
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([ms_local, float(n_local)], dtype=torch.float64, device=device)
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        tsum = t.clone()
+        dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+        ms_max = float(tmax[0].item())
+        total_n = int(round(float(tsum[1].item())))
+    return ms_max, total_n * steps / (ms_max / 1e3)
+
+
+def _roofline(stats: dict, n: int, G: int, hbm_gbs: float, traffic: dict):
+    best = None
+    for name, (launches, timed, ms) in stats.items():
+        if timed == 0 or ms <= 0:
+            continue
+        if best is None or ms > best[3]:
+            best = (name, launches, timed, ms)
+    if best is None:
+        return None
+    name, _, timed, ms = best
+    kind, b = ALGO_BYTES.get(name, (None, None))
+    if kind is None:
+        return {"kernel": name, "bound": "hbm", "achieved": None, "peak": hbm_gbs, "unit": "GB/s", "frac": None,
+                "traffic": None}
+    units = n if kind == "particle" else G**3
+    per_launch_bytes = b * units
+    avg_s = ms / timed / 1e3
+    achieved = per_launch_bytes / avg_s / 1e9
+    tr = traffic.get(name)
+    return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_gbs, "unit": "GB/s",
+            "frac": round(achieved / hbm_gbs, 4), "traffic": (tr * units if tr is not None else None),
+            "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": round(avg_s * 1e3, 4),
+            "launches_timed": timed, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"}
+
+
+def _load_traffic() -> dict:
+    """Per-unit DRAM bytes of each kernel from the committed ncu summary (or {})."""
+    p = ROOT / "profiles" / "dram_traffic_per_unit.txt"
+    out = {}
+    if p.exists():
+        for line in p.read_text().splitlines():
+            if line.startswith("#") or ":" not in line:
+                continue
+            k, v = line.split(":", 1)
+            try:
+                out[k.strip()] = float(v.split()[0])
+            except (ValueError, IndexError):
+                pass
+    return out
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = _dist()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group(backend="nccl", device_id=torch.device("cuda", local))
+    from galaxy_collision_gb300 import _build, ic
+    from galaxy_collision_gb300.engine import PMEngine
+
+    _build.build()
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    t0 = time.time()
+    icr, cfg = ic.build(args.config, scale=args.scale)
+    _log(args, f"IC {icr.n} particles in {time.time() - t0:.1f}s")
+    G, dx, dt = cfg["grid"], cfg["dx"], cfg["dt"]
+    bits = cfg.get("fixed_point_bits", 52)
+    n = icr.n
+
+    def make_engine():
+        return PMEngine(G, dx, grav=1.0, origin=cfg["origin"], tol=args.tol, max_cycles=60, fixed_point_bits=bits,
+                        sort_every=20)
+
+    eng = make_engine()
+    eng.load(icr.pos, icr.vel, icr.mass, icr.gid, sort=True)
+    eng.prime(dt)
+    for _ in range(args.warmup):
+        eng.advance(dt)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+
+    counts0 = {k: v[0] for k, v in eng.ctx.kernel_stats().items()}
+    sampler = ClockSampler(local)
+    sampler.start()
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    results = []
+    for _ in range(args.steps):
+        results.append(eng.advance(dt))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms_max, value = aggregate(ms, n, args.steps, world, device="cuda")
+    counts1 = {k: v[0] for k, v in eng.ctx.kernel_stats().items()}
+    launches = int(sum(counts1.values()) - sum(counts0.get(k, 0) for k in counts1))
+    cycles = [r.cycles for r in results]
+    rel = [r.rel_residual for r in results]
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": value / REFERENCE_PUBLISHED, "dtype": "f32", "data": "synthetic",
+        "config": {
+            "workload": f"{args.config}: {n:,} particles (two-disk collision), {G}^3 grid, box "
+                        f"[{cfg['origin'][0]:g},{-cfg['origin'][0]:g}]^3, dt={dt}, seed {cfg['seed']}, "
+                        f"multigrid to {args.tol:g} relative residual, int64 deposit quantum 2^-{bits} of the total",
+            "particles_per_gpu": n, "grid": G, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2: 32 B/particle state = %.1f GB per GPU" % (n * 32 / 1e9),
+            "vs_baseline_ref": "reference RTX 3070 published 6.95 steps/s at 100M, 256^3 (its tol 1e-3)",
+        },
+        "clocks": clocks,
+        "gpu_launches": launches,
+        "poisson": {"mean_vcycles": float(np.mean(cycles)), "max_rel_residual": float(max(rel)),
+                    "all_converged": bool(all(r.converged for r in results))},
+    }
+
+    if rank == 0:
+        # roofline: CUDA-event time of each kernel's launches over a few more steps
+        eng.ctx.profile_reset()
+        eng.ctx.profile(True)
+        for _ in range(args.profile_steps):
+            eng.advance(dt)
+        stats = eng.ctx.kernel_stats()
+        eng.ctx.profile(False)
+        tot = sum(v[2] for v in stats.values()) or 1.0
+        line["per_kernel_ms_per_step"] = {k: round(v[2] / args.profile_steps, 4) for k, v in
+                                          sorted(stats.items(), key=lambda kv: -kv[1][2])}
+        line["kernel_share"] = {k: round(v[2] / tot, 4) for k, v in sorted(stats.items(), key=lambda kv: -kv[1][2])}
+        line["roofline"] = _roofline(stats, n, G, hbm, _load_traffic())
+        poisson_ms = sum(v[2] for k, v in stats.items() if k in (
+            "smooth0", "resid0", "restrict", "smooth", "resid", "prolong", "prolong0", "tail", "faces", "reduce",
+            "convert_q")) / args.profile_steps
+        line["poisson"]["ms_per_solve"] = round(poisson_ms, 4)
+
+        if not args.no_e2e:
+            line["e2e"] = _e2e(args, icr, make_engine, dt)
+        if not args.no_cpu_baseline and world == 1:
+            pos_grid = (icr.pos.astype(np.float64) - np.asarray(cfg["origin"])).astype(np.float32)
+            times, cyc, ratio = _reference_chain(pos_grid, icr.vel, icr.mass, G, dx, dt, 3, args.cpu_budget_s)
+            line["cpu_baseline"] = {
+                "value": n * len(times) / sum(times), "unit": UNIT, "cores": _cpu_cores(), "kind": "port",
+                "sample": f"{len(times)} KDK step(s) of the full workload ({n:,} particles, {G}^3) after one priming "
+                          f"force evaluation; reference schedule tol=1e-3, n_cycles=20, warm start (last solve "
+                          f"{cyc} cycles, residual ratio {ratio:.2e})",
+            }
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def _e2e(args, icr, make_engine, dt):
+    """Same metric through the public API with host buffers: pinned host state ->
+    device (load + cell sort), prime, K-1 steps, close, state back to the host."""
+    import torch
+
+    pos = torch.from_numpy(icr.pos).pin_memory()
+    vel = torch.from_numpy(icr.vel).pin_memory()
+    mass = torch.from_numpy(icr.mass).pin_memory()
+    gid = torch.from_numpy(icr.gid).pin_memory()
+    out_pos = torch.empty((icr.n, 3), dtype=torch.float32).pin_memory()
+    out_vel = torch.empty((icr.n, 3), dtype=torch.float32).pin_memory()
+    eng = make_engine()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.load(pos.cuda(non_blocking=True), vel.cuda(non_blocking=True), mass.cuda(non_blocking=True),
+             gid.cuda(non_blocking=True), sort=True)
+    eng.prime(dt)
+    for _ in range(args.steps - 1):
+        eng.advance(dt)
+    eng.synchronize(dt, diagnostics=True)
+    p, v, _, _ = eng.state_arrays(physical=True)
+    out_pos.copy_(p.to(torch.float32), non_blocking=True)
+    out_vel.copy_(v, non_blocking=True)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    n = icr.n
+    return {"value": n * args.steps / t, "unit": UNIT, "h2d_bytes_per_step": int(n * 32 / args.steps),
+            "d2h_bytes_per_step": int((n * 24 + 12 * 8) / args.steps),
+            "note": "wall clock around load (pinned H2D + sort), prime, steps-1 advances, close with FP64 "
+                    "diagnostics, state D2H"}
+
+
+def run_reference(args):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    from galaxy_collision_gb300 import ic
+
+    icr, cfg = ic.build(args.config, scale=args.scale)
+    G, dx, dt = cfg["grid"], cfg["dx"], cfg["dt"]
+    pos_grid = (icr.pos.astype(np.float64) - np.asarray(cfg["origin"])).astype(np.float32)
+    budget = max(30.0, min(150.0, 12.0 * (args.steps + args.warmup)))
+    from oracle import pm
+
+    w_times, _, _ = _reference_chain(pos_grid, icr.vel, icr.mass, G, dx, dt, min(args.warmup, 1), budget / 4)
+    times, cyc, ratio = _reference_chain(pos_grid, icr.vel, icr.mass, G, dx, dt, args.steps, budget)
+    n = icr.n
+    value = n * len(times) / sum(times)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": len(times),
+        "warmup": len(w_times), "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": value / REFERENCE_PUBLISHED, "dtype": "f32", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": f"{args.config}: {n:,} particles, {G}^3 grid (the same workload as the GPU arm)",
+                   "implementation": "reference PM chain (deposit f32 atomics, multigrid tol=1e-3 n_cycles=20, "
+                                     "grad, gather, KDK) restated in C from its Taichi kernels; OpenMP on all "
+                                     "host threads",
+                   "requested_steps": args.steps},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": pm.num_threads(), "kind": "port",
+                         "sample": f"{len(times)} of {args.steps} requested KDK steps of the full workload "
+                                   f"(bounded to ~{budget:.0f} s); last solve {cyc} cycles, residual ratio "
+                                   f"{ratio:.2e}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main(argv=None):
+    args = _parse(argv)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -7,11 +7,15 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <utility>
+
 #include "../../include/gcpm.h"
 
 #define GC_MAX_LEVELS 24
 // Levels with at most this many nodes per axis are relaxed together by one CTA.
+#ifndef GC_TAIL_MAX_N
 #define GC_TAIL_MAX_N 17
+#endif
 
 struct LevelGeom {
   int n;        // nodes per axis (array extent)
@@ -33,6 +37,28 @@ enum {
   GC_S_MASS_PM = 7,  // engine: total density-mass of its particles
   GC_S_QEXP_PM = 8,  // engine: quantum exponent
   GC_S_NSLOTS = 64
+};
+
+// Kernel ids for launch counting and event timing (gc_profile_*).
+enum gc_kernel_id {
+  GK_DEPOSIT = 0, GK_DEPOSIT_RUNS, GK_CONVERT_Q, GK_MASS, GK_SMOOTH0, GK_RESID0, GK_RESTRICT, GK_SMOOTH,
+  GK_RESID, GK_PROLONG, GK_PROLONG0, GK_TAIL, GK_FACES, GK_MOMENTS, GK_RHS, GK_REDUCE, GK_GATHER_KD,
+  GK_GRAD, GK_GATHER, GK_AXPY, GK_KEYS, GK_SORT, GK_PERMUTE, GK_DIAG, GK_HIST, GK_RESID64, GK_COPY,
+  GK_COUNT
+};
+extern const char *const gc_kernel_names[GK_COUNT];
+
+#define GC_PROF_MAX_EVENTS 8192
+
+struct gc_profiler {
+  int enabled;
+  long long launches[GK_COUNT];      // always counted
+  int nrec;                          // recorded (start, stop) pairs since the last read
+  int kid[GC_PROF_MAX_EVENTS];
+  cudaEvent_t ev[2 * GC_PROF_MAX_EVENTS];
+  int nev_created;
+  double ms[GK_COUNT];               // accumulated by gc_profile_read
+  long long timed[GK_COUNT];
 };
 
 struct gc_ctx {
@@ -74,8 +100,23 @@ struct gc_ctx {
   int solved_once;
   gc_mg_stats last_stats;
 
+  gc_profiler prof;
+
   char err[512];
 };
+
+// Launch `k` on ctx's stream, counting it under `kid` and bracketing it with
+// CUDA events when profiling is enabled.
+int gc_prof_slot(gc_ctx *ctx, int kid);
+template <typename... KArgs, typename... Args>
+static inline void gc_launch(gc_ctx *ctx, int kid, void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                             Args &&...args) {
+  ctx->prof.launches[kid]++;
+  const int slot = ctx->prof.enabled ? gc_prof_slot(ctx, kid) : -1;
+  if (slot >= 0) cudaEventRecord(ctx->prof.ev[2 * slot], ctx->stream);
+  k<<<grid, block, smem, ctx->stream>>>(std::forward<Args>(args)...);
+  if (slot >= 0) cudaEventRecord(ctx->prof.ev[2 * slot + 1], ctx->stream);
+}
 
 // ---- error helpers -----------------------------------------------------------
 void gc_set_error(gc_ctx *ctx, const char *fmt, ...);
@@ -156,8 +197,10 @@ __device__ __forceinline__ bool gc_finite3(float x, float y, float z) {
 template <int NV>
 __device__ __forceinline__ void block_partials(double (&v)[NV], double *out) {
   __shared__ double sh[32][NV];
-  const int lane = threadIdx.x & 31;
-  const int wid = threadIdx.x >> 5;
+  // flat thread index: the 2-D launches (32 x 8) have one warp per threadIdx.y row
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int lane = tid & 31;
+  const int wid = tid >> 5;
   const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
 #pragma unroll
   for (int i = 0; i < NV; ++i) {
@@ -180,6 +223,25 @@ __device__ __forceinline__ void block_partials(double (&v)[NV], double *out) {
   }
 }
 
+// Single-value block sum reduced in FP32 (for norms, where ~1e-6 relative
+// accuracy is ample) and written as a double partial; avoids per-element FP64,
+// which runs at a small fraction of the FP32 rate on this part.
+__device__ __forceinline__ void block_sum_f32(float v, double *out) {
+  __shared__ float shf[32];
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int lane = tid & 31;
+  const int wid = tid >> 5;
+  const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) shf[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    float x = lane < nw ? shf[lane] : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) *out = (double)x;
+  }
+}
+
 // Internals shared between translation units
 int gc_mg_build_levels(gc_ctx *ctx);
 int gc_mg_alloc(gc_ctx *ctx);
@@ -198,6 +260,9 @@ int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, co
 // zero q, and reduce the ten moments into ctx->dmom and ||b||^2 into dsmall[GC_S_BNORM2].
 int gc_convert_q(gc_ctx *ctx, const double *qexp, float *rho_out, float *b_out);
 int gc_mg_check_params(gc_ctx *ctx, const gc_mg_params *p);
+// The exact integer column moments of the fixed-point grid need
+// (G-1) * 2^bits < 2^62: the largest allowed fixed_point_bits for this grid.
+int gc_max_fixed_point_bits(const gc_ctx *ctx);
 // Fused gather(-grad phi of ctx->hi) + kicks + drift over p (mode: gc_step_mode).
 // With diag, writes nparts rows of 11 FP64 partials into ctx->red.
 int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode, int diag, float *axo, float *ayo,

@@ -5,6 +5,70 @@
 
 static char g_create_err[512] = "";
 
+const char *const gc_kernel_names[GK_COUNT] = {
+    "deposit", "deposit_runs", "convert_q", "mass_setup", "smooth0", "resid0", "restrict", "smooth",
+    "resid", "prolong", "prolong0", "tail", "faces", "moments", "rhs", "reduce", "gather_kick_drift",
+    "grad", "gather", "axpy", "cell_keys", "radix_sort", "permute", "diag", "radial_hist", "resid64", "copy"};
+
+int gc_prof_slot(gc_ctx *ctx, int kid) {
+  gc_profiler &p = ctx->prof;
+  if (p.nrec >= GC_PROF_MAX_EVENTS) return -1;
+  const int slot = p.nrec;
+  if (slot >= p.nev_created) {
+    if (cudaEventCreate(&p.ev[2 * slot]) != cudaSuccess) return -1;
+    if (cudaEventCreate(&p.ev[2 * slot + 1]) != cudaSuccess) return -1;
+    p.nev_created = slot + 1;
+  }
+  p.kid[slot] = kid;
+  p.nrec++;
+  return slot;
+}
+
+extern "C" int gc_profile_enable(gc_ctx *ctx, int enable) {
+  if (!ctx) return GC_ERR_ARG;
+  ctx->prof.enabled = enable ? 1 : 0;
+  return GC_OK;
+}
+
+extern "C" int gc_num_kernel_ids(void) { return GK_COUNT; }
+
+extern "C" const char *gc_kernel_name(int kid) { return (kid >= 0 && kid < GK_COUNT) ? gc_kernel_names[kid] : ""; }
+
+// Fold the recorded event pairs into per-kernel totals (synchronises), then
+// report launches (always counted), timed launches and milliseconds of kid.
+extern "C" int gc_profile_read(gc_ctx *ctx, int kid, long long *launches, long long *timed, double *ms) {
+  if (!ctx || kid < 0 || kid >= GK_COUNT) return GC_ERR_ARG;
+  gc_profiler &p = ctx->prof;
+  if (p.nrec > 0) {
+    GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < p.nrec; ++i) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, p.ev[2 * i], p.ev[2 * i + 1]) == cudaSuccess) {
+        p.ms[p.kid[i]] += t;
+        p.timed[p.kid[i]]++;
+      }
+    }
+    p.nrec = 0;
+  }
+  if (launches) *launches = p.launches[kid];
+  if (timed) *timed = p.timed[kid];
+  if (ms) *ms = p.ms[kid];
+  return GC_OK;
+}
+
+extern "C" int gc_profile_reset(gc_ctx *ctx) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  gc_profiler &p = ctx->prof;
+  p.nrec = 0;
+  for (int k = 0; k < GK_COUNT; ++k) {
+    p.launches[k] = 0;
+    p.timed[k] = 0;
+    p.ms[k] = 0.0;
+  }
+  return GC_OK;
+}
+
 void gc_set_error(gc_ctx *ctx, const char *fmt, ...) {
   char *dst = ctx ? ctx->err : g_create_err;
   va_list ap;
@@ -60,8 +124,8 @@ extern "C" int gc_ctx_create(gc_ctx **out, int grid_size, double dx, double grav
     return GC_ERR_ARG;
   }
   *out = nullptr;
-  if (grid_size < 2 || grid_size > 2048) {
-    gc_set_error(nullptr, "grid_size must be in [2, 2048], got %d", grid_size);
+  if (grid_size < 2 || grid_size > 1024) {
+    gc_set_error(nullptr, "grid_size must be in [2, 1024], got %d", grid_size);
     return GC_ERR_ARG;
   }
   if (!(dx > 0.0) || !(dx < 1e30)) {
@@ -136,6 +200,7 @@ extern "C" int gc_ctx_destroy(gc_ctx *ctx) {
   cudaFree(ctx->ddiag);
   cudaFree(ctx->keys); cudaFree(ctx->keys2); cudaFree(ctx->vals); cudaFree(ctx->vals2);
   cudaFree(ctx->hist); cudaFree(ctx->hist_aux);
+  for (int i = 0; i < 2 * ctx->prof.nev_created; ++i) cudaEventDestroy(ctx->prof.ev[i]);
   free(ctx);
   return GC_OK;
 }

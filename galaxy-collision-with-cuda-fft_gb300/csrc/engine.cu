@@ -21,7 +21,8 @@ extern "C" int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_para
              "gc_pm_step: particle arrays required");
   GC_REQUIRE(ctx, sp->mode >= GC_STEP_PRIME && sp->mode <= GC_STEP_CLOSE, "gc_pm_step: bad mode %d", sp->mode);
   GC_REQUIRE(ctx, sp->dt == sp->dt, "gc_pm_step: dt must be finite");
-  GC_REQUIRE(ctx, sp->fixed_point_bits >= 24 && sp->fixed_point_bits <= 60, "fixed_point_bits must be in [24, 60]");
+  GC_REQUIRE(ctx, sp->fixed_point_bits >= 24 && sp->fixed_point_bits <= gc_max_fixed_point_bits(ctx),
+             "fixed_point_bits must be in [24, %d] for a %d^3 grid", gc_max_fixed_point_bits(ctx), ctx->G);
   if (sp->mode != GC_STEP_PRIME && !ctx->last_step_valid) {
     gc_set_error(ctx, "gc_pm_step: ADVANCE/CLOSE before PRIME");
     return GC_ERR_STATE;

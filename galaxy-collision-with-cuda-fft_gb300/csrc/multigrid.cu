@@ -123,9 +123,6 @@ void gc_mg_free(gc_ctx *ctx) {
 // ------------------------------------------------------------------------------
 // reductions: per-block partials written in a fixed order, then one block sums them
 // ------------------------------------------------------------------------------
-// Flattened thread id for the 1D-launched reductions below.
-__device__ __forceinline__ int flat_tid() { return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); }
-
 // Sum nparts rows of NV partials into dst[0..NV) (single block, fixed order).
 __global__ void k_finalize(const double *__restrict__ parts, int nparts, int nv, double *__restrict__ dst,
                            int accumulate) {
@@ -204,18 +201,18 @@ __global__ void __launch_bounds__(256)
   const int k = blockIdx.x * 32 + threadIdx.x + 1;
   const int j = blockIdx.y * 8 + threadIdx.y + 1;
   const int i = blockIdx.z + 1;
-  double acc[1] = {0.0};
+  float acc = 0.0f;
   if (k <= G - 2 && j <= G - 2) {
     const size_t sj = (size_t)G, si = (size_t)G * G;
     const size_t c = (size_t)i * si + (size_t)j * sj + k;
     float hc, lc;
     const float rv = df_residual(hi, lo, b[c], c, sj, si, hc, lc);
     if (r) r[c] = rv;
-    acc[0] = (double)rv * (double)rv;
+    acc = rv * rv;
   }
   if (parts) {
     const size_t bid = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    block_partials<1>(acc, parts + bid);
+    block_sum_f32(acc, parts + bid);
   }
 }
 
@@ -679,23 +676,21 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(256)
     k_rhs_from_rho(const float *__restrict__ rho, float *__restrict__ b0, size_t n, float fpg, float h2,
                    double *__restrict__ parts) {
-  double acc[1] = {0.0};
+  float acc = 0.0f;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
     const float rhs = __fmul_rn(fpg, rho[t]);
     const float bv = __fmul_rn(rhs, h2);
     b0[t] = bv;
-    acc[0] += (double)bv * (double)bv;
+    acc += bv * bv;
   }
-  block_partials<1>(acc, parts + blockIdx.x);
+  block_sum_f32(acc, parts + blockIdx.x);
 }
 
 __global__ void __launch_bounds__(256) k_sumsq(const float *__restrict__ a, size_t n, double *__restrict__ parts) {
-  double acc[1] = {0.0};
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
-    const double v = a[t];
-    acc[0] += v * v;
-  }
-  block_partials<1>(acc, parts + blockIdx.x);
+  float acc = 0.0f;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    acc += a[t] * a[t];
+  block_sum_f32(acc, parts + blockIdx.x);
 }
 
 __global__ void k_copy_hi_to(const float *__restrict__ hi, float *__restrict__ out, size_t n) {
@@ -716,7 +711,7 @@ static int launch_smooth0(gc_ctx *ctx, int sweeps) {
   const LevelGeom &g = ctx->lev[0];
   for (int s = 0; s < sweeps; ++s)
     for (int color = 0; color < 2; ++color)
-      k_smooth0<<<rb_grid(g), dim3(RB_TX, RB_TY), 0, ctx->stream>>>(ctx->hi, ctx->lo, ctx->b0, ctx->G, color);
+      gc_launch(ctx, GK_SMOOTH0, k_smooth0, dim3(rb_grid(g)), dim3(dim3(RB_TX, RB_TY)), 0, ctx->hi, ctx->lo, ctx->b0, ctx->G, color);
   GC_LAUNCH_CHECK(ctx, "smooth0");
   return GC_OK;
 }
@@ -725,7 +720,7 @@ static int launch_smooth(gc_ctx *ctx, int l, int sweeps) {
   const LevelGeom &g = ctx->lev[l];
   for (int s = 0; s < sweeps; ++s)
     for (int color = 0; color < 2; ++color)
-      k_smooth<<<rb_grid(g), dim3(RB_TX, RB_TY), 0, ctx->stream>>>(ctx->e[l], ctx->b[l], g, color);
+      gc_launch(ctx, GK_SMOOTH, k_smooth, dim3(rb_grid(g)), dim3(dim3(RB_TX, RB_TY)), 0, ctx->e[l], ctx->b[l], g, color);
   GC_LAUNCH_CHECK(ctx, "smooth");
   return GC_OK;
 }
@@ -744,7 +739,7 @@ static int launch_tail(gc_ctx *ctx, const gc_mg_params *p) {
     GC_CUDA(ctx, cudaFuncSetAttribute(k_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set_for = (int)smem;
   }
-  k_tail<<<1, 512, smem, ctx->stream>>>(ctx->b[ctx->tail], ctx->e[ctx->tail], d);
+  gc_launch(ctx, GK_TAIL, k_tail, dim3(1), dim3(512), smem, ctx->b[ctx->tail], ctx->e[ctx->tail], d);
   GC_LAUNCH_CHECK(ctx, "tail");
   return GC_OK;
 }
@@ -756,33 +751,33 @@ static int vcycle(gc_ctx *ctx, const gc_mg_params *p) {
   int st;
   if ((st = launch_smooth0(ctx, p->pre_sweeps))) return st;
   const LevelGeom &g0 = ctx->lev[0];
-  k_resid0<<<node_grid(g0), dim3(32, 8), 0, ctx->stream>>>(ctx->hi, ctx->lo, ctx->b0, ctx->r0, nullptr, ctx->G);
-  k_restrict<<<node_grid(ctx->lev[1]), dim3(32, 8), 0, ctx->stream>>>(ctx->r0, g0, ctx->b[1], ctx->lev[1]);
+  gc_launch(ctx, GK_RESID0, k_resid0, dim3(node_grid(g0)), dim3(dim3(32, 8)), 0, ctx->hi, ctx->lo, ctx->b0, ctx->r0, nullptr, ctx->G);
+  gc_launch(ctx, GK_RESTRICT, k_restrict, dim3(node_grid(ctx->lev[1])), dim3(dim3(32, 8)), 0, ctx->r0, g0, ctx->b[1], ctx->lev[1]);
   GC_LAUNCH_CHECK(ctx, "resid0/restrict");
   for (int l = 1; l < ctx->tail; ++l) {
     const LevelGeom &g = ctx->lev[l];
     const size_t n3 = (size_t)g.n * g.n * g.n;
     GC_CUDA(ctx, cudaMemsetAsync(ctx->e[l], 0, n3 * sizeof(float), ctx->stream));
     if ((st = launch_smooth(ctx, l, p->pre_sweeps))) return st;
-    k_resid<<<node_grid(g), dim3(32, 8), 0, ctx->stream>>>(ctx->e[l], ctx->b[l], ctx->rc, g);
-    k_restrict<<<node_grid(ctx->lev[l + 1]), dim3(32, 8), 0, ctx->stream>>>(ctx->rc, g, ctx->b[l + 1], ctx->lev[l + 1]);
+    gc_launch(ctx, GK_RESID, k_resid, dim3(node_grid(g)), dim3(dim3(32, 8)), 0, ctx->e[l], ctx->b[l], ctx->rc, g);
+    gc_launch(ctx, GK_RESTRICT, k_restrict, dim3(node_grid(ctx->lev[l + 1])), dim3(dim3(32, 8)), 0, ctx->rc, g, ctx->b[l + 1], ctx->lev[l + 1]);
     GC_LAUNCH_CHECK(ctx, "resid/restrict");
   }
   if (ctx->tail < L) {
     if ((st = launch_tail(ctx, p))) return st;
   }
   for (int l = ctx->tail - 1; l >= 1; --l) {
-    k_prolong<<<node_grid(ctx->lev[l]), dim3(32, 8), 0, ctx->stream>>>(ctx->e[l + 1], ctx->lev[l + 1], ctx->e[l], ctx->lev[l]);
+    gc_launch(ctx, GK_PROLONG, k_prolong, dim3(node_grid(ctx->lev[l])), dim3(dim3(32, 8)), 0, ctx->e[l + 1], ctx->lev[l + 1], ctx->e[l], ctx->lev[l]);
     GC_LAUNCH_CHECK(ctx, "prolong");
     if ((st = launch_smooth(ctx, l, p->post_sweeps))) return st;
   }
-  k_prolong0<<<node_grid(g0), dim3(32, 8), 0, ctx->stream>>>(ctx->e[1], ctx->lev[1], ctx->hi, ctx->lo, g0);
+  gc_launch(ctx, GK_PROLONG0, k_prolong0, dim3(node_grid(g0)), dim3(dim3(32, 8)), 0, ctx->e[1], ctx->lev[1], ctx->hi, ctx->lo, g0);
   GC_LAUNCH_CHECK(ctx, "prolong0");
   return launch_smooth0(ctx, p->post_sweeps);
 }
 
 int gc_finalize(gc_ctx *ctx, const double *parts, int nparts, int nv, double *dst) {
-  k_finalize<<<1, 1024, 0, ctx->stream>>>(parts, nparts, nv, dst, 0);
+  gc_launch(ctx, GK_REDUCE, k_finalize, dim3(1), dim3(1024), 0, parts, nparts, nv, dst, 0);
   GC_LAUNCH_CHECK(ctx, "finalize");
   return GC_OK;
 }
@@ -798,7 +793,7 @@ static int resid_norm_async(gc_ctx *ctx) {
   const size_t nb = (size_t)grid.x * grid.y * grid.z;
   int st = gc_ensure_red(ctx, nb);
   if (st) return st;
-  k_resid0<<<grid, dim3(32, 8), 0, ctx->stream>>>(ctx->hi, ctx->lo, ctx->b0, nullptr, ctx->red, ctx->G);
+  gc_launch(ctx, GK_RESID0, k_resid0, dim3(grid), dim3(dim3(32, 8)), 0, ctx->hi, ctx->lo, ctx->b0, nullptr, ctx->red, ctx->G);
   GC_LAUNCH_CHECK(ctx, "resid0 norm");
   return finalize_to(ctx, (int)nb, 1, GC_S_RNORM2);
 }
@@ -813,17 +808,17 @@ static int read_small(gc_ctx *ctx, int slot, int count) {
 // ||b0||^2 into dsmall[GC_S_BNORM2] (async).
 int gc_norm_b(gc_ctx *ctx) {
   const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
-  const int nb = 1024;
+  const int nb = 2048;
   int st = gc_ensure_red(ctx, nb);
   if (st) return st;
-  k_sumsq<<<nb, 256, 0, ctx->stream>>>(ctx->b0, g3, ctx->red);
+  gc_launch(ctx, GK_REDUCE, k_sumsq, dim3(nb), dim3(256), 0, ctx->b0, g3, ctx->red);
   GC_LAUNCH_CHECK(ctx, "sumsq");
   return finalize_to(ctx, nb, 1, GC_S_BNORM2);
 }
 
 int gc_faces_from_moments(gc_ctx *ctx) {
   const long long tot = 6LL * ctx->G * ctx->G;
-  k_faces<<<gc_blocks(tot, 256), 256, 0, ctx->stream>>>(ctx->hi, ctx->lo, ctx->G, ctx->dx, ctx->grav, ctx->dmom);
+  gc_launch(ctx, GK_FACES, k_faces, dim3(gc_blocks(tot, 256)), dim3(256), 0, ctx->hi, ctx->lo, ctx->G, ctx->dx, ctx->grav, ctx->dmom);
   GC_LAUNCH_CHECK(ctx, "faces");
   return GC_OK;
 }
@@ -887,9 +882,9 @@ static int moments_rho_async(gc_ctx *ctx, const float *rho) {
   const unsigned nb = gc_blocks(cols, 8);
   int s = gc_ensure_red(ctx, (size_t)nb * 10);
   if (s) return s;
-  k_moments_rho<<<nb, 256, 0, ctx->stream>>>(rho, ctx->G, ctx->dx, ctx->red, ctx->dstatus);
+  gc_launch(ctx, GK_MOMENTS, k_moments_rho, dim3(nb), dim3(256), 0, rho, ctx->G, ctx->dx, ctx->red, ctx->dstatus);
   GC_LAUNCH_CHECK(ctx, "moments");
-  k_finalize<<<1, 1024, 0, ctx->stream>>>(ctx->red, (int)nb, 10, ctx->dmom, 0);
+  gc_launch(ctx, GK_REDUCE, k_finalize, dim3(1), dim3(1024), 0, ctx->red, (int)nb, 10, ctx->dmom, 0);
   GC_LAUNCH_CHECK(ctx, "moments finalize");
   return GC_OK;
 }
@@ -920,11 +915,11 @@ extern "C" int gc_mg_solve(gc_ctx *ctx, const float *rho, float *phi, int warm_s
   if ((s = moments_rho_async(ctx, rho))) return s;
   // b0 = h^2 * 4 pi G rho (multigrid.py:463) and ||b0||^2 (multigrid.py:477)
   {
-    const int nb = 1024;
+    const int nb = 2048;
     if ((s = gc_ensure_red(ctx, nb))) return s;
     const float fpg = (float)(4.0 * M_PI * ctx->grav);
     const float h2 = (float)(ctx->dx * ctx->dx);
-    k_rhs_from_rho<<<nb, 256, 0, ctx->stream>>>(rho, ctx->b0, g3, fpg, h2, ctx->red);
+    gc_launch(ctx, GK_RHS, k_rhs_from_rho, dim3(nb), dim3(256), 0, rho, ctx->b0, g3, fpg, h2, ctx->red);
     GC_LAUNCH_CHECK(ctx, "rhs");
     if ((s = finalize_to(ctx, nb, 1, GC_S_BNORM2))) return s;
   }
@@ -938,7 +933,7 @@ extern "C" int gc_mg_solve(gc_ctx *ctx, const float *rho, float *phi, int warm_s
   if ((s = gc_faces_from_moments(ctx))) return s;
   if ((s = gc_mg_run(ctx, &p, stats))) return s;
   // phi = f32(hi + lo) == hi (the pair is normalised)
-  k_copy_hi_to<<<1024, 256, 0, ctx->stream>>>(ctx->hi, phi, g3);
+  gc_launch(ctx, GK_COPY, k_copy_hi_to, dim3(1024), dim3(256), 0, ctx->hi, phi, g3);
   GC_LAUNCH_CHECK(ctx, "copy phi");
   uint32_t flags = 0;
   if ((s = gc_status(ctx, &flags, 0))) return s;
@@ -962,9 +957,9 @@ extern "C" int gc_mg_residual_norm(gc_ctx *ctx, const float *phi_f32, double *ou
   int s = gc_ensure_red(ctx, nb);
   if (s) return s;
   if (phi_f32)
-    k_resid64<<<grid, dim3(32, 8), 0, ctx->stream>>>(phi_f32, nullptr, ctx->b0, ctx->red, ctx->G);
+    gc_launch(ctx, GK_RESID64, k_resid64, dim3(grid), dim3(dim3(32, 8)), 0, phi_f32, nullptr, ctx->b0, ctx->red, ctx->G);
   else
-    k_resid64<<<grid, dim3(32, 8), 0, ctx->stream>>>(ctx->hi, ctx->lo, ctx->b0, ctx->red, ctx->G);
+    gc_launch(ctx, GK_RESID64, k_resid64, dim3(grid), dim3(dim3(32, 8)), 0, ctx->hi, ctx->lo, ctx->b0, ctx->red, ctx->G);
   GC_LAUNCH_CHECK(ctx, "resid64");
   if ((s = finalize_to(ctx, (int)nb, 1, GC_S_RNORM64))) return s;
   if ((s = read_small(ctx, GC_S_RNORM64, 1))) return s;

@@ -82,9 +82,9 @@ int gc_fixed_point_setup(gc_ctx *ctx, const float *m, int64_t n, int bits, int m
   unsigned nb = gc_blocks(n, 256);
   if (nb > 152u * 8u) nb = 152u * 8u;
   const int L = ceil_log2((long long)n);
-  k_mass_max<<<nb, 256, 0, ctx->stream>>>(m, (long long)n, inv_vol, maxbits);
-  k_mass_isum<<<nb, 256, 0, ctx->stream>>>(m, (long long)n, inv_vol, maxbits, L, isum);
-  k_qexp<<<1, 32, 0, ctx->stream>>>(maxbits, isum, L, ctx->dsmall, mass_slot, exp_slot, bits);
+  gc_launch(ctx, GK_MASS, k_mass_max, dim3(nb), dim3(256), 0, m, (long long)n, inv_vol, maxbits);
+  gc_launch(ctx, GK_MASS, k_mass_isum, dim3(nb), dim3(256), 0, m, (long long)n, inv_vol, maxbits, L, isum);
+  gc_launch(ctx, GK_MASS, k_qexp, dim3(1), dim3(32), 0, maxbits, isum, L, ctx->dsmall, mass_slot, exp_slot, bits);
   GC_LAUNCH_CHECK(ctx, "fixed-point set-up");
   return GC_OK;
 }
@@ -175,64 +175,83 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Cell-sorted particles: each thread walks RUN consecutive particles and keeps a
-// running 8-corner sum while the cell does not change; the warp then merges the
-// final runs when all lanes end in one cell.
-#define DEP_RUN 8
+// Cell-sorted particles. Each warp owns a contiguous range of DEP_WARP_ITEMS
+// particles and walks it 32 at a time (coalesced loads). Lanes holding the same
+// cell are adjacent after the sort, so a segmented inclusive scan over the warp
+// sums each run of equal cells; the last lane of a run adds its 8 corner sums
+// with one int64 atomic each. The run that reaches lane 31 is carried into the
+// next group of 32 and merged there when the cell continues.
+#define DEP_WARP_ITEMS 512
 __global__ void __launch_bounds__(256)
-    k_deposit_runs(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
-                   const float *__restrict__ m, long long n, DepCtx d, const double *__restrict__ qexp,
-                   long long *__restrict__ qg, unsigned *__restrict__ status) {
+    k_deposit_sorted(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
+                     const float *__restrict__ m, long long n, DepCtx d, const double *__restrict__ qexp,
+                     long long *__restrict__ qg, unsigned *__restrict__ status) {
   const float qscale = ldexpf(1.0f, -(int)(*qexp));
   const int lane = threadIdx.x & 31;
-  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long nthreads = (long long)gridDim.x * blockDim.x;
-  const long long nchunks = (n + DEP_RUN - 1) / DEP_RUN;
-  const long long iters = (nchunks + nthreads - 1) / nthreads;
-  for (long long it = 0; it < iters; ++it) {
-    const long long chunk = it * nthreads + tid;
-    const long long p0 = chunk * DEP_RUN;
-    long long acc[8];
-    CellPos cur;
-    unsigned cur_key = 0xffffffffu;
-    bool have = false;
+  const long long gwarp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const unsigned invalid = 0x80000000u | (unsigned)lane;
+  for (long long base = gwarp * DEP_WARP_ITEMS; base < n; base += nwarps * DEP_WARP_ITEMS) {
+    unsigned ckey = 0xffffffffu;  // carried run (same value in every lane)
+    long long cq[8];
+    int cix = 0, ciy = 0, ciz = 0;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) acc[t] = 0;
-    if (p0 < n) {
-      const long long p1 = (p0 + DEP_RUN < n) ? p0 + DEP_RUN : n;
-      for (long long p = p0; p < p1; ++p) {
+    for (int t = 0; t < 8; ++t) cq[t] = 0;
+    for (int g = 0; g < DEP_WARP_ITEMS; g += 32) {
+      const long long p = base + g + lane;
+      CellPos c;
+      long long q[8];
+      bool ok = false;
+      if (p < n) {
         const float px = x[p], py = y[p], pz = z[p];
         if (!gc_finite3(px, py, pz)) atomicOr(status, GC_FLAG_NONFINITE_POS);
-        CellPos c;
-        long long q[8];
-        if (!cic_contrib(px, py, pz, m[p], d, qscale, c, q)) continue;
-        const unsigned key = (unsigned)(((c.ix + 1) * (d.G + 1) + (c.iy + 1)) * (d.G + 1) + (c.iz + 1));
-        if (have && key == cur_key) {
+        ok = cic_contrib(px, py, pz, m[p], d, qscale, c, q);
+      }
+      if (!ok) {
+        c.ix = c.iy = c.iz = 0;
 #pragma unroll
-          for (int t = 0; t < 8; ++t) acc[t] += q[t];
+        for (int t = 0; t < 8; ++t) q[t] = 0;
+      }
+      const unsigned key = ok ? (unsigned)(((c.ix + 1) * (d.G + 1) + (c.iy + 1)) * (d.G + 1) + (c.iz + 1)) : invalid;
+      // the carried run continues into lane 0, or is flushed by lane 0
+      if (lane == 0 && ckey != 0xffffffffu) {
+        if (key == ckey) {
+#pragma unroll
+          for (int t = 0; t < 8; ++t) q[t] += cq[t];
         } else {
-          if (have) flush_corners(qg, cur, d.G, acc);
-          cur = c;
-          cur_key = key;
-          have = true;
-#pragma unroll
-          for (int t = 0; t < 8; ++t) acc[t] = q[t];
+          CellPos cc;
+          cc.ix = cix; cc.iy = ciy; cc.iz = ciz;
+          flush_corners(qg, cc, d.G, cq);
         }
       }
-    }
-    const unsigned mkey = have ? cur_key : (0x80000000u | (unsigned)lane);
-    int all_same = 0;
-    __match_all_sync(0xffffffffu, mkey, &all_same);
-    if (all_same) {
+      // segmented inclusive scan: head = lane 0 or key differs from the lane below
+      const unsigned kprev = __shfl_up_sync(0xffffffffu, key, 1);
+      bool head = (lane == 0) || (kprev != key);
 #pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        long long v = acc[t];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        acc[t] = v;
+      for (int off = 1; off < 32; off <<= 1) {
+        const bool hprev = __shfl_up_sync(0xffffffffu, head, off);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          const long long v = __shfl_up_sync(0xffffffffu, q[t], off);
+          if (lane >= off && !head) q[t] += v;
+        }
+        if (lane >= off) head = head || hprev;
       }
-      if (lane == 0) flush_corners(qg, cur, d.G, acc);
-    } else if (have) {
-      flush_corners(qg, cur, d.G, acc);
+      const unsigned knext = __shfl_down_sync(0xffffffffu, key, 1);
+      const bool tail = (lane != 31) && (knext != key);
+      if (tail && ok) flush_corners(qg, c, d.G, q);
+      // lane 31's run is carried
+      ckey = __shfl_sync(0xffffffffu, ok ? key : 0xffffffffu, 31);
+      cix = __shfl_sync(0xffffffffu, c.ix, 31);
+      ciy = __shfl_sync(0xffffffffu, c.iy, 31);
+      ciz = __shfl_sync(0xffffffffu, c.iz, 31);
+#pragma unroll
+      for (int t = 0; t < 8; ++t) cq[t] = __shfl_sync(0xffffffffu, q[t], 31);
+    }
+    if (lane == 0 && ckey != 0xffffffffu) {
+      CellPos cc;
+      cc.ix = cix; cc.iy = ciy; cc.iz = ciz;
+      flush_corners(qg, cc, d.G, cq);
     }
   }
 }
@@ -245,14 +264,14 @@ int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, co
   d.inv_vol = 1.0f / ((d.dx * d.dx) * d.dx);
   d.G = ctx->G;
   if (sorted_runs) {
-    const long long nchunks = (n + DEP_RUN - 1) / DEP_RUN;
-    unsigned nb = gc_blocks(nchunks, 256);
-    if (nb > 152u * 16u) nb = 152u * 16u;
-    k_deposit_runs<<<nb, 256, 0, ctx->stream>>>(x, y, z, m, (long long)n, d, qexp, ctx->q, ctx->dstatus);
+    const long long nranges = (n + DEP_WARP_ITEMS - 1) / DEP_WARP_ITEMS;
+    unsigned nb = gc_blocks(nranges, 8);
+    if (nb > 152u * 8u) nb = 152u * 8u;
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted, dim3(nb), dim3(256), 0, x, y, z, m, (long long)n, d, qexp, ctx->q, ctx->dstatus);
   } else {
     unsigned nb = gc_blocks(n, 256);
     if (nb > 152u * 32u) nb = 152u * 32u;
-    k_deposit<<<nb, 256, 0, ctx->stream>>>(x, y, z, m, (long long)n, d, qexp, ctx->q, ctx->dstatus);
+    gc_launch(ctx, GK_DEPOSIT, k_deposit, dim3(nb), dim3(256), 0, x, y, z, m, (long long)n, d, qexp, ctx->q, ctx->dstatus);
   }
   GC_LAUNCH_CHECK(ctx, "deposit");
   return GC_OK;
@@ -295,25 +314,33 @@ __global__ void __launch_bounds__(256)
       S2h += (qv >> 32) * (kk * kk);
       S2l += (unsigned long long)(qv & 0xffffffffLL) * (unsigned long long)(kk * kk);
     }
-    double d0 = (double)S0, d1 = (double)S1, d2 = (double)S2h * 4294967296.0 + (double)S2l;
-    double db = (double)bb;
+    // exact integer warp sums (no FP64 per lane)
     for (int o = 16; o > 0; o >>= 1) {
-      d0 += __shfl_down_sync(0xffffffffu, d0, o);
-      d1 += __shfl_down_sync(0xffffffffu, d1, o);
-      d2 += __shfl_down_sync(0xffffffffu, d2, o);
-      db += __shfl_down_sync(0xffffffffu, db, o);
+      S0 += __shfl_down_sync(0xffffffffu, S0, o);
+      S1 += __shfl_down_sync(0xffffffffu, S1, o);
+      S2h += __shfl_down_sync(0xffffffffu, S2h, o);
+      S2l += __shfl_down_sync(0xffffffffu, S2l, o);
+      bb += __shfl_down_sync(0xffffffffu, bb, o);
     }
     if (lane == 0) {
+      const double d0 = (double)S0, d1 = (double)S1, d2 = (double)S2h * 4294967296.0 + (double)S2l;
       const double msc = ldexp(1.0, E) * dx * dx * dx;  // mass of one quantum
       const double x = i * dx, y = j * dx;
       const double m0 = d0 * msc, m1 = d1 * msc * dx, m2 = d2 * msc * dx * dx;
       v[0] = m0; v[1] = m0 * x; v[2] = m0 * y; v[3] = m1;
       v[4] = m0 * x * x; v[5] = m0 * y * y; v[6] = m2;
       v[7] = m0 * x * y; v[8] = m1 * x; v[9] = m1 * y;
-      v[10] = db;
+      v[10] = (double)bb;
     }
   }
   block_partials<11>(v, parts + (size_t)blockIdx.x * 11);
+}
+
+int gc_max_fixed_point_bits(const gc_ctx *ctx) {
+  int lg = 0;
+  while ((1 << lg) < ctx->G) ++lg;
+  const int b = 62 - lg;
+  return b > 60 ? 60 : b;
 }
 
 int gc_convert_q(gc_ctx *ctx, const double *qexp, float *rho_out, float *b_out) {
@@ -322,7 +349,7 @@ int gc_convert_q(gc_ctx *ctx, const double *qexp, float *rho_out, float *b_out) 
   int s = gc_ensure_red(ctx, (size_t)nb * 11);
   if (s) return s;
   const double bfac = 4.0 * M_PI * ctx->grav * ctx->dx * ctx->dx;
-  k_convert_q<<<nb, 256, 0, ctx->stream>>>(ctx->q, ctx->G, ctx->dx, qexp, rho_out, b_out, bfac, ctx->red);
+  gc_launch(ctx, GK_CONVERT_Q, k_convert_q, dim3(nb), dim3(256), 0, ctx->q, ctx->G, ctx->dx, qexp, rho_out, b_out, bfac, ctx->red);
   GC_LAUNCH_CHECK(ctx, "convert q");
   if ((s = gc_finalize(ctx, ctx->red, (int)nb, 11, ctx->dmom))) return s;
   GC_CUDA(ctx, cudaMemcpyAsync(ctx->dsmall + GC_S_BNORM2, ctx->dmom + 10, sizeof(double), cudaMemcpyDeviceToDevice,
@@ -336,7 +363,8 @@ extern "C" int gc_deposit_cic(gc_ctx *ctx, const float *x, const float *y, const
   GC_REQUIRE(ctx, rho, "gc_deposit_cic: NULL rho");
   GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range: %lld", (long long)n);
   GC_REQUIRE(ctx, n == 0 || (x && y && z && m), "gc_deposit_cic: NULL particle array");
-  GC_REQUIRE(ctx, fixed_point_bits >= 24 && fixed_point_bits <= 60, "fixed_point_bits must be in [24, 60]");
+  GC_REQUIRE(ctx, fixed_point_bits >= 24 && fixed_point_bits <= gc_max_fixed_point_bits(ctx),
+             "fixed_point_bits must be in [24, %d] for a %d^3 grid", gc_max_fixed_point_bits(ctx), ctx->G);
   int s;
   if (n > 0) {
     if ((s = gc_fixed_point_setup(ctx, m, n, fixed_point_bits, GC_S_MASS, GC_S_QEXP))) return s;
@@ -387,7 +415,7 @@ extern "C" int gc_potential_to_accel(gc_ctx *ctx, const float *phi, float *ax, f
   if (!ctx) return GC_ERR_ARG;
   GC_REQUIRE(ctx, phi && ax && ay && az, "gc_potential_to_accel: NULL pointer");
   const GradCtx g = make_grad(ctx);
-  k_grad<<<dim3(gc_blocks(g.G, 32), gc_blocks(g.G, 8), g.G), dim3(32, 8), 0, ctx->stream>>>(phi, ax, ay, az, g);
+  gc_launch(ctx, GK_GRAD, k_grad, dim3(dim3(gc_blocks(g.G, 32), gc_blocks(g.G, 8), g.G)), dim3(dim3(32, 8)), 0, phi, ax, ay, az, g);
   GC_LAUNCH_CHECK(ctx, "grad");
   return GC_OK;
 }
@@ -437,7 +465,7 @@ extern "C" int gc_gather_accel(gc_ctx *ctx, const float *x, const float *y, cons
   GC_REQUIRE(ctx, x && y && z && ax_g && ay_g && az_g && acc_x && acc_y && acc_z, "gc_gather_accel: NULL pointer");
   unsigned nb = gc_blocks(n, 256);
   if (nb > 152u * 32u) nb = 152u * 32u;
-  k_gather<<<nb, 256, 0, ctx->stream>>>(x, y, z, (long long)n, ax_g, ay_g, az_g, acc_x, acc_y, acc_z,
+  gc_launch(ctx, GK_GATHER, k_gather, dim3(nb), dim3(256), 0, x, y, z, (long long)n, ax_g, ay_g, az_g, acc_x, acc_y, acc_z,
                                         (float)ctx->dx, ctx->G);
   GC_LAUNCH_CHECK(ctx, "gather");
   return GC_OK;
@@ -463,7 +491,7 @@ static int axpy3(gc_ctx *ctx, float *u, float *v, float *w, const float *a, cons
   GC_REQUIRE(ctx, u && v && w && a && b && c, "%s: NULL pointer", what);
   unsigned nb = gc_blocks(n, 256);
   if (nb > 152u * 32u) nb = 152u * 32u;
-  k_axpy3<<<nb, 256, 0, ctx->stream>>>(u, v, w, a, b, c, (long long)n, dt);
+  gc_launch(ctx, GK_AXPY, k_axpy3, dim3(nb), dim3(256), 0, u, v, w, a, b, c, (long long)n, dt);
   GC_LAUNCH_CHECK(ctx, what);
   return GC_OK;
 }
@@ -591,7 +619,7 @@ int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode,
   if (nb > 152u * 16u) nb = 152u * 16u;
   int s = gc_ensure_red(ctx, (size_t)nb * 11);
   if (s) return s;
-  k_gather_kick_drift<<<nb, 256, 0, ctx->stream>>>(p->x, p->y, p->z, p->vx, p->vy, p->vz, p->m, (long long)p->n,
+  gc_launch(ctx, GK_GATHER_KD, k_gather_kick_drift, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx, p->vy, p->vz, p->m, (long long)p->n,
                                                    ctx->hi, f, axo, ayo, azo, ctx->red);
   GC_LAUNCH_CHECK(ctx, "gather_kick_drift");
   if (nparts_out) *nparts_out = (int)nb;
@@ -635,7 +663,7 @@ extern "C" int gc_diag_particles(gc_ctx *ctx, const float *x, const float *y, co
   const int nb = 512;
   int s = gc_ensure_red(ctx, nb * 11);
   if (s) return s;
-  k_diag_particles<<<nb, 256, 0, ctx->stream>>>(x, y, z, vx, vy, vz, m, (long long)n, ctx->red);
+  gc_launch(ctx, GK_DIAG, k_diag_particles, dim3(nb), dim3(256), 0, x, y, z, vx, vy, vz, m, (long long)n, ctx->red);
   GC_LAUNCH_CHECK(ctx, "diag particles");
   if ((s = gc_finalize(ctx, ctx->red, nb, 11, ctx->ddiag))) return s;
   GC_CUDA(ctx, cudaMemcpyAsync(out, ctx->ddiag, 11 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -655,7 +683,7 @@ int gc_dot_async(gc_ctx *ctx, const float *a, const float *b, size_t n, double *
   const int nb = 1024;
   int s = gc_ensure_red(ctx, nb);
   if (s) return s;
-  k_dot<<<nb, 256, 0, ctx->stream>>>(a, b, n, ctx->red);
+  gc_launch(ctx, GK_REDUCE, k_dot, dim3(nb), dim3(256), 0, a, b, n, ctx->red);
   GC_LAUNCH_CHECK(ctx, "dot");
   return gc_finalize(ctx, ctx->red, nb, 1, dst);
 }
@@ -706,7 +734,7 @@ extern "C" int gc_radial_histogram(gc_ctx *ctx, const float *x, const float *y, 
     GC_CUDA(ctx, cudaFuncSetAttribute(k_radial_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   unsigned nb = gc_blocks(n, 256);
   if (nb > 152u * 4u) nb = 152u * 4u;
-  k_radial_hist<<<nb, 256, smem, ctx->stream>>>(x, y, z, m, (long long)n, cx, cy, cz, inv_binw, nbins, hist);
+  gc_launch(ctx, GK_HIST, k_radial_hist, dim3(nb), dim3(256), smem, x, y, z, m, (long long)n, cx, cy, cz, inv_binw, nbins, hist);
   GC_LAUNCH_CHECK(ctx, "radial hist");
   return GC_OK;
 }

@@ -175,9 +175,9 @@ __global__ void __launch_bounds__(RS_THREADS)
 static int exclusive_scan(gc_ctx *ctx, unsigned *a, long long n) {
   const long long nt = (n + SC_TILE - 1) / SC_TILE;
   unsigned *sums = ctx->hist_aux;
-  k_scan_tile_sums<<<(unsigned)nt, SC_THREADS, 0, ctx->stream>>>(a, n, sums);
-  k_scan_sums<<<1, SC_THREADS, 0, ctx->stream>>>(sums, (int)nt);
-  k_scan_apply<<<(unsigned)nt, SC_THREADS, 0, ctx->stream>>>(a, n, sums);
+  gc_launch(ctx, GK_SORT, k_scan_tile_sums, dim3((unsigned)nt), dim3(SC_THREADS), 0, a, n, sums);
+  gc_launch(ctx, GK_SORT, k_scan_sums, dim3(1), dim3(SC_THREADS), 0, sums, (int)nt);
+  gc_launch(ctx, GK_SORT, k_scan_apply, dim3((unsigned)nt), dim3(SC_THREADS), 0, a, n, sums);
   GC_LAUNCH_CHECK(ctx, "scan");
   return GC_OK;
 }
@@ -211,10 +211,10 @@ int gc_radix_sort_pairs(gc_ctx *ctx, const uint32_t *keys_in, const uint32_t *va
       ko = (ko == ka) ? kb : ka;
       vo = (vo == va) ? vb : va;
     }
-    k_rs_hist<<<ntiles, RS_THREADS, 0, ctx->stream>>>(kin, (long long)n, shift, ctx->hist, ntiles);
+    gc_launch(ctx, GK_SORT, k_rs_hist, dim3(ntiles), dim3(RS_THREADS), 0, kin, (long long)n, shift, ctx->hist, ntiles);
     GC_LAUNCH_CHECK(ctx, "radix hist");
     if ((s = exclusive_scan(ctx, ctx->hist, (long long)hn))) return s;
-    k_rs_scatter<<<ntiles, RS_THREADS, 0, ctx->stream>>>(kin, vin, (long long)n, shift, ctx->hist, ntiles, ko, vo);
+    gc_launch(ctx, GK_SORT, k_rs_scatter, dim3(ntiles), dim3(RS_THREADS), 0, kin, vin, (long long)n, shift, ctx->hist, ntiles, ko, vo);
     GC_LAUNCH_CHECK(ctx, "radix scatter");
     kin = ko;
     vin = vo;
@@ -240,7 +240,7 @@ extern "C" int gc_cell_keys(gc_ctx *ctx, const float *x, const float *y, const f
              "grid too large for 32-bit cell keys");
   unsigned nb = gc_blocks(n, 256);
   if (nb > 152u * 32u) nb = 152u * 32u;
-  k_cell_keys<<<nb, 256, 0, ctx->stream>>>(x, y, z, (long long)n, (float)ctx->dx, ctx->G, keys, nullptr);
+  gc_launch(ctx, GK_KEYS, k_cell_keys, dim3(nb), dim3(256), 0, x, y, z, (long long)n, (float)ctx->dx, ctx->G, keys, nullptr);
   GC_LAUNCH_CHECK(ctx, "cell keys");
   return GC_OK;
 }
@@ -259,7 +259,7 @@ extern "C" int gc_sort_keys(gc_ctx *ctx, const uint32_t *keys, int64_t n, uint32
   if (s) return s;
   // values start as the identity in keys2's partner buffer
   uint32_t *iota = ctx->vals2;
-  k_iota<<<gc_blocks(n, 256) > 4096 ? 4096 : gc_blocks(n, 256), 256, 0, ctx->stream>>>(iota, (long long)n);
+  gc_launch(ctx, GK_KEYS, k_iota, dim3(gc_blocks(n, 256) > 4096 ? 4096 : gc_blocks(n, 256)), dim3(256), 0, iota, (long long)n);
   GC_LAUNCH_CHECK(ctx, "iota");
   uint32_t *ko, *vo;
   // full 32-bit keys: any caller key is sorted stably
@@ -288,7 +288,7 @@ extern "C" int gc_pm_sort(gc_ctx *ctx, const gc_particles *in, const gc_particle
   if (s) return s;
   unsigned nb = gc_blocks(n, 256);
   if (nb > 152u * 32u) nb = 152u * 32u;
-  k_cell_keys<<<nb, 256, 0, ctx->stream>>>(in->x, in->y, in->z, (long long)n, (float)ctx->dx, ctx->G, ctx->keys2,
+  gc_launch(ctx, GK_KEYS, k_cell_keys, dim3(nb), dim3(256), 0, in->x, in->y, in->z, (long long)n, (float)ctx->dx, ctx->G, ctx->keys2,
                                            ctx->vals2);
   GC_LAUNCH_CHECK(ctx, "cell keys");
   uint32_t *ko, *vo;
@@ -298,14 +298,14 @@ extern "C" int gc_pm_sort(gc_ctx *ctx, const gc_particles *in, const gc_particle
   for (int a = 0; a < 7; ++a) {
     if (!fin[a]) continue;
     GC_REQUIRE(ctx, fout[a] && fout[a] != fin[a], "gc_pm_sort: output array %d missing or aliases its input", a);
-    k_gather_perm<float><<<nb, 256, 0, ctx->stream>>>(fin[a], fout[a], vo, (long long)n);
+    gc_launch(ctx, GK_PERMUTE, k_gather_perm<float>, dim3(nb), dim3(256), 0, fin[a], fout[a], vo, (long long)n);
   }
   const int32_t *iin[2] = {in->gid, in->pid};
   int32_t *iout[2] = {out->gid, out->pid};
   for (int a = 0; a < 2; ++a) {
     if (!iin[a]) continue;
     GC_REQUIRE(ctx, iout[a] && iout[a] != iin[a], "gc_pm_sort: id array %d missing or aliases its input", a);
-    k_gather_perm<int32_t><<<nb, 256, 0, ctx->stream>>>(iin[a], iout[a], vo, (long long)n);
+    gc_launch(ctx, GK_PERMUTE, k_gather_perm<int32_t>, dim3(nb), dim3(256), 0, iin[a], iout[a], vo, (long long)n);
   }
   GC_LAUNCH_CHECK(ctx, "permute");
   return GC_OK;

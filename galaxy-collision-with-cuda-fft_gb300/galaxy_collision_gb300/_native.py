@@ -113,6 +113,12 @@ _PROTOS = {
     "gc_pm_step": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(StepParams), C.POINTER(StepStats)]),
     "gc_pm_potential": (_vp, [_ctxp]),
     "gc_pm_copy_potential": (C.c_int, [_ctxp, _vp]),
+    "gc_profile_enable": (C.c_int, [_ctxp, C.c_int]),
+    "gc_profile_reset": (C.c_int, [_ctxp]),
+    "gc_profile_read": (C.c_int, [_ctxp, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                  C.POINTER(C.c_double)]),
+    "gc_num_kernel_ids": (C.c_int, []),
+    "gc_kernel_name": (C.c_char_p, [C.c_int]),
 }
 
 EXPORTED = tuple(_PROTOS)
@@ -231,6 +237,25 @@ class Context:
         f = C.c_uint32()
         check(self._lib.gc_status(self._h, C.byref(f), int(clear)), self._h, "gc_status")
         return int(f.value)
+
+    def profile(self, enable: bool = True) -> None:
+        check(self._lib.gc_profile_enable(self._h, int(enable)), self._h, "profile")
+
+    def profile_reset(self) -> None:
+        self.bind_stream()
+        check(self._lib.gc_profile_reset(self._h), self._h, "profile reset")
+
+    def kernel_stats(self) -> dict:
+        """{kernel name: (launches, timed launches, total ms)} since the last reset."""
+        self.bind_stream()
+        out = {}
+        for kid in range(self._lib.gc_num_kernel_ids()):
+            n, t, ms = C.c_longlong(), C.c_longlong(), C.c_double()
+            check(self._lib.gc_profile_read(self._h, kid, C.byref(n), C.byref(t), C.byref(ms)), self._h, "profile")
+            name = self._lib.gc_kernel_name(kid).decode()
+            if n.value:
+                out[name] = (int(n.value), int(t.value), float(ms.value))
+        return out
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:

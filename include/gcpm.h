@@ -90,7 +90,7 @@ typedef struct gc_step_params {
   int warm_start;    /* reuse the previous potential (hi+lo) as the initial guess */
   int diagnostics;   /* 1: accumulate FP64 particle diagnostics at the synchronised time */
   gc_mg_params mg;
-  int fixed_point_bits; /* deposit quantum = 2^-bits of the total deposited mass (40..56) */
+  int fixed_point_bits; /* deposit quantum = 2^-bits of the total mass; 24 <= bits <= 62 - ceil(log2 G) */
   int reserved;
 } gc_step_params;
 
@@ -102,7 +102,7 @@ typedef struct gc_step_stats {
 
 /* ---- context ------------------------------------------------------------ */
 
-/* Create a context for a G^3 grid of node spacing dx and gravitational
+/* Create a context for a G^3 grid (2 <= G <= 1024) of node spacing dx and gravitational
  * constant grav. Allocates the multigrid hierarchy, the int64 mass grid and
  * reduction scratch on the current device. Replaces the per-solver state of
  * MultigridPoissonSolver.__init__ (solver/multigrid.py:301-360) and the grid
@@ -125,6 +125,7 @@ int gc_level_info(const gc_ctx *ctx, int level, int *n_nodes, int *last_interior
 /* Zero rho, then CIC-deposit m*w/dx^3 onto the G^3 nodes, dropping out-of-box
  * weight. Accumulates in int64 fixed point (quantum 2^-fixed_point_bits of the
  * total), so rho is bit-identical run to run whatever the particle order.
+ * fixed_point_bits must be in [24, 62 - ceil(log2 G)] (GC_ERR_ARG otherwise).
  * Replaces _deposit_cic / deposit_density (deposit.py:47-82, 177-182). */
 int gc_deposit_cic(gc_ctx *ctx, const float *x, const float *y, const float *z, const float *m,
                    int64_t n, int fixed_point_bits, float *rho);
@@ -223,6 +224,19 @@ int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp, gc_
 const float *gc_pm_potential(const gc_ctx *ctx);
 /* Stream-ordered copy of the current finest-level potential into phi (G^3 f32). */
 int gc_pm_copy_potential(gc_ctx *ctx, float *phi);
+
+/* ---- instrumentation (no kernel counterpart in the reference: it replaces the
+ * sync-bracketed per-stage wall clock of bench.py:66-73, 176-186) ---------- */
+
+/* Every launch is counted per kernel id; with profiling enabled each launch is
+ * also bracketed by CUDA events on the context's stream. */
+int gc_profile_enable(gc_ctx *ctx, int enable);
+int gc_profile_reset(gc_ctx *ctx);
+/* Launches, event-timed launches and their total milliseconds for kernel id kid
+ * since the last reset (synchronises when events are pending). */
+int gc_profile_read(gc_ctx *ctx, int kid, long long *launches, long long *timed, double *ms);
+int gc_num_kernel_ids(void);
+const char *gc_kernel_name(int kid);
 
 #ifdef __cplusplus
 }

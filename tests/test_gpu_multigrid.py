@@ -39,7 +39,7 @@ def test_level_geometry(cuda):
     assert [J for (_n, J, _p) in ctx.levels()] == [254, 127, 63, 31, 15, 7, 3, 1]
     assert [p for (_n, _J, p) in ctx.levels()][:3] == [255.0, 127.5, 63.75]
     ctx48 = _native.Context(48, 1.0, 1.0)
-    assert [J for (_n, J, _p) in ctx48.levels()] == [46, 23, 11, 5, 2]
+    assert [J for (_n, J, _p) in ctx48.levels()] == [46, 23, 11, 5, 2, 1]
 
 
 @pytest.mark.parametrize("n,dx,center", [(16, 1.0, None), (33, 0.5, (7.0, 8.5, 9.0)), (48, 2.0, (40.0, 50.0, 44.0)),
@@ -67,6 +67,25 @@ def test_residual_target_reached_in_fp64(cuda):
     # limited by f32 storage, the double-float pair is not
     rn, bn = pm.residual64(rho, phi.to_numpy().astype(np.float64), 1.0, 1.0)
     assert rn / bn < 1e-3
+
+
+@pytest.mark.parametrize("n,dx", [(32, 1.0), (64, 0.375), (100, 2.0)])
+def test_residual_norms_match_numpy(cuda, n, dx):
+    """With zero V-cycles the iterate is the multipole faces and a zero interior;
+    both residual norms the solver reports must equal an FP64 evaluation."""
+    rho = gaussian_rho(n, dx, 3.0 * dx, 2.0, center=(0.4 * n * dx, 0.55 * n * dx, 0.5 * n * dx))
+    s, _, phi = _solve(rho, dx, 1.0, n_cycles=0, tol=0.0)
+    p0 = dst.multipole_faces64(rho, dx, 1.0)
+    p0[1:-1, 1:-1, 1:-1] = 0.0
+    np.testing.assert_allclose(phi.to_numpy(), p0.astype(np.float32), rtol=2e-6, atol=1e-7 * np.abs(p0).max())
+    b = (np.float32(4.0 * np.pi) * rho).astype(np.float64)
+    lap = (p0[2:, 1:-1, 1:-1] + p0[:-2, 1:-1, 1:-1] + p0[1:-1, 2:, 1:-1] + p0[1:-1, :-2, 1:-1]
+           + p0[1:-1, 1:-1, 2:] + p0[1:-1, 1:-1, :-2] - 6.0 * p0[1:-1, 1:-1, 1:-1]) / dx**2
+    r = b[1:-1, 1:-1, 1:-1] - lap
+    rn, bn = float(np.sqrt((r**2).sum())), float(np.sqrt((b**2).sum()))
+    assert s.last_stats["rhs_norm"] == pytest.approx(bn, rel=1e-5)
+    assert s.last_stats["res_norm"] == pytest.approx(rn, rel=1e-4)
+    assert s.residual_norm() == pytest.approx(rn, rel=1e-4)
 
 
 def test_convergence_factor_per_vcycle(cuda):

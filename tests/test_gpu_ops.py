@@ -103,7 +103,7 @@ def test_pm_sort_permutes_all_arrays(cuda):
     np.testing.assert_array_equal(cur["gid"], gid[perm])
 
 
-@pytest.mark.parametrize("G,dx,bits", [(16, 1.0, 52), (48, 0.375, 52), (64, 2.5, 40), (33, 1.0, 60)])
+@pytest.mark.parametrize("G,dx,bits", [(16, 1.0, 52), (48, 0.375, 52), (64, 2.5, 40), (33, 1.0, 56)])
 def test_deposit_bit_exact_vs_fixed_point_oracle(cuda, G, dx, bits):
     from galaxy_collision_gb300.data import Field
     from galaxy_collision_gb300.deposit import deposit_density
@@ -165,6 +165,15 @@ def test_deposit_order_independent_and_reproducible(cuda):
         out.append(rho.to_numpy())
     np.testing.assert_array_equal(out[0], out[1])
     np.testing.assert_array_equal(out[0], out[2])
+
+
+def test_fixed_point_bits_limit_is_enforced(cuda):
+    from galaxy_collision_gb300.data import Field
+    from galaxy_collision_gb300.deposit import deposit_density
+
+    G = 33  # (G-1) * 2^bits must stay below 2^62 for the exact moment sums: bits <= 56
+    with pytest.raises(ValueError, match="fixed_point_bits"):
+        deposit_density(_parts([[4.0, 4.0, 4.0]], [1.0]), Field((G, G, G)), 1.0, fixed_point_bits=57)
 
 
 def test_nonfinite_position_flagged_and_skipped(cuda):
