@@ -187,6 +187,13 @@ __device__ __forceinline__ bool gc_cell_of(float x, float y, float z, float dx, 
   return true;
 }
 
+// Parameters of the deposit kernels.
+struct DepCtx {
+  float dx;
+  float inv_vol;  // 1/(dx*dx*dx) in f32, as the reference (deposit.py:58)
+  int G;
+};
+
 // Is (x,y,z) finite? Used to raise GC_FLAG_NONFINITE_POS.
 __device__ __forceinline__ bool gc_finite3(float x, float y, float z) {
   return isfinite(x) && isfinite(y) && isfinite(z);

@@ -92,12 +92,6 @@ int gc_fixed_point_setup(gc_ctx *ctx, const float *m, int64_t n, int bits, int m
 // ------------------------------------------------------------------------------
 // deposit (deposit.py:47-82)
 // ------------------------------------------------------------------------------
-struct DepCtx {
-  float dx;
-  float inv_vol;  // 1/(dx*dx*dx) in f32, as the reference (deposit.py:58)
-  int G;
-};
-
 // Per-corner int64 contributions of one particle; corners outside the box are 0.
 // Returns false when the particle deposits nothing.
 __device__ __forceinline__ bool cic_contrib(float x, float y, float z, float mass, const DepCtx &d, float qscale,

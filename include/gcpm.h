@@ -130,6 +130,22 @@ int gc_level_info(const gc_ctx *ctx, int level, int *n_nodes, int *last_interior
 int gc_deposit_cic(gc_ctx *ctx, const float *x, const float *y, const float *z, const float *m,
                    int64_t n, int fixed_point_bits, float *rho);
 
+/* Allocation-free variant of gc_deposit_cic, with no counterpart in the
+ * reference. For callers that cannot allocate device memory where they need a
+ * density (a memory pool that already owns the device, a loop that must not take
+ * cudaMalloc's device-wide synchronisation, or no context object to own
+ * scratch): it needs no gc_ctx and calls no allocating routine. Its int64 mass
+ * grid and reduction scratch are one file-scope device array (about 2.2 MiB per
+ * GPU that loads the library, held until exit), so grid_size is limited to
+ * [2, 64]; larger grids are rejected with GC_ERR_ARG. The first call on each
+ * device looks the array's address up (make it before any stream capture);
+ * every call clears the part it needs. All calls share the array: calls whose
+ * work overlaps on the GPU race and must be serialised by the caller. On failure
+ * the message is gc_last_error(NULL). Same result, bit for bit, as
+ * gc_deposit_cic with the same fixed_point_bits. */
+int gc_deposit_cic_noalloc(const float *x, const float *y, const float *z, const float *m, int64_t n,
+                           int grid_size, double dx, int fixed_point_bits, float *rho, void *stream);
+
 /* g = -grad(phi) at every node: central differences inside, one-sided on faces.
  * Replaces _potential_to_accel / potential_to_accel (deposit.py:132-174, 204-207). */
 int gc_potential_to_accel(gc_ctx *ctx, const float *phi, float *ax, float *ay, float *az);
