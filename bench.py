@@ -48,9 +48,11 @@ L2_BYTES = 126 * 1024**2
 # Algorithmic bytes per unit (per particle, or per finest cell) for each kernel.
 ALGO_BYTES = {
     "gather_kick_drift": ("particle", 48.0),  # read x,y,z,vx,vy,vz; write them back
+    "grad": ("cell", 20.0),                   # read phi, write the float4 node field
     "deposit_runs": ("particle", 16.0),       # read x,y,z,m
     "deposit": ("particle", 16.0),
     "smooth0": ("cell", 10.0),                # one colour: half of (read hi,lo,b + write hi,lo)
+    "sweep0": ("cell", 20.0),                 # one full sweep: read hi,lo,b + write hi,lo
     "convert_q": ("cell", 20.0),              # read q, clear q, write b
     "resid0": ("cell", 14.0),                 # read hi,lo,b; write r (restriction launches)
     "prolong0": ("cell", 16.0),               # read/write hi,lo
@@ -70,6 +72,12 @@ def _parse(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget-s", type=float, default=25.0)
     ap.add_argument("--profile-steps", type=int, default=3)
+    ap.add_argument("--grad-grid", type=int, default=1,
+                    help="1: gather from a float4 -grad(phi) grid; 0: form the gradient at the corners on the fly")
+    ap.add_argument("--plain-steps", type=int, default=5,
+                    help="steps of the stepwise (unfused) chain timed for comparison; 0 skips it")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the potential/force error against the FP64 FFT and the converged multigrid")
     ap.add_argument("--verbose", action="store_true")
     return ap.parse_args(argv)
 
@@ -256,6 +264,7 @@ def run_ours(args):
 
         dist.init_process_group(backend="nccl", device_id=torch.device("cuda", local))
     from galaxy_collision_gb300 import _build, ic
+    from galaxy_collision_gb300.accuracy import force_chain_errors
     from galaxy_collision_gb300.engine import PMEngine
 
     _build.build()
@@ -270,7 +279,7 @@ def run_ours(args):
 
     def make_engine():
         return PMEngine(G, dx, grav=1.0, origin=cfg["origin"], tol=args.tol, max_cycles=60, fixed_point_bits=bits,
-                        sort_every=20)
+                        sort_every=20, grad_grid=bool(args.grad_grid))
 
     eng = make_engine()
     eng.load(icr.pos, icr.vel, icr.mass, icr.gid, sort=True)
@@ -335,10 +344,24 @@ def run_ours(args):
         line["kernel_share"] = {k: round(v[2] / tot, 4) for k, v in sorted(stats.items(), key=lambda kv: -kv[1][2])}
         line["roofline"] = _roofline(stats, n, G, hbm, _load_traffic())
         poisson_ms = sum(v[2] for k, v in stats.items() if k in (
-            "smooth0", "resid0", "restrict", "smooth", "resid", "prolong", "prolong0", "tail", "faces", "reduce",
+            "smooth0", "sweep0", "resid0", "restrict", "smooth", "resid", "prolong", "prolong0", "tail", "faces", "reduce",
             "convert_q")) / args.profile_steps
         line["poisson"]["ms_per_solve"] = round(poisson_ms, 4)
 
+        if not args.no_accuracy:
+            eng.synchronize(dt)
+            acc = force_chain_errors(eng)
+            line["accuracy"] = {k: (round(v, 9) if isinstance(v, float) else v) for k, v in acc.items()}
+            line["accuracy"]["note"] = ("relative L2 over the grid (phi) and over all particles and components "
+                                        "(CIC-gathered -grad phi) of the engine's synchronised state after the "
+                                        "timed and profiled steps, against the FP64 zero-padded FFT of the same "
+                                        "density and against the multigrid converged to 1e-10")
+        del eng
+        torch.cuda.empty_cache()
+        if args.plain_steps > 0:
+            line["plain_chain"] = _plain_chain(icr, cfg, args.tol, args.plain_steps, min(args.warmup, 3))
+            line["plain_chain"]["fused_speedup"] = round(line["plain_chain"]["ms_per_step"] /
+                                                         line["ms_per_step"], 3)
         if not args.no_e2e:
             line["e2e"] = _e2e(args, icr, make_engine, dt)
         if not args.no_cpu_baseline and world == 1:
@@ -354,6 +377,69 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def _plain_chain(icr, cfg, tol, steps, warmup):
+    """The reference's stepwise chain on this GPU through the package's drop-in API:
+    per force evaluation deposit_density, MultigridPoissonSolver.solve (warm start
+    from the previous potential), potential_to_accel into three node grids and
+    gather_acceleration into per-particle arrays; kdk_step's kick/drift/kick as
+    separate launches (sim.py:320-327, integrator.py:100-131). Same kernels,
+    fixed-point quantum and solver tolerance as the fused engine; what differs is
+    the fusion, so the ratio is what the fused step buys."""
+    import torch
+    from galaxy_collision_gb300.data import Field, GridState, ParticleState
+    from galaxy_collision_gb300.deposit import deposit_density, gather_acceleration, potential_to_accel
+    from galaxy_collision_gb300.integrator import kdk_step
+    from galaxy_collision_gb300.solver import make_solver
+
+    G, dx, dt = cfg["grid"], cfg["dx"], cfg["dt"]
+    bits = cfg.get("fixed_point_bits", 52)
+    n = icr.n
+    parts = ParticleState(n)
+    pos = torch.from_numpy(icr.pos).cuda().to(torch.float64) - torch.tensor(cfg["origin"], dtype=torch.float64,
+                                                                              device="cuda")
+    vel = torch.from_numpy(icr.vel).cuda()
+    for i, f in enumerate((parts.pos_x, parts.pos_y, parts.pos_z)):
+        f.tensor.copy_(pos[:, i].to(torch.float32))
+    for i, f in enumerate((parts.vel_x, parts.vel_y, parts.vel_z)):
+        f.tensor.copy_(vel[:, i])
+    parts.mass.tensor.copy_(torch.from_numpy(icr.mass).cuda())
+    del pos, vel
+    grid = GridState(G)
+    acc = [Field(n) for _ in range(3)]
+    solver = make_solver("multigrid", G, dx=dx, grav_constant=1.0, tol=tol, n_cycles=60)
+    warm = {"on": False}
+    cycles = []
+
+    def accel_fn():
+        deposit_density(parts, grid.rho, dx, fixed_point_bits=bits)
+        solver.solve(grid.rho, grid.phi, warm_start=warm["on"])
+        warm["on"] = True
+        cycles.append(solver.last_cycles)
+        potential_to_accel(grid.phi, grid.ax, grid.ay, grid.az, dx)
+        gather_acceleration(parts, grid.ax, grid.ay, grid.az, *acc, dx)
+
+    accel_fn()
+    for _ in range(warmup):
+        kdk_step(parts, *acc, accel_fn, dt)
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    cycles.clear()
+    ev0.record(stream)
+    for _ in range(steps):
+        kdk_step(parts, *acc, accel_fn, dt)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    out = {"value": n / (ms / 1e3), "unit": UNIT, "ms_per_step": round(ms, 4), "steps": steps,
+           "mean_vcycles": float(np.mean(cycles)),
+           "note": "stepwise chain through deposit_density / MultigridPoissonSolver.solve(warm_start) / "
+                   "potential_to_accel / gather_acceleration / kdk_step on this GPU, same solver tolerance"}
+    del parts, grid, acc, solver
+    torch.cuda.empty_cache()
+    return out
 
 
 def _e2e(args, icr, make_engine, dt):

@@ -44,7 +44,7 @@ enum gc_kernel_id {
   GK_DEPOSIT = 0, GK_DEPOSIT_RUNS, GK_CONVERT_Q, GK_MASS, GK_SMOOTH0, GK_RESID0, GK_RESTRICT, GK_SMOOTH,
   GK_RESID, GK_PROLONG, GK_PROLONG0, GK_TAIL, GK_FACES, GK_MOMENTS, GK_RHS, GK_REDUCE, GK_GATHER_KD,
   GK_GRAD, GK_GATHER, GK_AXPY, GK_KEYS, GK_SORT, GK_PERMUTE, GK_DIAG, GK_HIST, GK_RESID64, GK_COPY,
-  GK_COUNT
+  GK_SWEEP0, GK_PROJECT, GK_COUNT
 };
 extern const char *const gc_kernel_names[GK_COUNT];
 
@@ -72,14 +72,16 @@ struct gc_ctx {
   int tail;             // first level handled by the single-CTA tail kernel (== nlev if none)
   LevelGeom lev[GC_MAX_LEVELS];
 
-  // finest level: double-float potential, h^2-scaled right-hand side, residual scratch
-  float *hi, *lo, *b0, *r0;
+  // finest level: double-float potential (current hi/lo and the ping-pong
+  // buffers hi2/lo2 of the streaming sweep), h^2-scaled right-hand side, residual scratch
+  float *hi, *lo, *hi2, *lo2, *b0, *r0;
   // coarse levels (index >= 1): correction e and h^2-scaled right-hand side b
   float *e[GC_MAX_LEVELS];
   float *b[GC_MAX_LEVELS];
   float *rc;            // residual scratch for coarse levels (sized for level 1)
 
   long long *q;         // int64 fixed-point mass grid (G^3)
+  void *g4;             // float4 node field -grad(phi) (G^3), allocated on first use
   double *red;          // reduction scratch (block partials)
   size_t red_cap;       // doubles in red
   double *dmom;         // 10 moments
@@ -194,6 +196,58 @@ struct DepCtx {
   int G;
 };
 
+// ---- exact int64 <-> f32 conversions in integer arithmetic --------------------
+// cvt between f32 and 64-bit integers issues on the FP64 pipe, a small fraction
+// of the FP32 rate on this part; these give the same results (round to nearest
+// even) from the float bits and a leading-zero count, on the integer ALUs.
+__device__ __forceinline__ long long f32_to_i64_rn(float v) {
+  const unsigned u = __float_as_uint(v);
+  int ex = (int)((u >> 23) & 0xffu);
+  const unsigned mant = (u & 0x7fffffu) | (ex ? 0x800000u : 0u);
+  if (ex == 0) ex = 1;
+  const int sh = ex - 150;  // |v| = mant * 2^sh
+  long long r;
+  if (sh >= 0) {
+    r = (long long)((unsigned long long)mant << sh);  // callers keep |v| < 2^62
+  } else if (sh < -25) {
+    r = 0;  // |v| < 0.25
+  } else {
+    const int rs = -sh;
+    const unsigned long long m = mant;
+    unsigned long long q = m >> rs;
+    const unsigned long long rem = m & ((1ull << rs) - 1ull);
+    const unsigned long long half = 1ull << (rs - 1);
+    if (rem > half || (rem == half && (q & 1ull))) q += 1ull;
+    r = (long long)q;
+  }
+  return (u >> 31) ? -r : r;
+}
+
+__device__ __forceinline__ float i64_to_f32_rn(long long q) {
+  if (q == 0) return 0.0f;
+  const unsigned long long a = q < 0 ? (0ull - (unsigned long long)q) : (unsigned long long)q;
+  int msb = 63 - __clzll((long long)a);
+  unsigned bits;
+  if (msb <= 23) {
+    bits = ((unsigned)(msb + 127) << 23) | ((unsigned)(a << (23 - msb)) & 0x7fffffu);
+  } else {
+    const int rs = msb - 23;
+    unsigned long long m = a >> rs;
+    const unsigned long long rem = a & ((1ull << rs) - 1ull);
+    const unsigned long long half = 1ull << (rs - 1);
+    if (rem > half || (rem == half && (m & 1ull))) {
+      m += 1ull;
+      if (m == (1ull << 24)) {
+        m >>= 1;
+        msb += 1;
+      }
+    }
+    bits = ((unsigned)(msb + 127) << 23) | ((unsigned)m & 0x7fffffu);
+  }
+  if (q < 0) bits |= 0x80000000u;
+  return __uint_as_float(bits);
+}
+
 // Is (x,y,z) finite? Used to raise GC_FLAG_NONFINITE_POS.
 __device__ __forceinline__ bool gc_finite3(float x, float y, float z) {
   return isfinite(x) && isfinite(y) && isfinite(z);
@@ -272,8 +326,8 @@ int gc_mg_check_params(gc_ctx *ctx, const gc_mg_params *p);
 int gc_max_fixed_point_bits(const gc_ctx *ctx);
 // Fused gather(-grad phi of ctx->hi) + kicks + drift over p (mode: gc_step_mode).
 // With diag, writes nparts rows of 11 FP64 partials into ctx->red.
-int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode, int diag, float *axo, float *ayo,
-                         float *azo, int *nparts_out);
+int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode, int diag, int grad_grid,
+                         float *axo, float *ayo, float *azo, int *nparts_out);
 // dst = sum a*b in FP64 (async).
 int gc_dot_async(gc_ctx *ctx, const float *a, const float *b, size_t n, double *dst);
 // Stable LSD radix sort of (keys, vals) pairs on the low `bits` bits; results in

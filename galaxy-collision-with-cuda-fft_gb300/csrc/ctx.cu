@@ -8,7 +8,8 @@ static char g_create_err[512] = "";
 const char *const gc_kernel_names[GK_COUNT] = {
     "deposit", "deposit_runs", "convert_q", "mass_setup", "smooth0", "resid0", "restrict", "smooth",
     "resid", "prolong", "prolong0", "tail", "faces", "moments", "rhs", "reduce", "gather_kick_drift",
-    "grad", "gather", "axpy", "cell_keys", "radix_sort", "permute", "diag", "radial_hist", "resid64", "copy"};
+    "grad", "gather", "axpy", "cell_keys", "radix_sort", "permute", "diag", "radial_hist", "resid64", "copy",
+    "sweep0", "project_ngp"};
 
 int gc_prof_slot(gc_ctx *ctx, int kid) {
   gc_profiler &p = ctx->prof;
@@ -192,6 +193,7 @@ extern "C" int gc_ctx_destroy(gc_ctx *ctx) {
   cudaStreamSynchronize(ctx->stream);
   gc_mg_free(ctx);
   cudaFree(ctx->q);
+  cudaFree(ctx->g4);
   cudaFree(ctx->red);
   cudaFree(ctx->dmom);
   cudaFree(ctx->dsmall);
@@ -239,6 +241,6 @@ extern "C" void gc_mg_default_params(gc_mg_params *p) {
   p->coarse_sweeps = 40;
   p->max_cycles = 20;
   p->min_cycles = 1;
-  p->reserved = 0;
+  p->flags = 0;
   p->tol = 1e-3;
 }

@@ -48,7 +48,8 @@ extern "C" int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_para
   if ((s = gc_mg_run(ctx, &sp->mg, &mst))) return s;
   // 4. particle pass
   int nparts = 0;
-  if ((s = gc_gather_kick_drift(ctx, p, sp->dt, sp->mode, sp->diagnostics, nullptr, nullptr, nullptr, &nparts)))
+  if ((s = gc_gather_kick_drift(ctx, p, sp->dt, sp->mode, sp->diagnostics, (sp->flags & GC_STEP_GRAD_GRID) != 0,
+                                nullptr, nullptr, nullptr, &nparts)))
     return s;
   if (sp->diagnostics) {
     if ((s = gc_finalize(ctx, ctx->red, nparts, 11, ctx->ddiag))) return s;

@@ -88,6 +88,10 @@ int gc_mg_alloc(gc_ctx *ctx) {
   const size_t g3 = G * G * G;
   GC_CUDA(ctx, cudaMalloc(&ctx->hi, g3 * sizeof(float)));
   GC_CUDA(ctx, cudaMalloc(&ctx->lo, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMalloc(&ctx->hi2, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMalloc(&ctx->lo2, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMemset(ctx->hi2, 0, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMemset(ctx->lo2, 0, g3 * sizeof(float)));
   GC_CUDA(ctx, cudaMalloc(&ctx->b0, g3 * sizeof(float)));
   GC_CUDA(ctx, cudaMalloc(&ctx->r0, g3 * sizeof(float)));
   GC_CUDA(ctx, cudaMemset(ctx->hi, 0, g3 * sizeof(float)));
@@ -111,13 +115,14 @@ int gc_mg_alloc(gc_ctx *ctx) {
 }
 
 void gc_mg_free(gc_ctx *ctx) {
-  cudaFree(ctx->hi); cudaFree(ctx->lo); cudaFree(ctx->b0); cudaFree(ctx->r0);
+  cudaFree(ctx->hi); cudaFree(ctx->lo); cudaFree(ctx->hi2); cudaFree(ctx->lo2);
+  cudaFree(ctx->b0); cudaFree(ctx->r0);
   for (int l = 1; l < GC_MAX_LEVELS; ++l) {
     cudaFree(ctx->e[l]); cudaFree(ctx->b[l]);
     ctx->e[l] = ctx->b[l] = nullptr;
   }
   cudaFree(ctx->rc);
-  ctx->hi = ctx->lo = ctx->b0 = ctx->r0 = ctx->rc = nullptr;
+  ctx->hi = ctx->lo = ctx->hi2 = ctx->lo2 = ctx->b0 = ctx->r0 = ctx->rc = nullptr;
 }
 
 // ------------------------------------------------------------------------------
@@ -415,6 +420,136 @@ __global__ void __launch_bounds__(256)
 }
 
 // ------------------------------------------------------------------------------
+// finest level, fused: one red-black sweep per pass, streamed along i
+// ------------------------------------------------------------------------------
+// A CTA owns a SW_TJ x SW_TK tile of (j,k) columns and a chunk of i planes. It
+// streams the planes through a 4-slot shared-memory ring (hi, lo, b with a halo
+// of 2 in j and k): after loading plane p it relaxes the red nodes of plane p-1
+// on the tile plus a 1-node halo (from old black values only) and then the black
+// nodes of plane p-2 on the tile (from the new red values), and stores plane p-2.
+// Reading from one potential buffer and writing to the other keeps every CTA on
+// old values outside its own tile, so the result is exactly the two in-place
+// half-sweeps of k_smooth0, with each datum read and written once per sweep.
+// With `corr` set, the level-1 correction is prolongated into every loaded node
+// first (the prolongation kernel fused into the first post-smoothing sweep).
+#define SW_TJ 16
+#define SW_TK 32
+#define SW_H 2
+#define SW_EJ (SW_TJ + 2 * SW_H)
+#define SW_EK (SW_TK + 2 * SW_H)
+#define SW_THREADS 256
+
+struct SweepSmem {
+  float hi[4][SW_EJ][SW_EK];
+  float lo[4][SW_EJ][SW_EK];
+  float b[4][SW_EJ][SW_EK];
+};
+
+// The red-black Gauss-Seidel update of one node from the ring (same arithmetic
+// order as df_residual + k_smooth0).
+__device__ __forceinline__ void sw_update(SweepSmem &S, int sm, int sc, int sp, int jj, int kk) {
+  const float hc = S.hi[sc][jj][kk];
+  const float d0 = __fsub_rn(S.hi[sp][jj][kk], hc);
+  const float d1 = __fsub_rn(S.hi[sm][jj][kk], hc);
+  const float d2 = __fsub_rn(S.hi[sc][jj + 1][kk], hc);
+  const float d3 = __fsub_rn(S.hi[sc][jj - 1][kk], hc);
+  const float d4 = __fsub_rn(S.hi[sc][jj][kk + 1], hc);
+  const float d5 = __fsub_rn(S.hi[sc][jj][kk - 1], hc);
+  float s, e, t;
+  df_two_sum(d0, d1, s, e);
+  df_two_sum(s, d2, s, t); e = __fadd_rn(e, t);
+  df_two_sum(s, d3, s, t); e = __fadd_rn(e, t);
+  df_two_sum(s, d4, s, t); e = __fadd_rn(e, t);
+  df_two_sum(s, d5, s, t); e = __fadd_rn(e, t);
+  const float lc = S.lo[sc][jj][kk];
+  const float ln = ((((S.lo[sp][jj][kk] + S.lo[sm][jj][kk]) + S.lo[sc][jj + 1][kk]) + S.lo[sc][jj - 1][kk]) +
+                    S.lo[sc][jj][kk + 1]) + S.lo[sc][jj][kk - 1];
+  const float ll = __fsub_rn(ln, __fmul_rn(6.0f, lc));
+  float r1, r1e;
+  df_two_sum(S.b[sc][jj][kk], -s, r1, r1e);
+  const float r = __fadd_rn(r1, __fsub_rn(r1e, __fadd_rn(e, ll)));
+  const float delta = __fmul_rn(r, -0.16666667f);
+  float s2, e2, h3, l3;
+  df_two_sum(hc, delta, s2, e2);
+  const float lnew = __fadd_rn(lc, e2);
+  df_fast_two_sum(s2, lnew, h3, l3);
+  S.hi[sc][jj][kk] = h3;
+  S.lo[sc][jj][kk] = l3;
+}
+
+__global__ void __launch_bounds__(SW_THREADS)
+    k_sweep0(const float *__restrict__ hi_in, const float *__restrict__ lo_in, const float *__restrict__ b,
+             float *__restrict__ hi_out, float *__restrict__ lo_out, int G, int chunk,
+             const float *__restrict__ corr, LevelGeom gc, LevelGeom gf) {
+  extern __shared__ __align__(16) unsigned char sw_raw[];
+  SweepSmem &S = *reinterpret_cast<SweepSmem *>(sw_raw);
+  const int tid = threadIdx.x;
+  const int j0 = 1 + blockIdx.y * SW_TJ;
+  const int k0 = 1 + blockIdx.x * SW_TK;
+  const int i0 = 1 + blockIdx.z * chunk;
+  const int i1 = min(i0 + chunk, G - 1);  // planes [i0, i1) are relaxed and stored
+  const size_t sj = (size_t)G, si = (size_t)G * G;
+  for (int p = i0 - 2; p <= i1 + 1; ++p) {
+    const int s = (p + 4) & 3;
+    for (int t = tid; t < SW_EJ * SW_EK; t += SW_THREADS) {
+      const int jj = t / SW_EK, kk = t - jj * SW_EK;
+      const int j = j0 - SW_H + jj, k = k0 - SW_H + kk;
+      float h = 0.f, l = 0.f, bb = 0.f;
+      if (p >= 0 && p < G && j >= 0 && j < G && k >= 0 && k < G) {
+        const size_t c = (size_t)p * si + (size_t)j * sj + k;
+        h = hi_in[c];
+        l = lo_in[c];
+        bb = b[c];
+        if (corr && p >= 1 && p <= G - 2 && j >= 1 && j <= G - 2 && k >= 1 && k <= G - 2) {
+          const float v = prolong_value(corr, p, j, k, gf, gc);
+          float s1, e1, h1, l1;
+          df_two_sum(h, v, s1, e1);
+          const float ln1 = __fadd_rn(l, e1);
+          df_fast_two_sum(s1, ln1, h1, l1);
+          h = h1;
+          l = l1;
+        }
+      }
+      S.hi[s][jj][kk] = h;
+      S.lo[s][jj][kk] = l;
+      S.b[s][jj][kk] = bb;
+    }
+    __syncthreads();
+    const int q = p - 1;  // red on plane q, tile + 1 halo
+    if (q >= i0 - 1 && q <= i1 && q >= 1 && q <= G - 2) {
+      const int sc = (q + 4) & 3, sm = (q + 3) & 3, sp = (q + 5) & 3;
+      for (int t = tid; t < (SW_EJ - 2) * (SW_EK - 2); t += SW_THREADS) {
+        const int jj = 1 + t / (SW_EK - 2), kk = 1 + t % (SW_EK - 2);
+        const int j = j0 - SW_H + jj, k = k0 - SW_H + kk;
+        if (((q + j + k) & 1) != 0 || j < 1 || j > G - 2 || k < 1 || k > G - 2) continue;
+        sw_update(S, sm, sc, sp, jj, kk);
+      }
+    }
+    __syncthreads();
+    const int r = p - 2;  // black on plane r, tile only; then store plane r
+    if (r >= i0 && r < i1) {
+      const int sc = (r + 4) & 3, sm = (r + 3) & 3, sp = (r + 5) & 3;
+      for (int t = tid; t < SW_TJ * SW_TK; t += SW_THREADS) {
+        const int jj = SW_H + t / SW_TK, kk = SW_H + t % SW_TK;
+        const int j = j0 - SW_H + jj, k = k0 - SW_H + kk;
+        if (((r + j + k) & 1) != 1 || j > G - 2 || k > G - 2) continue;
+        sw_update(S, sm, sc, sp, jj, kk);
+      }
+      __syncthreads();
+      for (int t = tid; t < SW_TJ * SW_TK; t += SW_THREADS) {
+        const int jj = SW_H + t / SW_TK, kk = SW_H + t % SW_TK;
+        const int j = j0 - SW_H + jj, k = k0 - SW_H + kk;
+        if (j > G - 2 || k > G - 2) continue;
+        const size_t c = (size_t)r * si + (size_t)j * sj + k;
+        hi_out[c] = S.hi[sc][jj][kk];
+        lo_out[c] = S.lo[sc][jj][kk];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------------
 // tail: all levels with n <= GC_TAIL_MAX_N relaxed by one CTA in shared memory
 // ------------------------------------------------------------------------------
 struct TailDesc {
@@ -511,7 +646,7 @@ __device__ void t_prolong(const T *ec, const LevelGeom &cg, float *ef, const Lev
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(512) k_tail(const float *__restrict__ b_in, float *__restrict__ e_out, TailDesc d) {
+__global__ void __launch_bounds__(1024) k_tail(const float *__restrict__ b_in, float *__restrict__ e_out, TailDesc d) {
   extern __shared__ __align__(16) unsigned char tsm[];
   float *E[GC_MAX_LEVELS], *B[GC_MAX_LEVELS], *R[GC_MAX_LEVELS];
   double *E64 = nullptr, *B64 = nullptr;
@@ -589,8 +724,8 @@ __global__ void __launch_bounds__(512) k_tail(const float *__restrict__ b_in, fl
 // ------------------------------------------------------------------------------
 // Multipole Dirichlet faces (multigrid.py:261-295) evaluated in FP64 from the raw
 // moments (multigrid.py:378-389), written as double-float pairs.
-__global__ void k_faces(float *__restrict__ hi, float *__restrict__ lo, int G, double dx, double grav,
-                        const double *__restrict__ mom) {
+__global__ void k_faces(float *__restrict__ hi, float *__restrict__ lo, float *__restrict__ hi2,
+                        float *__restrict__ lo2, int G, double dx, double grav, const double *__restrict__ mom) {
   const long long tot = 6LL * G * G;
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= tot) return;
@@ -623,8 +758,11 @@ __global__ void k_faces(float *__restrict__ hi, float *__restrict__ lo, int G, d
   }
   const size_t c = ((size_t)i * G + j) * G + k;
   const float h = (float)phi;
+  const float l = (float)(phi - (double)h);
   hi[c] = h;
-  lo[c] = (float)(phi - (double)h);
+  lo[c] = l;
+  hi2[c] = h;  // both buffers of the streaming sweep carry the faces
+  lo2[c] = l;
 }
 
 // Column moments of an f32 density: one warp per (i,j) column, Kahan-compensated
@@ -707,12 +845,40 @@ static dim3 rb_grid(const LevelGeom &g) {
 }
 static dim3 node_grid(const LevelGeom &g) { return dim3(gc_blocks(g.J, 32), gc_blocks(g.J, 8), (unsigned)g.J); }
 
-static int launch_smooth0(gc_ctx *ctx, int sweeps) {
+// Finest-level smoothing: `sweeps` red-black sweeps, the first one preceded by
+// the prolongation of the level-1 correction when `with_corr` is set. Default:
+// in-place red and black half-sweep kernels. GC_MG_FUSED_SWEEP streams each
+// sweep from (hi, lo) into (hi2, lo2) and swaps the buffers (same arithmetic).
+static int launch_smooth0(gc_ctx *ctx, int sweeps, int with_corr, int flags) {
   const LevelGeom &g = ctx->lev[0];
-  for (int s = 0; s < sweeps; ++s)
-    for (int color = 0; color < 2; ++color)
-      gc_launch(ctx, GK_SMOOTH0, k_smooth0, dim3(rb_grid(g)), dim3(dim3(RB_TX, RB_TY)), 0, ctx->hi, ctx->lo, ctx->b0, ctx->G, color);
-  GC_LAUNCH_CHECK(ctx, "smooth0");
+  const int G = ctx->G;
+  if (!(flags & GC_MG_FUSED_SWEEP) || sweeps == 0) {
+    if (with_corr) {
+      gc_launch(ctx, GK_PROLONG0, k_prolong0, dim3(node_grid(g)), dim3(dim3(32, 8)), 0, ctx->e[1], ctx->lev[1],
+                ctx->hi, ctx->lo, g);
+    }
+    for (int s = 0; s < sweeps; ++s)
+      for (int color = 0; color < 2; ++color)
+        gc_launch(ctx, GK_SMOOTH0, k_smooth0, dim3(rb_grid(g)), dim3(dim3(RB_TX, RB_TY)), 0, ctx->hi, ctx->lo,
+                  ctx->b0, ctx->G, color);
+    GC_LAUNCH_CHECK(ctx, "smooth0");
+    return GC_OK;
+  }
+  const int tk = (G - 2 + SW_TK - 1) / SW_TK, tj = (G - 2 + SW_TJ - 1) / SW_TJ;
+  int nchunks = (640 + tk * tj - 1) / (tk * tj);
+  const int max_chunks = (G - 2 + 7) / 8;
+  if (nchunks > max_chunks) nchunks = max_chunks;
+  if (nchunks < 1) nchunks = 1;
+  const int chunk = (G - 2 + nchunks - 1) / nchunks;
+  nchunks = (G - 2 + chunk - 1) / chunk;
+  for (int s = 0; s < sweeps; ++s) {
+    const float *corr = (with_corr && s == 0) ? ctx->e[1] : nullptr;
+    gc_launch(ctx, GK_SWEEP0, k_sweep0, dim3(tk, tj, nchunks), dim3(SW_THREADS), sizeof(SweepSmem), ctx->hi,
+              ctx->lo, ctx->b0, ctx->hi2, ctx->lo2, G, chunk, corr, ctx->nlev > 1 ? ctx->lev[1] : g, g);
+    float *t = ctx->hi; ctx->hi = ctx->hi2; ctx->hi2 = t;
+    t = ctx->lo; ctx->lo = ctx->lo2; ctx->lo2 = t;
+  }
+  GC_LAUNCH_CHECK(ctx, "sweep0");
   return GC_OK;
 }
 
@@ -731,15 +897,18 @@ static int launch_tail(gc_ctx *ctx, const gc_mg_params *p) {
   d.nl = ctx->nlev - ctx->tail;
   d.pre = p->pre_sweeps;
   d.post = p->post_sweeps;
-  d.coarse = p->coarse_sweeps;
   for (int l = 0; l < d.nl; ++l) d.g[l] = ctx->lev[ctx->tail + l];
+  // The coarsest level has at most 3^3 unknowns: a few FP64 Gauss-Seidel sweeps
+  // solve it far below the V-cycle's contraction (J = 1 is exact in one sweep).
+  const int Jc = d.g[d.nl - 1].J;
+  d.coarse = p->coarse_sweeps < 8 * Jc ? p->coarse_sweeps : 8 * Jc;
   const size_t smem = tail_smem_bytes(ctx);
   static int attr_set_for = -1;
   if (smem > 48 * 1024 && attr_set_for != (int)smem) {
     GC_CUDA(ctx, cudaFuncSetAttribute(k_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set_for = (int)smem;
   }
-  gc_launch(ctx, GK_TAIL, k_tail, dim3(1), dim3(512), smem, ctx->b[ctx->tail], ctx->e[ctx->tail], d);
+  gc_launch(ctx, GK_TAIL, k_tail, dim3(1), dim3(1024), smem, ctx->b[ctx->tail], ctx->e[ctx->tail], d);
   GC_LAUNCH_CHECK(ctx, "tail");
   return GC_OK;
 }
@@ -747,9 +916,9 @@ static int launch_tail(gc_ctx *ctx, const gc_mg_params *p) {
 static int vcycle(gc_ctx *ctx, const gc_mg_params *p) {
   const int L = ctx->nlev;
   if (L == 0) return GC_OK;
-  if (L == 1) return launch_smooth0(ctx, p->coarse_sweeps);
+  if (L == 1) return launch_smooth0(ctx, p->coarse_sweeps, 0, p->flags);
   int st;
-  if ((st = launch_smooth0(ctx, p->pre_sweeps))) return st;
+  if ((st = launch_smooth0(ctx, p->pre_sweeps, 0, p->flags))) return st;
   const LevelGeom &g0 = ctx->lev[0];
   gc_launch(ctx, GK_RESID0, k_resid0, dim3(node_grid(g0)), dim3(dim3(32, 8)), 0, ctx->hi, ctx->lo, ctx->b0, ctx->r0, nullptr, ctx->G);
   gc_launch(ctx, GK_RESTRICT, k_restrict, dim3(node_grid(ctx->lev[1])), dim3(dim3(32, 8)), 0, ctx->r0, g0, ctx->b[1], ctx->lev[1]);
@@ -771,9 +940,7 @@ static int vcycle(gc_ctx *ctx, const gc_mg_params *p) {
     GC_LAUNCH_CHECK(ctx, "prolong");
     if ((st = launch_smooth(ctx, l, p->post_sweeps))) return st;
   }
-  gc_launch(ctx, GK_PROLONG0, k_prolong0, dim3(node_grid(g0)), dim3(dim3(32, 8)), 0, ctx->e[1], ctx->lev[1], ctx->hi, ctx->lo, g0);
-  GC_LAUNCH_CHECK(ctx, "prolong0");
-  return launch_smooth0(ctx, p->post_sweeps);
+  return launch_smooth0(ctx, p->post_sweeps, 1, p->flags);
 }
 
 int gc_finalize(gc_ctx *ctx, const double *parts, int nparts, int nv, double *dst) {
@@ -818,7 +985,7 @@ int gc_norm_b(gc_ctx *ctx) {
 
 int gc_faces_from_moments(gc_ctx *ctx) {
   const long long tot = 6LL * ctx->G * ctx->G;
-  gc_launch(ctx, GK_FACES, k_faces, dim3(gc_blocks(tot, 256)), dim3(256), 0, ctx->hi, ctx->lo, ctx->G, ctx->dx, ctx->grav, ctx->dmom);
+  gc_launch(ctx, GK_FACES, k_faces, dim3(gc_blocks(tot, 256)), dim3(256), 0, ctx->hi, ctx->lo, ctx->hi2, ctx->lo2, ctx->G, ctx->dx, ctx->grav, ctx->dmom);
   GC_LAUNCH_CHECK(ctx, "faces");
   return GC_OK;
 }

@@ -39,11 +39,17 @@ __global__ void __launch_bounds__(256) k_mass_isum(const float *__restrict__ m, 
                                                    const unsigned *__restrict__ maxbits, int log2n,
                                                    unsigned long long *__restrict__ isum) {
   const int s = mass_shift(*maxbits, log2n);
-  const double scale = ldexp(1.0, s);
   unsigned long long acc = 0;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     const float mm = __fmul_rn(m[p], inv_vol);
-    if (isfinite(mm) && mm > 0.0f) acc += __double2ull_rz((double)mm * scale);
+    if (isfinite(mm) && mm > 0.0f) {  // floor(mm * 2^s) from the float bits (no FP64)
+      const unsigned u = __float_as_uint(mm);
+      int ex = (int)((u >> 23) & 0xffu);
+      const unsigned long long mant = (u & 0x7fffffu) | (ex ? 0x800000u : 0u);
+      if (ex == 0) ex = 1;
+      const int e2 = ex - 150 + s;
+      acc += e2 >= 0 ? (mant << e2) : (e2 > -64 ? (mant >> -e2) : 0ull);
+    }
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0 && acc) atomicAdd(isum, acc);
@@ -110,7 +116,7 @@ __device__ __forceinline__ bool cic_contrib(float x, float y, float z, float mas
         const int jx = c.ix + cx, jy = c.iy + cy, jz = c.iz + cz;
         const bool in = (unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G && (unsigned)jz < (unsigned)d.G;
         const float w = __fmul_rn(__fmul_rn(__fmul_rn(mm, wx[cx]), wy[cy]), wz[cz]);
-        q[(cx * 2 + cy) * 2 + cz] = in ? __float2ll_rn(__fmul_rn(w, qscale)) : 0LL;
+        q[(cx * 2 + cy) * 2 + cz] = in ? f32_to_i64_rn(__fmul_rn(w, qscale)) : 0LL;
       }
   return true;
 }
@@ -207,6 +213,33 @@ __global__ void __launch_bounds__(256)
         for (int t = 0; t < 8; ++t) q[t] = 0;
       }
       const unsigned key = ok ? (unsigned)(((c.ix + 1) * (d.G + 1) + (c.iy + 1)) * (d.G + 1) + (c.iz + 1)) : invalid;
+      // Fast path for the dense case: the whole warp is one cell and every
+      // contribution fits in 26 bits, so the 32 lanes' 8 corner sums are exact
+      // 32-bit warp reductions (redux.sync), merged into the carried run.
+      const unsigned key0 = __shfl_sync(0xffffffffu, key, 0);
+      bool small = true;
+#pragma unroll
+      for (int t = 0; t < 8; ++t) small = small && (q[t] < (1LL << 26)) && (q[t] > -(1LL << 26));
+      if (__all_sync(0xffffffffu, ok && key == key0 && small)) {
+        long long tot[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) tot[t] = (long long)__reduce_add_sync(0xffffffffu, (int)q[t]);
+        if (ckey != key) {  // previous run ends here
+          if (lane == 0 && ckey != 0xffffffffu) {
+            CellPos cc;
+            cc.ix = cix; cc.iy = ciy; cc.iz = ciz;
+            flush_corners(qg, cc, d.G, cq);
+          }
+          ckey = key;
+          cix = c.ix; ciy = c.iy; ciz = c.iz;
+#pragma unroll
+          for (int t = 0; t < 8; ++t) cq[t] = tot[t];
+        } else {
+#pragma unroll
+          for (int t = 0; t < 8; ++t) cq[t] += tot[t];
+        }
+        continue;
+      }
       // the carried run continues into lane 0, or is flushed by lane 0
       if (lane == 0 && ckey != 0xffffffffu) {
         if (key == ckey) {
@@ -280,8 +313,9 @@ int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, co
 __global__ void __launch_bounds__(256)
     k_convert_q(long long *__restrict__ qg, int G, double dx, const double *__restrict__ qexp, float *__restrict__ rho,
                 float *__restrict__ b, double bfac, double *__restrict__ parts) {
-  const int lane = threadIdx.x & 31;
-  const long long col = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+  __shared__ double wsum[8][11];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const long long col = (long long)blockIdx.x * 8 + wid;
   const int E = (int)(*qexp);
   const float qinv = ldexpf(1.0f, E);
   const float bscale = (float)(ldexp(1.0, E) * bfac);
@@ -291,22 +325,34 @@ __global__ void __launch_bounds__(256)
   if (col < (long long)G * G) {
     const int i = (int)(col / G), j = (int)(col % G);
     long long *p = qg + (size_t)col * G;
+    float *rp = rho ? rho + (size_t)col * G : nullptr;
+    float *bp = b ? b + (size_t)col * G : nullptr;
     long long S0 = 0, S1 = 0, S2h = 0;
     unsigned long long S2l = 0;
     float bb = 0.0f;
-    for (int k = lane; k < G; k += 32) {
-      const long long qv = p[k];
-      p[k] = 0;
-      const float qf = (float)qv;  // one rounding (cvt.rn)
-      if (rho) rho[(size_t)col * G + k] = __fmul_rn(qf, qinv);
-      const float bv = __fmul_rn(qf, bscale);
-      if (b) b[(size_t)col * G + k] = bv;
-      bb += bv * bv;
-      const long long kk = k;
-      S0 += qv;
-      S1 += qv * kk;
-      S2h += (qv >> 32) * (kk * kk);
-      S2l += (unsigned long long)(qv & 0xffffffffLL) * (unsigned long long)(kk * kk);
+    for (int k0 = 0; k0 < G; k0 += 32 * 8) {
+      long long qv[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {  // all loads of the lane in flight together
+        const int k = k0 + 32 * t + lane;
+        qv[t] = k < G ? p[k] : 0;
+      }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int k = k0 + 32 * t + lane;
+        if (k >= G) continue;
+        p[k] = 0;
+        const float qf = i64_to_f32_rn(qv[t]);  // one rounding, as (float)q
+        if (rp) rp[k] = __fmul_rn(qf, qinv);
+        const float bv = __fmul_rn(qf, bscale);
+        if (bp) bp[k] = bv;
+        bb += bv * bv;
+        const long long kk = k;
+        S0 += qv[t];
+        S1 += qv[t] * kk;
+        S2h += (qv[t] >> 32) * (kk * kk);
+        S2l += (unsigned long long)(qv[t] & 0xffffffffLL) * (unsigned long long)(kk * kk);
+      }
     }
     // exact integer warp sums (no FP64 per lane)
     for (int o = 16; o > 0; o >>= 1) {
@@ -327,7 +373,17 @@ __global__ void __launch_bounds__(256)
       v[10] = (double)bb;
     }
   }
-  block_partials<11>(v, parts + (size_t)blockIdx.x * 11);
+  // only lane 0 of each warp holds a column total: sum the 8 warps directly
+  if (lane == 0) {
+#pragma unroll
+    for (int t = 0; t < 11; ++t) wsum[wid][t] = v[t];
+  }
+  __syncthreads();
+  if (threadIdx.x < 11) {
+    double a = 0.0;
+    for (int w = 0; w < 8; ++w) a += wsum[w][threadIdx.x];
+    parts[(size_t)blockIdx.x * 11 + threadIdx.x] = a;
+  }
 }
 
 int gc_max_fixed_point_bits(const gc_ctx *ctx) {
@@ -545,6 +601,7 @@ __device__ __forceinline__ void gather_grad(const float *__restrict__ phi, float
       }
 }
 
+template <bool DIAG>
 __global__ void __launch_bounds__(256)
     k_gather_kick_drift(float *__restrict__ x, float *__restrict__ y, float *__restrict__ z, float *__restrict__ vx,
                         float *__restrict__ vy, float *__restrict__ vz, const float *__restrict__ m, long long n,
@@ -568,7 +625,7 @@ __global__ void __launch_bounds__(256)
       uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
       uz = __fadd_rn(uz, __fmul_rn(az, f.h));
     }
-    if (f.diag) {  // synchronised state (diagnostics_device.py:56-74)
+    if (DIAG) {  // synchronised state (diagnostics_device.py:56-74)
       const double mm = m[p];
       const double X = px, Y = py, Z = pz, VX = ux, VY = uy, VZ = uz;
       dv[0] += mm;
@@ -595,11 +652,102 @@ __global__ void __launch_bounds__(256)
     vy[p] = uy;
     vz[p] = uz;
   }
-  if (f.diag) block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
+  if (DIAG) block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
 }
 
-int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode, int diag, float *axo, float *ayo,
-                         float *azo, int *nparts_out) {
+// Variant with the node field g = -grad(phi) precomputed as float4 (x, y, z, 0):
+// one pass over phi writes it (k_grad4), then each particle reads its 8 corner
+// nodes with one 16-byte load each. Same arithmetic as gather_grad.
+__global__ void __launch_bounds__(256) k_grad4(const float *__restrict__ phi, float4 *__restrict__ g4, GradCtx g) {
+  const int k = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y;
+  const int i = blockIdx.z;
+  if (k >= g.G || j >= g.G) return;
+  const size_t G = g.G;
+  const size_t c = ((size_t)i * G + j) * G + k;
+  g4[c] = make_float4(grad_comp(phi, c, G * G, i, g.G, g.inv_dx, g.inv_2dx),
+                      grad_comp(phi, c, G, j, g.G, g.inv_dx, g.inv_2dx),
+                      grad_comp(phi, c, 1, k, g.G, g.inv_dx, g.inv_2dx), 0.0f);
+}
+
+__device__ __forceinline__ void gather_g4(const float4 *__restrict__ g4, float x, float y, float z, const FusedCtx &f,
+                                          float &ax, float &ay, float &az) {
+  ax = ay = az = 0.0f;
+  CellPos c;
+  if (!gc_cell_of(x, y, z, f.dx, f.G, c)) return;
+  const int G = f.G;
+  const float wx[2] = {__fsub_rn(1.0f, c.fx), c.fx};
+  const float wy[2] = {__fsub_rn(1.0f, c.fy), c.fy};
+  const float wz[2] = {__fsub_rn(1.0f, c.fz), c.fz};
+  const bool interior = c.ix >= 0 && c.iy >= 0 && c.iz >= 0 && c.ix + 1 < G && c.iy + 1 < G && c.iz + 1 < G;
+  const int base = (c.ix * G + c.iy) * G + c.iz;  // G^3 < 2^31 (G <= 1024)
+#pragma unroll
+  for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+      for (int cz = 0; cz < 2; ++cz) {
+        const int jx = c.ix + cx, jy = c.iy + cy, jz = c.iz + cz;
+        if (interior || ((unsigned)jx < (unsigned)G && (unsigned)jy < (unsigned)G && (unsigned)jz < (unsigned)G)) {
+          const float4 gv = __ldg(g4 + base + (cx * G + cy) * G + cz);
+          const float w = __fmul_rn(__fmul_rn(wx[cx], wy[cy]), wz[cz]);
+          ax = __fadd_rn(ax, __fmul_rn(w, gv.x));
+          ay = __fadd_rn(ay, __fmul_rn(w, gv.y));
+          az = __fadd_rn(az, __fmul_rn(w, gv.z));
+        }
+      }
+}
+
+template <bool DIAG>
+__global__ void __launch_bounds__(256)
+    k_gather4_kick_drift(float *__restrict__ x, float *__restrict__ y, float *__restrict__ z, float *__restrict__ vx,
+                         float *__restrict__ vy, float *__restrict__ vz, const float *__restrict__ m, long long n,
+                         const float4 *__restrict__ g4, FusedCtx f, double *__restrict__ parts) {
+  double dv[11];
+#pragma unroll
+  for (int t = 0; t < 11; ++t) dv[t] = 0.0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const float px = x[p], py = y[p], pz = z[p];
+    float ux = vx[p], uy = vy[p], uz = vz[p];
+    float ax, ay, az;
+    gather_g4(g4, px, py, pz, f, ax, ay, az);
+    if (f.mode != GC_STEP_PRIME) {
+      ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
+      uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
+      uz = __fadd_rn(uz, __fmul_rn(az, f.h));
+    }
+    if (DIAG) {
+      const double mm = m[p];
+      const double X = px, Y = py, Z = pz, VX = ux, VY = uy, VZ = uz;
+      dv[0] += mm;
+      dv[1] += 0.5 * mm * (VX * VX + VY * VY + VZ * VZ);
+      dv[2] += mm * VX;
+      dv[3] += mm * VY;
+      dv[4] += mm * VZ;
+      dv[5] += mm * (Y * VZ - Z * VY);
+      dv[6] += mm * (Z * VX - X * VZ);
+      dv[7] += mm * (X * VY - Y * VX);
+      dv[8] += mm * X;
+      dv[9] += mm * Y;
+      dv[10] += mm * Z;
+    }
+    if (f.mode != GC_STEP_CLOSE) {
+      ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
+      uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
+      uz = __fadd_rn(uz, __fmul_rn(az, f.h));
+      x[p] = __fadd_rn(px, __fmul_rn(ux, f.dt));
+      y[p] = __fadd_rn(py, __fmul_rn(uy, f.dt));
+      z[p] = __fadd_rn(pz, __fmul_rn(uz, f.dt));
+    }
+    vx[p] = ux;
+    vy[p] = uy;
+    vz[p] = uz;
+  }
+  if (DIAG) block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
+}
+
+int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode, int diag, int grad_grid,
+                         float *axo, float *ayo, float *azo, int *nparts_out) {
   FusedCtx f;
   f.dx = (float)ctx->dx;
   f.inv_dx = 1.0f / f.dx;
@@ -613,8 +761,25 @@ int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode,
   if (nb > 152u * 16u) nb = 152u * 16u;
   int s = gc_ensure_red(ctx, (size_t)nb * 11);
   if (s) return s;
-  gc_launch(ctx, GK_GATHER_KD, k_gather_kick_drift, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx, p->vy, p->vz, p->m, (long long)p->n,
-                                                   ctx->hi, f, axo, ayo, azo, ctx->red);
+  if (grad_grid && !axo) {
+    const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
+    if (!ctx->g4) GC_CUDA(ctx, cudaMalloc(&ctx->g4, g3 * sizeof(float4)));
+    const GradCtx g = make_grad(ctx);
+    gc_launch(ctx, GK_GRAD, k_grad4, dim3(gc_blocks(g.G, 32), gc_blocks(g.G, 8), g.G), dim3(32, 8), 0, ctx->hi,
+              (float4 *)ctx->g4, g);
+    if (diag)
+      gc_launch(ctx, GK_GATHER_KD, k_gather4_kick_drift<true>, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx,
+                p->vy, p->vz, p->m, (long long)p->n, (const float4 *)ctx->g4, f, ctx->red);
+    else
+      gc_launch(ctx, GK_GATHER_KD, k_gather4_kick_drift<false>, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx,
+                p->vy, p->vz, p->m, (long long)p->n, (const float4 *)ctx->g4, f, ctx->red);
+  } else if (diag) {
+    gc_launch(ctx, GK_GATHER_KD, k_gather_kick_drift<true>, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx, p->vy,
+              p->vz, p->m, (long long)p->n, ctx->hi, f, axo, ayo, azo, ctx->red);
+  } else {
+    gc_launch(ctx, GK_GATHER_KD, k_gather_kick_drift<false>, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx, p->vy,
+              p->vz, p->m, (long long)p->n, ctx->hi, f, axo, ayo, azo, ctx->red);
+  }
   GC_LAUNCH_CHECK(ctx, "gather_kick_drift");
   if (nparts_out) *nparts_out = (int)nb;
   return GC_OK;
@@ -730,5 +895,39 @@ extern "C" int gc_radial_histogram(gc_ctx *ctx, const float *x, const float *y, 
   if (nb > 152u * 4u) nb = 152u * 4u;
   gc_launch(ctx, GK_HIST, k_radial_hist, dim3(nb), dim3(256), smem, x, y, z, m, (long long)n, cx, cy, cz, inv_binw, nbins, hist);
   GC_LAUNCH_CHECK(ctx, "radial hist");
+  return GC_OK;
+}
+
+// ------------------------------------------------------------------------------
+// headless 2-D projection (viz/project.py:26-46)
+// ------------------------------------------------------------------------------
+// Nearest-bin mass histogram over two in-plane axes: ia = floor((a - lo_a)/binw_a)
+// in f32 as the reference; mass outside [0, bins) is dropped.
+__global__ void __launch_bounds__(256)
+    k_project_ngp(const float *__restrict__ pa, const float *__restrict__ pb, const float *__restrict__ m, long long n,
+                  float lo_a, float lo_b, float bw_a, float bw_b, int bins, float *__restrict__ img) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const float ga = floorf(__fdiv_rn(__fsub_rn(pa[p], lo_a), bw_a));
+    const float gb = floorf(__fdiv_rn(__fsub_rn(pb[p], lo_b), bw_b));
+    if (!(ga >= 0.0f && ga < (float)bins && gb >= 0.0f && gb < (float)bins)) continue;
+    atomicAdd(img + (size_t)(int)ga * bins + (int)gb, m[p]);
+  }
+}
+
+extern "C" int gc_project_ngp(gc_ctx *ctx, const float *pa, const float *pb, const float *m, int64_t n, double lo_a,
+                              double lo_b, double binw_a, double binw_b, int bins, float *img) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, img, "gc_project_ngp: NULL image");
+  GC_REQUIRE(ctx, bins >= 1 && bins <= 16384, "bins must be in [1, 16384]");
+  GC_REQUIRE(ctx, binw_a > 0.0 && binw_b > 0.0, "bin widths must be positive");
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  GC_CUDA(ctx, cudaMemsetAsync(img, 0, (size_t)bins * bins * sizeof(float), ctx->stream));
+  if (n == 0) return GC_OK;
+  GC_REQUIRE(ctx, pa && pb && m, "gc_project_ngp: NULL particle array");
+  unsigned nb = gc_blocks(n, 256);
+  if (nb > 152u * 16u) nb = 152u * 16u;
+  gc_launch(ctx, GK_PROJECT, k_project_ngp, dim3(nb), dim3(256), 0, pa, pb, m, (long long)n, (float)lo_a, (float)lo_b,
+            (float)binw_a, (float)binw_b, bins, img);
+  GC_LAUNCH_CHECK(ctx, "project");
   return GC_OK;
 }

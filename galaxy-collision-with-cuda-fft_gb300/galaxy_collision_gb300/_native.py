@@ -23,6 +23,8 @@ GC_ERR_STATE = -6
 
 GC_FLAG_NONFINITE_POS = 0x1
 GC_FLAG_NONFINITE_RHO = 0x2
+GC_MG_FUSED_SWEEP = 0x1
+GC_STEP_GRAD_GRID = 0x1
 
 GC_STEP_PRIME = 0
 GC_STEP_ADVANCE = 1
@@ -41,7 +43,7 @@ class MGParams(C.Structure):
         ("coarse_sweeps", C.c_int),
         ("max_cycles", C.c_int),
         ("min_cycles", C.c_int),
-        ("reserved", C.c_int),
+        ("flags", C.c_int),
         ("tol", C.c_double),
     ]
 
@@ -72,7 +74,7 @@ class StepParams(C.Structure):
         ("diagnostics", C.c_int),
         ("mg", MGParams),
         ("fixed_point_bits", C.c_int),
-        ("reserved", C.c_int),
+        ("flags", C.c_int),
     ]
 
 
@@ -110,6 +112,8 @@ _PROTOS = {
     "gc_diag_grid_pe": (C.c_int, [_ctxp, _vp, _vp, C.POINTER(C.c_double)]),
     "gc_radial_histogram": (C.c_int, [_ctxp, _vp, _vp, _vp, _vp, _i64, C.c_double, C.c_double, C.c_double,
                                       C.c_double, C.c_int, _vp]),
+    "gc_project_ngp": (C.c_int, [_ctxp, _vp, _vp, _vp, _i64, C.c_double, C.c_double, C.c_double, C.c_double,
+                                 C.c_int, _vp]),
     "gc_pm_sort": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(Particles)]),
     "gc_pm_step": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(StepParams), C.POINTER(StepStats)]),
     "gc_pm_potential": (_vp, [_ctxp]),

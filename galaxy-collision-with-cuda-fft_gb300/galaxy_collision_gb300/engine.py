@@ -40,7 +40,7 @@ class StepResult:
 class PMEngine:
     def __init__(self, grid_size: int, dx: float, grav: float = 1.0, *, origin=(0.0, 0.0, 0.0), tol: float = 1e-6,
                  max_cycles: int = 50, pre_sweeps: int = 2, post_sweeps: int = 2, coarse_sweeps: int = 40,
-                 fixed_point_bits: int = 52, sort_every: int = 20):
+                 fixed_point_bits: int = 52, sort_every: int = 20, grad_grid: bool = True):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
         self.grav = float(grav)
@@ -55,6 +55,7 @@ class PMEngine:
         self.mg.tol = float(tol)
         self.fixed_point_bits = int(fixed_point_bits)
         self.sort_every = int(sort_every)
+        self.grad_grid = bool(grad_grid)  # gather from a float4 -grad(phi) grid (same results)
         self.n = 0
         self.state = "empty"   # empty -> synced -> open -> synced ...
         self.steps_since_sort = 0
@@ -120,6 +121,7 @@ class PMEngine:
         sp.diagnostics = int(bool(diagnostics))
         sp.mg = self.mg
         sp.fixed_point_bits = self.fixed_point_bits
+        sp.flags = _native.GC_STEP_GRAD_GRID if self.grad_grid else 0
         st = _native.StepStats()
         p = self._struct(self.cur)
         self.ctx.call("gc_pm_step", C.byref(p), C.byref(sp), C.byref(st), what="gc_pm_step")
@@ -130,6 +132,13 @@ class PMEngine:
             res.grid_pe_raw = float(st.grid_pe_raw)
         self.last = res
         return res
+
+    def evaluate(self, diagnostics: bool = True) -> StepResult:
+        """Force evaluation (and FP64 diagnostics) of the synchronised state without
+        moving it: a PRIME with dt = 0 leaves x and v unchanged."""
+        if self.state != "synced":
+            raise RuntimeError(f"evaluate needs synchronised state, engine is {self.state!r}")
+        return self._step(_native.GC_STEP_PRIME, 0.0, diagnostics)
 
     def prime(self, dt: float, diagnostics: bool = False) -> StepResult:
         if self.state != "synced":

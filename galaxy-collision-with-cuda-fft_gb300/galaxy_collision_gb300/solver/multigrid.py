@@ -35,6 +35,8 @@ class MultigridPoissonSolver(PoissonSolver):
         coarse_sweeps: int = 40,
         tol: float = 1e-3,
         min_cycles: int = 1,
+        *,
+        fused_sweep: bool = False,
     ):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
@@ -47,6 +49,7 @@ class MultigridPoissonSolver(PoissonSolver):
         self.min_cycles = max(1, int(min_cycles))
         self.last_cycles = 0
         self.last_stats = None
+        self.fused_sweep = bool(fused_sweep)  # finest level by the streaming sweep kernel (same results)
         self._ctx = _native.Context(self.grid_size, self.dx, self.G)
         self.sizes = [n for (n, _J, _p) in self._ctx.levels()]
 
@@ -58,6 +61,7 @@ class MultigridPoissonSolver(PoissonSolver):
         p.max_cycles = self.n_cycles
         p.min_cycles = self.min_cycles
         p.tol = self.tol
+        p.flags = _native.GC_MG_FUSED_SWEEP if self.fused_sweep else 0
         return p
 
     def solve(self, rho, phi, warm_start: bool = False) -> None:

@@ -46,6 +46,12 @@ enum gc_status_code {
 #define GC_FLAG_NONFINITE_POS 0x1u  /* a particle position was NaN/Inf: it deposited nothing */
 #define GC_FLAG_NONFINITE_RHO 0x2u  /* the density handed to the solver had NaN/Inf */
 
+/* gc_mg_params.flags: relax the finest level with the streaming sweep (one
+ * red+black sweep per pass through shared memory, ping-pong buffers, the
+ * prolongation folded into the first post-sweep) instead of the in-place
+ * red and black half-sweep kernels. Identical results. */
+#define GC_MG_FUSED_SWEEP 0x1
+
 typedef struct gc_ctx gc_ctx;
 
 /* Multigrid controls. Defaults follow MultigridPoissonSolver.__init__
@@ -56,7 +62,7 @@ typedef struct gc_mg_params {
   int coarse_sweeps;  /* FP64 Gauss-Seidel sweeps on the coarsest level (reference: 40) */
   int max_cycles;     /* V-cycle cap (reference n_cycles: 20) */
   int min_cycles;     /* never fewer V-cycles than this (reference: 1) */
-  int reserved;
+  int flags;          /* GC_MG_* bits; 0 = default */
   double tol;         /* stop when ||r||_2 < tol * ||4 pi G rho||_2 (reference: 1e-3) */
 } gc_mg_params;
 
@@ -91,8 +97,13 @@ typedef struct gc_step_params {
   int diagnostics;   /* 1: accumulate FP64 particle diagnostics at the synchronised time */
   gc_mg_params mg;
   int fixed_point_bits; /* deposit quantum = 2^-bits of the total mass; 24 <= bits <= 62 - ceil(log2 G) */
-  int reserved;
+  int flags;         /* GC_STEP_* bits */
 } gc_step_params;
+
+/* gc_step_params.flags: form g = -grad(phi) once per step as a float4 node grid
+ * and gather it with one vector load per corner (same arithmetic as forming it
+ * on the fly from phi; costs a G^3 float4 buffer held by the context). */
+#define GC_STEP_GRAD_GRID 0x1
 
 typedef struct gc_step_stats {
   gc_mg_stats mg;
@@ -221,6 +232,13 @@ int gc_diag_grid_pe(gc_ctx *ctx, const float *rho, const float *phi, double *out
 int gc_radial_histogram(gc_ctx *ctx, const float *x, const float *y, const float *z,
                         const float *m, int64_t n, double cx, double cy, double cz,
                         double inv_binw, int nbins, double *hist);
+
+/* Nearest-bin 2-D mass histogram of the particles over two in-plane axes
+ * (img[ia*bins + ib], ia = floor((a - lo_a)/binw_a) in f32; out-of-range mass
+ * dropped), the device projection behind movie frames and the 2-D view.
+ * Replaces viz/project.py _project / scatter_density (viz/project.py:26-70). */
+int gc_project_ngp(gc_ctx *ctx, const float *pa, const float *pb, const float *m, int64_t n, double lo_a,
+                   double lo_b, double binw_a, double binw_b, int bins, float *img);
 
 /* ---- fused engine (callers: bench.py:145-152, sim.py:320-325) ------------ */
 

@@ -26,10 +26,10 @@ def _cluster(n, G, seed, spread=2.5, vscale=0.15):
     return pos, vel, mass
 
 
-def _engine_run(pos, vel, mass, G, dt, steps, sort_every=5, tol=1e-7):
+def _engine_run(pos, vel, mass, G, dt, steps, sort_every=5, tol=1e-7, grad_grid=True):
     from galaxy_collision_gb300.engine import PMEngine
 
-    eng = PMEngine(G, 1.0, grav=1.0, tol=tol, max_cycles=60, sort_every=sort_every)
+    eng = PMEngine(G, 1.0, grav=1.0, tol=tol, max_cycles=60, sort_every=sort_every, grad_grid=grad_grid)
     eng.load(pos, vel, mass, sort=sort_every > 0)
     eng.prime(dt)
     for _ in range(steps - 1):
@@ -111,6 +111,18 @@ def test_engine_bitwise_reproducible_and_sort_invariant(cuda):
     # independent, so sorting changes nothing but memory order
     np.testing.assert_array_equal(p1, p3)
     np.testing.assert_array_equal(v1, v3)
+
+
+def test_engine_gradient_grid_gather_is_bitwise_identical(cuda):
+    """Gathering from a precomputed float4 -grad(phi) grid is the same arithmetic
+    as forming the gradient at the corners on the fly."""
+    G, n, dt, steps = 40, 30000, 0.05, 5
+    pos, vel, mass = _cluster(n, G, 5)
+    pos[:50] = np.random.default_rng(9).uniform(-0.9, G - 0.1, size=(50, 3))  # include edge cells
+    p1, v1, _ = _engine_run(pos, vel, mass, G, dt, steps, sort_every=2, grad_grid=False)
+    p2, v2, _ = _engine_run(pos, vel, mass, G, dt, steps, sort_every=2, grad_grid=True)
+    np.testing.assert_array_equal(p1, p2)
+    np.testing.assert_array_equal(v1, v2)
 
 
 def test_engine_diagnostics_match_host(cuda):

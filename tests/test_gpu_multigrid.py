@@ -88,6 +88,16 @@ def test_residual_norms_match_numpy(cuda, n, dx):
     assert s.residual_norm() == pytest.approx(rn, rel=1e-4)
 
 
+@pytest.mark.parametrize("n,dx", [(16, 1.0), (37, 0.5), (100, 2.0), (130, 0.25)])
+def test_fused_sweep_bitwise_equals_half_sweeps(cuda, n, dx):
+    """The streaming sweep (and its fused prolongation) is the same arithmetic as
+    the in-place red and black half-sweeps: identical potentials."""
+    rho = gaussian_rho(n, dx, 3.0 * dx, 1.5, center=(0.45 * n * dx, 0.5 * n * dx, 0.6 * n * dx))
+    _, _, a = _solve(rho, dx, 1.0, n_cycles=4, tol=0.0)
+    _, _, b = _solve(rho, dx, 1.0, n_cycles=4, tol=0.0, fused_sweep=True)
+    np.testing.assert_array_equal(a.to_numpy(), b.to_numpy())
+
+
 def test_convergence_factor_per_vcycle(cuda):
     n = 128
     rho = gaussian_rho(n, 1.0, 6.0, 1.0, center=(70.0, 60.0, 66.0))
