@@ -44,7 +44,7 @@ enum gc_kernel_id {
   GK_DEPOSIT = 0, GK_DEPOSIT_RUNS, GK_CONVERT_Q, GK_MASS, GK_SMOOTH0, GK_RESID0, GK_RESTRICT, GK_SMOOTH,
   GK_RESID, GK_PROLONG, GK_PROLONG0, GK_TAIL, GK_FACES, GK_MOMENTS, GK_RHS, GK_REDUCE, GK_GATHER_KD,
   GK_GRAD, GK_GATHER, GK_AXPY, GK_KEYS, GK_SORT, GK_PERMUTE, GK_DIAG, GK_HIST, GK_RESID64, GK_COPY,
-  GK_SWEEP0, GK_PROJECT, GK_COUNT
+  GK_SWEEP0, GK_PROJECT, GK_WARMSTART, GK_COUNT
 };
 extern const char *const gc_kernel_names[GK_COUNT];
 
@@ -104,8 +104,20 @@ struct gc_ctx {
 
   gc_profiler prof;
 
+  // warm-start hook (coarse history of the potential on the (G/2)^3 grid)
+  struct gc_ws *ws;     // attached network (learned mode), not owned
+  int ws_mode;          // GC_WS_PLAIN / GC_WS_LEARNED / GC_WS_EXTRAPOLATE
+  int ws_track;         // maintain the coarse history
+  int ws_hist;          // solves recorded in the history (0, 1, 2+)
+  void *ws_record;      // one-shot f16 [4][R^3] sample destination
+  float *ws_buf;        // rho_c, phi_c, delta_c, y (R^3 each) + scalars + partials
+  size_t ws_buf_cap;
+
   char err[512];
 };
+
+int gc_ws_pre_solve(gc_ctx *ctx, int warm);
+int gc_ws_post_solve(gc_ctx *ctx);
 
 // Launch `k` on ctx's stream, counting it under `kid` and bracketing it with
 // CUDA events when profiling is enabled.
@@ -313,10 +325,10 @@ int gc_finalize(gc_ctx *ctx, const double *parts, int nparts, int nv, double *ds
 // Sum of m/dx^3 (FP64, deterministic) into dsmall[mass_slot] and the fixed-point
 // exponent E (quantum 2^E, total <= 2^bits quanta) into dsmall[exp_slot].
 int gc_fixed_point_setup(gc_ctx *ctx, const float *m, int64_t n, int bits, int mass_slot, int exp_slot);
-// int64 fixed-point CIC deposit into ctx->q (which must be zero on entry).
-// sorted_runs != 0 selects the run-aggregated kernel meant for cell-sorted particles.
+// int64 fixed-point CIC deposit into ctx->q (which must be zero on entry). Any
+// particle order; runs of equal cells (cell-sorted input) are summed in registers.
 int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, const float *m, int64_t n,
-                 const double *qexp, int sorted_runs);
+                 const double *qexp);
 // Read ctx->q, write rho (may be NULL) and b = f32(q 2^E 4 pi G h^2) (may be NULL),
 // zero q, and reduce the ten moments into ctx->dmom and ||b||^2 into dsmall[GC_S_BNORM2].
 int gc_convert_q(gc_ctx *ctx, const double *qexp, float *rho_out, float *b_out);

@@ -35,17 +35,21 @@ extern "C" int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_para
   if (sp->mode == GC_STEP_PRIME) {
     if ((s = gc_fixed_point_setup(ctx, p->m, p->n, sp->fixed_point_bits, GC_S_MASS_PM, GC_S_QEXP_PM))) return s;
   }
-  if ((s = gc_deposit_q(ctx, p->x, p->y, p->z, p->m, p->n, ctx->dsmall + GC_S_QEXP_PM, 1))) return s;
+  if ((s = gc_deposit_q(ctx, p->x, p->y, p->z, p->m, p->n, ctx->dsmall + GC_S_QEXP_PM))) return s;
   // 2. b0, moments, ||b0||
   if ((s = gc_convert_q(ctx, ctx->dsmall + GC_S_QEXP_PM, nullptr, ctx->b0))) return s;
   // 3. initial guess and faces, then V-cycles
-  if (!sp->warm_start || !ctx->solved_once) {
+  const int warm = sp->warm_start && ctx->solved_once;
+  if (!warm) {
     GC_CUDA(ctx, cudaMemsetAsync(ctx->hi, 0, g3 * sizeof(float), ctx->stream));
     GC_CUDA(ctx, cudaMemsetAsync(ctx->lo, 0, g3 * sizeof(float), ctx->stream));
   }
+  // learned / extrapolated correction of the previous potential, sample recording
+  if ((s = gc_ws_pre_solve(ctx, warm))) return s;
   if ((s = gc_faces_from_moments(ctx))) return s;
   gc_mg_stats mst;
   if ((s = gc_mg_run(ctx, &sp->mg, &mst))) return s;
+  if ((s = gc_ws_post_solve(ctx))) return s;
   // 4. particle pass
   int nparts = 0;
   if ((s = gc_gather_kick_drift(ctx, p, sp->dt, sp->mode, sp->diagnostics, (sp->flags & GC_STEP_GRAD_GRID) != 0,

@@ -11,6 +11,9 @@
 
 #include <math.h>
 
+#include <cmath>
+#include <cstdint>
+
 // ------------------------------------------------------------------------------
 // fixed-point set-up: total density-mass and quantum exponent
 // ------------------------------------------------------------------------------
@@ -121,7 +124,7 @@ __device__ __forceinline__ bool cic_contrib(float x, float y, float z, float mas
   return true;
 }
 
-__device__ __forceinline__ void flush_corners(long long *__restrict__ qg, const CellPos &c, int G,
+__device__ __forceinline__ void flush_corners(long long *__restrict__ qg, int ix, int iy, int iz, int G,
                                               const long long (&q)[8]) {
 #pragma unroll
   for (int cx = 0; cx < 2; ++cx)
@@ -130,8 +133,9 @@ __device__ __forceinline__ void flush_corners(long long *__restrict__ qg, const 
 #pragma unroll
       for (int cz = 0; cz < 2; ++cz) {
         const long long v = q[(cx * 2 + cy) * 2 + cz];
-        if (v != 0) {
-          const size_t idx = ((size_t)(c.ix + cx) * G + (c.iy + cy)) * G + (c.iz + cz);
+        const int jx = ix + cx, jy = iy + cy, jz = iz + cz;
+        if (v != 0 && (unsigned)jx < (unsigned)G && (unsigned)jy < (unsigned)G && (unsigned)jz < (unsigned)G) {
+          const size_t idx = ((size_t)jx * G + jy) * G + jz;
           atomicAdd((unsigned long long *)(qg + idx), (unsigned long long)v);
         }
       }
@@ -168,138 +172,216 @@ __global__ void __launch_bounds__(256)
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         q[t] = v;
       }
-      if (lane == 0) flush_corners(qg, c, d.G, q);
+      if (lane == 0) flush_corners(qg, c.ix, c.iy, c.iz, d.G, q);
     } else if (ok) {
-      flush_corners(qg, c, d.G, q);
+      flush_corners(qg, c.ix, c.iy, c.iz, d.G, q);
     }
   }
 }
 
-// Cell-sorted particles. Each warp owns a contiguous range of DEP_WARP_ITEMS
-// particles and walks it 32 at a time (coalesced loads). Lanes holding the same
-// cell are adjacent after the sort, so a segmented inclusive scan over the warp
-// sums each run of equal cells; the last lane of a run adds its 8 corner sums
-// with one int64 atomic each. The run that reaches lane 31 is carried into the
-// next group of 32 and merged there when the cell continues.
-#define DEP_WARP_ITEMS 512
+// Cell-sorted particles. Each thread walks DEP_SEQ consecutive particles of the
+// array, so the particles of one cell (adjacent after the sort) are summed in
+// registers. Two runs are cached per thread, so particles that drifted into a
+// neighbouring cell since the last sort do not break the run of the cell they
+// are interleaved with; a run evicted from the cache is added to the grid with
+// one int64 atomic per in-box corner. Lanes hold consecutive slices: at the end
+// lanes whose cached runs are the same cell (__match_any_sync) reduce them with
+// redux.sync and one lane adds the sums. Correct for any particle order; the
+// sort only makes the runs long.
+#define DEP_SEQ 8
+#define DEP_NONE 0xffffffffu
+
+// Round-to-nearest-even integer of v (|v| < 2^22): the f32 add of 1.5*2^23 lands
+// in [2^23, 2^24), where the f32 spacing is 1, and the integer is read from the
+// bits. Same result as f32_to_i64_rn.
+__device__ __forceinline__ int rne_small(float v) { return __float_as_int(__fadd_rn(v, 12582912.0f)) - 0x4B400000; }
+
+// Corner contributions of a particle whose mass exceeds 2^22 quanta.
+__device__ __forceinline__ void cic_q_large(float mm, float fx, float fy, float fz, float qscale, long long (&q)[8]) {
+  const float wx[2] = {__fsub_rn(1.0f, fx), fx};
+  const float wy[2] = {__fsub_rn(1.0f, fy), fy};
+  const float wz[2] = {__fsub_rn(1.0f, fz), fz};
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const float w = __fmul_rn(__fmul_rn(__fmul_rn(mm, wx[c >> 2]), wy[(c >> 1) & 1]), wz[c & 1]);
+    q[c] = f32_to_i64_rn(__fmul_rn(w, qscale));
+  }
+}
+
+// Add a run's 8 corner sums to the grid (out-of-box corners dropped). Out of
+// line: called once per run, and the values travel in registers.
+__device__ __noinline__ void flush_run(long long *__restrict__ qg, unsigned key, int G, long long q0, long long q1,
+                                       long long q2, long long q3, long long q4, long long q5, long long q6,
+                                       long long q7) {
+  const int G1 = G + 1;
+  const int ix = (int)(key / (unsigned)(G1 * G1)) - 1, iy = (int)((key / (unsigned)G1) % (unsigned)G1) - 1,
+            iz = (int)(key % (unsigned)G1) - 1;
+  const long long q[8] = {q0, q1, q2, q3, q4, q5, q6, q7};
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const long long v = q[c];
+    const int jx = ix + (c >> 2), jy = iy + ((c >> 1) & 1), jz = iz + (c & 1);
+    if (v != 0 && (unsigned)jx < (unsigned)G && (unsigned)jy < (unsigned)G && (unsigned)jz < (unsigned)G)
+      atomicAdd((unsigned long long *)(qg + ((size_t)jx * G + jy) * G + jz), (unsigned long long)v);
+  }
+}
+#define FLUSH_RUN(qg, key, G, q) flush_run(qg, key, G, q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7])
+
+struct DepRun {
+  unsigned key;  // cell key, DEP_NONE when empty
+  bool small;    // every contribution summed here was below 2^22 quanta
+  long long q[8];
+};
+
+// Deposit one particle into the two-run cache; returns nothing, may evict.
+template <bool POW2>
+__device__ __forceinline__ void dep_particle(float px, float py, float pz, float pm, const DepCtx &d, float inv_dx,
+                                             float qscale, long long *__restrict__ qg, unsigned *__restrict__ status,
+                                             DepRun &r0, DepRun &r1) {
+  if (!gc_finite3(px, py, pz)) atomicOr(status, GC_FLAG_NONFINITE_POS);
+  float gx, gy, gz;
+  if (POW2) {  // x / dx == x * (1/dx) exactly when dx is a power of two
+    gx = __fmul_rn(px, inv_dx); gy = __fmul_rn(py, inv_dx); gz = __fmul_rn(pz, inv_dx);
+  } else {
+    gx = __fdiv_rn(px, d.dx); gy = __fdiv_rn(py, d.dx); gz = __fdiv_rn(pz, d.dx);
+  }
+  const float hi = (float)d.G;
+  if (!(gx >= -1.0f && gx < hi && gy >= -1.0f && gy < hi && gz >= -1.0f && gz < hi)) return;
+  const float flx = floorf(gx), fly = floorf(gy), flz = floorf(gz);
+  const int ix = (int)flx, iy = (int)fly, iz = (int)flz;
+  const float fx = __fsub_rn(gx, flx), fy = __fsub_rn(gy, fly), fz = __fsub_rn(gz, flz);
+  const float mm = __fmul_rn(pm, d.inv_vol);
+  const unsigned key = (unsigned)(((ix + 1) * (d.G + 1) + (iy + 1)) * (d.G + 1) + (iz + 1));
+  const bool small = __fmul_rn(fabsf(mm), qscale) < 4194304.0f;  // every |w| <= |mm|
+  long long q[8];
+  if (small) {
+    const float wx0 = __fsub_rn(1.0f, fx), wy0 = __fsub_rn(1.0f, fy), wz0 = __fsub_rn(1.0f, fz);
+    const float a0 = __fmul_rn(mm, wx0), a1 = __fmul_rn(mm, fx);
+    const float b00 = __fmul_rn(a0, wy0), b01 = __fmul_rn(a0, fy), b10 = __fmul_rn(a1, wy0), b11 = __fmul_rn(a1, fy);
+    q[0] = rne_small(__fmul_rn(__fmul_rn(b00, wz0), qscale));
+    q[1] = rne_small(__fmul_rn(__fmul_rn(b00, fz), qscale));
+    q[2] = rne_small(__fmul_rn(__fmul_rn(b01, wz0), qscale));
+    q[3] = rne_small(__fmul_rn(__fmul_rn(b01, fz), qscale));
+    q[4] = rne_small(__fmul_rn(__fmul_rn(b10, wz0), qscale));
+    q[5] = rne_small(__fmul_rn(__fmul_rn(b10, fz), qscale));
+    q[6] = rne_small(__fmul_rn(__fmul_rn(b11, wz0), qscale));
+    q[7] = rne_small(__fmul_rn(__fmul_rn(b11, fz), qscale));
+  } else {
+    cic_q_large(mm, fx, fy, fz, qscale, q);
+  }
+  if (key == r0.key) {
+    r0.small = r0.small && small;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) r0.q[t] += q[t];
+  } else if (key == r1.key) {
+    r1.small = r1.small && small;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) r1.q[t] += q[t];
+  } else {  // evict run 1, demote run 0, start a new run 0
+    if (r1.key != DEP_NONE) FLUSH_RUN(qg, r1.key, d.G, r1.q);
+    r1.key = r0.key;
+    r1.small = r0.small;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) r1.q[t] = r0.q[t];
+    r0.key = key;
+    r0.small = small;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) r0.q[t] = q[t];
+  }
+}
+
+// Merge the cached runs of lanes holding the same cell and add them to the grid.
+__device__ __forceinline__ void dep_merge(const DepRun &r, long long *__restrict__ qg, int G, int lane) {
+  const unsigned peers = __match_any_sync(0xffffffffu, r.key);
+  const unsigned large = __ballot_sync(0xffffffffu, !r.small);
+  if (r.key == DEP_NONE) return;
+  if ((large & peers) == 0 && __popc(peers) > 1) {
+    // each lane's sums are below DEP_SEQ * 2^22, a group's below 2^30
+    long long tot[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) tot[t] = (long long)__reduce_add_sync(peers, (int)r.q[t]);
+    if (lane == __ffs(peers) - 1) FLUSH_RUN(qg, r.key, G, tot);
+  } else {
+    FLUSH_RUN(qg, r.key, G, r.q);
+  }
+}
+
+template <bool POW2, bool VEC>
 __global__ void __launch_bounds__(256)
     k_deposit_sorted(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
-                     const float *__restrict__ m, long long n, DepCtx d, const double *__restrict__ qexp,
-                     long long *__restrict__ qg, unsigned *__restrict__ status) {
+                     const float *__restrict__ m, long long n, DepCtx d, float inv_dx,
+                     const double *__restrict__ qexp, long long *__restrict__ qg, unsigned *__restrict__ status) {
   const float qscale = ldexpf(1.0f, -(int)(*qexp));
   const int lane = threadIdx.x & 31;
-  const long long gwarp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long span = 32LL * DEP_SEQ;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  const unsigned invalid = 0x80000000u | (unsigned)lane;
-  for (long long base = gwarp * DEP_WARP_ITEMS; base < n; base += nwarps * DEP_WARP_ITEMS) {
-    unsigned ckey = 0xffffffffu;  // carried run (same value in every lane)
-    long long cq[8];
-    int cix = 0, ciy = 0, ciz = 0;
+  for (long long w0 = ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * span; w0 < n;
+       w0 += nwarps * span) {
+    const long long s0 = w0 + (long long)lane * DEP_SEQ;
+    const long long left = n - s0;
+    const int cnt = left <= 0 ? 0 : (left >= DEP_SEQ ? DEP_SEQ : (int)left);
+    DepRun r0, r1;
+    r0.key = r1.key = DEP_NONE;
+    r0.small = r1.small = true;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) cq[t] = 0;
-    for (int g = 0; g < DEP_WARP_ITEMS; g += 32) {
-      const long long p = base + g + lane;
-      CellPos c;
-      long long q[8];
-      bool ok = false;
-      if (p < n) {
-        const float px = x[p], py = y[p], pz = z[p];
-        if (!gc_finite3(px, py, pz)) atomicOr(status, GC_FLAG_NONFINITE_POS);
-        ok = cic_contrib(px, py, pz, m[p], d, qscale, c, q);
-      }
-      if (!ok) {
-        c.ix = c.iy = c.iz = 0;
+    for (int t = 0; t < 8; ++t) r0.q[t] = r1.q[t] = 0;
 #pragma unroll
-        for (int t = 0; t < 8; ++t) q[t] = 0;
-      }
-      const unsigned key = ok ? (unsigned)(((c.ix + 1) * (d.G + 1) + (c.iy + 1)) * (d.G + 1) + (c.iz + 1)) : invalid;
-      // Fast path for the dense case: the whole warp is one cell and every
-      // contribution fits in 26 bits, so the 32 lanes' 8 corner sums are exact
-      // 32-bit warp reductions (redux.sync), merged into the carried run.
-      const unsigned key0 = __shfl_sync(0xffffffffu, key, 0);
-      bool small = true;
+    for (int h = 0; h < DEP_SEQ / 4; ++h) {
+      float px[4], py[4], pz[4], pm[4];
+      if (VEC && cnt == DEP_SEQ) {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(x + s0) + h);
+        const float4 b = __ldg(reinterpret_cast<const float4 *>(y + s0) + h);
+        const float4 c = __ldg(reinterpret_cast<const float4 *>(z + s0) + h);
+        const float4 e = __ldg(reinterpret_cast<const float4 *>(m + s0) + h);
+        px[0] = a.x; px[1] = a.y; px[2] = a.z; px[3] = a.w;
+        py[0] = b.x; py[1] = b.y; py[2] = b.z; py[3] = b.w;
+        pz[0] = c.x; pz[1] = c.y; pz[2] = c.z; pz[3] = c.w;
+        pm[0] = e.x; pm[1] = e.y; pm[2] = e.z; pm[3] = e.w;
+      } else {
 #pragma unroll
-      for (int t = 0; t < 8; ++t) small = small && (q[t] < (1LL << 26)) && (q[t] > -(1LL << 26));
-      if (__all_sync(0xffffffffu, ok && key == key0 && small)) {
-        long long tot[8];
-#pragma unroll
-        for (int t = 0; t < 8; ++t) tot[t] = (long long)__reduce_add_sync(0xffffffffu, (int)q[t]);
-        if (ckey != key) {  // previous run ends here
-          if (lane == 0 && ckey != 0xffffffffu) {
-            CellPos cc;
-            cc.ix = cix; cc.iy = ciy; cc.iz = ciz;
-            flush_corners(qg, cc, d.G, cq);
-          }
-          ckey = key;
-          cix = c.ix; ciy = c.iy; ciz = c.iz;
-#pragma unroll
-          for (int t = 0; t < 8; ++t) cq[t] = tot[t];
-        } else {
-#pragma unroll
-          for (int t = 0; t < 8; ++t) cq[t] += tot[t];
-        }
-        continue;
-      }
-      // the carried run continues into lane 0, or is flushed by lane 0
-      if (lane == 0 && ckey != 0xffffffffu) {
-        if (key == ckey) {
-#pragma unroll
-          for (int t = 0; t < 8; ++t) q[t] += cq[t];
-        } else {
-          CellPos cc;
-          cc.ix = cix; cc.iy = ciy; cc.iz = ciz;
-          flush_corners(qg, cc, d.G, cq);
+        for (int j = 0; j < 4; ++j) {
+          const bool in = 4 * h + j < cnt;
+          px[j] = in ? x[s0 + 4 * h + j] : 0.0f;
+          py[j] = in ? y[s0 + 4 * h + j] : 0.0f;
+          pz[j] = in ? z[s0 + 4 * h + j] : 0.0f;
+          pm[j] = in ? m[s0 + 4 * h + j] : 0.0f;
         }
       }
-      // segmented inclusive scan: head = lane 0 or key differs from the lane below
-      const unsigned kprev = __shfl_up_sync(0xffffffffu, key, 1);
-      bool head = (lane == 0) || (kprev != key);
 #pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const bool hprev = __shfl_up_sync(0xffffffffu, head, off);
-#pragma unroll
-        for (int t = 0; t < 8; ++t) {
-          const long long v = __shfl_up_sync(0xffffffffu, q[t], off);
-          if (lane >= off && !head) q[t] += v;
-        }
-        if (lane >= off) head = head || hprev;
-      }
-      const unsigned knext = __shfl_down_sync(0xffffffffu, key, 1);
-      const bool tail = (lane != 31) && (knext != key);
-      if (tail && ok) flush_corners(qg, c, d.G, q);
-      // lane 31's run is carried
-      ckey = __shfl_sync(0xffffffffu, ok ? key : 0xffffffffu, 31);
-      cix = __shfl_sync(0xffffffffu, c.ix, 31);
-      ciy = __shfl_sync(0xffffffffu, c.iy, 31);
-      ciz = __shfl_sync(0xffffffffu, c.iz, 31);
-#pragma unroll
-      for (int t = 0; t < 8; ++t) cq[t] = __shfl_sync(0xffffffffu, q[t], 31);
+      for (int j = 0; j < 4; ++j)
+        if (4 * h + j < cnt) dep_particle<POW2>(px[j], py[j], pz[j], pm[j], d, inv_dx, qscale, qg, status, r0, r1);
     }
-    if (lane == 0 && ckey != 0xffffffffu) {
-      CellPos cc;
-      cc.ix = cix; cc.iy = ciy; cc.iz = ciz;
-      flush_corners(qg, cc, d.G, cq);
-    }
+    dep_merge(r0, qg, d.G, lane);
+    dep_merge(r1, qg, d.G, lane);
   }
 }
 
 int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, const float *m, int64_t n,
-                 const double *qexp, int sorted_runs) {
+                 const double *qexp) {
   if (n <= 0) return GC_OK;
   DepCtx d;
   d.dx = (float)ctx->dx;
   d.inv_vol = 1.0f / ((d.dx * d.dx) * d.dx);
   d.G = ctx->G;
-  if (sorted_runs) {
-    const long long nranges = (n + DEP_WARP_ITEMS - 1) / DEP_WARP_ITEMS;
-    unsigned nb = gc_blocks(nranges, 8);
-    if (nb > 152u * 8u) nb = 152u * 8u;
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted, dim3(nb), dim3(256), 0, x, y, z, m, (long long)n, d, qexp, ctx->q, ctx->dstatus);
-  } else {
-    unsigned nb = gc_blocks(n, 256);
-    if (nb > 152u * 32u) nb = 152u * 32u;
-    gc_launch(ctx, GK_DEPOSIT, k_deposit, dim3(nb), dim3(256), 0, x, y, z, m, (long long)n, d, qexp, ctx->q, ctx->dstatus);
-  }
+  const long long nspans = (n + 32LL * DEP_SEQ - 1) / (32LL * DEP_SEQ);
+  unsigned nb = gc_blocks(nspans, 8);
+  if (nb > 152u * 8u) nb = 152u * 8u;
+  int fe = 0;
+  const bool pow2 = std::frexp(d.dx, &fe) == 0.5f;
+  const float inv_dx = pow2 ? std::ldexp(1.0f, 1 - fe) : 0.0f;
+  const bool vec = ((((uintptr_t)x) | ((uintptr_t)y) | ((uintptr_t)z) | ((uintptr_t)m)) & 15u) == 0;
+  if (pow2 && vec)
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true, true>, dim3(nb), dim3(256), 0, x, y, z, m,
+              (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
+  else if (pow2)
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true, false>, dim3(nb), dim3(256), 0, x, y, z, m,
+              (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
+  else if (vec)
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false, true>, dim3(nb), dim3(256), 0, x, y, z, m,
+              (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
+  else
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false, false>, dim3(nb), dim3(256), 0, x, y, z, m,
+              (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
   GC_LAUNCH_CHECK(ctx, "deposit");
   return GC_OK;
 }
@@ -418,7 +500,7 @@ extern "C" int gc_deposit_cic(gc_ctx *ctx, const float *x, const float *y, const
   int s;
   if (n > 0) {
     if ((s = gc_fixed_point_setup(ctx, m, n, fixed_point_bits, GC_S_MASS, GC_S_QEXP))) return s;
-    if ((s = gc_deposit_q(ctx, x, y, z, m, n, ctx->dsmall + GC_S_QEXP, 0))) return s;
+    if ((s = gc_deposit_q(ctx, x, y, z, m, n, ctx->dsmall + GC_S_QEXP))) return s;
   }
   return gc_convert_q(ctx, ctx->dsmall + GC_S_QEXP, rho, nullptr);
 }

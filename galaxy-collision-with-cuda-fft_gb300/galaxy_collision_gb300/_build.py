@@ -21,7 +21,7 @@ INCLUDE = PKG_DIR.parent.parent / "include"
 BUILD_DIR = PKG_DIR / "_build"
 LIB_PATH = PKG_DIR / "libgcpm.so"
 
-SOURCES = ("ctx.cu", "multigrid.cu", "particles.cu", "sort.cu", "engine.cu", "noalloc.cu")
+SOURCES = ("ctx.cu", "multigrid.cu", "particles.cu", "sort.cu", "engine.cu", "noalloc.cu", "warmstart.cu")
 ARCH_FLAGS = ("-gencode", "arch=compute_103a,code=sm_103a")
 NVCC_FLAGS = ("-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2")
 
@@ -47,7 +47,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     """Compile ``libgcpm.so`` (sm_103a) if any source is newer than it. Returns its path."""
     nvcc = nvcc_path()
     BUILD_DIR.mkdir(parents=True, exist_ok=True)
-    headers = [CSRC / "common.cuh", INCLUDE / "gcpm.h"]
+    headers = [CSRC / "common.cuh", CSRC / "umma.cuh", INCLUDE / "gcpm.h"]
     objs = []
     jobs = []
     for src in SOURCES:

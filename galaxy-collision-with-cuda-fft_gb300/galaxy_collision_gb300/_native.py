@@ -26,6 +26,10 @@ GC_FLAG_NONFINITE_RHO = 0x2
 GC_MG_FUSED_SWEEP = 0x1
 GC_STEP_GRAD_GRID = 0x1
 
+GC_WS_PLAIN = 0
+GC_WS_LEARNED = 1
+GC_WS_EXTRAPOLATE = 2
+
 GC_STEP_PRIME = 0
 GC_STEP_ADVANCE = 1
 GC_STEP_CLOSE = 2
@@ -124,6 +128,23 @@ _PROTOS = {
                                   C.POINTER(C.c_double)]),
     "gc_num_kernel_ids": (C.c_int, []),
     "gc_kernel_name": (C.c_char_p, [C.c_int]),
+    "gc_ws_selftest_gemm": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp]),
+    "gc_ws_create": (C.c_int, [C.POINTER(_vp), C.c_int]),
+    "gc_ws_destroy": (C.c_int, [_vp]),
+    "gc_ws_last_error": (C.c_char_p, [_vp]),
+    "gc_ws_set_stream": (C.c_int, [_vp, _vp]),
+    "gc_ws_layer_info": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int)]),
+    "gc_ws_num_params": (C.c_int, [_vp, C.POINTER(_i64)]),
+    "gc_ws_set_params": (C.c_int, [_vp, _vp]),
+    "gc_ws_get_params": (C.c_int, [_vp, _vp]),
+    "gc_ws_get_grads": (C.c_int, [_vp, _vp]),
+    "gc_ws_forward": (C.c_int, [_vp, _vp, _vp]),
+    "gc_ws_backward": (C.c_int, [_vp, _vp, _vp]),
+    "gc_ws_adam": (C.c_int, [_vp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int]),
+    "gc_ws_status": (C.c_int, [_vp, C.POINTER(C.c_uint32), C.c_int]),
+    "gc_pm_set_warmstart": (C.c_int, [_ctxp, _vp, C.c_int, C.c_int]),
+    "gc_pm_record_sample": (C.c_int, [_ctxp, _vp]),
 }
 
 EXPORTED = tuple(_PROTOS)

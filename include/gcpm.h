@@ -272,6 +272,62 @@ int gc_profile_read(gc_ctx *ctx, int kid, long long *launches, long long *timed,
 int gc_num_kernel_ids(void);
 const char *gc_kernel_name(int kid);
 
+/* ---- learned warm start (new: replaces the previous-step initial guess of the
+ * multigrid, solver/multigrid.py:464-467, by a convolutional prediction) ----- */
+
+/* Device check of the tensor-core operand conventions: D (128 x N, f32, row-major)
+ * = A (128 x K) * B (N x K)^T with A, B row-major bf16 bits; a_mn / b_mn stage the
+ * operand MN-major instead of K-major; swap exchanges the descriptor's two byte
+ * offsets of MN-major operands. 16 <= N <= 256, 16 <= K <= 64, both multiples of
+ * 16. *status (device) gets bit 0 on a completion timeout. */
+int gc_ws_selftest_gemm(const void *A, const void *B, float *D, int N, int K, int a_mn, int b_mn, int swap,
+                        void *stream, unsigned *status);
+
+/* The warm-start network: a 3-D convolutional encoder-decoder on an R^3 grid
+ * (R = G/2; levels R, R/2, R/4, R/8 with 16, 32, 64, 128 channels; 3x3x3
+ * kernels; BF16 weights and activations, FP32 accumulation on the tensor cores).
+ * Parameters are one f32 vector: for each of the 11 layers (gc_ws_layer_info)
+ * the weights [27][cout][cin] (tap t = (dz+1)*9 + (dy+1)*3 + (dx+1)) then the
+ * bias [cout]. All pointers are device pointers; calls are ordered on the
+ * object's stream. */
+typedef struct gc_ws gc_ws;
+int gc_ws_create(gc_ws **out, int R);           /* 16 <= R <= 512, R % 8 == 0 */
+int gc_ws_destroy(gc_ws *ws);
+const char *gc_ws_last_error(const gc_ws *ws);
+int gc_ws_set_stream(gc_ws *ws, void *stream);
+int gc_ws_layer_info(int layer, int *cin, int *cout, int *level, int *relu);
+int gc_ws_num_params(const gc_ws *ws, int64_t *n);
+/* Replace the parameters (resets the Adam moments) / read them / read the last gradient. */
+int gc_ws_set_params(gc_ws *ws, const float *params);
+int gc_ws_get_params(gc_ws *ws, float *params);
+int gc_ws_get_grads(gc_ws *ws, float *grads);
+/* Forward pass: feat = f16 [3][R^3] input channels; y_out (nullable) = f32 [R^3]. */
+int gc_ws_forward(gc_ws *ws, const void *feat, float *y_out);
+/* Backward pass of the last forward for the loss 0.5 * mean((y - target)^2),
+ * target f16 [R^3]; the loss goes to *loss_out (device f32, nullable) and the
+ * parameter gradient to the object's gradient vector. */
+int gc_ws_backward(gc_ws *ws, const void *target, float *loss_out);
+/* One Adam step (bias-corrected, step >= 1) with the last gradient. */
+int gc_ws_adam(gc_ws *ws, float lr, float beta1, float beta2, float eps, int step);
+/* Device status bits (bit 0: a tensor-core completion wait timed out); clear resets them. */
+int gc_ws_status(gc_ws *ws, unsigned *flags, int clear);
+
+/* Initial guess of the engine's solve (gc_pm_step with warm_start != 0):
+ *   GC_WS_PLAIN       the previous potential (the reference's warm start);
+ *   GC_WS_LEARNED     previous + the network's predicted change (R = G/2);
+ *   GC_WS_EXTRAPOLATE previous + the previous change (a non-learned comparison).
+ * The multigrid always iterates to the same residual: only the start changes.
+ * With track != 0 (implied by the non-plain modes) the context keeps the
+ * coarse (G/2)^3 history of the potential that the features need. G even. */
+#define GC_WS_PLAIN 0
+#define GC_WS_LEARNED 1
+#define GC_WS_EXTRAPOLATE 2
+int gc_pm_set_warmstart(gc_ctx *ctx, gc_ws *ws, int mode, int track);
+/* One-shot: the next gc_pm_step writes its network input features and the
+ * change its solve produced (the training target) to out, f16 [4][(G/2)^3]:
+ * channels 0..2 the features, 3 the target (see gc_ws_forward). */
+int gc_pm_record_sample(gc_ctx *ctx, void *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -117,6 +117,39 @@ def test_deposit_bit_exact_vs_fixed_point_oracle(cuda, G, dx, bits):
     np.testing.assert_array_equal(rho.to_numpy(), ref)
 
 
+@pytest.mark.parametrize("dx,offset", [(0.25, 0), (0.25, 1), (0.375, 0), (0.375, 3)])
+def test_deposit_dense_sorted_runs_bit_exact(cuda, dx, offset):
+    """Cell-sorted particles packed into a dozen cells (long runs merged across
+    the warp), a few heavy particles (contributions above 2^22 quanta, the
+    general conversion), edge cells, and array starts that are not 16-byte
+    aligned (scalar loads). dx = 0.25 takes the exact reciprocal multiply."""
+    from types import SimpleNamespace
+
+    from galaxy_collision_gb300.data import Field
+    from galaxy_collision_gb300.deposit import deposit_density
+
+    G, bits, n = 32, 40, 70001
+    rng = np.random.default_rng(int(dx * 1000) + offset)
+    cells = rng.integers(-1, G, size=(12, 3))
+    pick = rng.integers(0, 12, size=n)
+    pos = ((cells[pick] + rng.uniform(0.0, 1.0, size=(n, 3))) * dx).astype(np.float32)
+    mass = rng.uniform(0.5, 1.5, size=n).astype(np.float32)
+    mass[rng.integers(0, n, size=20)] = 5.0e4
+    order = pm.stable_sort_perm(pm.cell_keys(pos, dx, G))
+    pos, mass = pos[order], mass[order]
+
+    def dev(a):
+        t = torch.zeros(n + offset, dtype=torch.float32, device="cuda")
+        t[offset:] = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        return t[offset:]
+
+    parts = SimpleNamespace(n=n, pos_x=dev(pos[:, 0]), pos_y=dev(pos[:, 1]), pos_z=dev(pos[:, 2]), mass=dev(mass))
+    rho = Field((G, G, G))
+    deposit_density(parts, rho, dx, fixed_point_bits=bits)
+    ref, _, _ = pm.deposit_fixed(pos, mass, dx, G, bits)
+    np.testing.assert_array_equal(rho.to_numpy(), ref)
+
+
 def test_deposit_vs_fp64_oracle(cuda):
     from galaxy_collision_gb300.data import Field
     from galaxy_collision_gb300.deposit import deposit_density

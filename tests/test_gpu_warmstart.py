@@ -1,0 +1,180 @@
+"""The learned warm start's tensor-core kernels against the CPU oracle.
+
+* the single-tile tcgen05 GEMM for every operand major-ness (descriptor check);
+* the network's forward pass and its parameter gradient (BF16 operands, FP32
+  accumulation) against oracle/warmstart.py emulating the same bf16 roundings;
+* a short Adam run that must fit a fixed target.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+from oracle import warmstart as ows
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("N,K", [(16, 16), (64, 32), (128, 64), (256, 64)])
+@pytest.mark.parametrize("a_mn,b_mn", [(0, 0), (1, 1), (0, 1), (1, 0)])
+def test_tensor_core_tile_gemm(cuda, N, K, a_mn, b_mn):
+    from galaxy_collision_gb300 import _native
+
+    L = _native.lib()
+    g = torch.Generator(device="cpu").manual_seed(N * 131 + K + 7 * a_mn + 3 * b_mn)
+    A = torch.randn(128, K, generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+    D = torch.full((128, N), float("nan"), device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    rc = L.gc_ws_selftest_gemm(C.c_void_p(A.data_ptr()), C.c_void_p(B.data_ptr()), C.c_void_p(D.data_ptr()), N, K,
+                               a_mn, b_mn, 0, _native.current_stream_handle(), C.c_void_p(st.data_ptr()))
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    ref = A.double() @ B.double().T
+    assert torch.allclose(D.double(), ref, rtol=1e-5, atol=1e-4)
+
+
+def _rand_params(seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for ci, co, _, _ in ows.LAYERS:
+        out += [rng.normal(0.0, np.sqrt(2.0 / (27 * ci)), size=(27, co, ci)).ravel(), rng.normal(0.0, 0.05, size=co)]
+    return np.concatenate(out).astype(np.float32)
+
+
+def _feat(R, seed):
+    rng = np.random.default_rng(seed)
+    return rng.normal(size=(3, R, R, R)).astype(np.float16)
+
+
+@pytest.mark.parametrize("R", [16, 32])
+def test_forward_matches_oracle(cuda, R):
+    from galaxy_collision_gb300.warmstart import WarmStartNet
+
+    p = _rand_params(R)
+    feat = _feat(R, R + 1)
+    net = WarmStartNet(R, params=p)
+    y = net.forward(torch.from_numpy(feat).cuda()).cpu().numpy()
+    assert net.status() == 0
+    yo, _ = ows.forward(p, feat, emulate=True)
+    assert rel_l2(y, yo) < 1e-2
+
+
+def test_backward_matches_oracle(cuda):
+    from galaxy_collision_gb300.warmstart import WarmStartNet, param_slices
+
+    R = 16
+    p = _rand_params(5)
+    feat = _feat(R, 6)
+    target = (0.1 * np.random.default_rng(7).normal(size=(R, R, R))).astype(np.float16)
+    net = WarmStartNet(R, params=p)
+    net.forward(torch.from_numpy(feat).cuda())
+    loss = float(net.backward(torch.from_numpy(target).cuda()).item())
+    g = net.grads().cpu().numpy()
+    assert net.status() == 0
+    _, cache = ows.forward(p, feat, emulate=True)
+    lo, go = ows.backward(cache, target.astype(np.float64), emulate=True)
+    assert loss == pytest.approx(lo, rel=1e-3)
+    for i, (ws, bs) in enumerate(param_slices()):
+        assert rel_l2(g[ws], go[ws]) < 3e-2, f"layer {i} weights"
+        assert rel_l2(g[bs], go[bs]) < 3e-2, f"layer {i} bias"
+
+
+def test_adam_fits_a_fixed_target(cuda):
+    """A smooth target that depends on the inputs: 80 Adam steps on one sample."""
+    from galaxy_collision_gb300.warmstart import WarmStartNet
+
+    R = 32
+    rng = np.random.default_rng(11)
+    z, y, x = np.meshgrid(*[np.linspace(-1, 1, R)] * 3, indexing="ij")
+    feat = np.stack([np.exp(-4 * (x**2 + y**2 + z**2)), x * y, np.sin(3 * z)]).astype(np.float16)
+    target = (0.5 * feat[0] - 0.3 * feat[2] + 0.05 * rng.normal(size=(R, R, R))).astype(np.float16)
+    net = WarmStartNet(R, seed=3)
+    f, t = torch.from_numpy(feat).cuda(), torch.from_numpy(target).cuda()
+    losses = []
+    for _ in range(80):
+        net.forward(f)
+        losses.append(float(net.backward(t).item()))
+        net.adam_step(lr=3e-3)
+    assert net.status() == 0
+    assert losses[-1] < 0.3 * losses[0], losses[::10]
+
+
+def _cluster(n, G, seed):
+    rng = np.random.default_rng(seed)
+    pos = (rng.normal(size=(n, 3)) * 3.0 + (G - 1) / 2.0).astype(np.float32)
+    vel = (rng.normal(size=(n, 3)) * 0.3).astype(np.float32)
+    mass = rng.uniform(0.5, 1.5, size=n).astype(np.float32) / n
+    return pos, vel, mass
+
+
+def _coarse(phi):
+    G = phi.shape[0]
+    return phi.reshape(G // 2, 2, G // 2, 2, G // 2, 2).mean(axis=(1, 3, 5))
+
+
+def test_engine_records_features_and_target(cuda):
+    """The recorded sample is the features of the step and the coarse change of the
+    potential its solve produced, scaled by the rms of the previous change."""
+    from galaxy_collision_gb300.engine import PMEngine
+
+    G, dt = 32, 0.05
+    pos, vel, mass = _cluster(20000, G, 1)
+    eng = PMEngine(G, 1.0, tol=1e-9, max_cycles=80, sort_every=0)
+    eng.set_warmstart("plain", track=True)
+    eng.load(pos, vel, mass)
+    eng.prime(dt)
+    phis = [eng.potential().double().cpu().numpy()]
+    for _ in range(2):
+        eng.advance(dt)
+        phis.append(eng.potential().double().cpu().numpy())
+    rec = torch.zeros((4, G // 2, G // 2, G // 2), dtype=torch.float16, device="cuda")
+    eng.record_sample(rec)
+    eng.advance(dt)
+    phis.append(eng.potential().double().cpu().numpy())
+    r = rec.float().cpu().numpy()
+    c = [_coarse(p) for p in phis]
+    d_prev, d_new = c[2] - c[1], c[3] - c[2]
+    s_prev = np.sqrt(np.mean(d_prev**2))
+    assert np.all(np.isfinite(r))
+    np.testing.assert_allclose(r[1], c[2] / np.sqrt(np.mean(c[2] ** 2)), rtol=0, atol=2e-3 * np.abs(r[1]).max())
+    np.testing.assert_allclose(r[2], d_prev / s_prev, rtol=0, atol=3e-3 * np.abs(r[2]).max())
+    np.testing.assert_allclose(r[3], d_new / s_prev, rtol=0, atol=3e-3 * np.abs(r[3]).max() + 1e-3)
+    assert r[0].min() >= 0.0  # log(1 + rho / mean)
+
+
+@pytest.mark.parametrize("mode", ["extrapolate", "learned"])
+def test_warm_start_modes_reach_the_same_solution(cuda, mode):
+    """Only the initial guess changes: trajectories agree with the plain warm start
+    to the solver tolerance, and an untrained network (zero output layer) needs
+    exactly the plain warm start's V-cycles."""
+    from galaxy_collision_gb300.engine import PMEngine
+    from galaxy_collision_gb300.warmstart import WarmStartNet
+
+    G, dt, steps = 32, 0.05, 8
+    pos, vel, mass = _cluster(30000, G, 2)
+
+    def run(m, net=None):
+        eng = PMEngine(G, 1.0, tol=1e-8, max_cycles=80, sort_every=0)
+        eng.set_warmstart(m, net=net, track=True)
+        eng.load(pos, vel, mass)
+        eng.prime(dt)
+        cyc = [eng.advance(dt).cycles for _ in range(steps)]
+        eng.synchronize(dt)
+        p, v, _, _ = eng.state_arrays()
+        return p.cpu().numpy(), v.cpu().numpy(), cyc
+
+    p0, v0, c0 = run("plain")
+    net = WarmStartNet(G // 2, seed=0) if mode == "learned" else None
+    p1, v1, c1 = run(mode, net)
+    assert np.abs(p1 - p0).max() < 1e-5
+    assert np.abs(v1 - v0).max() < 1e-5 * np.abs(v0).max() + 1e-7
+    if mode == "learned":
+        assert c1 == c0
+        assert net.status() == 0
