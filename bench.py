@@ -3,8 +3,11 @@
 
 One *step* is one KDK step of the fused engine on the resident state: int64
 fixed-point CIC deposit, multigrid to a 1e-6 relative residual (FP64-class
-double-float finest level, FP64 faces and coarsest solve), and the fused
-gather(-grad phi) + kick + drift particle pass. Workload (default): the
+double-float finest level, FP64 faces and coarsest solve) started from the
+linear extrapolation of the previous potentials (``--warmstart``), and the
+fused gather(-grad phi) + kick + drift particle pass. A Poisson comparison
+reports V-cycles and solve time from the plain, extrapolated and learned
+initial guesses. Workload (default): the
 two-disk collision with 40M + 60M particles on a 256^3 grid over [-32, 32]^3,
 dt = 0.005, seed 2, mass quantum 2^-40 of the total.
 
@@ -74,6 +77,14 @@ def _parse(argv=None):
     ap.add_argument("--profile-steps", type=int, default=3)
     ap.add_argument("--grad-grid", type=int, default=1,
                     help="1: gather from a float4 -grad(phi) grid; 0: form the gradient at the corners on the fly")
+    ap.add_argument("--warmstart", choices=("plain", "extrapolate", "learned"), default="extrapolate",
+                    help="initial guess of each solve: previous potential (the reference's), its linear "
+                         "extrapolation, or the extrapolation + the trained network's correction")
+    ap.add_argument("--pre-sweeps", type=int, default=2, help="red-black sweeps before restriction (reference: 2)")
+    ap.add_argument("--post-sweeps", type=int, default=2, help="red-black sweeps after prolongation (reference: 2)")
+    ap.add_argument("--sort-every", type=int, default=20, help="steps between cell sorts of the particles")
+    ap.add_argument("--compare-steps", type=int, default=6,
+                    help="steps per initial guess in the Poisson comparison (0 skips it)")
     ap.add_argument("--plain-steps", type=int, default=5,
                     help="steps of the stepwise (unfused) chain timed for comparison; 0 skips it")
     ap.add_argument("--no-accuracy", action="store_true",
@@ -277,9 +288,15 @@ def run_ours(args):
     bits = cfg.get("fixed_point_bits", 52)
     n = icr.n
 
-    def make_engine():
-        return PMEngine(G, dx, grav=1.0, origin=cfg["origin"], tol=args.tol, max_cycles=60, fixed_point_bits=bits,
-                        sort_every=20, grad_grid=bool(args.grad_grid))
+    net = _load_net() if args.warmstart == "learned" else None
+
+    def make_engine(mode=None):
+        e = PMEngine(G, dx, grav=1.0, origin=cfg["origin"], tol=args.tol, max_cycles=60, fixed_point_bits=bits,
+                     sort_every=args.sort_every, grad_grid=bool(args.grad_grid), pre_sweeps=args.pre_sweeps,
+                     post_sweeps=args.post_sweeps)
+        m = mode or args.warmstart
+        e.set_warmstart(m, net=(net if net is not None else _load_net()) if m == "learned" else None)
+        return e
 
     eng = make_engine()
     eng.load(icr.pos, icr.vel, icr.mass, icr.gid, sort=True)
@@ -320,7 +337,8 @@ def run_ours(args):
             "workload": f"{args.config}: {n:,} particles (two-disk collision), {G}^3 grid, box "
                         f"[{cfg['origin'][0]:g},{-cfg['origin'][0]:g}]^3, dt={dt}, seed {cfg['seed']}, "
                         f"multigrid to {args.tol:g} relative residual, int64 deposit quantum 2^-{bits} of the total",
-            "particles_per_gpu": n, "grid": G, "parallelism": f"replicas x{world}",
+            "warm_start": args.warmstart, "sweeps": [args.pre_sweeps, args.post_sweeps],
+            "sort_every": args.sort_every, "particles_per_gpu": n, "grid": G, "parallelism": f"replicas x{world}",
             "l2": "inputs larger than L2: 32 B/particle state = %.1f GB per GPU" % (n * 32 / 1e9),
             "vs_baseline_ref": "reference RTX 3070 published 6.95 steps/s at 100M, 256^3 (its tol 1e-3)",
         },
@@ -347,6 +365,7 @@ def run_ours(args):
             "smooth0", "sweep0", "resid0", "restrict", "smooth", "resid", "prolong", "prolong0", "tail", "faces", "reduce",
             "convert_q")) / args.profile_steps
         line["poisson"]["ms_per_solve"] = round(poisson_ms, 4)
+        line["poisson"]["warm_start"] = args.warmstart
 
         if not args.no_accuracy:
             eng.synchronize(dt)
@@ -358,6 +377,8 @@ def run_ours(args):
                                         "density and against the multigrid converged to 1e-10")
         del eng
         torch.cuda.empty_cache()
+        if args.compare_steps > 0:
+            line["poisson_comparison"] = _compare_warm_starts(icr, make_engine, dt, args.compare_steps)
         if args.plain_steps > 0:
             line["plain_chain"] = _plain_chain(icr, cfg, args.tol, args.plain_steps, min(args.warmup, 3))
             line["plain_chain"]["fused_speedup"] = round(line["plain_chain"]["ms_per_step"] /
@@ -377,6 +398,53 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def _load_net():
+    """The trained warm-start network shipped with the package (None if absent)."""
+    from galaxy_collision_gb300.warmstart import WEIGHTS_PATH, WarmStartNet
+
+    return WarmStartNet.load(WEIGHTS_PATH) if WEIGHTS_PATH.exists() else None
+
+
+def _compare_warm_starts(icr, make_engine, dt, steps, warm=4):
+    """V-cycles and solve time to the same relative residual from each initial
+    guess: plain (previous potential, the reference's warm start), linear
+    extrapolation, and extrapolation + the trained network (when its weights are
+    present). Same initial conditions; CUDA-event time of each kernel."""
+    import torch
+
+    out = {}
+    modes = ["plain", "extrapolate"] + (["learned"] if _load_net() is not None else [])
+    for mode in modes:
+        eng = make_engine(mode)
+        eng.load(icr.pos, icr.vel, icr.mass, icr.gid, sort=True)
+        eng.prime(dt)
+        for _ in range(warm):
+            eng.advance(dt)
+        eng.ctx.profile_reset()
+        eng.ctx.profile(True)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record()
+        res = [eng.advance(dt) for _ in range(steps)]
+        ev1.record()
+        torch.cuda.synchronize()
+        stats = eng.ctx.kernel_stats()
+        eng.ctx.profile(False)
+        solve = sum(v[2] for k, v in stats.items() if k in (
+            "smooth0", "sweep0", "resid0", "restrict", "smooth", "resid", "prolong", "prolong0", "tail", "faces",
+            "reduce", "warmstart")) / steps
+        out[mode] = {"mean_vcycles": float(np.mean([r.cycles for r in res])),
+                     "max_rel_residual": float(max(r.rel_residual for r in res)),
+                     "ms_per_solve": round(solve, 4),
+                     "initial_guess_ms": round(stats.get("warmstart", (0, 0, 0.0))[2] / steps, 4),
+                     "ms_per_step": round(ev0.elapsed_time(ev1) / steps, 4)}
+        del eng
+        torch.cuda.empty_cache()
+    out["note"] = ("same initial conditions, steps after a short warm-up; solve = multigrid kernels + faces + "
+                   "initial-guess kernels (network included); all reach the same relative residual")
+    return out
 
 
 def _plain_chain(icr, cfg, tol, steps, warmup):

@@ -109,14 +109,15 @@ struct gc_ctx {
   int ws_mode;          // GC_WS_PLAIN / GC_WS_LEARNED / GC_WS_EXTRAPOLATE
   int ws_track;         // maintain the coarse history
   int ws_hist;          // solves recorded in the history (0, 1, 2+)
-  void *ws_record;      // one-shot f16 [4][R^3] sample destination
+  void *ws_record;      // one-shot f16 [5][R^3] sample destination
+  int ws_skip;          // this step leaves the history alone (PRIME after CLOSE)
   float *ws_buf;        // rho_c, phi_c, delta_c, y (R^3 each) + scalars + partials
   size_t ws_buf_cap;
 
   char err[512];
 };
 
-int gc_ws_pre_solve(gc_ctx *ctx, int warm);
+int gc_ws_pre_solve(gc_ctx *ctx, int warm, int mode);
 int gc_ws_post_solve(gc_ctx *ctx);
 
 // Launch `k` on ctx's stream, counting it under `kid` and bracketing it with

@@ -45,7 +45,7 @@ extern "C" int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_para
     GC_CUDA(ctx, cudaMemsetAsync(ctx->lo, 0, g3 * sizeof(float), ctx->stream));
   }
   // learned / extrapolated correction of the previous potential, sample recording
-  if ((s = gc_ws_pre_solve(ctx, warm))) return s;
+  if ((s = gc_ws_pre_solve(ctx, warm, sp->mode))) return s;
   if ((s = gc_faces_from_moments(ctx))) return s;
   gc_mg_stats mst;
   if ((s = gc_mg_run(ctx, &sp->mg, &mst))) return s;

@@ -227,6 +227,36 @@ __device__ __noinline__ void flush_run(long long *__restrict__ qg, unsigned key,
 }
 #define FLUSH_RUN(qg, key, G, q) flush_run(qg, key, G, q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7])
 
+// Where runs go: the global int64 grid, or (box != null) a shared-memory box of
+// nodes [x0, x0+nx) x [y0, y0+ny) x [z0, z0+nz) that holds every corner of the
+// CTA's current particles and is added to the grid afterwards.
+struct DepSink {
+  long long *qg;
+  unsigned long long *box;
+  int x0, y0, z0, ny, nz, G;
+};
+
+__device__ __noinline__ void flush_run_box(DepSink k, unsigned key, long long q0, long long q1, long long q2,
+                                           long long q3, long long q4, long long q5, long long q6, long long q7) {
+  const int G1 = k.G + 1;
+  const int ix = (int)(key / (unsigned)(G1 * G1)) - 1 - k.x0, iy = (int)((key / (unsigned)G1) % (unsigned)G1) - 1 - k.y0,
+            iz = (int)(key % (unsigned)G1) - 1 - k.z0;
+  const long long q[8] = {q0, q1, q2, q3, q4, q5, q6, q7};
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    if (q[c] != 0)
+      atomicAdd(k.box + ((ix + (c >> 2)) * k.ny + (iy + ((c >> 1) & 1))) * k.nz + (iz + (c & 1)),
+                (unsigned long long)q[c]);
+  }
+}
+
+__device__ __forceinline__ void sink_run(const DepSink &k, unsigned key, const long long (&q)[8]) {
+  if (k.box)
+    flush_run_box(k, key, q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7]);
+  else
+    FLUSH_RUN(k.qg, key, k.G, q);
+}
+
 struct DepRun {
   unsigned key;  // cell key, DEP_NONE when empty
   bool small;    // every contribution summed here was below 2^22 quanta
@@ -235,10 +265,8 @@ struct DepRun {
 
 // Deposit one particle into the two-run cache; returns nothing, may evict.
 template <bool POW2>
-__device__ __forceinline__ void dep_particle(float px, float py, float pz, float pm, const DepCtx &d, float inv_dx,
-                                             float qscale, long long *__restrict__ qg, unsigned *__restrict__ status,
-                                             DepRun &r0, DepRun &r1) {
-  if (!gc_finite3(px, py, pz)) atomicOr(status, GC_FLAG_NONFINITE_POS);
+__device__ __forceinline__ bool dep_cell(float px, float py, float pz, const DepCtx &d, float inv_dx, int &ix, int &iy,
+                                         int &iz, float &fx, float &fy, float &fz) {
   float gx, gy, gz;
   if (POW2) {  // x / dx == x * (1/dx) exactly when dx is a power of two
     gx = __fmul_rn(px, inv_dx); gy = __fmul_rn(py, inv_dx); gz = __fmul_rn(pz, inv_dx);
@@ -246,10 +274,21 @@ __device__ __forceinline__ void dep_particle(float px, float py, float pz, float
     gx = __fdiv_rn(px, d.dx); gy = __fdiv_rn(py, d.dx); gz = __fdiv_rn(pz, d.dx);
   }
   const float hi = (float)d.G;
-  if (!(gx >= -1.0f && gx < hi && gy >= -1.0f && gy < hi && gz >= -1.0f && gz < hi)) return;
+  if (!(gx >= -1.0f && gx < hi && gy >= -1.0f && gy < hi && gz >= -1.0f && gz < hi)) return false;
   const float flx = floorf(gx), fly = floorf(gy), flz = floorf(gz);
-  const int ix = (int)flx, iy = (int)fly, iz = (int)flz;
-  const float fx = __fsub_rn(gx, flx), fy = __fsub_rn(gy, fly), fz = __fsub_rn(gz, flz);
+  ix = (int)flx; iy = (int)fly; iz = (int)flz;
+  fx = __fsub_rn(gx, flx); fy = __fsub_rn(gy, fly); fz = __fsub_rn(gz, flz);
+  return true;
+}
+
+template <bool POW2>
+__device__ __forceinline__ void dep_particle(float px, float py, float pz, float pm, const DepCtx &d, float inv_dx,
+                                             float qscale, const DepSink &sink, unsigned *__restrict__ status,
+                                             DepRun &r0, DepRun &r1) {
+  if (!gc_finite3(px, py, pz)) atomicOr(status, GC_FLAG_NONFINITE_POS);
+  int ix, iy, iz;
+  float fx, fy, fz;
+  if (!dep_cell<POW2>(px, py, pz, d, inv_dx, ix, iy, iz, fx, fy, fz)) return;
   const float mm = __fmul_rn(pm, d.inv_vol);
   const unsigned key = (unsigned)(((ix + 1) * (d.G + 1) + (iy + 1)) * (d.G + 1) + (iz + 1));
   const bool small = __fmul_rn(fabsf(mm), qscale) < 4194304.0f;  // every |w| <= |mm|
@@ -278,7 +317,7 @@ __device__ __forceinline__ void dep_particle(float px, float py, float pz, float
 #pragma unroll
     for (int t = 0; t < 8; ++t) r1.q[t] += q[t];
   } else {  // evict run 1, demote run 0, start a new run 0
-    if (r1.key != DEP_NONE) FLUSH_RUN(qg, r1.key, d.G, r1.q);
+    if (r1.key != DEP_NONE) sink_run(sink, r1.key, r1.q);
     r1.key = r0.key;
     r1.small = r0.small;
 #pragma unroll
@@ -291,7 +330,7 @@ __device__ __forceinline__ void dep_particle(float px, float py, float pz, float
 }
 
 // Merge the cached runs of lanes holding the same cell and add them to the grid.
-__device__ __forceinline__ void dep_merge(const DepRun &r, long long *__restrict__ qg, int G, int lane) {
+__device__ __forceinline__ void dep_merge(const DepRun &r, const DepSink &sink, int lane) {
   const unsigned peers = __match_any_sync(0xffffffffu, r.key);
   const unsigned large = __ballot_sync(0xffffffffu, !r.small);
   if (r.key == DEP_NONE) return;
@@ -300,59 +339,125 @@ __device__ __forceinline__ void dep_merge(const DepRun &r, long long *__restrict
     long long tot[8];
 #pragma unroll
     for (int t = 0; t < 8; ++t) tot[t] = (long long)__reduce_add_sync(peers, (int)r.q[t]);
-    if (lane == __ffs(peers) - 1) FLUSH_RUN(qg, r.key, G, tot);
+    if (lane == __ffs(peers) - 1) sink_run(sink, r.key, tot);
   } else {
-    FLUSH_RUN(qg, r.key, G, r.q);
+    sink_run(sink, r.key, r.q);
   }
 }
 
+// The CTA stages a tile of DEP_TILE consecutive particles in shared memory with
+// coalesced loads (one padding word per 32 keeps the per-thread reads of 8
+// consecutive particles conflict-free) and finds the box of cells they touch.
+// When the box's corner nodes fit DEP_BOX_CAP int64 words, the runs are added
+// to that box in shared memory (cheap atomics, whatever the order of particles
+// that drifted between sorts) and the box is added to the grid once, one
+// atomic per nonzero node; otherwise the runs go straight to the grid. Every
+// thread walks its 8 particles in a rolled loop (small code).
+#define DEP_TILE (256 * DEP_SEQ)
+#define DEP_PAD(i) ((i) + ((i) >> 5))
+#define DEP_BOX_CAP 4096
+#define DEP_SMEM_BYTES (DEP_BOX_CAP * 8 + 4 * DEP_PAD(DEP_TILE) * 4 + 64)
 template <bool POW2, bool VEC>
 __global__ void __launch_bounds__(256)
     k_deposit_sorted(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
                      const float *__restrict__ m, long long n, DepCtx d, float inv_dx,
                      const double *__restrict__ qexp, long long *__restrict__ qg, unsigned *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned long long dep_smem[];  // DEP_SMEM_BYTES
+  unsigned long long *box = dep_smem;
+  float *sx = reinterpret_cast<float *>(box + DEP_BOX_CAP), *sy = sx + DEP_PAD(DEP_TILE), *sz = sy + DEP_PAD(DEP_TILE),
+        *sm_ = sz + DEP_PAD(DEP_TILE);
+  int *bnd = reinterpret_cast<int *>(sm_ + DEP_PAD(DEP_TILE));
   const float qscale = ldexpf(1.0f, -(int)(*qexp));
-  const int lane = threadIdx.x & 31;
-  const long long span = 32LL * DEP_SEQ;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long w0 = ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * span; w0 < n;
-       w0 += nwarps * span) {
-    const long long s0 = w0 + (long long)lane * DEP_SEQ;
-    const long long left = n - s0;
-    const int cnt = left <= 0 ? 0 : (left >= DEP_SEQ ? DEP_SEQ : (int)left);
+  const int tid = threadIdx.x, lane = tid & 31;
+  for (long long t0 = (long long)blockIdx.x * DEP_TILE; t0 < n; t0 += (long long)gridDim.x * DEP_TILE) {
+    const int cnt_tile = (int)(n - t0 < DEP_TILE ? n - t0 : DEP_TILE);
+    __syncthreads();  // the previous tile and box have been consumed
+    if (tid < 3) { bnd[tid] = 0x7fffffff; bnd[3 + tid] = -0x7fffffff; }
+    if (VEC && cnt_tile == DEP_TILE) {
+#pragma unroll
+      for (int h = 0; h < DEP_SEQ / 4; ++h) {
+        const int q4 = h * 256 + tid;  // float4 index inside the tile
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(x + t0) + q4);
+        const float4 b = __ldg(reinterpret_cast<const float4 *>(y + t0) + q4);
+        const float4 c = __ldg(reinterpret_cast<const float4 *>(z + t0) + q4);
+        const float4 e = __ldg(reinterpret_cast<const float4 *>(m + t0) + q4);
+        const int i = 4 * q4;
+        sx[DEP_PAD(i)] = a.x; sx[DEP_PAD(i + 1)] = a.y; sx[DEP_PAD(i + 2)] = a.z; sx[DEP_PAD(i + 3)] = a.w;
+        sy[DEP_PAD(i)] = b.x; sy[DEP_PAD(i + 1)] = b.y; sy[DEP_PAD(i + 2)] = b.z; sy[DEP_PAD(i + 3)] = b.w;
+        sz[DEP_PAD(i)] = c.x; sz[DEP_PAD(i + 1)] = c.y; sz[DEP_PAD(i + 2)] = c.z; sz[DEP_PAD(i + 3)] = c.w;
+        sm_[DEP_PAD(i)] = e.x; sm_[DEP_PAD(i + 1)] = e.y; sm_[DEP_PAD(i + 2)] = e.z; sm_[DEP_PAD(i + 3)] = e.w;
+      }
+    } else {
+      for (int i = tid; i < cnt_tile; i += 256) {
+        sx[DEP_PAD(i)] = x[t0 + i];
+        sy[DEP_PAD(i)] = y[t0 + i];
+        sz[DEP_PAD(i)] = z[t0 + i];
+        sm_[DEP_PAD(i)] = m[t0 + i];
+      }
+    }
+    __syncthreads();
+    const int i0 = tid * DEP_SEQ;
+    const int cnt = cnt_tile - i0 < 0 ? 0 : (cnt_tile - i0 > DEP_SEQ ? DEP_SEQ : cnt_tile - i0);
+    // box of the cells that receive mass
+    int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {-0x7fffffff, -0x7fffffff, -0x7fffffff};
+#pragma unroll 1
+    for (int j = 0; j < cnt; ++j) {
+      const int i = DEP_PAD(i0 + j);
+      int ix, iy, iz;
+      float fx, fy, fz;
+      if (dep_cell<POW2>(sx[i], sy[i], sz[i], d, inv_dx, ix, iy, iz, fx, fy, fz)) {
+        lo[0] = min(lo[0], ix); lo[1] = min(lo[1], iy); lo[2] = min(lo[2], iz);
+        hi[0] = max(hi[0], ix); hi[1] = max(hi[1], iy); hi[2] = max(hi[2], iz);
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = __reduce_min_sync(0xffffffffu, lo[a]);
+      hi[a] = __reduce_max_sync(0xffffffffu, hi[a]);
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) { atomicMin(&bnd[a], lo[a]); atomicMax(&bnd[3 + a], hi[a]); }
+    }
+    __syncthreads();
+    DepSink sink;
+    sink.qg = qg;
+    sink.G = d.G;
+    sink.box = nullptr;
+    sink.x0 = bnd[0]; sink.y0 = bnd[1]; sink.z0 = bnd[2];
+    const int nx = bnd[3] - bnd[0] + 2, ny = bnd[4] - bnd[1] + 2, nz = bnd[5] - bnd[2] + 2;
+    sink.ny = ny; sink.nz = nz;
+    const bool any = bnd[3] >= bnd[0];
+    const int vol = any ? nx * ny * nz : 0;  // at most (G+2)^3 < 2^31 nodes
+    const bool use_box = any && (long long)nx * ny * nz <= DEP_BOX_CAP;
+    if (use_box) {
+      sink.box = box;
+      for (int i = tid; i < vol; i += 256) box[i] = 0ull;
+      __syncthreads();
+    }
     DepRun r0, r1;
     r0.key = r1.key = DEP_NONE;
     r0.small = r1.small = true;
 #pragma unroll
     for (int t = 0; t < 8; ++t) r0.q[t] = r1.q[t] = 0;
-#pragma unroll
-    for (int h = 0; h < DEP_SEQ / 4; ++h) {
-      float px[4], py[4], pz[4], pm[4];
-      if (VEC && cnt == DEP_SEQ) {
-        const float4 a = __ldg(reinterpret_cast<const float4 *>(x + s0) + h);
-        const float4 b = __ldg(reinterpret_cast<const float4 *>(y + s0) + h);
-        const float4 c = __ldg(reinterpret_cast<const float4 *>(z + s0) + h);
-        const float4 e = __ldg(reinterpret_cast<const float4 *>(m + s0) + h);
-        px[0] = a.x; px[1] = a.y; px[2] = a.z; px[3] = a.w;
-        py[0] = b.x; py[1] = b.y; py[2] = b.z; py[3] = b.w;
-        pz[0] = c.x; pz[1] = c.y; pz[2] = c.z; pz[3] = c.w;
-        pm[0] = e.x; pm[1] = e.y; pm[2] = e.z; pm[3] = e.w;
-      } else {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const bool in = 4 * h + j < cnt;
-          px[j] = in ? x[s0 + 4 * h + j] : 0.0f;
-          py[j] = in ? y[s0 + 4 * h + j] : 0.0f;
-          pz[j] = in ? z[s0 + 4 * h + j] : 0.0f;
-          pm[j] = in ? m[s0 + 4 * h + j] : 0.0f;
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-        if (4 * h + j < cnt) dep_particle<POW2>(px[j], py[j], pz[j], pm[j], d, inv_dx, qscale, qg, status, r0, r1);
+#pragma unroll 1
+    for (int j = 0; j < cnt; ++j) {
+      const int i = DEP_PAD(i0 + j);
+      dep_particle<POW2>(sx[i], sy[i], sz[i], sm_[i], d, inv_dx, qscale, sink, status, r0, r1);
     }
-    dep_merge(r0, qg, d.G, lane);
-    dep_merge(r1, qg, d.G, lane);
+    dep_merge(r0, sink, lane);
+    dep_merge(r1, sink, lane);
+    if (use_box) {
+      __syncthreads();
+      for (int i = tid; i < vol; i += 256) {
+        const unsigned long long v = box[i];
+        if (v == 0ull) continue;
+        const int bx = i / (ny * nz), rem = i - bx * ny * nz, by = rem / nz, bz = rem - by * nz;
+        const int jx = sink.x0 + bx, jy = sink.y0 + by, jz = sink.z0 + bz;
+        if ((unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G && (unsigned)jz < (unsigned)d.G)
+          atomicAdd((unsigned long long *)(qg + ((size_t)jx * d.G + jy) * d.G + jz), v);
+      }
+    }
   }
 }
 
@@ -363,24 +468,31 @@ int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, co
   d.dx = (float)ctx->dx;
   d.inv_vol = 1.0f / ((d.dx * d.dx) * d.dx);
   d.G = ctx->G;
-  const long long nspans = (n + 32LL * DEP_SEQ - 1) / (32LL * DEP_SEQ);
-  unsigned nb = gc_blocks(nspans, 8);
-  if (nb > 152u * 8u) nb = 152u * 8u;
+  const long long ntiles = (n + DEP_TILE - 1) / DEP_TILE;
+  unsigned nb = (unsigned)(ntiles < 152LL * 8 ? ntiles : 152LL * 8);
   int fe = 0;
   const bool pow2 = std::frexp(d.dx, &fe) == 0.5f;
   const float inv_dx = pow2 ? std::ldexp(1.0f, 1 - fe) : 0.0f;
   const bool vec = ((((uintptr_t)x) | ((uintptr_t)y) | ((uintptr_t)z) | ((uintptr_t)m)) & 15u) == 0;
+  static bool attr_set = false;  // dynamic shared memory above the 48 KB default, once per process
+  if (!attr_set) {
+    GC_CUDA(ctx, cudaFuncSetAttribute(k_deposit_sorted<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DEP_SMEM_BYTES));
+    GC_CUDA(ctx, cudaFuncSetAttribute(k_deposit_sorted<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, DEP_SMEM_BYTES));
+    GC_CUDA(ctx, cudaFuncSetAttribute(k_deposit_sorted<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DEP_SMEM_BYTES));
+    GC_CUDA(ctx, cudaFuncSetAttribute(k_deposit_sorted<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, DEP_SMEM_BYTES));
+    attr_set = true;
+  }
   if (pow2 && vec)
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true, true>, dim3(nb), dim3(256), 0, x, y, z, m,
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true, true>, dim3(nb), dim3(256), DEP_SMEM_BYTES, x, y, z, m,
               (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
   else if (pow2)
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true, false>, dim3(nb), dim3(256), 0, x, y, z, m,
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true, false>, dim3(nb), dim3(256), DEP_SMEM_BYTES, x, y, z, m,
               (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
   else if (vec)
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false, true>, dim3(nb), dim3(256), 0, x, y, z, m,
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false, true>, dim3(nb), dim3(256), DEP_SMEM_BYTES, x, y, z, m,
               (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
   else
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false, false>, dim3(nb), dim3(256), 0, x, y, z, m,
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false, false>, dim3(nb), dim3(256), DEP_SMEM_BYTES, x, y, z, m,
               (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
   GC_LAUNCH_CHECK(ctx, "deposit");
   return GC_OK;
@@ -752,11 +864,21 @@ __global__ void __launch_bounds__(256) k_grad4(const float *__restrict__ phi, fl
                       grad_comp(phi, c, 1, k, g.G, g.inv_dx, g.inv_2dx), 0.0f);
 }
 
+template <bool POW2>
 __device__ __forceinline__ void gather_g4(const float4 *__restrict__ g4, float x, float y, float z, const FusedCtx &f,
                                           float &ax, float &ay, float &az) {
   ax = ay = az = 0.0f;
   CellPos c;
-  if (!gc_cell_of(x, y, z, f.dx, f.G, c)) return;
+  if (POW2) {  // x / dx == x * (1/dx) exactly when dx is a power of two
+    const float gx = __fmul_rn(x, f.inv_dx), gy = __fmul_rn(y, f.inv_dx), gz = __fmul_rn(z, f.inv_dx);
+    const float hi = (float)f.G;
+    if (!(gx >= -1.0f && gx < hi && gy >= -1.0f && gy < hi && gz >= -1.0f && gz < hi)) return;
+    const float flx = floorf(gx), fly = floorf(gy), flz = floorf(gz);
+    c.ix = (int)flx; c.iy = (int)fly; c.iz = (int)flz;
+    c.fx = __fsub_rn(gx, flx); c.fy = __fsub_rn(gy, fly); c.fz = __fsub_rn(gz, flz);
+  } else if (!gc_cell_of(x, y, z, f.dx, f.G, c)) {
+    return;
+  }
   const int G = f.G;
   const float wx[2] = {__fsub_rn(1.0f, c.fx), c.fx};
   const float wy[2] = {__fsub_rn(1.0f, c.fy), c.fy};
@@ -780,7 +902,50 @@ __device__ __forceinline__ void gather_g4(const float4 *__restrict__ g4, float x
       }
 }
 
+// One particle of the fused pass (closing half-kick, diagnostics, opening
+// half-kick, drift) given its acceleration; writes back x, v.
 template <bool DIAG>
+__device__ __forceinline__ void kd_update(long long p, float px, float py, float pz, float ux, float uy, float uz,
+                                          float ax, float ay, float az, float *__restrict__ x, float *__restrict__ y,
+                                          float *__restrict__ z, float *__restrict__ vx, float *__restrict__ vy,
+                                          float *__restrict__ vz, const float *__restrict__ m, const FusedCtx &f,
+                                          double (&dv)[11]) {
+  if (f.mode != GC_STEP_PRIME) {
+    ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
+    uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
+    uz = __fadd_rn(uz, __fmul_rn(az, f.h));
+  }
+  if (DIAG) {
+    const double mm = m[p];
+    const double X = px, Y = py, Z = pz, VX = ux, VY = uy, VZ = uz;
+    dv[0] += mm;
+    dv[1] += 0.5 * mm * (VX * VX + VY * VY + VZ * VZ);
+    dv[2] += mm * VX;
+    dv[3] += mm * VY;
+    dv[4] += mm * VZ;
+    dv[5] += mm * (Y * VZ - Z * VY);
+    dv[6] += mm * (Z * VX - X * VZ);
+    dv[7] += mm * (X * VY - Y * VX);
+    dv[8] += mm * X;
+    dv[9] += mm * Y;
+    dv[10] += mm * Z;
+  }
+  if (f.mode != GC_STEP_CLOSE) {
+    ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
+    uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
+    uz = __fadd_rn(uz, __fmul_rn(az, f.h));
+    x[p] = __fadd_rn(px, __fmul_rn(ux, f.dt));
+    y[p] = __fadd_rn(py, __fmul_rn(uy, f.dt));
+    z[p] = __fadd_rn(pz, __fmul_rn(uz, f.dt));
+  }
+  vx[p] = ux;
+  vy[p] = uy;
+  vz[p] = uz;
+}
+
+// Two particles per thread per iteration (p and p + stride): their loads and
+// corner gathers are independent, so twice as many requests are in flight.
+template <bool DIAG, bool POW2>
 __global__ void __launch_bounds__(256)
     k_gather4_kick_drift(float *__restrict__ x, float *__restrict__ y, float *__restrict__ z, float *__restrict__ vx,
                          float *__restrict__ vy, float *__restrict__ vz, const float *__restrict__ m, long long n,
@@ -788,42 +953,18 @@ __global__ void __launch_bounds__(256)
   double dv[11];
 #pragma unroll
   for (int t = 0; t < 11; ++t) dv[t] = 0.0;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
-    const float px = x[p], py = y[p], pz = z[p];
-    float ux = vx[p], uy = vy[p], uz = vz[p];
-    float ax, ay, az;
-    gather_g4(g4, px, py, pz, f, ax, ay, az);
-    if (f.mode != GC_STEP_PRIME) {
-      ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
-      uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
-      uz = __fadd_rn(uz, __fmul_rn(az, f.h));
-    }
-    if (DIAG) {
-      const double mm = m[p];
-      const double X = px, Y = py, Z = pz, VX = ux, VY = uy, VZ = uz;
-      dv[0] += mm;
-      dv[1] += 0.5 * mm * (VX * VX + VY * VY + VZ * VZ);
-      dv[2] += mm * VX;
-      dv[3] += mm * VY;
-      dv[4] += mm * VZ;
-      dv[5] += mm * (Y * VZ - Z * VY);
-      dv[6] += mm * (Z * VX - X * VZ);
-      dv[7] += mm * (X * VY - Y * VX);
-      dv[8] += mm * X;
-      dv[9] += mm * Y;
-      dv[10] += mm * Z;
-    }
-    if (f.mode != GC_STEP_CLOSE) {
-      ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
-      uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
-      uz = __fadd_rn(uz, __fmul_rn(az, f.h));
-      x[p] = __fadd_rn(px, __fmul_rn(ux, f.dt));
-      y[p] = __fadd_rn(py, __fmul_rn(uy, f.dt));
-      z[p] = __fadd_rn(pz, __fmul_rn(uz, f.dt));
-    }
-    vx[p] = ux;
-    vy[p] = uy;
-    vz[p] = uz;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += 2 * stride) {
+    const long long q = p + stride;
+    const bool hq = q < n;
+    const float px = x[p], py = y[p], pz = z[p], ux = vx[p], uy = vy[p], uz = vz[p];
+    float qx = 0.0f, qy = 0.0f, qz = 0.0f, wx = 0.0f, wy = 0.0f, wz = 0.0f;
+    if (hq) { qx = x[q]; qy = y[q]; qz = z[q]; wx = vx[q]; wy = vy[q]; wz = vz[q]; }
+    float ax, ay, az, bx = 0.0f, by = 0.0f, bz = 0.0f;
+    gather_g4<POW2>(g4, px, py, pz, f, ax, ay, az);
+    if (hq) gather_g4<POW2>(g4, qx, qy, qz, f, bx, by, bz);
+    kd_update<DIAG>(p, px, py, pz, ux, uy, uz, ax, ay, az, x, y, z, vx, vy, vz, m, f, dv);
+    if (hq) kd_update<DIAG>(q, qx, qy, qz, wx, wy, wz, bx, by, bz, x, y, z, vx, vy, vz, m, f, dv);
   }
   if (DIAG) block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
 }
@@ -849,12 +990,12 @@ int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode,
     const GradCtx g = make_grad(ctx);
     gc_launch(ctx, GK_GRAD, k_grad4, dim3(gc_blocks(g.G, 32), gc_blocks(g.G, 8), g.G), dim3(32, 8), 0, ctx->hi,
               (float4 *)ctx->g4, g);
-    if (diag)
-      gc_launch(ctx, GK_GATHER_KD, k_gather4_kick_drift<true>, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx,
-                p->vy, p->vz, p->m, (long long)p->n, (const float4 *)ctx->g4, f, ctx->red);
-    else
-      gc_launch(ctx, GK_GATHER_KD, k_gather4_kick_drift<false>, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx,
-                p->vy, p->vz, p->m, (long long)p->n, (const float4 *)ctx->g4, f, ctx->red);
+    int fe = 0;
+    const bool pow2 = std::frexp(f.dx, &fe) == 0.5f;  // then inv_dx is exact
+    auto k = diag ? (pow2 ? k_gather4_kick_drift<true, true> : k_gather4_kick_drift<true, false>)
+                  : (pow2 ? k_gather4_kick_drift<false, true> : k_gather4_kick_drift<false, false>);
+    gc_launch(ctx, GK_GATHER_KD, k, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx, p->vy, p->vz, p->m,
+              (long long)p->n, (const float4 *)ctx->g4, f, ctx->red);
   } else if (diag) {
     gc_launch(ctx, GK_GATHER_KD, k_gather_kick_drift<true>, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx, p->vy,
               p->vz, p->m, (long long)p->n, ctx->hi, f, axo, ayo, azo, ctx->red);

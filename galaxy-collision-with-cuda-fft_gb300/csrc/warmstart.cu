@@ -13,6 +13,8 @@
 
 // Clock budget of every mbarrier wait (about one second at 2 GHz).
 #define WS_WAIT_BUDGET 2000000000LL
+// Warps whose lane 0 issues tensor-core MMAs (each commits once per phase).
+#define WS_ISSUERS 4
 
 // ------------------------------------------------------------------------------
 // single-tile GEMM check: D (128 x N, f32) = A (128 x K) * B (N x K)^T
@@ -178,7 +180,7 @@ __device__ __forceinline__ void load_taps(const uint4 *__restrict__ w, int g, in
   const uint4 *src = w + (size_t)t0 * (tap_bytes / 16u);
   uint4 *d = reinterpret_cast<uint4 *>(dst);
   const int n16 = (t1 - t0) * (int)(tap_bytes / 16u);
-  for (int i = tid; i < n16; i += blockDim.x) d[i] = __ldg(src + i);
+  for (int i = tid; i < n16; i += blockDim.x) umma::cp_async16(d + i, src + i, true);
 }
 
 __global__ void __launch_bounds__(256) k_conv_fwd(ConvFwd a) {
@@ -204,24 +206,33 @@ __global__ void __launch_bounds__(256) k_conv_fwd(ConvFwd a) {
     umma::tmem_alloc(tslot, a.tmem_cols);
     umma::tmem_relinquish();
   }
-  if (tid == 0) {
-    umma::mbar_init(&bars[0], 1);
-    umma::mbar_init(&bars[1], 1);
+  if (tid == 0) {  // one arrival per issuing warp (WS_ISSUERS commits per phase)
+    umma::mbar_init(&bars[0], WS_ISSUERS);
+    umma::mbar_init(&bars[1], WS_ISSUERS);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // input tile, zero outside the grid, plus a zero margin read by the last M tile
+  // input tile, zero outside the grid, plus a zero margin read by the last M tile;
+  // one warp per padded line, lanes along x
   uint4 *trow = reinterpret_cast<uint4 *>(tile);
-  for (int i = tid; i < kci * V; i += blockDim.x) {
-    const int kc = i / V, L = i - kc * V;
-    const int tz = L / P, rem = L - tz * P, ty = rem / W2, tx = rem - ty * W2;
-    const int gz = z0 - 1 + tz, gy = y0 - 1 + ty, gx = tx - 1;
-    uint4 v = make_uint4(0u, 0u, 0u, 0u);
-    if ((unsigned)gz < (unsigned)R && (unsigned)gy < (unsigned)R && (unsigned)gx < (unsigned)R)
-      v = __ldg(a.in + (size_t)kc * R3 + ((size_t)gz * R + gy) * R + gx);
-    trow[i] = v;
+  {
+    const int nzy = (a.BZ + 2) * (a.BY + 2), nrows = kci * nzy, nwarps = blockDim.x >> 5;
+    for (int row = warp; row < nrows; row += nwarps) {
+      const int kc = row / nzy, rr = row - kc * nzy;
+      const int tz = rr / (a.BY + 2), ty = rr - tz * (a.BY + 2);
+      const int gz = z0 - 1 + tz, gy = y0 - 1 + ty;
+      const bool rowin = (unsigned)gz < (unsigned)R && (unsigned)gy < (unsigned)R;
+      const uint4 *src = a.in + (size_t)kc * R3 + ((size_t)(rowin ? gz : 0) * R + (rowin ? gy : 0)) * R;
+      uint4 *dst = trow + (size_t)kc * V + (size_t)rr * W2;
+      for (int tx = lane; tx < W2; tx += 32) {
+        const int gx = tx - 1;
+        const bool in = rowin && (unsigned)gx < (unsigned)R;
+        umma::cp_async16(dst + tx, in ? (const void *)(src + gx) : (const void *)a.in, in);
+      }
+    }
   }
   for (int i = tid; i < 128; i += blockDim.x) trow[kci * V + i] = make_uint4(0u, 0u, 0u, 0u);
   load_taps(a.w, 0, a.tpg, tap_bytes, ring, tid);
+  umma::cp_async_wait_all();
   umma::fence_async_smem();
   umma::tc_fence_before();
   __syncthreads();
@@ -235,16 +246,19 @@ __global__ void __launch_bounds__(256) k_conv_fwd(ConvFwd a) {
   bool fail = false;
   for (int g = 0; g < ngroups; ++g) {
     const int s = g & 1;
-    if (tid == 0) {
+    if (lane == 0 && warp < WS_ISSUERS) {  // issuer w owns the M tiles mt = w (mod WS_ISSUERS)
+      umma::tc_fence_after();
       const int t0 = g * a.tpg, t1 = min(27, t0 + a.tpg);
+      // descriptors differ only in the start address (bits 0..13, address / 16)
+      const uint64_t ad0 = umma::sdesc(tile_u32, a_lbo, 128u), bd0 = umma::sdesc(ring_u32, b_lbo, 128u);
       for (int t = t0; t < t1; ++t) {
         const int off = tap_offset(t, P, W2);
-        for (int mt = 0; mt < a.n_mt; ++mt) {
-          const uint32_t arow = tile_u32 + (uint32_t)(L0 + 128 * mt + off) * 16u;
-          const uint32_t brow = ring_u32 + (uint32_t)s * slot_bytes + (uint32_t)(t - t0) * tap_bytes;
+        const uint32_t boff = ((uint32_t)s * slot_bytes + (uint32_t)(t - t0) * tap_bytes) >> 4;
+        for (int mt = warp; mt < a.n_mt; mt += WS_ISSUERS) {
+          const uint32_t aoff = ((uint32_t)(L0 + 128 * mt + off) * 16u) >> 4;
           for (int ks = 0; ks < kci / 2; ++ks) {
-            umma::mma_bf16(tmem + (uint32_t)(mt * a.Cout), umma::sdesc(arow + 2u * ks * a_lbo, a_lbo, 128u),
-                           umma::sdesc(brow + 2u * ks * b_lbo, b_lbo, 128u), idesc, (t > 0 || ks > 0) ? 1u : 0u);
+            umma::mma_bf16(tmem + (uint32_t)(mt * a.Cout), ad0 + aoff + ((2u * ks * a_lbo) >> 4),
+                           bd0 + boff + ((2u * ks * b_lbo) >> 4), idesc, (t > 0 || ks > 0) ? 1u : 0u);
           }
         }
       }
@@ -259,6 +273,7 @@ __global__ void __launch_bounds__(256) k_conv_fwd(ConvFwd a) {
       }
       if (__syncthreads_or(fail)) { fail = true; break; }
       load_taps(a.w, g + 1, a.tpg, tap_bytes, ring + (uint32_t)s1 * slot_bytes, tid);
+      umma::cp_async_wait_all();
       umma::fence_async_smem();
       __syncthreads();
     }
@@ -364,9 +379,9 @@ __global__ void __launch_bounds__(256) k_conv_wgrad(ConvW a) {
     umma::tmem_alloc(tslot, a.tmem_cols);
     umma::tmem_relinquish();
   }
-  if (tid == 0) {
-    umma::mbar_init(&bars[0], 1);
-    umma::mbar_init(&bars[1], 1);
+  if (tid == 0) {  // one arrival per issuing warp
+    umma::mbar_init(&bars[0], WS_ISSUERS);
+    umma::mbar_init(&bars[1], WS_ISSUERS);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   umma::tc_fence_before();
@@ -390,14 +405,21 @@ __global__ void __launch_bounds__(256) k_conv_wgrad(ConvW a) {
       if (pend0) { fail |= !umma::mbar_wait(&bars[0], ph0, WS_WAIT_BUDGET); ph0 ^= 1u; pend0 = false; }
       if (pend1) { fail |= !umma::mbar_wait(&bars[1], ph1, WS_WAIT_BUDGET); ph1 ^= 1u; pend1 = false; }
       if (__syncthreads_or(fail)) { fail = true; break; }
-      for (int i = tid; i < kci * V; i += blockDim.x) {
-        const int kc = i / V, L = i - kc * V;
-        const int tz = L / P, rem = L - tz * P, ty = rem / W2, tx = rem - ty * W2;
-        const int gz = z0 - 1 + tz, gy_ = y0 - 1 + ty, gx = tx - 1;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if ((unsigned)gz < (unsigned)R && (unsigned)gy_ < (unsigned)R && (unsigned)gx < (unsigned)R)
-          v = __ldg(a.x + (size_t)kc * R3 + ((size_t)gz * R + gy_) * R + gx);
-        trow[i] = v;
+      {
+        const int nzy = (a.BZ + 2) * (a.BY + 2), nrows = kci * nzy, nwarps = blockDim.x >> 5;
+        for (int row = warp; row < nrows; row += nwarps) {
+          const int kc = row / nzy, rr = row - kc * nzy;
+          const int tz = rr / (a.BY + 2), ty = rr - tz * (a.BY + 2);
+          const int gz = z0 - 1 + tz, gy_ = y0 - 1 + ty;
+          const bool rowin = (unsigned)gz < (unsigned)R && (unsigned)gy_ < (unsigned)R;
+          const uint4 *src = a.x + (size_t)kc * R3 + ((size_t)(rowin ? gz : 0) * R + (rowin ? gy_ : 0)) * R;
+          uint4 *dst = trow + (size_t)kc * V + (size_t)rr * W2;
+          for (int tx = lane; tx < W2; tx += 32) {
+            const int gx = tx - 1;
+            const bool in = rowin && (unsigned)gx < (unsigned)R;
+            umma::cp_async16(dst + tx, in ? (const void *)(src + gx) : (const void *)a.x, in);
+          }
+        }
       }
       for (int i = tid; i < 128; i += blockDim.x) trow[kci * V + i] = make_uint4(0u, 0u, 0u, 0u);
       for (int st = 0; st < nst; ++st, ++gs) {
@@ -414,20 +436,22 @@ __global__ void __launch_bounds__(256) k_conv_wgrad(ConvW a) {
           const int L = Ls + r;
           const int tz = L / P, rem = L - tz * P, ty = rem / W2, tx = rem - ty * W2;
           const bool valid = L <= L1 && tz >= 1 && tz <= a.BZ && ty >= 1 && ty <= a.BY && tx >= 1 && tx <= R;
-          uint4 v = make_uint4(0u, 0u, 0u, 0u);
-          if (valid) v = __ldg(a.gy + (size_t)c * R3 + ((size_t)(z0 + tz - 1) * R + (y0 + ty - 1)) * R + (tx - 1));
-          *reinterpret_cast<uint4 *>(sbuf + (r >> 3) * 2048 + c * 128 + (r & 7) * 16) = v;
+          const uint4 *src =
+              valid ? a.gy + (size_t)c * R3 + ((size_t)(z0 + tz - 1) * R + (y0 + ty - 1)) * R + (tx - 1) : a.gy;
+          umma::cp_async16(sbuf + (r >> 3) * 2048 + c * 128 + (r & 7) * 16, src, valid);
         }
+        umma::cp_async_wait_all();
         umma::fence_async_smem();
         __syncthreads();
-        if (tid == 0) {
+        if (lane == 0 && warp < WS_ISSUERS) {  // issuer w owns the taps t0 + w (mod WS_ISSUERS)
           umma::tc_fence_after();
-          for (int t = t0; t < t1; ++t) {
+          const uint64_t ad0 = umma::sdesc_mn(stg_u32 + (uint32_t)s * WG_STAGE_BYTES, 2048u, 128u);
+          const uint64_t bd0 = umma::sdesc_mn(tile_u32, 128u, (uint32_t)V * 16u);
+          for (int t = t0 + warp; t < t1; t += WS_ISSUERS) {
             const int off = tap_offset(t, P, W2);
             for (int ks = 0; ks < WG_STAGE_ROWS / 16; ++ks) {
-              const uint64_t ad = umma::sdesc_mn(stg_u32 + (uint32_t)s * WG_STAGE_BYTES + (uint32_t)ks * 4096u, 2048u, 128u);
-              const uint64_t bd = umma::sdesc_mn(tile_u32 + (uint32_t)(Ls + 16 * ks + off) * 16u, 128u, (uint32_t)V * 16u);
-              umma::mma_bf16(tmem + (uint32_t)((t - t0) * a.Cin), ad, bd, idesc, (first && ks == 0) ? 0u : 1u);
+              umma::mma_bf16(tmem + (uint32_t)((t - t0) * a.Cin), ad0 + (uint32_t)ks * 256u,
+                             bd0 + (uint32_t)(Ls + 16 * ks + off), idesc, (first && ks == 0) ? 0u : 1u);
             }
           }
           umma::mma_commit(&bars[s]);
@@ -485,89 +509,83 @@ __global__ void __launch_bounds__(256) k_wgrad_reduce(const float *__restrict__ 
 // elementwise network stages (bf16 chunk-planar activations)
 // ------------------------------------------------------------------------------
 // Coarse voxel (I,J,K) of an R/2 grid covers fine voxels (2I..2I+1, 2J.., 2K..).
+// The elementwise kernels run one thread per voxel of a line: blockIdx.z = chunk *
+// R_line + z, blockIdx.y = y, x from blockIdx.x (no index division).
 __device__ __forceinline__ size_t child_index(int R, int I, int J, int K, int c) {
   return ((size_t)(2 * I + (c >> 2)) * R + (2 * J + ((c >> 1) & 1))) * R + (2 * K + (c & 1));
 }
 
+static dim3 line_grid(int Rl, int kc, int tpb) { return dim3((Rl + tpb - 1) / tpb, Rl, Rl * kc); }
+
 // out (R/2) = mean of the 8 children of in (R)
-__global__ void __launch_bounds__(256) k_pool2(const uint4 *__restrict__ in, uint4 *__restrict__ out, int R, int kc) {
+__global__ void __launch_bounds__(64) k_pool2(const uint4 *__restrict__ in, uint4 *__restrict__ out, int R) {
   const int Rc = R >> 1;
-  const size_t Rc3 = (size_t)Rc * Rc * Rc, R3 = (size_t)R * R * R;
-  const size_t n = (size_t)kc * Rc3;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const size_t c = i / Rc3, v = i - c * Rc3;
-    const int I = (int)(v / ((size_t)Rc * Rc)), J = (int)((v / Rc) % Rc), K = (int)(v % Rc);
-    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const int K = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y, c = blockIdx.z / Rc, I = blockIdx.z - c * Rc;
+  if (K >= Rc) return;
+  const size_t R3 = (size_t)R * R * R, Rc3 = (size_t)Rc * Rc * Rc;
+  float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
-    for (int ch = 0; ch < 8; ++ch) {
-      float f[8];
-      unpack8(__ldg(in + c * R3 + child_index(R, I, J, K, ch)), f);
+  for (int ch = 0; ch < 8; ++ch) {
+    float f[8];
+    unpack8(__ldg(in + c * R3 + child_index(R, I, J, K, ch)), f);
 #pragma unroll
-      for (int j = 0; j < 8; ++j) acc[j] += f[j];
-    }
-#pragma unroll
-    for (int j = 0; j < 8; ++j) acc[j] *= 0.125f;
-    out[i] = pack8<0>(acc);
+    for (int j = 0; j < 8; ++j) acc[j] += f[j];
   }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) acc[j] *= 0.125f;
+  out[c * Rc3 + ((size_t)I * Rc + J) * Rc + K] = pack8<0>(acc);
 }
 
 // out (R) = relu(u[parent] + skip)
-__global__ void __launch_bounds__(256) k_up_add_relu(const uint4 *__restrict__ u, const uint4 *__restrict__ skip,
-                                                     uint4 *__restrict__ out, int R, int kc) {
+__global__ void __launch_bounds__(64) k_up_add_relu(const uint4 *__restrict__ u, const uint4 *__restrict__ skip,
+                                                    uint4 *__restrict__ out, int R) {
   const int Rc = R >> 1;
-  const size_t Rc3 = (size_t)Rc * Rc * Rc, R3 = (size_t)R * R * R;
-  const size_t n = (size_t)kc * R3;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const size_t c = i / R3, v = i - c * R3;
-    const int x = (int)(v / ((size_t)R * R)), y = (int)((v / R) % R), z = (int)(v % R);
-    float a[8], b[8];
-    unpack8(__ldg(u + c * Rc3 + ((size_t)(x >> 1) * Rc + (y >> 1)) * Rc + (z >> 1)), a);
-    unpack8(__ldg(skip + i), b);
+  const int z = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, c = blockIdx.z / R, x = blockIdx.z - c * R;
+  if (z >= R) return;
+  const size_t R3 = (size_t)R * R * R, Rc3 = (size_t)Rc * Rc * Rc;
+  const size_t i = c * R3 + ((size_t)x * R + y) * R + z;
+  float a[8], b[8];
+  unpack8(__ldg(u + c * Rc3 + ((size_t)(x >> 1) * Rc + (y >> 1)) * Rc + (z >> 1)), a);
+  unpack8(__ldg(skip + i), b);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) a[j] = fmaxf(a[j] + b[j], 0.0f);
-    out[i] = pack8<0>(a);
-  }
+  for (int j = 0; j < 8; ++j) a[j] = fmaxf(a[j] + b[j], 0.0f);
+  out[i] = pack8<0>(a);
 }
 
 // out (R/2) = sum of the 8 children of g (R): adjoint of the nearest-neighbour upsample
-__global__ void __launch_bounds__(256) k_up_adjoint(const uint4 *__restrict__ g, uint4 *__restrict__ out, int R, int kc) {
+__global__ void __launch_bounds__(64) k_up_adjoint(const uint4 *__restrict__ g, uint4 *__restrict__ out, int R) {
   const int Rc = R >> 1;
-  const size_t Rc3 = (size_t)Rc * Rc * Rc, R3 = (size_t)R * R * R;
-  const size_t n = (size_t)kc * Rc3;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const size_t c = i / Rc3, v = i - c * Rc3;
-    const int I = (int)(v / ((size_t)Rc * Rc)), J = (int)((v / Rc) % Rc), K = (int)(v % Rc);
-    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const int K = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y, c = blockIdx.z / Rc, I = blockIdx.z - c * Rc;
+  if (K >= Rc) return;
+  const size_t R3 = (size_t)R * R * R, Rc3 = (size_t)Rc * Rc * Rc;
+  float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
-    for (int ch = 0; ch < 8; ++ch) {
-      float f[8];
-      unpack8(__ldg(g + c * R3 + child_index(R, I, J, K, ch)), f);
+  for (int ch = 0; ch < 8; ++ch) {
+    float f[8];
+    unpack8(__ldg(g + c * R3 + child_index(R, I, J, K, ch)), f);
 #pragma unroll
-      for (int j = 0; j < 8; ++j) acc[j] += f[j];
-    }
-    out[i] = pack8<0>(acc);
+    for (int j = 0; j < 8; ++j) acc[j] += f[j];
   }
+  out[c * Rc3 + ((size_t)I * Rc + J) * Rc + K] = pack8<0>(acc);
 }
 
 // out (R) = (skipgrad + gp[parent] / 8) where act > 0, else 0: the gradient of an
 // encoder activation that feeds both a skip connection and the average pool.
-__global__ void __launch_bounds__(256) k_pool_adj_add_mask(const uint4 *__restrict__ skipgrad,
-                                                           const uint4 *__restrict__ gp, const uint4 *__restrict__ act,
-                                                           uint4 *__restrict__ out, int R, int kc) {
+__global__ void __launch_bounds__(64) k_pool_adj_add_mask(const uint4 *__restrict__ skipgrad,
+                                                          const uint4 *__restrict__ gp, const uint4 *__restrict__ act,
+                                                          uint4 *__restrict__ out, int R) {
   const int Rc = R >> 1;
-  const size_t Rc3 = (size_t)Rc * Rc * Rc, R3 = (size_t)R * R * R;
-  const size_t n = (size_t)kc * R3;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const size_t c = i / R3, v = i - c * R3;
-    const int x = (int)(v / ((size_t)R * R)), y = (int)((v / R) % R), z = (int)(v % R);
-    float p[8], s[8], m[8];
-    unpack8(__ldg(gp + c * Rc3 + ((size_t)(x >> 1) * Rc + (y >> 1)) * Rc + (z >> 1)), p);
-    unpack8(__ldg(skipgrad + i), s);
-    unpack8(__ldg(act + i), m);
+  const int z = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, c = blockIdx.z / R, x = blockIdx.z - c * R;
+  if (z >= R) return;
+  const size_t R3 = (size_t)R * R * R, Rc3 = (size_t)Rc * Rc * Rc;
+  const size_t i = c * R3 + ((size_t)x * R + y) * R + z;
+  float p[8], s[8], m[8];
+  unpack8(__ldg(gp + c * Rc3 + ((size_t)(x >> 1) * Rc + (y >> 1)) * Rc + (z >> 1)), p);
+  unpack8(__ldg(skipgrad + i), s);
+  unpack8(__ldg(act + i), m);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) p[j] = m[j] > 0.0f ? s[j] + 0.125f * p[j] : 0.0f;
-    out[i] = pack8<0>(p);
-  }
+  for (int j = 0; j < 8; ++j) p[j] = m[j] > 0.0f ? s[j] + 0.125f * p[j] : 0.0f;
+  out[i] = pack8<0>(p);
 }
 
 // Per-block partial channel sums of g (C = 8*kc channels): part[block][C].
@@ -602,10 +620,11 @@ __global__ void __launch_bounds__(256) k_chan_sum(const uint4 *__restrict__ g, i
   }
 }
 
-// Network input: channels 0..2 from f16 planar features [3][R^3]; channels 3..15 zero.
+// Network input: channels 0..3 from f16 planar features [4][R^3]; channels 4..15 zero.
 __global__ void __launch_bounds__(256) k_pack_input(const __half *__restrict__ feat, uint4 *__restrict__ x0, size_t R3) {
   for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < R3; v += (size_t)gridDim.x * blockDim.x) {
-    float f[8] = {__half2float(feat[v]), __half2float(feat[R3 + v]), __half2float(feat[2 * R3 + v]), 0, 0, 0, 0, 0};
+    float f[8] = {__half2float(feat[v]), __half2float(feat[R3 + v]), __half2float(feat[2 * R3 + v]),
+                  __half2float(feat[3 * R3 + v]), 0, 0, 0, 0};
     x0[v] = pack8<0>(f);
     x0[R3 + v] = make_uint4(0u, 0u, 0u, 0u);
   }
@@ -746,11 +765,15 @@ static size_t smem_for_residency(size_t smem, int k) {
 
 static const size_t WS_SMEM_MAX = 232448;
 
+// Tile plan of the forward kernel from a cycle estimate per SM: staging the
+// input tile (L2 -> shared, ~64 B/clk), the MMAs (one 128 x Cout x 16 step every
+// max(8, 128*Cout*16/4096) clocks, issued by four threads) and the epilogue,
+// with at most `occ` CTAs overlapping on an SM.
 static bool plan_fwd(int R, int Cin, int Cout, int sm_count, FwdPlan &best) {
   bool found = false;
-  double best_score = -1.0;
+  double best_cost = 1e300;
   const int bys[] = {32, 16, 8, 4, 2, 1};
-  const int bzs[] = {1, 2, 4};
+  const int bzs[] = {1, 2, 4, 8};
   for (int BY : bys) {
     if (BY > R || R % BY) continue;
     for (int BZ : bzs) {
@@ -764,17 +787,23 @@ static bool plan_fwd(int R, int Cin, int Cout, int sm_count, FwdPlan &best) {
       if (tile + 2 * tap + 64 > WS_SMEM_MAX) continue;
       const int tpg = (int)std::min<size_t>(27, (WS_SMEM_MAX - tile - 64) / (2 * tap));
       const int ngroups = (27 + tpg - 1) / tpg;
-      const int tpg_even = (27 + ngroups - 1) / ngroups;  // same number of groups, smaller slots
+      const int tpg_even = (27 + ngroups - 1) / ngroups;
       const size_t smem = tile + 2 * (size_t)tpg_even * tap + 64;
       const uint32_t cols = pow2_cols(n_mt * Cout);
+      const size_t smem_launch = smem_for_residency(smem, (int)(512 / cols));
+      const int occ = std::max(1, std::min(8, (int)(233472 / (smem_launch + 1024))));
       const int ctas = (R / BZ) * (R / BY);
-      const double useful = (double)BZ * BY * R / (128.0 * n_mt);
-      const double fill = std::min(1.0, (double)ctas / (2.0 * sm_count));
-      const double score = useful * fill + 1e-6 * BZ * BY;
-      if (score > best_score) {
-        best_score = score;
+      const double load = (double)(Cin / 8) * V * 16 / 64.0 + (double)27 * tap / 64.0;
+      const double mma = 27.0 * n_mt * (Cin / 16) * std::max(8.0, 128.0 * Cout * 16 / 4096.0) / 4.0 + 300.0;
+      const double epi = (double)n_mt * 128 * Cout * 2 / 64.0;
+      const double per_cta = load + mma + epi + 2000.0;
+      const double busiest = std::max(load, std::max(mma, epi));
+      const double waves = std::ceil((double)ctas / (sm_count * occ));
+      const double cost = waves * std::max(per_cta, occ * busiest);
+      if (cost < best_cost) {
+        best_cost = cost;
         best.BZ = BZ; best.BY = BY; best.tpg = tpg_even; best.n_mt = n_mt; best.grid = ctas; best.cols = cols;
-        best.smem = smem_for_residency(smem, (int)(512 / cols));
+        best.smem = smem_launch;
         found = true;
       }
     }
@@ -1054,23 +1083,21 @@ extern "C" int gc_ws_status(gc_ws *ws, unsigned *flags, int clear) {
 static int ws_forward_packed(gc_ws *ws, float *y_out) {
   const int R = ws->R;
   int s;
-  const size_t R3 = (size_t)R * R * R;
-  const int sm = ws->sm_count;
   if ((s = ws_fwd_layer(ws, 0, ws->x0, nullptr, ws->e0, nullptr))) return s;
-  k_pool2<<<ew_blocks(R3 / 8 * 2, sm), 256, 0, ws->stream>>>(ws->e0, ws->p1, R, 2);
+  k_pool2<<<line_grid(R / 2, 2, 64), 64, 0, ws->stream>>>(ws->e0, ws->p1, R);
   if ((s = ws_fwd_layer(ws, 1, ws->p1, nullptr, ws->e1, nullptr))) return s;
-  k_pool2<<<ew_blocks(R3 / 64 * 4, sm), 256, 0, ws->stream>>>(ws->e1, ws->p2, R / 2, 4);
+  k_pool2<<<line_grid(R / 4, 4, 64), 64, 0, ws->stream>>>(ws->e1, ws->p2, R / 2);
   if ((s = ws_fwd_layer(ws, 2, ws->p2, nullptr, ws->e2, nullptr))) return s;
-  k_pool2<<<ew_blocks(R3 / 512 * 8, sm), 256, 0, ws->stream>>>(ws->e2, ws->p3, R / 4, 8);
+  k_pool2<<<line_grid(R / 8, 8, 64), 64, 0, ws->stream>>>(ws->e2, ws->p3, R / 4);
   if ((s = ws_fwd_layer(ws, 3, ws->p3, nullptr, ws->e3, nullptr))) return s;
   if ((s = ws_fwd_layer(ws, 4, ws->e3, nullptr, ws->u2, nullptr))) return s;
-  k_up_add_relu<<<ew_blocks(R3 / 64 * 8, sm), 256, 0, ws->stream>>>(ws->u2, ws->e2, ws->d2, R / 4, 8);
+  k_up_add_relu<<<line_grid(R / 4, 8, 64), 64, 0, ws->stream>>>(ws->u2, ws->e2, ws->d2, R / 4);
   if ((s = ws_fwd_layer(ws, 5, ws->d2, nullptr, ws->f2, nullptr))) return s;
   if ((s = ws_fwd_layer(ws, 6, ws->f2, nullptr, ws->u1, nullptr))) return s;
-  k_up_add_relu<<<ew_blocks(R3 / 8 * 4, sm), 256, 0, ws->stream>>>(ws->u1, ws->e1, ws->d1, R / 2, 4);
+  k_up_add_relu<<<line_grid(R / 2, 4, 64), 64, 0, ws->stream>>>(ws->u1, ws->e1, ws->d1, R / 2);
   if ((s = ws_fwd_layer(ws, 7, ws->d1, nullptr, ws->f1, nullptr))) return s;
   if ((s = ws_fwd_layer(ws, 8, ws->f1, nullptr, ws->u0, nullptr))) return s;
-  k_up_add_relu<<<ew_blocks(R3 * 2, sm), 256, 0, ws->stream>>>(ws->u0, ws->e0, ws->d0, R, 2);
+  k_up_add_relu<<<line_grid(R, 2, 64), 64, 0, ws->stream>>>(ws->u0, ws->e0, ws->d0, R);
   if ((s = ws_fwd_layer(ws, 9, ws->d0, nullptr, ws->f0, nullptr))) return s;
   if ((s = ws_fwd_layer(ws, 10, ws->f0, nullptr, nullptr, y_out ? y_out : ws->y))) return s;
   WS_CUDA(ws, cudaGetLastError());
@@ -1103,33 +1130,33 @@ extern "C" int gc_ws_backward(gc_ws *ws, const void *target, float *loss_out) {
   if ((s = ws_dgrad(ws, 10, ws->gy, ws->f0, ws->g_f0))) return s;
   if ((s = ws_wgrad(ws, 9, ws->d0, ws->g_f0))) return s;
   if ((s = ws_dgrad(ws, 9, ws->g_f0, ws->d0, ws->g_d0))) return s;
-  k_up_adjoint<<<ew_blocks(R3 / 8 * 2, sm), 256, 0, ws->stream>>>(ws->g_d0, ws->g_u0, R, 2);
+  k_up_adjoint<<<line_grid(R / 2, 2, 64), 64, 0, ws->stream>>>(ws->g_d0, ws->g_u0, R);
   // I, H
   if ((s = ws_wgrad(ws, 8, ws->f1, ws->g_u0))) return s;
   if ((s = ws_dgrad(ws, 8, ws->g_u0, ws->f1, ws->g_f1))) return s;
   if ((s = ws_wgrad(ws, 7, ws->d1, ws->g_f1))) return s;
   if ((s = ws_dgrad(ws, 7, ws->g_f1, ws->d1, ws->g_d1))) return s;
-  k_up_adjoint<<<ew_blocks(R3 / 64 * 4, sm), 256, 0, ws->stream>>>(ws->g_d1, ws->g_u1, R / 2, 4);
+  k_up_adjoint<<<line_grid(R / 4, 4, 64), 64, 0, ws->stream>>>(ws->g_d1, ws->g_u1, R / 2);
   // G, F
   if ((s = ws_wgrad(ws, 6, ws->f2, ws->g_u1))) return s;
   if ((s = ws_dgrad(ws, 6, ws->g_u1, ws->f2, ws->g_f2))) return s;
   if ((s = ws_wgrad(ws, 5, ws->d2, ws->g_f2))) return s;
   if ((s = ws_dgrad(ws, 5, ws->g_f2, ws->d2, ws->g_d2))) return s;
-  k_up_adjoint<<<ew_blocks(R3 / 512 * 8, sm), 256, 0, ws->stream>>>(ws->g_d2, ws->g_u2, R / 4, 8);
+  k_up_adjoint<<<line_grid(R / 8, 8, 64), 64, 0, ws->stream>>>(ws->g_d2, ws->g_u2, R / 4);
   // E, D
   if ((s = ws_wgrad(ws, 4, ws->e3, ws->g_u2))) return s;
   if ((s = ws_dgrad(ws, 4, ws->g_u2, ws->e3, ws->g_e3))) return s;
   if ((s = ws_wgrad(ws, 3, ws->p3, ws->g_e3))) return s;
   if ((s = ws_dgrad(ws, 3, ws->g_e3, nullptr, ws->g_p3))) return s;
-  k_pool_adj_add_mask<<<ew_blocks(R3 / 64 * 8, sm), 256, 0, ws->stream>>>(ws->g_d2, ws->g_p3, ws->e2, ws->g_e2, R / 4, 8);
+  k_pool_adj_add_mask<<<line_grid(R / 4, 8, 64), 64, 0, ws->stream>>>(ws->g_d2, ws->g_p3, ws->e2, ws->g_e2, R / 4);
   // C
   if ((s = ws_wgrad(ws, 2, ws->p2, ws->g_e2))) return s;
   if ((s = ws_dgrad(ws, 2, ws->g_e2, nullptr, ws->g_p2))) return s;
-  k_pool_adj_add_mask<<<ew_blocks(R3 / 8 * 4, sm), 256, 0, ws->stream>>>(ws->g_d1, ws->g_p2, ws->e1, ws->g_e1, R / 2, 4);
+  k_pool_adj_add_mask<<<line_grid(R / 2, 4, 64), 64, 0, ws->stream>>>(ws->g_d1, ws->g_p2, ws->e1, ws->g_e1, R / 2);
   // B
   if ((s = ws_wgrad(ws, 1, ws->p1, ws->g_e1))) return s;
   if ((s = ws_dgrad(ws, 1, ws->g_e1, nullptr, ws->g_p1))) return s;
-  k_pool_adj_add_mask<<<ew_blocks(R3 * 2, sm), 256, 0, ws->stream>>>(ws->g_d0, ws->g_p1, ws->e0, ws->g_e0, R, 2);
+  k_pool_adj_add_mask<<<line_grid(R, 2, 64), 64, 0, ws->stream>>>(ws->g_d0, ws->g_p1, ws->e0, ws->g_e0, R);
   // A
   if ((s = ws_wgrad(ws, 0, ws->x0, ws->g_e0))) return s;
   WS_CUDA(ws, cudaGetLastError());
@@ -1147,88 +1174,104 @@ extern "C" int gc_ws_adam(gc_ws *ws, float lr, float beta1, float beta2, float e
 }
 
 // ------------------------------------------------------------------------------
-// engine hook: coarse history, input features, applying the prediction
+// engine hook: history, input features, applying the prediction
 // ------------------------------------------------------------------------------
+// Initial guess of step n from the previous potentials:
+//   plain        phi(n-1)                                   (the reference's warm start)
+//   extrapolate  phi(n-1) + d(n-1),  d(k) = phi(k) - phi(k-1) at full resolution
+//   learned      the extrapolation + s * trilinear(y): the network predicts the
+//                next second difference dd(n) = d(n) - d(n-1) on the (G/2)^3 grid
+//                in units of s = rms(dd_c(n-1)); a zero output is the extrapolation.
 // The coarse grid has R = G/2 cells per axis; cell (I,J,K) is the mean of the
 // fine nodes (2I..2I+1, 2J.., 2K..), centred at fine coordinate 2I + 0.5.
-// History kept per context: phi_c of the last solve and delta_c, its change
-// from the solve before. Features of step n (f16 [3][R^3]):
-//   log(1 + rho_c / mean rho_c), phi_c(n-1) / rms, delta_c(n-1) / rms(delta_c(n-1)).
-// The network predicts delta_c(n) / rms(delta_c(n-1)); the multigrid starts from
-// phi(n-1) + rms * trilinear(prediction) instead of phi(n-1).
-__global__ void __launch_bounds__(256) k_ws_coarsen(const float *__restrict__ f, int G, float *__restrict__ out) {
+// Coarse history per context: phi_c(n-1), d_c(n-1), dd_c(n-1). Features of step
+// n (f16 [4][R^3]): log(1 + rho_c / mean rho_c), phi_c / rms, d_c / rms(d_c),
+// dd_c / rms(dd_c); training target dd_c(n) / rms(dd_c(n-1)).
+__global__ void __launch_bounds__(64) k_ws_coarsen(const float *__restrict__ f, int G, float *__restrict__ out) {
   const int R = G >> 1;
-  const size_t R3 = (size_t)R * R * R;
-  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < R3; v += (size_t)gridDim.x * blockDim.x) {
-    const int I = (int)(v / ((size_t)R * R)), J = (int)((v / R) % R), K = (int)(v % R);
-    float s = 0.0f;
+  const int K = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y, I = blockIdx.z;
+  if (K >= R) return;
+  float s = 0.0f;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) s += __ldg(f + child_index(G, I, J, K, c));
-    out[v] = 0.125f * s;
-  }
+  for (int c = 0; c < 8; ++c) s += __ldg(f + child_index(G, I, J, K, c));
+  out[((size_t)I * R + J) * R + K] = 0.125f * s;
 }
 
+// per-block sums: rho_c, phi_c^2, d_c^2, dd_c^2
 __global__ void __launch_bounds__(256) k_ws_stats(const float *__restrict__ rho, const float *__restrict__ phi,
-                                                  const float *__restrict__ dlt, size_t n, float *__restrict__ part) {
-  __shared__ float red[3][8];
-  float a = 0.0f, b = 0.0f, c = 0.0f;
+                                                  const float *__restrict__ dlt, const float *__restrict__ ddl,
+                                                  size_t n, float *__restrict__ part) {
+  __shared__ float red[4][8];
+  float a = 0.0f, b = 0.0f, c = 0.0f, e = 0.0f;
   for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
     a += rho[v];
     b += phi[v] * phi[v];
     c += dlt[v] * dlt[v];
+    e += ddl[v] * ddl[v];
   }
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_xor_sync(0xffffffffu, a, o);
     b += __shfl_xor_sync(0xffffffffu, b, o);
     c += __shfl_xor_sync(0xffffffffu, c, o);
+    e += __shfl_xor_sync(0xffffffffu, e, o);
   }
   const int w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) { red[0][w] = a; red[1][w] = b; red[2][w] = c; }
+  if ((threadIdx.x & 31) == 0) { red[0][w] = a; red[1][w] = b; red[2][w] = c; red[3][w] = e; }
   __syncthreads();
-  if (threadIdx.x < 3) {
+  if (threadIdx.x < 4) {
     float s = 0.0f;
     for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[threadIdx.x][i];
-    part[3 * blockIdx.x + threadIdx.x] = s;
+    part[4 * blockIdx.x + threadIdx.x] = s;
   }
 }
 
-// scal[0] mean rho_c, scal[1] rms phi_c, scal[2] rms delta_c, scal[3] 1 when delta_c is usable
+// scal: [0] mean rho_c, [1] rms phi_c, [2] rms d_c, [3] d usable, [4] rms dd_c, [5] dd usable
 __global__ void k_ws_scales(const float *__restrict__ part, int nb, size_t n, int hist, float *__restrict__ scal) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double a = 0.0, b = 0.0, c = 0.0;
-  for (int i = 0; i < nb; ++i) { a += part[3 * i]; b += part[3 * i + 1]; c += part[3 * i + 2]; }
-  const double mr = a / (double)n, rp = sqrt(b / (double)n), rd = sqrt(c / (double)n);
+  double a = 0.0, b = 0.0, c = 0.0, e = 0.0;
+  for (int i = 0; i < nb; ++i) { a += part[4 * i]; b += part[4 * i + 1]; c += part[4 * i + 2]; e += part[4 * i + 3]; }
+  const double mr = a / (double)n, rp = sqrt(b / (double)n), rd = sqrt(c / (double)n), rdd = sqrt(e / (double)n);
+  const double tiny = 1e-30 * (rp > 0.0 ? rp : 1.0);
   scal[0] = mr > 0.0 ? (float)mr : 1.0f;
   scal[1] = (hist >= 1 && rp > 0.0) ? (float)rp : 1.0f;
-  const bool dok = hist >= 2 && rd > 1e-30 * (rp > 0.0 ? rp : 1.0) && rd > 0.0;
+  const bool dok = hist >= 2 && rd > tiny;
   scal[2] = dok ? (float)rd : 1.0f;
   scal[3] = dok ? 1.0f : 0.0f;
+  const bool ddok = hist >= 3 && rdd > tiny;
+  scal[4] = ddok ? (float)rdd : 1.0f;
+  scal[5] = ddok ? 1.0f : 0.0f;
 }
 
 __global__ void __launch_bounds__(256) k_ws_features(const float *__restrict__ rho, const float *__restrict__ phi,
-                                                     const float *__restrict__ dlt, const float *__restrict__ scal,
-                                                     int hist, size_t n, __half *__restrict__ feat,
-                                                     __half *__restrict__ rec) {
-  const float ir = 1.0f / scal[0], ip = 1.0f / scal[1], id = 1.0f / scal[2];
-  const bool has_p = hist >= 1, has_d = scal[3] != 0.0f;
+                                                     const float *__restrict__ dlt, const float *__restrict__ ddl,
+                                                     const float *__restrict__ scal, int hist, size_t n,
+                                                     __half *__restrict__ feat, __half *__restrict__ rec) {
+  const float ir = 1.0f / scal[0], ip = 1.0f / scal[1], id = 1.0f / scal[2], idd = 1.0f / scal[4];
+  const bool has_p = hist >= 1, has_d = scal[3] != 0.0f, has_dd = scal[5] != 0.0f;
   for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
     const __half a = __float2half_rn(log1pf(fmaxf(rho[v] * ir, 0.0f)));
     const __half b = __float2half_rn(has_p ? phi[v] * ip : 0.0f);
     const __half c = __float2half_rn(has_d ? dlt[v] * id : 0.0f);
-    feat[v] = a; feat[n + v] = b; feat[2 * n + v] = c;
-    if (rec) { rec[v] = a; rec[n + v] = b; rec[2 * n + v] = c; }
+    const __half e = __float2half_rn(has_dd ? ddl[v] * idd : 0.0f);
+    feat[v] = a; feat[n + v] = b; feat[2 * n + v] = c; feat[3 * n + v] = e;
+    if (rec) { rec[v] = a; rec[n + v] = b; rec[2 * n + v] = c; rec[3 * n + v] = e; }
   }
 }
 
-// hi/lo += s * trilinear(yc) on every fine node (s = scal[2] or 1); no-op without history
-__global__ void __launch_bounds__(256) k_ws_apply(const float *__restrict__ yc, const float *__restrict__ scal,
-                                                  int use_scale, int G, float *__restrict__ hi, float *__restrict__ lo) {
-  if (scal[3] == 0.0f) return;
-  const float s = use_scale ? scal[2] : 1.0f;
+// Initial guess on every fine node: prev holds phi(n-2) on entry and phi(n-1)
+// on exit; hi/lo (phi(n-1) on entry) get + d(n-1) when extrapolating (and the
+// history allows it) and + s * trilinear(yc) when yc is given.
+__global__ void __launch_bounds__(128) k_ws_apply(const float *__restrict__ yc, const float *__restrict__ scal,
+                                                  int extrap, int G, float *__restrict__ hi, float *__restrict__ lo,
+                                                  float *__restrict__ prev) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
+  if (k >= G) return;
   const int R = G >> 1;
-  const size_t G3 = (size_t)G * G * G;
-  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < G3; v += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(v / ((size_t)G * G)), j = (int)((v / G) % G), k = (int)(v % G);
+  const size_t v = ((size_t)i * G + j) * G + k;
+  const float h = hi[v], l = lo[v];
+  float corr = 0.0f;
+  if (extrap && scal[3] != 0.0f) corr = __fsub_rn(h, prev[v]);
+  if (yc && scal[5] != 0.0f) {
     int i0[3];
     float f[3];
     const int ii[3] = {i, j, k};
@@ -1247,40 +1290,47 @@ __global__ void __launch_bounds__(256) k_ws_apply(const float *__restrict__ yc, 
       const float w = (dx ? f[0] : 1.0f - f[0]) * (dy ? f[1] : 1.0f - f[1]) * (dz ? f[2] : 1.0f - f[2]);
       acc += w * __ldg(yc + ((size_t)(i0[0] + dx) * R + (i0[1] + dy)) * R + (i0[2] + dz));
     }
+    corr += scal[4] * acc;
+  }
+  prev[v] = h;
+  if (corr != 0.0f) {
     float sh, eh;
-    df_two_sum(hi[v], s * acc, sh, eh);
+    df_two_sum(h, corr, sh, eh);
     float h2, l2;
-    df_fast_two_sum(sh, __fadd_rn(lo[v], eh), h2, l2);
+    df_fast_two_sum(sh, __fadd_rn(l, eh), h2, l2);
     hi[v] = h2;
     lo[v] = l2;
   }
 }
 
-// after the solve: new phi_c, its change, the training target, history update
-__global__ void __launch_bounds__(256) k_ws_post(const float *__restrict__ hi, int G, float *__restrict__ phi,
-                                                 float *__restrict__ dlt, const float *__restrict__ scal, int hist,
-                                                 __half *__restrict__ rec) {
+// after the solve: new phi_c, its first and second differences, the training
+// target, history update
+__global__ void __launch_bounds__(64) k_ws_post(const float *__restrict__ hi, int G, float *__restrict__ phi,
+                                                float *__restrict__ dlt, float *__restrict__ ddl,
+                                                const float *__restrict__ scal, int hist, __half *__restrict__ rec) {
   const int R = G >> 1;
+  const int K = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y, I = blockIdx.z;
+  if (K >= R) return;
   const size_t R3 = (size_t)R * R * R;
-  const float id = 1.0f / scal[2];
-  const bool has_d = scal[3] != 0.0f;
-  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < R3; v += (size_t)gridDim.x * blockDim.x) {
-    const int I = (int)(v / ((size_t)R * R)), J = (int)((v / R) % R), K = (int)(v % R);
-    float s = 0.0f;
+  const size_t v = ((size_t)I * R + J) * R + K;
+  const float idd = 1.0f / scal[4];
+  const bool has_dd = scal[5] != 0.0f;
+  float s = 0.0f;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) s += __ldg(hi + child_index(G, I, J, K, c));
-    const float nw = 0.125f * s;
-    const float d = hist >= 1 ? nw - phi[v] : 0.0f;
-    if (rec) rec[3 * R3 + v] = __float2half_rn(has_d ? d * id : 0.0f);
-    phi[v] = nw;
-    dlt[v] = d;
-  }
+  for (int c = 0; c < 8; ++c) s += __ldg(hi + child_index(G, I, J, K, c));
+  const float nw = 0.125f * s;
+  const float d = hist >= 1 ? nw - phi[v] : 0.0f;
+  const float dd = hist >= 2 ? d - dlt[v] : 0.0f;
+  if (rec) rec[4 * R3 + v] = __float2half_rn(has_dd ? dd * idd : 0.0f);
+  phi[v] = nw;
+  dlt[v] = d;
+  ddl[v] = dd;
 }
 
 static int ws_hook_buffers(gc_ctx *ctx) {
   const int R = ctx->G / 2;
-  const size_t R3 = (size_t)R * R * R;
-  const size_t need = 4 * R3 + (3 * R3 + 1) / 2 + 16 + 3 * 1024;
+  const size_t R3 = (size_t)R * R * R, G3 = (size_t)ctx->G * ctx->G * ctx->G;
+  const size_t need = 5 * R3 + 2 * R3 + 16 + 4 * 1024 + G3;
   if (ctx->ws_buf && ctx->ws_buf_cap >= need) return GC_OK;
   cudaFree(ctx->ws_buf);
   ctx->ws_buf = nullptr;
@@ -1291,7 +1341,7 @@ static int ws_hook_buffers(gc_ctx *ctx) {
 }
 
 struct WsViews {
-  float *rho, *phi, *dlt, *y, *scal, *part;
+  float *rho, *phi, *dlt, *ddl, *y, *scal, *part, *prev;
   __half *feat;
 };
 static WsViews ws_views(gc_ctx *ctx) {
@@ -1301,67 +1351,74 @@ static WsViews ws_views(gc_ctx *ctx) {
   w.rho = ctx->ws_buf;
   w.phi = w.rho + R3;
   w.dlt = w.phi + R3;
-  w.y = w.dlt + R3;
-  w.feat = reinterpret_cast<__half *>(w.y + R3);
-  w.scal = w.y + R3 + (3 * R3 + 1) / 2;
+  w.ddl = w.dlt + R3;
+  w.y = w.ddl + R3;
+  w.feat = reinterpret_cast<__half *>(w.y + R3);  // 4 R^3 halves
+  w.scal = w.y + 3 * R3;
   w.part = w.scal + 16;
+  w.prev = w.part + 4 * 1024;
   return w;
 }
 
-int gc_ws_pre_solve(gc_ctx *ctx, int warm) {
+int gc_ws_pre_solve(gc_ctx *ctx, int warm, int mode) {
+  ctx->ws_skip = 0;
   if (!ctx->ws_track && !ctx->ws_record) return GC_OK;
   if (ctx->G % 2) return GC_OK;
+  // a PRIME after a CLOSE solves at the positions of the last solve again: it
+  // neither uses nor extends the history
+  if (mode == GC_STEP_PRIME && ctx->ws_hist > 0 && warm) {
+    ctx->ws_skip = 1;
+    return GC_OK;
+  }
+  if (!warm) ctx->ws_hist = 0;  // a cold solve restarts the history
   int s;
   if ((s = ws_hook_buffers(ctx))) return s;
   const WsViews w = ws_views(ctx);
   const int R = ctx->G / 2;
   const size_t R3 = (size_t)R * R * R;
   unsigned nb = (unsigned)std::min<size_t>((R3 + 255) / 256, 1024);
-  gc_launch(ctx, GK_WARMSTART, k_ws_coarsen, dim3(nb), dim3(256), 0, (const float *)ctx->b0, ctx->G, w.rho);
+  gc_launch(ctx, GK_WARMSTART, k_ws_coarsen, dim3((R + 63) / 64, R, R), dim3(64), 0, (const float *)ctx->b0, ctx->G,
+            w.rho);
   gc_launch(ctx, GK_WARMSTART, k_ws_stats, dim3(nb), dim3(256), 0, (const float *)w.rho, (const float *)w.phi,
-            (const float *)w.dlt, R3, w.part);
+            (const float *)w.dlt, (const float *)w.ddl, R3, w.part);
   gc_launch(ctx, GK_WARMSTART, k_ws_scales, dim3(1), dim3(32), 0, (const float *)w.part, (int)nb, R3, ctx->ws_hist,
             w.scal);
   gc_launch(ctx, GK_WARMSTART, k_ws_features, dim3(nb), dim3(256), 0, (const float *)w.rho, (const float *)w.phi,
-            (const float *)w.dlt, (const float *)w.scal, ctx->ws_hist, R3, w.feat, (__half *)ctx->ws_record);
+            (const float *)w.dlt, (const float *)w.ddl, (const float *)w.scal, ctx->ws_hist, R3, w.feat,
+            (__half *)ctx->ws_record);
   GC_LAUNCH_CHECK(ctx, "warm-start features");
-  if (warm && ctx->ws_hist >= 2 && ctx->ws_mode != GC_WS_PLAIN) {
-    const size_t G3 = (size_t)ctx->G * ctx->G * ctx->G;
-    const unsigned na = (unsigned)std::min<size_t>((G3 + 255) / 256, 152u * 16u);
-    if (ctx->ws_mode == GC_WS_LEARNED) {
-      gc_ws *ws = ctx->ws;
-      if (!ws || ws->R != R) {
-        gc_set_error(ctx, "learned warm start needs a network with R = G/2 = %d", R);
-        return GC_ERR_STATE;
-      }
-      ws->stream = ctx->stream;
-      if ((s = gc_ws_forward(ws, w.feat, w.y))) {
-        gc_set_error(ctx, "warm-start network: %s", ws->err);
-        return s;
-      }
-      ctx->prof.launches[GK_WARMSTART] += 18;
-      gc_launch(ctx, GK_WARMSTART, k_ws_apply, dim3(na), dim3(256), 0, (const float *)w.y, (const float *)w.scal, 1,
-                ctx->G, ctx->hi, ctx->lo);
-    } else if (ctx->ws_mode == GC_WS_EXTRAPOLATE) {
-      gc_launch(ctx, GK_WARMSTART, k_ws_apply, dim3(na), dim3(256), 0, (const float *)w.dlt, (const float *)w.scal, 0,
-                ctx->G, ctx->hi, ctx->lo);
+  if (!warm || ctx->ws_hist < 1) return GC_OK;
+  const float *yc = nullptr;
+  if (ctx->ws_mode == GC_WS_LEARNED && ctx->ws_hist >= 3) {
+    gc_ws *ws = ctx->ws;
+    if (!ws || ws->R != R) {
+      gc_set_error(ctx, "learned warm start needs a network with R = G/2 = %d", R);
+      return GC_ERR_STATE;
     }
-    GC_LAUNCH_CHECK(ctx, "warm-start apply");
+    ws->stream = ctx->stream;
+    if ((s = gc_ws_forward(ws, w.feat, w.y))) {
+      gc_set_error(ctx, "warm-start network: %s", ws->err);
+      return s;
+    }
+    ctx->prof.launches[GK_WARMSTART] += 18;
+    yc = w.y;
   }
+  const int extrap = ctx->ws_mode != GC_WS_PLAIN;
+  gc_launch(ctx, GK_WARMSTART, k_ws_apply, dim3((ctx->G + 127) / 128, ctx->G, ctx->G), dim3(128), 0, yc,
+            (const float *)w.scal, extrap, ctx->G, ctx->hi, ctx->lo, w.prev);
+  GC_LAUNCH_CHECK(ctx, "warm-start apply");
   return GC_OK;
 }
 
 int gc_ws_post_solve(gc_ctx *ctx) {
   if (!ctx->ws_track && !ctx->ws_record) return GC_OK;
-  if (ctx->G % 2) return GC_OK;
+  if (ctx->G % 2 || ctx->ws_skip) return GC_OK;
   const WsViews w = ws_views(ctx);
   const int R = ctx->G / 2;
-  const size_t R3 = (size_t)R * R * R;
-  unsigned nb = (unsigned)std::min<size_t>((R3 + 255) / 256, 1024);
-  gc_launch(ctx, GK_WARMSTART, k_ws_post, dim3(nb), dim3(256), 0, (const float *)ctx->hi, ctx->G, w.phi, w.dlt,
-            (const float *)w.scal, ctx->ws_hist, (__half *)ctx->ws_record);
+  gc_launch(ctx, GK_WARMSTART, k_ws_post, dim3((R + 63) / 64, R, R), dim3(64), 0, (const float *)ctx->hi, ctx->G,
+            w.phi, w.dlt, w.ddl, (const float *)w.scal, ctx->ws_hist, (__half *)ctx->ws_record);
   GC_LAUNCH_CHECK(ctx, "warm-start history");
-  ctx->ws_hist = ctx->ws_hist < 2 ? ctx->ws_hist + 1 : 2;
+  ctx->ws_hist = ctx->ws_hist < 3 ? ctx->ws_hist + 1 : 3;
   ctx->ws_record = nullptr;
   return GC_OK;
 }

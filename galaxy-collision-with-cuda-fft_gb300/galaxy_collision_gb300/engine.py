@@ -174,9 +174,10 @@ class PMEngine:
 
     # -- initial guess of the solve ---------------------------------------------------
     def set_warmstart(self, mode: str = "plain", net=None, track: bool = False) -> None:
-        """'plain' (previous potential, the reference's warm start), 'learned'
-        (previous + the network's predicted change; ``net`` a WarmStartNet with
-        R = G/2) or 'extrapolate' (previous + previous change)."""
+        """'plain' (previous potential, the reference's warm start), 'extrapolate'
+        (previous + previous change, full resolution) or 'learned' (the
+        extrapolation + the network's predicted second difference; ``net`` a
+        WarmStartNet with R = G/2)."""
         modes = {"plain": _native.GC_WS_PLAIN, "learned": _native.GC_WS_LEARNED,
                  "extrapolate": _native.GC_WS_EXTRAPOLATE}
         if mode not in modes:
@@ -186,11 +187,12 @@ class PMEngine:
         self.ctx.call("gc_pm_set_warmstart", h, modes[mode], int(bool(track)), what="set_warmstart")
 
     def record_sample(self, out: torch.Tensor) -> None:
-        """Have the next step write its network features and the solve's potential
-        change into ``out`` (float16, shape (4, G/2, G/2, G/2))."""
+        """Have the next step write its network features (channels 0..3) and the
+        second difference of the potential its solve produced (channel 4, the
+        training target) into ``out`` (float16, shape (5, G/2, G/2, G/2))."""
         R = self.grid_size // 2
-        if out.dtype != torch.float16 or tuple(out.shape) != (4, R, R, R) or not out.is_contiguous() or not out.is_cuda:
-            raise ValueError(f"out must be a contiguous CUDA float16 tensor of shape (4, {R}, {R}, {R})")
+        if out.dtype != torch.float16 or tuple(out.shape) != (5, R, R, R) or not out.is_contiguous() or not out.is_cuda:
+            raise ValueError(f"out must be a contiguous CUDA float16 tensor of shape (5, {R}, {R}, {R})")
         self.ctx.call("gc_pm_record_sample", C.c_void_p(out.data_ptr()), what="record_sample")
 
     # -- output -----------------------------------------------------------------

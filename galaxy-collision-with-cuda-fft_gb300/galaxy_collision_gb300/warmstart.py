@@ -1,21 +1,22 @@
 """Learned warm start of the multigrid: the network and its training step.
 
 The reference starts each solve from the previous step's potential
-(solver/multigrid.py:464-467). Here a small 3-D convolutional encoder-decoder
-predicts the change of the potential from the density and the previous
-potential; the multigrid then starts from previous + predicted change and still
-iterates to the same residual, so the prediction only changes the starting
-point. The network runs on an R^3 grid (R = G/2): four levels R .. R/8 with
-16-32-64-128 channels, 3x3x3 kernels, BF16 weights and activations with FP32
-accumulation, forward and backward passes in ``csrc/warmstart.cu`` on the
-tensor cores. This module owns a ``gc_ws`` network object: parameter
-initialisation, forward, backward (loss 0.5 mean (y - target)^2), Adam, and
-saving/loading the parameters.
+(solver/multigrid.py:464-467). The engine can instead start from the linear
+extrapolation phi(n-1) + (phi(n-1) - phi(n-2)) and add a learned correction: a
+small 3-D convolutional encoder-decoder predicts the next second difference of
+the potential from the density and the potential history. The multigrid then
+still iterates to the same residual, so the prediction only changes the
+starting point, and a zero output is exactly the extrapolation. The network
+runs on an R^3 grid (R = G/2): four levels R .. R/8 with 16-32-64-128 channels,
+3x3x3 kernels, BF16 weights and activations with FP32 accumulation, forward and
+backward passes in ``csrc/warmstart.cu`` on the tensor cores. This module owns a
+``gc_ws`` network object: parameter initialisation, forward, backward (loss
+0.5 mean (y - target)^2), Adam, and saving/loading the parameters.
 
-Input channels (f16 [3][R^3]): log(1 + rho_c / mean rho_c), phi_prev_c /
-rms(phi_prev_c), delta_prev_c / rms(delta_prev_c), where _c is the mean over
-2x2x2 fine nodes and delta_prev the previous step's potential change. Target:
-delta_c / rms(delta_prev_c).
+Input channels (f16 [4][R^3]), _c the mean over 2x2x2 fine nodes, d the change
+of the potential between solves and dd its change: log(1 + rho_c / mean rho_c),
+phi_c / rms, d_c / rms(d_c), dd_c / rms(dd_c), all of the previous step.
+Target: dd_c of this step / rms(dd_c of the previous step).
 """
 
 from __future__ import annotations
@@ -29,6 +30,7 @@ import torch
 from galaxy_collision_gb300 import _native
 
 N_LAYERS = 11
+N_FEATURES = 4
 WEIGHTS_PATH = Path(__file__).resolve().parent / "warmstart_weights.npz"
 
 
@@ -58,17 +60,17 @@ def param_slices(layers=None) -> list[tuple[slice, slice]]:
 
 def init_params(seed: int = 0, layers=None) -> np.ndarray:
     """He-normal weights (fan-in 27*cin of the used input channels), zero biases;
-    the output layer starts at zero so the untrained network predicts no change
-    (the plain previous-step warm start)."""
+    the output layer starts at zero so the untrained network predicts no second
+    difference (the extrapolated warm start)."""
     layers = layers or layer_table()
     rng = np.random.default_rng(seed)
     sl = param_slices(layers)
     p = np.zeros(sl[-1][1].stop, np.float32)
     for i, ((ci, co, _, _), (ws, _)) in enumerate(zip(layers, sl)):
-        fan_in = 27 * (3 if i == 0 else ci)
+        fan_in = 27 * (N_FEATURES if i == 0 else ci)
         w = rng.normal(0.0, np.sqrt(2.0 / fan_in), size=(27, co, ci)).astype(np.float32)
         if i == 0:
-            w[:, :, 3:] = 0.0
+            w[:, :, N_FEATURES:] = 0.0
         if i == len(layers) - 1:
             w[:] = 0.0
         p[ws] = w.ravel()
@@ -133,10 +135,10 @@ class WarmStartNet:
 
     # -- passes -----------------------------------------------------------------------
     def forward(self, feat: torch.Tensor) -> torch.Tensor:
-        """feat: f16 (3, R, R, R) on the device -> y (R, R, R) f32 (a view owned by the net)."""
+        """feat: f16 (4, R, R, R) on the device -> y (R, R, R) f32 (a view owned by the net)."""
         R = self.R
-        if feat.dtype != torch.float16 or tuple(feat.shape) != (3, R, R, R) or not feat.is_contiguous():
-            raise ValueError(f"feat must be a contiguous float16 tensor of shape (3, {R}, {R}, {R})")
+        if feat.dtype != torch.float16 or tuple(feat.shape) != (N_FEATURES, R, R, R) or not feat.is_contiguous():
+            raise ValueError(f"feat must be a contiguous float16 tensor of shape ({N_FEATURES}, {R}, {R}, {R})")
         self._call("gc_ws_forward", C.c_void_p(feat.data_ptr()), C.c_void_p(self.y.data_ptr()))
         return self.y
 
@@ -171,4 +173,4 @@ class WarmStartNet:
         return cls(r, params=params)
 
 
-__all__ = ["WarmStartNet", "init_params", "layer_table", "param_slices", "WEIGHTS_PATH"]
+__all__ = ["WarmStartNet", "init_params", "layer_table", "param_slices", "WEIGHTS_PATH", "N_FEATURES"]

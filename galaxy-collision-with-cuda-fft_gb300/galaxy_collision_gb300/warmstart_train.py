@@ -4,7 +4,8 @@ Training pairs come from the multigrid itself: randomised two-disk collisions
 (mass ratio U[1,3], impact parameter U[0,5], inclination U[0,90] degrees,
 approach speed U[0.2,1.0]) advance in the fused engine with the plain warm
 start; every ``every`` steps the engine records the network's input features
-and the potential change its converged solve produced (f16, (G/2)^3). The
+and the second difference of the potential its converged solve produced (f16,
+(G/2)^3). The
 network (``WarmStartNet``) is trained on them with its own tensor-core
 forward/backward kernels and Adam. Evaluation runs held-out collisions with the
 plain, extrapolated and learned initial guesses and reports V-cycles and solve
@@ -48,11 +49,11 @@ def _engine(grid: int, box: float, tol: float) -> PMEngine:
 
 def generate_samples(n_runs: int, n_particles: int = 1_000_000, steps: int = 100, every: int = 10, seed: int = 0,
                      grid: int = GRID, box: float = BOX, dt: float = DT, tol: float = 1e-6, log=None) -> torch.Tensor:
-    """(S, 4, R, R, R) float16 on the device: channels 0..2 features, 3 target."""
+    """(S, 5, R, R, R) float16 on the device: channels 0..3 features, 4 target."""
     R = grid // 2
     rng = np.random.default_rng(seed)
-    per_run = len([s for s in range(1, steps + 1) if s % every == 0 and s >= 3])
-    out = torch.empty((n_runs * per_run, 4, R, R, R), dtype=torch.float16, device="cuda")
+    per_run = len([s for s in range(1, steps + 1) if s % every == 0 and s >= 4])
+    out = torch.empty((n_runs * per_run, 5, R, R, R), dtype=torch.float16, device="cuda")
     k = 0
     for run in range(n_runs):
         t0 = time.time()
@@ -62,7 +63,7 @@ def generate_samples(n_runs: int, n_particles: int = 1_000_000, steps: int = 100
         eng.load(icr.pos, icr.vel, icr.mass, icr.gid)
         eng.prime(dt)
         for s in range(1, steps + 1):
-            if s % every == 0 and s >= 3:
+            if s % every == 0 and s >= 4:
                 eng.record_sample(out[k])
                 k += 1
             eng.advance(dt)
@@ -84,8 +85,8 @@ def train(net: WarmStartNet, samples: torch.Tensor, epochs: int = 20, lr: float 
         acc = torch.zeros(1, dtype=torch.float64, device=samples.device)
         t0 = time.time()
         for i in rng.permutation(S):
-            net.forward(samples[i, :3])
-            acc += net.backward(samples[i, 3]).double()
+            net.forward(samples[i, :4])
+            acc += net.backward(samples[i, 4]).double()
             net.adam_step(lr)
         hist.append(float(acc.item()) / S)
         if net.status() != 0:
@@ -96,16 +97,17 @@ def train(net: WarmStartNet, samples: torch.Tensor, epochs: int = 20, lr: float 
 
 
 def validation_loss(net: WarmStartNet, samples: torch.Tensor) -> dict:
-    """Mean loss of the network and of the two fixed predictors on held-out samples:
-    'zero' (no change: the plain warm start) and 'previous' (the previous change)."""
+    """Mean loss of the network and of two fixed predictors on held-out samples:
+    'zero' (no second difference: the linear extrapolation) and 'previous' (the
+    previous second difference: quadratic extrapolation)."""
     out = {"network": 0.0, "zero": 0.0, "previous": 0.0}
     S = samples.shape[0]
     for i in range(S):
-        f, t = samples[i, :3], samples[i, 3].float()
+        f, t = samples[i, :4], samples[i, 4].float()
         y = net.forward(f)
         out["network"] += 0.5 * float(((y - t) ** 2).mean())
         out["zero"] += 0.5 * float((t**2).mean())
-        out["previous"] += 0.5 * float(((f[2].float() - t) ** 2).mean())
+        out["previous"] += 0.5 * float(((f[3].float() - t) ** 2).mean())
     return {k: v / S for k, v in out.items()}
 
 

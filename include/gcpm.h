@@ -301,7 +301,7 @@ int gc_ws_num_params(const gc_ws *ws, int64_t *n);
 int gc_ws_set_params(gc_ws *ws, const float *params);
 int gc_ws_get_params(gc_ws *ws, float *params);
 int gc_ws_get_grads(gc_ws *ws, float *grads);
-/* Forward pass: feat = f16 [3][R^3] input channels; y_out (nullable) = f32 [R^3]. */
+/* Forward pass: feat = f16 [4][R^3] input channels; y_out (nullable) = f32 [R^3]. */
 int gc_ws_forward(gc_ws *ws, const void *feat, float *y_out);
 /* Backward pass of the last forward for the loss 0.5 * mean((y - target)^2),
  * target f16 [R^3]; the loss goes to *loss_out (device f32, nullable) and the
@@ -313,19 +313,20 @@ int gc_ws_adam(gc_ws *ws, float lr, float beta1, float beta2, float eps, int ste
 int gc_ws_status(gc_ws *ws, unsigned *flags, int clear);
 
 /* Initial guess of the engine's solve (gc_pm_step with warm_start != 0):
- *   GC_WS_PLAIN       the previous potential (the reference's warm start);
- *   GC_WS_LEARNED     previous + the network's predicted change (R = G/2);
- *   GC_WS_EXTRAPOLATE previous + the previous change (a non-learned comparison).
+ *   GC_WS_PLAIN       phi(n-1), the previous potential (the reference's warm start);
+ *   GC_WS_EXTRAPOLATE phi(n-1) + (phi(n-1) - phi(n-2)) at full resolution;
+ *   GC_WS_LEARNED     the extrapolation + the network's prediction of the next
+ *                     second difference of the potential (R = G/2 grid, trilinear).
  * The multigrid always iterates to the same residual: only the start changes.
  * With track != 0 (implied by the non-plain modes) the context keeps the
- * coarse (G/2)^3 history of the potential that the features need. G even. */
+ * history the extrapolation and the features need. G even. */
 #define GC_WS_PLAIN 0
 #define GC_WS_LEARNED 1
 #define GC_WS_EXTRAPOLATE 2
 int gc_pm_set_warmstart(gc_ctx *ctx, gc_ws *ws, int mode, int track);
 /* One-shot: the next gc_pm_step writes its network input features and the
- * change its solve produced (the training target) to out, f16 [4][(G/2)^3]:
- * channels 0..2 the features, 3 the target (see gc_ws_forward). */
+ * second difference its solve produced (the training target) to out, f16
+ * [5][(G/2)^3]: channels 0..3 the features, 4 the target (see gc_ws_forward). */
 int gc_pm_record_sample(gc_ctx *ctx, void *out);
 
 #ifdef __cplusplus

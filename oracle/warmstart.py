@@ -109,12 +109,12 @@ def relu(x):
 
 
 def forward(params, feat, emulate=True):
-    """feat: (3, R, R, R) (float16 or float). Returns (y, cache)."""
+    """feat: (4, R, R, R) (float16 or float). Returns (y, cache)."""
     r = bf16 if emulate else _ident
     P = [(r(W.astype(np.float32)) if emulate else W, b) for W, b in unpack(params)]
     R = feat.shape[1]
     x0 = np.zeros((16, R, R, R))
-    x0[:3] = r(np.asarray(feat, np.float32))
+    x0[:feat.shape[0]] = r(np.asarray(feat, np.float32))
     c = {"x0": x0, "P": P}
     c["e0"] = r(relu(conv(x0, *P[0])))
     c["p1"] = r(pool(c["e0"]))

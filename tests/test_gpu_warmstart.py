@@ -50,7 +50,7 @@ def _rand_params(seed):
 
 def _feat(R, seed):
     rng = np.random.default_rng(seed)
-    return rng.normal(size=(3, R, R, R)).astype(np.float16)
+    return rng.normal(size=(4, R, R, R)).astype(np.float16)
 
 
 @pytest.mark.parametrize("R", [16, 32])
@@ -81,9 +81,15 @@ def test_backward_matches_oracle(cuda):
     _, cache = ows.forward(p, feat, emulate=True)
     lo, go = ows.backward(cache, target.astype(np.float64), emulate=True)
     assert loss == pytest.approx(lo, rel=1e-3)
+    # bf16 activations and gradients are rounded at ~20 points; fp32 (device) and
+    # fp64 (oracle) accumulation flip some of those roundings, so agreement is to
+    # bf16 resolution: a few percent per layer, ~1% over the whole gradient
+    assert rel_l2(g, go) < 2e-2
     for i, (ws, bs) in enumerate(param_slices()):
-        assert rel_l2(g[ws], go[ws]) < 3e-2, f"layer {i} weights"
-        assert rel_l2(g[bs], go[bs]) < 3e-2, f"layer {i} bias"
+        assert rel_l2(g[ws], go[ws]) < 6e-2, f"layer {i} weights"
+        assert rel_l2(g[bs], go[bs]) < 6e-2, f"layer {i} bias"
+        cos = float(np.dot(g[ws], go[ws]) / (np.linalg.norm(g[ws]) * np.linalg.norm(go[ws])))
+        assert cos > 0.998, f"layer {i} weights: cosine {cos}"
 
 
 def test_adam_fits_a_fixed_target(cuda):
@@ -93,7 +99,7 @@ def test_adam_fits_a_fixed_target(cuda):
     R = 32
     rng = np.random.default_rng(11)
     z, y, x = np.meshgrid(*[np.linspace(-1, 1, R)] * 3, indexing="ij")
-    feat = np.stack([np.exp(-4 * (x**2 + y**2 + z**2)), x * y, np.sin(3 * z)]).astype(np.float16)
+    feat = np.stack([np.exp(-4 * (x**2 + y**2 + z**2)), x * y, np.sin(3 * z), x + z]).astype(np.float16)
     target = (0.5 * feat[0] - 0.3 * feat[2] + 0.05 * rng.normal(size=(R, R, R))).astype(np.float16)
     net = WarmStartNet(R, seed=3)
     f, t = torch.from_numpy(feat).cuda(), torch.from_numpy(target).cuda()
@@ -120,8 +126,9 @@ def _coarse(phi):
 
 
 def test_engine_records_features_and_target(cuda):
-    """The recorded sample is the features of the step and the coarse change of the
-    potential its solve produced, scaled by the rms of the previous change."""
+    """The recorded sample: the step's features (coarse potential, its first and
+    second differences, normalised) and the second difference its solve produced,
+    in units of the previous second difference's rms."""
     from galaxy_collision_gb300.engine import PMEngine
 
     G, dt = 32, 0.05
@@ -131,29 +138,31 @@ def test_engine_records_features_and_target(cuda):
     eng.load(pos, vel, mass)
     eng.prime(dt)
     phis = [eng.potential().double().cpu().numpy()]
-    for _ in range(2):
+    for _ in range(3):
         eng.advance(dt)
         phis.append(eng.potential().double().cpu().numpy())
-    rec = torch.zeros((4, G // 2, G // 2, G // 2), dtype=torch.float16, device="cuda")
+    rec = torch.zeros((5, G // 2, G // 2, G // 2), dtype=torch.float16, device="cuda")
     eng.record_sample(rec)
     eng.advance(dt)
     phis.append(eng.potential().double().cpu().numpy())
     r = rec.float().cpu().numpy()
     c = [_coarse(p) for p in phis]
-    d_prev, d_new = c[2] - c[1], c[3] - c[2]
-    s_prev = np.sqrt(np.mean(d_prev**2))
+    d_prev, d_new = c[3] - c[2], c[4] - c[3]
+    dd_prev, dd_new = d_prev - (c[2] - c[1]), d_new - d_prev
+    rms = lambda a: np.sqrt(np.mean(a**2))  # noqa: E731
     assert np.all(np.isfinite(r))
-    np.testing.assert_allclose(r[1], c[2] / np.sqrt(np.mean(c[2] ** 2)), rtol=0, atol=2e-3 * np.abs(r[1]).max())
-    np.testing.assert_allclose(r[2], d_prev / s_prev, rtol=0, atol=3e-3 * np.abs(r[2]).max())
-    np.testing.assert_allclose(r[3], d_new / s_prev, rtol=0, atol=3e-3 * np.abs(r[3]).max() + 1e-3)
     assert r[0].min() >= 0.0  # log(1 + rho / mean)
+    np.testing.assert_allclose(r[1], c[3] / rms(c[3]), rtol=0, atol=2e-3 * np.abs(r[1]).max())
+    np.testing.assert_allclose(r[2], d_prev / rms(d_prev), rtol=0, atol=3e-3 * np.abs(r[2]).max())
+    np.testing.assert_allclose(r[3], dd_prev / rms(dd_prev), rtol=0, atol=2e-2 * np.abs(r[3]).max())
+    np.testing.assert_allclose(r[4], dd_new / rms(dd_prev), rtol=0, atol=2e-2 * np.abs(r[4]).max() + 1e-3)
 
 
 @pytest.mark.parametrize("mode", ["extrapolate", "learned"])
 def test_warm_start_modes_reach_the_same_solution(cuda, mode):
     """Only the initial guess changes: trajectories agree with the plain warm start
-    to the solver tolerance, and an untrained network (zero output layer) needs
-    exactly the plain warm start's V-cycles."""
+    to the solver tolerance; an untrained network (zero output layer) is exactly
+    the extrapolation."""
     from galaxy_collision_gb300.engine import PMEngine
     from galaxy_collision_gb300.warmstart import WarmStartNet
 
@@ -175,6 +184,32 @@ def test_warm_start_modes_reach_the_same_solution(cuda, mode):
     p1, v1, c1 = run(mode, net)
     assert np.abs(p1 - p0).max() < 1e-5
     assert np.abs(v1 - v0).max() < 1e-5 * np.abs(v0).max() + 1e-7
+    assert sum(c1) <= sum(c0)
     if mode == "learned":
-        assert c1 == c0
+        _, _, ce = run("extrapolate")
+        assert c1 == ce
         assert net.status() == 0
+
+
+def test_trained_network_gain(cuda):
+    """What the shipped network adds to the method without it. On held-out
+    collisions (seeds outside the training set) its prediction of the next second
+    difference of the potential has a lower loss than predicting none (the linear
+    extrapolation, the method without the network) and than repeating the last
+    one; and with it the multigrid needs no more V-cycles than with the
+    extrapolation, and fewer than from the previous potential (the reference's
+    warm start)."""
+    from galaxy_collision_gb300 import warmstart_train as wt
+    from galaxy_collision_gb300.warmstart import WEIGHTS_PATH, WarmStartNet
+
+    if not WEIGHTS_PATH.exists():
+        pytest.skip("no trained weights shipped")
+    net = WarmStartNet.load(WEIGHTS_PATH)
+    val = wt.generate_samples(2, 1_000_000, 40, 10, seed=987_654)
+    loss = wt.validation_loss(net, val)
+    assert loss["network"] < 0.85 * loss["zero"], loss
+    assert loss["network"] < loss["previous"], loss
+    ev = wt.evaluate(net, 2_000_000, steps=6, seed=424_242, warm_steps=4)
+    assert ev["learned"]["mean_vcycles"] <= ev["extrapolate"]["mean_vcycles"]
+    assert ev["extrapolate"]["mean_vcycles"] < ev["plain"]["mean_vcycles"]
+    assert net.status() == 0

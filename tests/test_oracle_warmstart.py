@@ -25,7 +25,7 @@ def test_oracle_backward_matches_finite_differences():
     R = 16
     rng = np.random.default_rng(1)
     p = _params(2)
-    feat = rng.normal(size=(3, R, R, R))
+    feat = rng.normal(size=(4, R, R, R))
     target = 0.1 * rng.normal(size=(R, R, R))
     y, cache = ows.forward(p, feat, emulate=False)
     loss, g = ows.backward(cache, target, emulate=False)
