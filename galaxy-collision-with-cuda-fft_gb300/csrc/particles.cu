@@ -208,62 +208,7 @@ __device__ __forceinline__ void cic_q_large(float mm, float fx, float fy, float 
   }
 }
 
-// Add a run's 8 corner sums to the grid (out-of-box corners dropped). Out of
-// line: called once per run, and the values travel in registers.
-__device__ __noinline__ void flush_run(long long *__restrict__ qg, unsigned key, int G, long long q0, long long q1,
-                                       long long q2, long long q3, long long q4, long long q5, long long q6,
-                                       long long q7) {
-  const int G1 = G + 1;
-  const int ix = (int)(key / (unsigned)(G1 * G1)) - 1, iy = (int)((key / (unsigned)G1) % (unsigned)G1) - 1,
-            iz = (int)(key % (unsigned)G1) - 1;
-  const long long q[8] = {q0, q1, q2, q3, q4, q5, q6, q7};
-#pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const long long v = q[c];
-    const int jx = ix + (c >> 2), jy = iy + ((c >> 1) & 1), jz = iz + (c & 1);
-    if (v != 0 && (unsigned)jx < (unsigned)G && (unsigned)jy < (unsigned)G && (unsigned)jz < (unsigned)G)
-      atomicAdd((unsigned long long *)(qg + ((size_t)jx * G + jy) * G + jz), (unsigned long long)v);
-  }
-}
-#define FLUSH_RUN(qg, key, G, q) flush_run(qg, key, G, q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7])
 
-// Where runs go: the global int64 grid, or (box != null) a shared-memory box of
-// nodes [x0, x0+nx) x [y0, y0+ny) x [z0, z0+nz) that holds every corner of the
-// CTA's current particles and is added to the grid afterwards.
-struct DepSink {
-  long long *qg;
-  unsigned long long *box;
-  int x0, y0, z0, ny, nz, G;
-};
-
-__device__ __noinline__ void flush_run_box(DepSink k, unsigned key, long long q0, long long q1, long long q2,
-                                           long long q3, long long q4, long long q5, long long q6, long long q7) {
-  const int G1 = k.G + 1;
-  const int ix = (int)(key / (unsigned)(G1 * G1)) - 1 - k.x0, iy = (int)((key / (unsigned)G1) % (unsigned)G1) - 1 - k.y0,
-            iz = (int)(key % (unsigned)G1) - 1 - k.z0;
-  const long long q[8] = {q0, q1, q2, q3, q4, q5, q6, q7};
-#pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    if (q[c] != 0)
-      atomicAdd(k.box + ((ix + (c >> 2)) * k.ny + (iy + ((c >> 1) & 1))) * k.nz + (iz + (c & 1)),
-                (unsigned long long)q[c]);
-  }
-}
-
-__device__ __forceinline__ void sink_run(const DepSink &k, unsigned key, const long long (&q)[8]) {
-  if (k.box)
-    flush_run_box(k, key, q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7]);
-  else
-    FLUSH_RUN(k.qg, key, k.G, q);
-}
-
-struct DepRun {
-  unsigned key;  // cell key, DEP_NONE when empty
-  bool small;    // every contribution summed here was below 2^22 quanta
-  long long q[8];
-};
-
-// Deposit one particle into the two-run cache; returns nothing, may evict.
 template <bool POW2>
 __device__ __forceinline__ bool dep_cell(float px, float py, float pz, const DepCtx &d, float inv_dx, int &ix, int &iy,
                                          int &iz, float &fx, float &fy, float &fz) {
@@ -281,56 +226,39 @@ __device__ __forceinline__ bool dep_cell(float px, float py, float pz, const Dep
   return true;
 }
 
-template <bool POW2>
-__device__ __forceinline__ void dep_particle(float px, float py, float pz, float pm, const DepCtx &d, float inv_dx,
-                                             float qscale, const DepSink &sink, unsigned *__restrict__ status,
-                                             DepRun &r0, DepRun &r1) {
-  if (!gc_finite3(px, py, pz)) atomicOr(status, GC_FLAG_NONFINITE_POS);
+// Runs of equal cells. A run carries the linear index of its (ix, iy, iz) node
+// and whether all 8 corners are inside the grid, so adding it to the grid is 8
+// fire-and-forget atomics with constant offsets (no key decoding, no call).
+struct DepRun {
+  unsigned key;   // cell key, DEP_NONE when empty
+  int base;       // (ix*G + iy)*G + iz (G^3 < 2^31)
   int ix, iy, iz;
-  float fx, fy, fz;
-  if (!dep_cell<POW2>(px, py, pz, d, inv_dx, ix, iy, iz, fx, fy, fz)) return;
-  const float mm = __fmul_rn(pm, d.inv_vol);
-  const unsigned key = (unsigned)(((ix + 1) * (d.G + 1) + (iy + 1)) * (d.G + 1) + (iz + 1));
-  const bool small = __fmul_rn(fabsf(mm), qscale) < 4194304.0f;  // every |w| <= |mm|
+  bool small;     // every contribution summed here was below 2^22 quanta
   long long q[8];
-  if (small) {
-    const float wx0 = __fsub_rn(1.0f, fx), wy0 = __fsub_rn(1.0f, fy), wz0 = __fsub_rn(1.0f, fz);
-    const float a0 = __fmul_rn(mm, wx0), a1 = __fmul_rn(mm, fx);
-    const float b00 = __fmul_rn(a0, wy0), b01 = __fmul_rn(a0, fy), b10 = __fmul_rn(a1, wy0), b11 = __fmul_rn(a1, fy);
-    q[0] = rne_small(__fmul_rn(__fmul_rn(b00, wz0), qscale));
-    q[1] = rne_small(__fmul_rn(__fmul_rn(b00, fz), qscale));
-    q[2] = rne_small(__fmul_rn(__fmul_rn(b01, wz0), qscale));
-    q[3] = rne_small(__fmul_rn(__fmul_rn(b01, fz), qscale));
-    q[4] = rne_small(__fmul_rn(__fmul_rn(b10, wz0), qscale));
-    q[5] = rne_small(__fmul_rn(__fmul_rn(b10, fz), qscale));
-    q[6] = rne_small(__fmul_rn(__fmul_rn(b11, wz0), qscale));
-    q[7] = rne_small(__fmul_rn(__fmul_rn(b11, fz), qscale));
+};
+
+__device__ __forceinline__ void run_to_grid(long long *__restrict__ qg, int G, const DepRun &r,
+                                            const long long (&q)[8]) {
+  const bool interior = r.ix >= 0 && r.iy >= 0 && r.iz >= 0 && r.ix + 1 < G && r.iy + 1 < G && r.iz + 1 < G;
+  if (interior) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (q[c] != 0)
+        atomicAdd((unsigned long long *)(qg + r.base + ((c >> 2) * G + ((c >> 1) & 1)) * G + (c & 1)),
+                  (unsigned long long)q[c]);
   } else {
-    cic_q_large(mm, fx, fy, fz, qscale, q);
-  }
-  if (key == r0.key) {
-    r0.small = r0.small && small;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) r0.q[t] += q[t];
-  } else if (key == r1.key) {
-    r1.small = r1.small && small;
-#pragma unroll
-    for (int t = 0; t < 8; ++t) r1.q[t] += q[t];
-  } else {  // evict run 1, demote run 0, start a new run 0
-    if (r1.key != DEP_NONE) sink_run(sink, r1.key, r1.q);
-    r1.key = r0.key;
-    r1.small = r0.small;
-#pragma unroll
-    for (int t = 0; t < 8; ++t) r1.q[t] = r0.q[t];
-    r0.key = key;
-    r0.small = small;
-#pragma unroll
-    for (int t = 0; t < 8; ++t) r0.q[t] = q[t];
+    for (int c = 0; c < 8; ++c) {
+      const int jx = r.ix + (c >> 2), jy = r.iy + ((c >> 1) & 1), jz = r.iz + (c & 1);
+      if (q[c] != 0 && (unsigned)jx < (unsigned)G && (unsigned)jy < (unsigned)G && (unsigned)jz < (unsigned)G)
+        atomicAdd((unsigned long long *)(qg + ((size_t)jx * G + jy) * G + jz), (unsigned long long)q[c]);
+    }
   }
 }
 
-// Merge the cached runs of lanes holding the same cell and add them to the grid.
-__device__ __forceinline__ void dep_merge(const DepRun &r, const DepSink &sink, int lane) {
+// Lanes whose run is the same cell (__match_any_sync) reduce it with redux.sync
+// and one of them adds it; runs with a large contribution are added per lane.
+__device__ __forceinline__ void dep_merge(const DepRun &r, long long *__restrict__ qg, int G, int lane) {
   const unsigned peers = __match_any_sync(0xffffffffu, r.key);
   const unsigned large = __ballot_sync(0xffffffffu, !r.small);
   if (r.key == DEP_NONE) return;
@@ -339,42 +267,33 @@ __device__ __forceinline__ void dep_merge(const DepRun &r, const DepSink &sink, 
     long long tot[8];
 #pragma unroll
     for (int t = 0; t < 8; ++t) tot[t] = (long long)__reduce_add_sync(peers, (int)r.q[t]);
-    if (lane == __ffs(peers) - 1) sink_run(sink, r.key, tot);
+    if (lane == __ffs(peers) - 1) run_to_grid(qg, G, r, tot);
   } else {
-    sink_run(sink, r.key, r.q);
+    run_to_grid(qg, G, r, r.q);
   }
 }
 
 // The CTA stages a tile of DEP_TILE consecutive particles in shared memory with
 // coalesced loads (one padding word per 32 keeps the per-thread reads of 8
-// consecutive particles conflict-free) and finds the box of cells they touch.
-// When the box's corner nodes fit DEP_BOX_CAP int64 words, the runs are added
-// to that box in shared memory (cheap atomics, whatever the order of particles
-// that drifted between sorts) and the box is added to the grid once, one
-// atomic per nonzero node; otherwise the runs go straight to the grid. Every
-// thread walks its 8 particles in a rolled loop (small code).
+// consecutive particles conflict-free); each thread walks its 8 particles in a
+// rolled loop with a two-run cache (particles that drifted into a neighbour
+// cell since the last sort do not break the run of the cell they are
+// interleaved with), and the warp merges the cached runs at the end.
 #define DEP_TILE (256 * DEP_SEQ)
 #define DEP_PAD(i) ((i) + ((i) >> 5))
-#define DEP_BOX_CAP 4096
-#define DEP_SMEM_BYTES (DEP_BOX_CAP * 8 + 4 * DEP_PAD(DEP_TILE) * 4 + 64)
 template <bool POW2, bool VEC>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
     k_deposit_sorted(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
                      const float *__restrict__ m, long long n, DepCtx d, float inv_dx,
                      const double *__restrict__ qexp, long long *__restrict__ qg, unsigned *__restrict__ status) {
-  extern __shared__ __align__(16) unsigned long long dep_smem[];  // DEP_SMEM_BYTES
-  unsigned long long *box = dep_smem;
-  float *sx = reinterpret_cast<float *>(box + DEP_BOX_CAP), *sy = sx + DEP_PAD(DEP_TILE), *sz = sy + DEP_PAD(DEP_TILE),
-        *sm_ = sz + DEP_PAD(DEP_TILE);
-  int *bnd = reinterpret_cast<int *>(sm_ + DEP_PAD(DEP_TILE));
+  __shared__ float sx[DEP_PAD(DEP_TILE)], sy[DEP_PAD(DEP_TILE)], sz[DEP_PAD(DEP_TILE)], sm_[DEP_PAD(DEP_TILE)];
   const float qscale = ldexpf(1.0f, -(int)(*qexp));
   const int tid = threadIdx.x, lane = tid & 31;
   for (long long t0 = (long long)blockIdx.x * DEP_TILE; t0 < n; t0 += (long long)gridDim.x * DEP_TILE) {
     const int cnt_tile = (int)(n - t0 < DEP_TILE ? n - t0 : DEP_TILE);
-    __syncthreads();  // the previous tile and box have been consumed
-    if (tid < 3) { bnd[tid] = 0x7fffffff; bnd[3 + tid] = -0x7fffffff; }
+    __syncthreads();  // the previous tile has been consumed
     if (VEC && cnt_tile == DEP_TILE) {
-#pragma unroll
+#pragma unroll 1
       for (int h = 0; h < DEP_SEQ / 4; ++h) {
         const int q4 = h * 256 + tid;  // float4 index inside the tile
         const float4 a = __ldg(reinterpret_cast<const float4 *>(x + t0) + q4);
@@ -398,66 +317,60 @@ __global__ void __launch_bounds__(256)
     __syncthreads();
     const int i0 = tid * DEP_SEQ;
     const int cnt = cnt_tile - i0 < 0 ? 0 : (cnt_tile - i0 > DEP_SEQ ? DEP_SEQ : cnt_tile - i0);
-    // box of the cells that receive mass
-    int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {-0x7fffffff, -0x7fffffff, -0x7fffffff};
-#pragma unroll 1
-    for (int j = 0; j < cnt; ++j) {
-      const int i = DEP_PAD(i0 + j);
-      int ix, iy, iz;
-      float fx, fy, fz;
-      if (dep_cell<POW2>(sx[i], sy[i], sz[i], d, inv_dx, ix, iy, iz, fx, fy, fz)) {
-        lo[0] = min(lo[0], ix); lo[1] = min(lo[1], iy); lo[2] = min(lo[2], iz);
-        hi[0] = max(hi[0], ix); hi[1] = max(hi[1], iy); hi[2] = max(hi[2], iz);
-      }
-    }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      lo[a] = __reduce_min_sync(0xffffffffu, lo[a]);
-      hi[a] = __reduce_max_sync(0xffffffffu, hi[a]);
-    }
-    if (lane == 0) {
-#pragma unroll
-      for (int a = 0; a < 3; ++a) { atomicMin(&bnd[a], lo[a]); atomicMax(&bnd[3 + a], hi[a]); }
-    }
-    __syncthreads();
-    DepSink sink;
-    sink.qg = qg;
-    sink.G = d.G;
-    sink.box = nullptr;
-    sink.x0 = bnd[0]; sink.y0 = bnd[1]; sink.z0 = bnd[2];
-    const int nx = bnd[3] - bnd[0] + 2, ny = bnd[4] - bnd[1] + 2, nz = bnd[5] - bnd[2] + 2;
-    sink.ny = ny; sink.nz = nz;
-    const bool any = bnd[3] >= bnd[0];
-    const int vol = any ? nx * ny * nz : 0;  // at most (G+2)^3 < 2^31 nodes
-    const bool use_box = any && (long long)nx * ny * nz <= DEP_BOX_CAP;
-    if (use_box) {
-      sink.box = box;
-      for (int i = tid; i < vol; i += 256) box[i] = 0ull;
-      __syncthreads();
-    }
     DepRun r0, r1;
     r0.key = r1.key = DEP_NONE;
     r0.small = r1.small = true;
+    r0.base = r1.base = r0.ix = r0.iy = r0.iz = r1.ix = r1.iy = r1.iz = 0;
 #pragma unroll
     for (int t = 0; t < 8; ++t) r0.q[t] = r1.q[t] = 0;
 #pragma unroll 1
     for (int j = 0; j < cnt; ++j) {
       const int i = DEP_PAD(i0 + j);
-      dep_particle<POW2>(sx[i], sy[i], sz[i], sm_[i], d, inv_dx, qscale, sink, status, r0, r1);
-    }
-    dep_merge(r0, sink, lane);
-    dep_merge(r1, sink, lane);
-    if (use_box) {
-      __syncthreads();
-      for (int i = tid; i < vol; i += 256) {
-        const unsigned long long v = box[i];
-        if (v == 0ull) continue;
-        const int bx = i / (ny * nz), rem = i - bx * ny * nz, by = rem / nz, bz = rem - by * nz;
-        const int jx = sink.x0 + bx, jy = sink.y0 + by, jz = sink.z0 + bz;
-        if ((unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G && (unsigned)jz < (unsigned)d.G)
-          atomicAdd((unsigned long long *)(qg + ((size_t)jx * d.G + jy) * d.G + jz), v);
+      const float px = sx[i], py = sy[i], pz = sz[i];
+      if (!gc_finite3(px, py, pz)) atomicOr(status, GC_FLAG_NONFINITE_POS);
+      int ix, iy, iz;
+      float fx, fy, fz;
+      if (!dep_cell<POW2>(px, py, pz, d, inv_dx, ix, iy, iz, fx, fy, fz)) continue;
+      const float mm = __fmul_rn(sm_[i], d.inv_vol);
+      const bool small = __fmul_rn(fabsf(mm), qscale) < 4194304.0f;  // every |w| <= |mm| < 2^22 quanta
+      long long q[8];
+      if (small) {
+        const float wx0 = __fsub_rn(1.0f, fx), wy0 = __fsub_rn(1.0f, fy), wz0 = __fsub_rn(1.0f, fz);
+        const float a0 = __fmul_rn(mm, wx0), a1 = __fmul_rn(mm, fx);
+        const float b00 = __fmul_rn(a0, wy0), b01 = __fmul_rn(a0, fy), b10 = __fmul_rn(a1, wy0), b11 = __fmul_rn(a1, fy);
+        q[0] = rne_small(__fmul_rn(__fmul_rn(b00, wz0), qscale));
+        q[1] = rne_small(__fmul_rn(__fmul_rn(b00, fz), qscale));
+        q[2] = rne_small(__fmul_rn(__fmul_rn(b01, wz0), qscale));
+        q[3] = rne_small(__fmul_rn(__fmul_rn(b01, fz), qscale));
+        q[4] = rne_small(__fmul_rn(__fmul_rn(b10, wz0), qscale));
+        q[5] = rne_small(__fmul_rn(__fmul_rn(b10, fz), qscale));
+        q[6] = rne_small(__fmul_rn(__fmul_rn(b11, wz0), qscale));
+        q[7] = rne_small(__fmul_rn(__fmul_rn(b11, fz), qscale));
+      } else {
+        cic_q_large(mm, fx, fy, fz, qscale, q);
+      }
+      const unsigned key = (unsigned)(((ix + 1) * (d.G + 1) + (iy + 1)) * (d.G + 1) + (iz + 1));
+      if (key == r0.key) {
+        r0.small = r0.small && small;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) r0.q[t] += q[t];
+      } else if (key == r1.key) {
+        r1.small = r1.small && small;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) r1.q[t] += q[t];
+      } else {  // evict run 1, demote run 0, start a new run 0
+        if (r1.key != DEP_NONE) run_to_grid(qg, d.G, r1, r1.q);
+        r1 = r0;
+        r0.key = key;
+        r0.base = (ix * d.G + iy) * d.G + iz;
+        r0.ix = ix; r0.iy = iy; r0.iz = iz;
+        r0.small = small;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) r0.q[t] = q[t];
       }
     }
+    dep_merge(r0, qg, d.G, lane);
+    dep_merge(r1, qg, d.G, lane);
   }
 }
 
@@ -474,25 +387,17 @@ int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, co
   const bool pow2 = std::frexp(d.dx, &fe) == 0.5f;
   const float inv_dx = pow2 ? std::ldexp(1.0f, 1 - fe) : 0.0f;
   const bool vec = ((((uintptr_t)x) | ((uintptr_t)y) | ((uintptr_t)z) | ((uintptr_t)m)) & 15u) == 0;
-  static bool attr_set = false;  // dynamic shared memory above the 48 KB default, once per process
-  if (!attr_set) {
-    GC_CUDA(ctx, cudaFuncSetAttribute(k_deposit_sorted<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DEP_SMEM_BYTES));
-    GC_CUDA(ctx, cudaFuncSetAttribute(k_deposit_sorted<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, DEP_SMEM_BYTES));
-    GC_CUDA(ctx, cudaFuncSetAttribute(k_deposit_sorted<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DEP_SMEM_BYTES));
-    GC_CUDA(ctx, cudaFuncSetAttribute(k_deposit_sorted<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, DEP_SMEM_BYTES));
-    attr_set = true;
-  }
   if (pow2 && vec)
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true, true>, dim3(nb), dim3(256), DEP_SMEM_BYTES, x, y, z, m,
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true, true>, dim3(nb), dim3(256), 0, x, y, z, m,
               (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
   else if (pow2)
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true, false>, dim3(nb), dim3(256), DEP_SMEM_BYTES, x, y, z, m,
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true, false>, dim3(nb), dim3(256), 0, x, y, z, m,
               (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
   else if (vec)
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false, true>, dim3(nb), dim3(256), DEP_SMEM_BYTES, x, y, z, m,
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false, true>, dim3(nb), dim3(256), 0, x, y, z, m,
               (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
   else
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false, false>, dim3(nb), dim3(256), DEP_SMEM_BYTES, x, y, z, m,
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false, false>, dim3(nb), dim3(256), 0, x, y, z, m,
               (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
   GC_LAUNCH_CHECK(ctx, "deposit");
   return GC_OK;

@@ -495,6 +495,23 @@ __global__ void __launch_bounds__(256) k_conv_wgrad(ConvW a) {
   if (warp == 0) umma::tmem_dealloc(tmem, a.tmem_cols);
 }
 
+// out[e] = sum over c of part[c*nelem + e] for few elements and many partials:
+// one block per element, a fixed strided split and a fixed tree (deterministic).
+__global__ void __launch_bounds__(256) k_reduce_cols(const float *__restrict__ part, int nparts, int nelem,
+                                                     float *__restrict__ out) {
+  __shared__ float red[256];
+  const int e = blockIdx.x;
+  float s = 0.0f;
+  for (int c = threadIdx.x; c < nparts; c += 256) s += part[(size_t)c * nelem + e];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[e] = red[0];
+}
+
 // dW[e] = sum over CTAs of the partials, in CTA order.
 __global__ void __launch_bounds__(256) k_wgrad_reduce(const float *__restrict__ part, int nparts, int nelem,
                                                       float *__restrict__ dw) {
@@ -881,7 +898,7 @@ static int ws_wgrad(gc_ws *ws, int l, const uint4 *x, const uint4 *gy) {
   const size_t R3 = (size_t)R * R * R;
   const unsigned nb = std::min<unsigned>(ew_blocks(R3, ws->sm_count), 1024u);
   k_chan_sum<<<nb, 256, 0, ws->stream>>>(gy, Cout / 8, R3, ws->cpart);
-  k_wgrad_reduce<<<1, 256, 0, ws->stream>>>(ws->cpart, (int)nb, Cout, ws->grads + ws->b_off[l]);
+  k_reduce_cols<<<Cout, 256, 0, ws->stream>>>(ws->cpart, (int)nb, Cout, ws->grads + ws->b_off[l]);
   WS_CUDA(ws, cudaGetLastError());
   return GC_OK;
 }
@@ -1123,7 +1140,7 @@ extern "C" int gc_ws_backward(gc_ws *ws, const void *target, float *loss_out) {
   int s;
   const unsigned nl = std::min<unsigned>(ew_blocks(R3, sm), 1024u);
   k_mse<<<nl, 256, 0, ws->stream>>>(ws->y, (const __half *)target, R3, ws->gy, ws->lpart);
-  k_wgrad_reduce<<<1, 32, 0, ws->stream>>>(ws->lpart, (int)nl, 1, ws->loss);
+  k_reduce_cols<<<1, 256, 0, ws->stream>>>(ws->lpart, (int)nl, 1, ws->loss);
   WS_CUDA(ws, cudaGetLastError());
   // K, J
   if ((s = ws_wgrad(ws, 10, ws->f0, ws->gy))) return s;
@@ -1226,10 +1243,24 @@ __global__ void __launch_bounds__(256) k_ws_stats(const float *__restrict__ rho,
 }
 
 // scal: [0] mean rho_c, [1] rms phi_c, [2] rms d_c, [3] d usable, [4] rms dd_c, [5] dd usable
-__global__ void k_ws_scales(const float *__restrict__ part, int nb, size_t n, int hist, float *__restrict__ scal) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double a = 0.0, b = 0.0, c = 0.0, e = 0.0;
-  for (int i = 0; i < nb; ++i) { a += part[4 * i]; b += part[4 * i + 1]; c += part[4 * i + 2]; e += part[4 * i + 3]; }
+// One block of 256 threads; fixed strided split and tree over the partials.
+__global__ void __launch_bounds__(256) k_ws_scales(const float *__restrict__ part, int nb, size_t n, int hist,
+                                                   float *__restrict__ scal) {
+  __shared__ double red[4][256];
+  const int t = threadIdx.x;
+  double ta = 0.0, tb = 0.0, tc = 0.0, te = 0.0;
+  for (int i = t; i < nb; i += 256) { ta += part[4 * i]; tb += part[4 * i + 1]; tc += part[4 * i + 2]; te += part[4 * i + 3]; }
+  red[0][t] = ta; red[1][t] = tb; red[2][t] = tc; red[3][t] = te;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (t < w) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) red[k][t] += red[k][t + w];
+    }
+    __syncthreads();
+  }
+  if (t != 0) return;
+  const double a = red[0][0], b = red[1][0], c = red[2][0], e = red[3][0];
   const double mr = a / (double)n, rp = sqrt(b / (double)n), rd = sqrt(c / (double)n), rdd = sqrt(e / (double)n);
   const double tiny = 1e-30 * (rp > 0.0 ? rp : 1.0);
   scal[0] = mr > 0.0 ? (float)mr : 1.0f;
@@ -1381,7 +1412,7 @@ int gc_ws_pre_solve(gc_ctx *ctx, int warm, int mode) {
             w.rho);
   gc_launch(ctx, GK_WARMSTART, k_ws_stats, dim3(nb), dim3(256), 0, (const float *)w.rho, (const float *)w.phi,
             (const float *)w.dlt, (const float *)w.ddl, R3, w.part);
-  gc_launch(ctx, GK_WARMSTART, k_ws_scales, dim3(1), dim3(32), 0, (const float *)w.part, (int)nb, R3, ctx->ws_hist,
+  gc_launch(ctx, GK_WARMSTART, k_ws_scales, dim3(1), dim3(256), 0, (const float *)w.part, (int)nb, R3, ctx->ws_hist,
             w.scal);
   gc_launch(ctx, GK_WARMSTART, k_ws_features, dim3(nb), dim3(256), 0, (const float *)w.rho, (const float *)w.phi,
             (const float *)w.dlt, (const float *)w.ddl, (const float *)w.scal, ctx->ws_hist, R3, w.feat,
