@@ -256,9 +256,30 @@ __device__ __forceinline__ void run_to_grid(long long *__restrict__ qg, int G, c
   }
 }
 
+// Where finished runs go: the int64 grid, or (box != null) an int32 box of nodes
+// [x0, x0+nx) x [y0, y0+ny) x [z0, z0+nz) in shared memory that holds every
+// corner of the CTA's current tile; the tile's bound on its total quanta keeps
+// every box value below 2^31.
+struct DepOut {
+  long long *qg;
+  int *box;
+  int x0, y0, z0, ny, nz, G;
+};
+
+__device__ __forceinline__ void run_out(const DepOut &o, const DepRun &r, const long long (&q)[8]) {
+  if (o.box) {
+    const int bi = ((r.ix - o.x0) * o.ny + (r.iy - o.y0)) * o.nz + (r.iz - o.z0);
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (q[c] != 0) atomicAdd(o.box + bi + ((c >> 2) * o.ny + ((c >> 1) & 1)) * o.nz + (c & 1), (int)q[c]);
+  } else {
+    run_to_grid(o.qg, o.G, r, q);
+  }
+}
+
 // Lanes whose run is the same cell (__match_any_sync) reduce it with redux.sync
 // and one of them adds it; runs with a large contribution are added per lane.
-__device__ __forceinline__ void dep_merge(const DepRun &r, long long *__restrict__ qg, int G, int lane) {
+__device__ __forceinline__ void dep_merge(const DepRun &r, const DepOut &o, int lane) {
   const unsigned peers = __match_any_sync(0xffffffffu, r.key);
   const unsigned large = __ballot_sync(0xffffffffu, !r.small);
   if (r.key == DEP_NONE) return;
@@ -267,9 +288,9 @@ __device__ __forceinline__ void dep_merge(const DepRun &r, long long *__restrict
     long long tot[8];
 #pragma unroll
     for (int t = 0; t < 8; ++t) tot[t] = (long long)__reduce_add_sync(peers, (int)r.q[t]);
-    if (lane == __ffs(peers) - 1) run_to_grid(qg, G, r, tot);
+    if (lane == __ffs(peers) - 1) run_out(o, r, tot);
   } else {
-    run_to_grid(qg, G, r, r.q);
+    run_out(o, r, r.q);
   }
 }
 
@@ -278,20 +299,30 @@ __device__ __forceinline__ void dep_merge(const DepRun &r, long long *__restrict
 // consecutive particles conflict-free); each thread walks its 8 particles in a
 // rolled loop with a two-run cache (particles that drifted into a neighbour
 // cell since the last sort do not break the run of the cell they are
-// interleaved with), and the warp merges the cached runs at the end.
+// interleaved with), and the warp merges the cached runs at the end. A first
+// pass finds the box of cells the tile touches and the tile's largest
+// contribution: when the box's nodes fit DEP_BOX_CAP and the tile's total stays
+// below 2^30 quanta per node, runs are added to an int32 box in shared memory
+// and the box is added to the grid with one int64 atomic per nonzero node, so
+// run ends caused by drift cost shared-memory atomics only.
 #define DEP_TILE (256 * DEP_SEQ)
 #define DEP_PAD(i) ((i) + ((i) >> 5))
+#define DEP_BOX_CAP 3072
 template <bool POW2, bool VEC>
 __global__ void __launch_bounds__(256, 3)
     k_deposit_sorted(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
                      const float *__restrict__ m, long long n, DepCtx d, float inv_dx,
                      const double *__restrict__ qexp, long long *__restrict__ qg, unsigned *__restrict__ status) {
   __shared__ float sx[DEP_PAD(DEP_TILE)], sy[DEP_PAD(DEP_TILE)], sz[DEP_PAD(DEP_TILE)], sm_[DEP_PAD(DEP_TILE)];
+  __shared__ int box[DEP_BOX_CAP];
+  __shared__ int bnd[7];
   const float qscale = ldexpf(1.0f, -(int)(*qexp));
   const int tid = threadIdx.x, lane = tid & 31;
   for (long long t0 = (long long)blockIdx.x * DEP_TILE; t0 < n; t0 += (long long)gridDim.x * DEP_TILE) {
     const int cnt_tile = (int)(n - t0 < DEP_TILE ? n - t0 : DEP_TILE);
-    __syncthreads();  // the previous tile has been consumed
+    __syncthreads();  // the previous tile and box have been consumed
+    if (tid < 3) { bnd[tid] = 0x7fffffff; bnd[3 + tid] = -0x7fffffff; }
+    if (tid == 3) bnd[6] = 0;
     if (VEC && cnt_tile == DEP_TILE) {
 #pragma unroll 1
       for (int h = 0; h < DEP_SEQ / 4; ++h) {
@@ -317,6 +348,49 @@ __global__ void __launch_bounds__(256, 3)
     __syncthreads();
     const int i0 = tid * DEP_SEQ;
     const int cnt = cnt_tile - i0 < 0 ? 0 : (cnt_tile - i0 > DEP_SEQ ? DEP_SEQ : cnt_tile - i0);
+    // box of the cells that receive mass and the largest |m/dx^3| in quanta
+    int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {-0x7fffffff, -0x7fffffff, -0x7fffffff};
+    float mq = 0.0f;
+#pragma unroll 1
+    for (int j = 0; j < cnt; ++j) {
+      const int i = DEP_PAD(i0 + j);
+      int ix, iy, iz;
+      float fx, fy, fz;
+      if (dep_cell<POW2>(sx[i], sy[i], sz[i], d, inv_dx, ix, iy, iz, fx, fy, fz)) {
+        lo[0] = min(lo[0], ix); lo[1] = min(lo[1], iy); lo[2] = min(lo[2], iz);
+        hi[0] = max(hi[0], ix); hi[1] = max(hi[1], iy); hi[2] = max(hi[2], iz);
+        const float a = __fmul_rn(fabsf(__fmul_rn(sm_[i], d.inv_vol)), qscale);
+        mq = (a > mq || a != a) ? (a == a ? a : 3.0e38f) : mq;
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = __reduce_min_sync(0xffffffffu, lo[a]);
+      hi[a] = __reduce_max_sync(0xffffffffu, hi[a]);
+    }
+    const unsigned mqb = __reduce_max_sync(0xffffffffu, __float_as_uint(mq));  // non-negative floats order as ints
+    if (lane == 0) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) { atomicMin(&bnd[a], lo[a]); atomicMax(&bnd[3 + a], hi[a]); }
+      atomicMax(&bnd[6], (int)mqb);
+    }
+    __syncthreads();
+    DepOut o;
+    o.qg = qg;
+    o.G = d.G;
+    o.box = nullptr;
+    o.x0 = bnd[0]; o.y0 = bnd[1]; o.z0 = bnd[2];
+    const int nx = bnd[3] - bnd[0] + 2, ny = bnd[4] - bnd[1] + 2, nz = bnd[5] - bnd[2] + 2;
+    o.ny = ny; o.nz = nz;
+    // every contribution is at most (largest |m/dx^3| in quanta) + 1/2 after rounding
+    const float tile_q = __fmul_rn(__uint_as_float((unsigned)bnd[6]) + 1.0f, (float)cnt_tile);
+    const bool use_box = bnd[3] >= bnd[0] && (long long)nx * ny * nz <= DEP_BOX_CAP && tile_q < 1073741824.0f;
+    const int vol = use_box ? nx * ny * nz : 0;
+    if (use_box) {
+      o.box = box;
+      for (int i = tid; i < vol; i += 256) box[i] = 0;
+      __syncthreads();
+    }
     DepRun r0, r1;
     r0.key = r1.key = DEP_NONE;
     r0.small = r1.small = true;
@@ -359,7 +433,7 @@ __global__ void __launch_bounds__(256, 3)
 #pragma unroll
         for (int t = 0; t < 8; ++t) r1.q[t] += q[t];
       } else {  // evict run 1, demote run 0, start a new run 0
-        if (r1.key != DEP_NONE) run_to_grid(qg, d.G, r1, r1.q);
+        if (r1.key != DEP_NONE) run_out(o, r1, r1.q);
         r1 = r0;
         r0.key = key;
         r0.base = (ix * d.G + iy) * d.G + iz;
@@ -369,8 +443,19 @@ __global__ void __launch_bounds__(256, 3)
         for (int t = 0; t < 8; ++t) r0.q[t] = q[t];
       }
     }
-    dep_merge(r0, qg, d.G, lane);
-    dep_merge(r1, qg, d.G, lane);
+    dep_merge(r0, o, lane);
+    dep_merge(r1, o, lane);
+    if (use_box) {
+      __syncthreads();
+      for (int i = tid; i < vol; i += 256) {
+        const int v = box[i];
+        if (v == 0) continue;
+        const int bx = i / (ny * nz), rem = i - bx * ny * nz, by = rem / nz, bz = rem - by * nz;
+        const int jx = o.x0 + bx, jy = o.y0 + by, jz = o.z0 + bz;
+        if ((unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G && (unsigned)jz < (unsigned)d.G)
+          atomicAdd((unsigned long long *)(qg + ((size_t)jx * d.G + jy) * d.G + jz), (unsigned long long)(long long)v);
+      }
+    }
   }
 }
 
@@ -848,8 +933,6 @@ __device__ __forceinline__ void kd_update(long long p, float px, float py, float
   vz[p] = uz;
 }
 
-// Two particles per thread per iteration (p and p + stride): their loads and
-// corner gathers are independent, so twice as many requests are in flight.
 template <bool DIAG, bool POW2>
 __global__ void __launch_bounds__(256)
     k_gather4_kick_drift(float *__restrict__ x, float *__restrict__ y, float *__restrict__ z, float *__restrict__ vx,
@@ -858,18 +941,11 @@ __global__ void __launch_bounds__(256)
   double dv[11];
 #pragma unroll
   for (int t = 0; t < 11; ++t) dv[t] = 0.0;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += 2 * stride) {
-    const long long q = p + stride;
-    const bool hq = q < n;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     const float px = x[p], py = y[p], pz = z[p], ux = vx[p], uy = vy[p], uz = vz[p];
-    float qx = 0.0f, qy = 0.0f, qz = 0.0f, wx = 0.0f, wy = 0.0f, wz = 0.0f;
-    if (hq) { qx = x[q]; qy = y[q]; qz = z[q]; wx = vx[q]; wy = vy[q]; wz = vz[q]; }
-    float ax, ay, az, bx = 0.0f, by = 0.0f, bz = 0.0f;
+    float ax, ay, az;
     gather_g4<POW2>(g4, px, py, pz, f, ax, ay, az);
-    if (hq) gather_g4<POW2>(g4, qx, qy, qz, f, bx, by, bz);
     kd_update<DIAG>(p, px, py, pz, ux, uy, uz, ax, ay, az, x, y, z, vx, vy, vz, m, f, dv);
-    if (hq) kd_update<DIAG>(q, qx, qy, qz, wx, wy, wz, bx, by, bz, x, y, z, vx, vy, vz, m, f, dv);
   }
   if (DIAG) block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
 }
