@@ -523,18 +523,35 @@ def _e2e(args, icr, make_engine, dt):
     out_vel = torch.empty((icr.n, 3), dtype=torch.float32).pin_memory()
     eng = make_engine()
     torch.cuda.synchronize()
+    marks = []
+
+    def mark(name):
+        if args.verbose:  # phase breakdown (synchronising) only when asked for
+            torch.cuda.synchronize()
+            marks.append((name, time.perf_counter()))
+
     t0 = time.perf_counter()
     eng.load(pos.cuda(non_blocking=True), vel.cuda(non_blocking=True), mass.cuda(non_blocking=True),
              gid.cuda(non_blocking=True), sort=True)
+    mark("load+sort")
     eng.prime(dt)
+    mark("prime")
     for _ in range(args.steps - 1):
         eng.advance(dt)
+    mark("advance")
     eng.synchronize(dt, diagnostics=True)
+    mark("close")
     p, v, _, _ = eng.state_arrays(physical=True)
     out_pos.copy_(p.to(torch.float32), non_blocking=True)
     out_vel.copy_(v, non_blocking=True)
     torch.cuda.synchronize()
     t = time.perf_counter() - t0
+    if args.verbose:
+        prev = t0
+        for name, tm in marks:
+            _log(args, f"e2e {name}: {1e3 * (tm - prev):.1f} ms")
+            prev = tm
+        _log(args, f"e2e state back: {1e3 * (t0 + t - prev):.1f} ms")
     n = icr.n
     return {"value": n * args.steps / t, "unit": UNIT, "h2d_bytes_per_step": int(n * 32 / args.steps),
             "d2h_bytes_per_step": int((n * 24 + 12 * 8) / args.steps),

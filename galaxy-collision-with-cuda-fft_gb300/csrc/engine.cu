@@ -76,6 +76,17 @@ extern "C" int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_para
   return GC_OK;
 }
 
+extern "C" int gc_pm_last_residual(gc_ctx *ctx, double *rel) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, rel, "gc_pm_last_residual: NULL output");
+  double h[2];
+  GC_CUDA(ctx, cudaMemcpyAsync(&h[0], ctx->dsmall + GC_S_BNORM2, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GC_CUDA(ctx, cudaMemcpyAsync(&h[1], ctx->dsmall + GC_S_RNORM2, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *rel = h[0] > 0.0 ? sqrt(h[1]) / sqrt(h[0]) : 0.0;
+  return GC_OK;
+}
+
 extern "C" int gc_pm_copy_potential(gc_ctx *ctx, float *phi) {
   if (!ctx) return GC_ERR_ARG;
   GC_REQUIRE(ctx, phi, "gc_pm_copy_potential: NULL phi");

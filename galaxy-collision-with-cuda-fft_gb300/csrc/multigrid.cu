@@ -995,7 +995,23 @@ int gc_faces_from_moments(gc_ctx *ctx) {
 int gc_mg_run(gc_ctx *ctx, const gc_mg_params *p, gc_mg_stats *stats) {
   gc_mg_stats st;
   memset(&st, 0, sizeof(st));
-  int s = read_small(ctx, GC_S_BNORM2, 1);
+  int s;
+  if (p->flags & GC_MG_FIXED_CYCLES) {
+    // exactly max_cycles V-cycles and no host read: the residual norm is left on
+    // the device (gc_pm_last_residual reads it), so the solve can be captured in
+    // a CUDA graph
+    for (int c = 0; c < p->max_cycles && ctx->nlev > 0; ++c)
+      if ((s = vcycle(ctx, p))) return s;
+    if (ctx->nlev > 0 && (s = resid_norm_async(ctx))) return s;
+    st.cycles = ctx->nlev > 0 ? p->max_cycles : 0;
+    st.converged = -1;
+    st.rhs_norm = st.res_norm = NAN;
+    ctx->last_stats = st;
+    ctx->solved_once = 1;
+    if (stats) *stats = st;
+    return GC_OK;
+  }
+  s = read_small(ctx, GC_S_BNORM2, 1);
   if (s) return s;
   const double bnorm = sqrt(ctx->hsmall[GC_S_BNORM2]);
   const double h2 = ctx->dx * ctx->dx;

@@ -782,13 +782,14 @@ static size_t smem_for_residency(size_t smem, int k) {
 
 static const size_t WS_SMEM_MAX = 232448;
 
-// Tile plan of the forward kernel from a cycle estimate per SM: staging the
-// input tile (L2 -> shared, ~64 B/clk), the MMAs (one 128 x Cout x 16 step every
-// max(8, 128*Cout*16/4096) clocks, issued by four threads) and the epilogue,
-// with at most `occ` CTAs overlapping on an SM.
-static bool plan_fwd(int R, int Cin, int Cout, int sm_count, FwdPlan &best) {
-  bool found = false;
-  double best_cost = 1e300;
+// Tile plans of the forward kernel. Every feasible (BZ, BY) is enumerated; the
+// default pick minimises a cycle estimate per SM -- staging the input tile (L2 ->
+// shared, ~64 B/clk), the MMAs (one 128 x Cout x 16 step every max(8,
+// 128*Cout*16/4096) clocks, issued by four threads) and the epilogue, with at
+// most `occ` CTAs overlapping on an SM -- and gc_ws_autotune replaces it by the
+// fastest measured candidate.
+static std::vector<FwdPlan> enum_fwd(int R, int Cin, int Cout, int sm_count, std::vector<double> *costs) {
+  std::vector<FwdPlan> out;
   const int bys[] = {32, 16, 8, 4, 2, 1};
   const int bzs[] = {1, 2, 4, 8};
   for (int BY : bys) {
@@ -806,31 +807,39 @@ static bool plan_fwd(int R, int Cin, int Cout, int sm_count, FwdPlan &best) {
       const int ngroups = (27 + tpg - 1) / tpg;
       const int tpg_even = (27 + ngroups - 1) / ngroups;
       const size_t smem = tile + 2 * (size_t)tpg_even * tap + 64;
-      const uint32_t cols = pow2_cols(n_mt * Cout);
-      const size_t smem_launch = smem_for_residency(smem, (int)(512 / cols));
-      const int occ = std::max(1, std::min(8, (int)(233472 / (smem_launch + 1024))));
-      const int ctas = (R / BZ) * (R / BY);
-      const double load = (double)(Cin / 8) * V * 16 / 64.0 + (double)27 * tap / 64.0;
-      const double mma = 27.0 * n_mt * (Cin / 16) * std::max(8.0, 128.0 * Cout * 16 / 4096.0) / 4.0 + 300.0;
-      const double epi = (double)n_mt * 128 * Cout * 2 / 64.0;
-      const double per_cta = load + mma + epi + 2000.0;
-      const double busiest = std::max(load, std::max(mma, epi));
-      const double waves = std::ceil((double)ctas / (sm_count * occ));
-      const double cost = waves * std::max(per_cta, occ * busiest);
-      if (cost < best_cost) {
-        best_cost = cost;
-        best.BZ = BZ; best.BY = BY; best.tpg = tpg_even; best.n_mt = n_mt; best.grid = ctas; best.cols = cols;
-        best.smem = smem_launch;
-        found = true;
+      FwdPlan p;
+      p.BZ = BZ; p.BY = BY; p.tpg = tpg_even; p.n_mt = n_mt; p.grid = (R / BZ) * (R / BY);
+      p.cols = pow2_cols(n_mt * Cout);
+      p.smem = smem_for_residency(smem, (int)(512 / p.cols));
+      out.push_back(p);
+      if (costs) {
+        const int occ = std::max(1, std::min(8, (int)(233472 / (p.smem + 1024))));
+        const double load = (double)(Cin / 8) * V * 16 / 64.0 + (double)27 * tap / 64.0;
+        const double mma = 27.0 * n_mt * (Cin / 16) * std::max(8.0, 128.0 * Cout * 16 / 4096.0) / 4.0 + 300.0;
+        const double epi = (double)n_mt * 128 * Cout * 2 / 64.0;
+        const double per_cta = load + mma + epi + 2000.0;
+        const double busiest = std::max(load, std::max(mma, epi));
+        const double waves = std::ceil((double)p.grid / (sm_count * occ));
+        costs->push_back(waves * std::max(per_cta, occ * busiest));
       }
     }
   }
-  return found;
+  return out;
 }
 
-static bool plan_wgrad(int R, int Cin, int Cout, int sm_count, WgPlan &best) {
-  bool found = false;
-  double best_score = -1.0;
+static bool plan_fwd(int R, int Cin, int Cout, int sm_count, FwdPlan &best) {
+  std::vector<double> cost;
+  const std::vector<FwdPlan> c = enum_fwd(R, Cin, Cout, sm_count, &cost);
+  if (c.empty()) return false;
+  size_t k = 0;
+  for (size_t i = 1; i < c.size(); ++i)
+    if (cost[i] < cost[k]) k = i;
+  best = c[k];
+  return true;
+}
+
+static std::vector<WgPlan> enum_wgrad(int R, int Cin, int Cout, int sm_count, std::vector<double> *scores) {
+  std::vector<WgPlan> out;
   const int bys[] = {32, 16, 8, 4, 2, 1};
   const int bzs[] = {1, 2, 4};
   const int tpp = std::min(27, 512 / Cin);
@@ -845,22 +854,32 @@ static bool plan_wgrad(int R, int Cin, int Cout, int sm_count, WgPlan &best) {
       const size_t smem = tile + 2 * WG_STAGE_BYTES + 64;
       if (smem > WS_SMEM_MAX) continue;
       const int nst = (L1 - L0 + WG_STAGE_ROWS) / WG_STAGE_ROWS;
-      const int nblocks = (R / BZ) * (R / BY);
-      const double useful = (double)BZ * BY * R / (128.0 * nst) * (double)V / (V + 0.0);
-      const double fill = std::min(1.0, (double)nblocks / (double)sm_count);
-      const double reload = (double)(BZ * BY) / ((BZ + 2.0) * (BY + 2.0));
-      const double score = useful * fill * (0.5 + 0.5 * reload);
-      if (score > best_score) {
-        best_score = score;
-        best.BZ = BZ; best.BY = BY; best.tpp = tpp; best.nblocks = nblocks; best.cols = cols;
-        best.smem = smem_for_residency(smem, (int)(512 / cols));
-        const int per_sm = std::max(1, (int)(233472 / (best.smem + 1024)));
-        best.grid = std::min(nblocks, sm_count * per_sm);
-        found = true;
+      WgPlan p;
+      p.BZ = BZ; p.BY = BY; p.tpp = tpp; p.nblocks = (R / BZ) * (R / BY); p.cols = cols;
+      p.smem = smem_for_residency(smem, (int)(512 / cols));
+      const int per_sm = std::max(1, (int)(233472 / (p.smem + 1024)));
+      p.grid = std::min(p.nblocks, sm_count * per_sm);
+      out.push_back(p);
+      if (scores) {
+        const double useful = (double)BZ * BY * R / (128.0 * nst);
+        const double fill = std::min(1.0, (double)p.nblocks / (double)sm_count);
+        const double reload = (double)(BZ * BY) / ((BZ + 2.0) * (BY + 2.0));
+        scores->push_back(useful * fill * (0.5 + 0.5 * reload));
       }
     }
   }
-  return found;
+  return out;
+}
+
+static bool plan_wgrad(int R, int Cin, int Cout, int sm_count, WgPlan &best) {
+  std::vector<double> sc;
+  const std::vector<WgPlan> c = enum_wgrad(R, Cin, Cout, sm_count, &sc);
+  if (c.empty()) return false;
+  size_t k = 0;
+  for (size_t i = 1; i < c.size(); ++i)
+    if (sc[i] > sc[k]) k = i;
+  best = c[k];
+  return true;
 }
 
 static unsigned ew_blocks(size_t n, int sm_count) {
@@ -1005,9 +1024,12 @@ extern "C" int gc_ws_create(gc_ws **out, int R) {
       rc = GC_ERR_ARG;
     }
   }
-  size_t part = 0;
-  for (int l = 0; l < WS_NL && rc == GC_OK; ++l)
-    part = std::max(part, (size_t)ws->pw[l].grid * 27 * kWsLayer[l][0] * kWsLayer[l][1]);
+  size_t part = 0;  // weight-gradient partials: the largest grid any candidate plan may use
+  for (int l = 0; l < WS_NL && rc == GC_OK; ++l) {
+    const int Rl = R >> kWsLayer[l][2];
+    for (const WgPlan &c : enum_wgrad(Rl, kWsLayer[l][0], kWsLayer[l][1], ws->sm_count, nullptr))
+      part = std::max(part, (size_t)c.grid * 27 * kWsLayer[l][0] * kWsLayer[l][1]);
+  }
   ws->part_cap = part;
   if (rc == GC_OK && cudaMalloc(&ws->part, part * sizeof(float) + (size_t)(1024 * 128 + 1024 + 16) * sizeof(float) +
                                                64) != cudaSuccess)
@@ -1178,6 +1200,112 @@ extern "C" int gc_ws_backward(gc_ws *ws, const void *target, float *loss_out) {
   if ((s = ws_wgrad(ws, 0, ws->x0, ws->g_e0))) return s;
   WS_CUDA(ws, cudaGetLastError());
   if (loss_out) WS_CUDA(ws, cudaMemcpyAsync(loss_out, ws->loss, sizeof(float), cudaMemcpyDeviceToDevice, ws->stream));
+  return GC_OK;
+}
+
+// ---- autotuner --------------------------------------------------------------------
+// Buffers each layer reads and writes in the forward, data-gradient and
+// weight-gradient passes (the autotuner times candidates on them).
+struct WsBufs {
+  const uint4 *in;
+  uint4 *out;
+  const uint4 *mask;
+  float *outf;
+};
+static WsBufs fwd_bufs(gc_ws *ws, int l) {
+  const uint4 *in[WS_NL] = {ws->x0, ws->p1, ws->p2, ws->p3, ws->e3, ws->d2, ws->f2, ws->d1, ws->f1, ws->d0, ws->f0};
+  uint4 *out[WS_NL] = {ws->e0, ws->e1, ws->e2, ws->e3, ws->u2, ws->f2, ws->u1, ws->f1, ws->u0, ws->f0, nullptr};
+  return {in[l], out[l], nullptr, l == WS_NL - 1 ? ws->y : nullptr};
+}
+static WsBufs dgrad_bufs(gc_ws *ws, int l) {  // l >= 1
+  const uint4 *in[WS_NL] = {nullptr, ws->g_e1, ws->g_e2, ws->g_e3, ws->g_u2, ws->g_f2, ws->g_u1, ws->g_f1, ws->g_u0,
+                            ws->g_f0, ws->gy};
+  uint4 *out[WS_NL] = {nullptr, ws->g_p1, ws->g_p2, ws->g_p3, ws->g_e3, ws->g_d2, ws->g_f2, ws->g_d1, ws->g_f1,
+                       ws->g_d0, ws->g_f0};
+  const uint4 *mask[WS_NL] = {nullptr, nullptr, nullptr, nullptr, ws->e3, ws->d2, ws->f2, ws->d1, ws->f1, ws->d0,
+                              ws->f0};
+  return {in[l], out[l], mask[l], nullptr};
+}
+static WsBufs wgrad_bufs(gc_ws *ws, int l) {  // in = layer input, mask = output gradient
+  const uint4 *x[WS_NL] = {ws->x0, ws->p1, ws->p2, ws->p3, ws->e3, ws->d2, ws->f2, ws->d1, ws->f1, ws->d0, ws->f0};
+  const uint4 *g[WS_NL] = {ws->g_e0, ws->g_e1, ws->g_e2, ws->g_e3, ws->g_u2, ws->g_f2, ws->g_u1, ws->g_f1, ws->g_u0,
+                           ws->g_f0, ws->gy};
+  return {x[l], nullptr, g[l], nullptr};
+}
+
+// Time every feasible tile plan of every layer's three passes (CUDA events,
+// `iters` launches after one untimed) and keep the fastest. Activations are
+// overwritten. ms_out (host, nullable) receives the best time per pass,
+// [layer][forward, data gradient, weight gradient], 0 where a pass does not exist.
+extern "C" int gc_ws_autotune(gc_ws *ws, int iters, float *ms_out) {
+  if (!ws || iters < 1) return GC_ERR_ARG;
+  cudaEvent_t ev0, ev1;
+  WS_CUDA(ws, cudaEventCreate(&ev0));
+  WS_CUDA(ws, cudaEventCreate(&ev1));
+  int rc = GC_OK;
+  for (int l = 0; l < WS_NL && rc == GC_OK; ++l) {
+    const int Cin = kWsLayer[l][0], Cout = kWsLayer[l][1], R = ws->R >> kWsLayer[l][2];
+    for (int kind = 0; kind < 3 && rc == GC_OK; ++kind) {
+      float best = 3.0e38f;
+      if (kind == 2) {
+        const std::vector<WgPlan> c = enum_wgrad(R, Cin, Cout, ws->sm_count, nullptr);
+        const WsBufs b = wgrad_bufs(ws, l);
+        WgPlan keep = ws->pw[l];
+        for (const WgPlan &p : c) {
+          ws->pw[l] = p;
+          if ((rc = ws_wgrad(ws, l, b.in, b.mask))) break;
+          cudaEventRecord(ev0, ws->stream);
+          for (int i = 0; i < iters && rc == GC_OK; ++i) rc = ws_wgrad(ws, l, b.in, b.mask);
+          cudaEventRecord(ev1, ws->stream);
+          cudaEventSynchronize(ev1);
+          float ms = 0.0f;
+          cudaEventElapsedTime(&ms, ev0, ev1);
+          if (ms < best) { best = ms; keep = p; }
+        }
+        ws->pw[l] = keep;
+      } else {
+        if (kind == 1 && l == 0) { if (ms_out) ms_out[3 * l + kind] = 0.0f; continue; }
+        const int ci = kind == 0 ? Cin : Cout, co = kind == 0 ? Cout : Cin;
+        const std::vector<FwdPlan> c = enum_fwd(R, ci, co, ws->sm_count, nullptr);
+        const WsBufs b = kind == 0 ? fwd_bufs(ws, l) : dgrad_bufs(ws, l);
+        FwdPlan &slot = kind == 0 ? ws->pf[l] : ws->pb[l];
+        FwdPlan keep = slot;
+        const uint16_t *w = kind == 0 ? ws->wf[l] : ws->wb[l];
+        const float *bias = kind == 0 ? ws->params + ws->b_off[l] : nullptr;
+        const int relu = kind == 0 ? kWsLayer[l][3] : 0;
+        for (const FwdPlan &p : c) {
+          if ((rc = ws_conv(ws, p, R, ci, co, b.in, w, bias, nullptr, b.mask, b.out, b.outf, relu))) break;
+          cudaEventRecord(ev0, ws->stream);
+          for (int i = 0; i < iters && rc == GC_OK; ++i)
+            rc = ws_conv(ws, p, R, ci, co, b.in, w, bias, nullptr, b.mask, b.out, b.outf, relu);
+          cudaEventRecord(ev1, ws->stream);
+          cudaEventSynchronize(ev1);
+          float ms = 0.0f;
+          cudaEventElapsedTime(&ms, ev0, ev1);
+          if (ms < best) { best = ms; keep = p; }
+        }
+        slot = keep;
+      }
+      if (ms_out) ms_out[3 * l + kind] = best < 3.0e38f ? best / (float)iters : 0.0f;
+    }
+  }
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  if (rc == GC_OK) WS_CUDA(ws, cudaGetLastError());
+  return rc;
+}
+
+// The plan in use: out[0..4] = BZ, BY, taps per group (or per pass), CTAs, M tiles
+// (0 for the weight gradient). kind 0 forward, 1 data gradient, 2 weight gradient.
+extern "C" int gc_ws_plan_info(const gc_ws *ws, int layer, int kind, int *out) {
+  if (!ws || !out || layer < 0 || layer >= WS_NL || kind < 0 || kind > 2) return GC_ERR_ARG;
+  if (kind == 2) {
+    const WgPlan &p = ws->pw[layer];
+    out[0] = p.BZ; out[1] = p.BY; out[2] = p.tpp; out[3] = p.grid; out[4] = 0;
+  } else {
+    const FwdPlan &p = kind == 0 ? ws->pf[layer] : ws->pb[layer];
+    out[0] = p.BZ; out[1] = p.BY; out[2] = p.tpg; out[3] = p.grid; out[4] = p.n_mt;
+  }
   return GC_OK;
 }
 

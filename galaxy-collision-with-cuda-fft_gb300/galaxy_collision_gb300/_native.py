@@ -24,6 +24,7 @@ GC_ERR_STATE = -6
 GC_FLAG_NONFINITE_POS = 0x1
 GC_FLAG_NONFINITE_RHO = 0x2
 GC_MG_FUSED_SWEEP = 0x1
+GC_MG_FIXED_CYCLES = 0x2
 GC_STEP_GRAD_GRID = 0x1
 
 GC_WS_PLAIN = 0
@@ -122,6 +123,7 @@ _PROTOS = {
     "gc_pm_step": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(StepParams), C.POINTER(StepStats)]),
     "gc_pm_potential": (_vp, [_ctxp]),
     "gc_pm_copy_potential": (C.c_int, [_ctxp, _vp]),
+    "gc_pm_last_residual": (C.c_int, [_ctxp, C.POINTER(C.c_double)]),
     "gc_profile_enable": (C.c_int, [_ctxp, C.c_int]),
     "gc_profile_reset": (C.c_int, [_ctxp]),
     "gc_profile_read": (C.c_int, [_ctxp, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
@@ -143,6 +145,8 @@ _PROTOS = {
     "gc_ws_backward": (C.c_int, [_vp, _vp, _vp]),
     "gc_ws_adam": (C.c_int, [_vp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int]),
     "gc_ws_status": (C.c_int, [_vp, C.POINTER(C.c_uint32), C.c_int]),
+    "gc_ws_autotune": (C.c_int, [_vp, C.c_int, _vp]),
+    "gc_ws_plan_info": (C.c_int, [_vp, C.c_int, C.c_int, _vp]),
     "gc_pm_set_warmstart": (C.c_int, [_ctxp, _vp, C.c_int, C.c_int]),
     "gc_pm_record_sample": (C.c_int, [_ctxp, _vp]),
 }

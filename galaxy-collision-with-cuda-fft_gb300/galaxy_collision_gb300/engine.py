@@ -40,7 +40,7 @@ class StepResult:
 class PMEngine:
     def __init__(self, grid_size: int, dx: float, grav: float = 1.0, *, origin=(0.0, 0.0, 0.0), tol: float = 1e-6,
                  max_cycles: int = 50, pre_sweeps: int = 2, post_sweeps: int = 2, coarse_sweeps: int = 40,
-                 fixed_point_bits: int = 52, sort_every: int = 20, grad_grid: bool = True):
+                 fixed_point_bits: int = 52, sort_every: int = 20, grad_grid: bool = True, fixed_cycles: int = 0):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
         self.grav = float(grav)
@@ -53,6 +53,14 @@ class PMEngine:
         self.mg.max_cycles = int(max_cycles)
         self.mg.min_cycles = 1
         self.mg.tol = float(tol)
+        # fixed_cycles > 0: exactly that many V-cycles per solve and no host read in
+        # the step (the residual stays on the device, see last_residual), which is
+        # what lets a step be captured as a CUDA graph
+        self.fixed_cycles = int(fixed_cycles)
+        if self.fixed_cycles > 0:
+            self.mg.flags |= _native.GC_MG_FIXED_CYCLES
+            self.mg.max_cycles = self.fixed_cycles
+            self.mg.min_cycles = self.fixed_cycles
         self.fixed_point_bits = int(fixed_point_bits)
         self.sort_every = int(sort_every)
         self.grad_grid = bool(grad_grid)  # gather from a float4 -grad(phi) grid (same results)
@@ -62,6 +70,7 @@ class PMEngine:
         self.cur = None
         self.alt = None
         self.last = None
+        self._graphs = {}
 
     # -- state ------------------------------------------------------------------
     def _alloc(self, n: int):
@@ -125,8 +134,11 @@ class PMEngine:
         st = _native.StepStats()
         p = self._struct(self.cur)
         self.ctx.call("gc_pm_step", C.byref(p), C.byref(sp), C.byref(st), what="gc_pm_step")
-        rel = st.mg.res_norm / st.mg.rhs_norm if st.mg.rhs_norm > 0 else 0.0
-        res = StepResult(int(st.mg.cycles), bool(st.mg.converged), float(rel))
+        if self.fixed_cycles > 0:
+            res = StepResult(int(st.mg.cycles), False, float("nan"))
+        else:
+            rel = st.mg.res_norm / st.mg.rhs_norm if st.mg.rhs_norm > 0 else 0.0
+            res = StepResult(int(st.mg.cycles), bool(st.mg.converged), float(rel))
         if diagnostics:
             res.diag = np.array(st.diag[:], dtype=np.float64)
             res.grid_pe_raw = float(st.grid_pe_raw)
@@ -162,6 +174,40 @@ class PMEngine:
         r = self._step(_native.GC_STEP_CLOSE, dt, diagnostics)
         self.state = "synced"
         return r
+
+    def last_residual(self) -> float:
+        """Relative residual of the last solve (reads the device; synchronises)."""
+        r = C.c_double()
+        self.ctx.call("gc_pm_last_residual", C.byref(r), what="last_residual")
+        return float(r.value)
+
+    # -- CUDA graphs ------------------------------------------------------------
+    def step_kernels(self, dt: float) -> None:
+        """Launch one ADVANCE step without any host synchronisation (needs
+        fixed_cycles > 0). Used to capture the step into a CUDA graph; the host-side
+        state does not advance, see advance_graph."""
+        if self.fixed_cycles <= 0:
+            raise RuntimeError("graph capture needs fixed_cycles > 0 (no host reads inside the step)")
+        self._step(_native.GC_STEP_ADVANCE, dt, False)
+
+    def advance_graph(self, dt: float) -> None:
+        """advance() through a CUDA graph of the whole step, captured on first use
+        for each particle-buffer parity (the sort, between graphs, swaps them). The
+        engine must be open with a complete warm-start history (3 steps)."""
+        if self.state != "open":
+            raise RuntimeError("advance_graph needs an open (primed) engine")
+        if self.sort_every > 0 and self.steps_since_sort >= self.sort_every:
+            self.sort()
+        key = (self.cur["x"].data_ptr(), float(dt))
+        g = self._graphs.get(key)
+        if g is None:
+            g = torch.cuda.CUDAGraph()
+            torch.cuda.synchronize()
+            with torch.cuda.graph(g):
+                self.step_kernels(dt)
+            self._graphs[key] = g
+        g.replay()
+        self.steps_since_sort += 1
 
     def run(self, steps: int, dt: float) -> None:
         """Advance ``steps`` KDK steps from a synchronised state and end synchronised."""

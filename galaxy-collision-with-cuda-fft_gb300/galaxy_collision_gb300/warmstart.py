@@ -154,6 +154,26 @@ class WarmStartNet:
         self.step += 1
         self._call("gc_ws_adam", C.c_float(lr), C.c_float(beta1), C.c_float(beta2), C.c_float(eps), int(self.step))
 
+    def autotune(self, iters: int = 3) -> np.ndarray:
+        """Time every feasible tile plan of each layer's three passes and keep the
+        fastest (activations are overwritten). Returns the best milliseconds,
+        shape (layers, 3): forward, data gradient, weight gradient."""
+        ms = (C.c_float * (3 * N_LAYERS))()
+        self._call("gc_ws_autotune", int(iters), C.cast(ms, C.c_void_p))
+        return np.array(ms[:], dtype=np.float64).reshape(N_LAYERS, 3)
+
+    def plans(self) -> list[list[tuple[int, ...]]]:
+        """Plan per layer and pass: (planes, lines, taps per group/pass, CTAs, M tiles)."""
+        out = []
+        for layer in range(N_LAYERS):
+            row = []
+            for kind in range(3):
+                v = (C.c_int * 5)()
+                st = self._lib.gc_ws_plan_info(self._h, layer, kind, C.cast(v, C.c_void_p))
+                row.append(tuple(v[:]) if st == _native.GC_OK else None)
+            out.append(row)
+        return out
+
     def status(self, clear: bool = True) -> int:
         f = C.c_uint32()
         self._call("gc_ws_status", C.byref(f), int(clear))
@@ -174,3 +194,51 @@ class WarmStartNet:
 
 
 __all__ = ["WarmStartNet", "init_params", "layer_table", "param_slices", "WEIGHTS_PATH", "N_FEATURES"]
+
+
+def _main(argv=None):
+    """Time the network at R: forward, and forward + backward + Adam (random
+    inputs and parameters); ``--iters 2`` is the small case profiled with ncu."""
+    import argparse
+
+    ap = argparse.ArgumentParser(description="time the warm-start network")
+    ap.add_argument("--R", type=int, default=128)
+    ap.add_argument("--iters", type=int, default=10)
+    ap.add_argument("--autotune", action="store_true")
+    args = ap.parse_args(argv)
+    from galaxy_collision_gb300 import _build
+
+    _build.build()
+    R = args.R
+    net = WarmStartNet(R, seed=1)
+    if args.autotune:
+        net.autotune()
+    g = torch.Generator(device="cuda").manual_seed(0)
+    feat = torch.randn((N_FEATURES, R, R, R), device="cuda", generator=g).half()
+    tgt = (0.1 * torch.randn((R, R, R), device="cuda", generator=g)).half()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    net.forward(feat)
+    net.backward(tgt)
+    net.adam_step(1e-3)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.iters):
+        net.forward(feat)
+    e1.record()
+    torch.cuda.synchronize()
+    fwd = e0.elapsed_time(e1) / args.iters
+    e0.record()
+    for _ in range(args.iters):
+        net.forward(feat)
+        net.backward(tgt)
+        net.adam_step(1e-3)
+    e1.record()
+    torch.cuda.synchronize()
+    train = e0.elapsed_time(e1) / args.iters
+    if net.status() != 0:
+        raise RuntimeError("tensor-core completion timed out")
+    print(f"R={R} forward {fwd:.3f} ms, forward+backward+Adam {train:.3f} ms", flush=True)
+
+
+if __name__ == "__main__":
+    _main()

@@ -51,6 +51,11 @@ enum gc_status_code {
  * prolongation folded into the first post-sweep) instead of the in-place
  * red and black half-sweep kernels. Identical results. */
 #define GC_MG_FUSED_SWEEP 0x1
+/* gc_mg_params.flags: run exactly max_cycles V-cycles without reading the
+ * residual norm on the host (it is left on the device; gc_pm_last_residual
+ * reads it). The engine's step then makes no host synchronisation, so it can be
+ * captured in a CUDA graph. Stats report converged = -1 and NaN norms. */
+#define GC_MG_FIXED_CYCLES 0x2
 
 typedef struct gc_ctx gc_ctx;
 
@@ -258,6 +263,8 @@ int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp, gc_
 const float *gc_pm_potential(const gc_ctx *ctx);
 /* Stream-ordered copy of the current finest-level potential into phi (G^3 f32). */
 int gc_pm_copy_potential(gc_ctx *ctx, float *phi);
+/* Relative residual ||r||/||4 pi G rho|| of the engine's last solve (synchronises). */
+int gc_pm_last_residual(gc_ctx *ctx, double *rel);
 
 /* ---- instrumentation (no kernel counterpart in the reference: it replaces the
  * sync-bracketed per-stage wall clock of bench.py:66-73, 176-186) ---------- */
@@ -311,6 +318,15 @@ int gc_ws_backward(gc_ws *ws, const void *target, float *loss_out);
 int gc_ws_adam(gc_ws *ws, float lr, float beta1, float beta2, float eps, int step);
 /* Device status bits (bit 0: a tensor-core completion wait timed out); clear resets them. */
 int gc_ws_status(gc_ws *ws, unsigned *flags, int clear);
+/* Autotuner: time every feasible tile plan (block of output planes x lines,
+ * taps per weight group) of each layer's forward, data-gradient and weight-
+ * gradient kernels with CUDA events over `iters` launches and keep the fastest.
+ * Overwrites activations. ms_out (host, nullable, 33 floats): best milliseconds
+ * per [layer][pass]. Synchronises the stream. */
+int gc_ws_autotune(gc_ws *ws, int iters, float *ms_out);
+/* Plan in use for (layer, pass 0/1/2): out[5] = {planes, lines, taps per group or
+ * pass, CTAs, M tiles per CTA (0 for the weight gradient)}. */
+int gc_ws_plan_info(const gc_ws *ws, int layer, int kind, int *out);
 
 /* Initial guess of the engine's solve (gc_pm_step with warm_start != 0):
  *   GC_WS_PLAIN       phi(n-1), the previous potential (the reference's warm start);

@@ -92,6 +92,29 @@ def test_backward_matches_oracle(cuda):
         assert cos > 0.998, f"layer {i} weights: cosine {cos}"
 
 
+def test_autotuned_plans_keep_the_results(cuda):
+    """The autotuner only changes tile shapes: forward and gradient still match
+    the oracle after it has picked the fastest plans."""
+    from galaxy_collision_gb300.warmstart import WarmStartNet
+
+    R = 32
+    p = _rand_params(8)
+    feat = _feat(R, 9)
+    target = (0.1 * np.random.default_rng(10).normal(size=(R, R, R))).astype(np.float16)
+    net = WarmStartNet(R, params=p)
+    ms = net.autotune(iters=2)
+    assert ms.shape == (11, 3) and np.all(ms[:, 0] > 0) and np.all(ms[:, 2] > 0)
+    assert all(len(row) == 3 for row in net.plans())
+    y = net.forward(torch.from_numpy(feat).cuda()).cpu().numpy()
+    net.backward(torch.from_numpy(target).cuda())
+    g = net.grads().cpu().numpy()
+    assert net.status() == 0
+    yo, cache = ows.forward(p, feat, emulate=True)
+    _, go = ows.backward(cache, target.astype(np.float64), emulate=True)
+    assert rel_l2(y, yo) < 1e-2
+    assert rel_l2(g, go) < 2e-2
+
+
 def test_adam_fits_a_fixed_target(cuda):
     """A smooth target that depends on the inputs: 80 Adam steps on one sample."""
     from galaxy_collision_gb300.warmstart import WarmStartNet
