@@ -229,31 +229,50 @@ __device__ __forceinline__ bool dep_cell(float px, float py, float pz, const Dep
 // Runs of equal cells. A run carries the linear index of its (ix, iy, iz) node
 // and whether all 8 corners are inside the grid, so adding it to the grid is 8
 // fire-and-forget atomics with constant offsets (no key decoding, no call).
+// A run of equal cells: its cell, and the int32 sums of its particles' small
+// contributions (each below 2^22 quanta, at most DEP_SEQ particles: < 2^25).
+// Particles with a larger contribution never enter a run; they are added to the
+// grid directly.
 struct DepRun {
   unsigned key;   // cell key, DEP_NONE when empty
-  int base;       // (ix*G + iy)*G + iz (G^3 < 2^31)
   int ix, iy, iz;
-  bool small;     // every contribution summed here was below 2^22 quanta
-  long long q[8];
+  int q[8];
 };
 
-__device__ __forceinline__ void run_to_grid(long long *__restrict__ qg, int G, const DepRun &r,
-                                            const long long (&q)[8]) {
-  const bool interior = r.ix >= 0 && r.iy >= 0 && r.iz >= 0 && r.ix + 1 < G && r.iy + 1 < G && r.iz + 1 < G;
+// Add 8 corner values to the int64 grid, dropping corners outside it.
+__device__ __forceinline__ void corners_to_grid(long long *__restrict__ qg, int G, int ix, int iy, int iz,
+                                                const long long (&q)[8]) {
+  const bool interior = ix >= 0 && iy >= 0 && iz >= 0 && ix + 1 < G && iy + 1 < G && iz + 1 < G;
   if (interior) {
+    const int base = (ix * G + iy) * G + iz;  // G^3 < 2^31
 #pragma unroll
     for (int c = 0; c < 8; ++c)
       if (q[c] != 0)
-        atomicAdd((unsigned long long *)(qg + r.base + ((c >> 2) * G + ((c >> 1) & 1)) * G + (c & 1)),
+        atomicAdd((unsigned long long *)(qg + base + ((c >> 2) * G + ((c >> 1) & 1)) * G + (c & 1)),
                   (unsigned long long)q[c]);
   } else {
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-      const int jx = r.ix + (c >> 2), jy = r.iy + ((c >> 1) & 1), jz = r.iz + (c & 1);
+      const int jx = ix + (c >> 2), jy = iy + ((c >> 1) & 1), jz = iz + (c & 1);
       if (q[c] != 0 && (unsigned)jx < (unsigned)G && (unsigned)jy < (unsigned)G && (unsigned)jz < (unsigned)G)
         atomicAdd((unsigned long long *)(qg + ((size_t)jx * G + jy) * G + jz), (unsigned long long)q[c]);
     }
   }
+}
+
+// A particle whose contribution exceeds 2^22 quanta (rare: point masses) goes
+// to the grid on its own, out of line.
+__device__ __noinline__ void large_to_grid(long long *__restrict__ qg, int G, int ix, int iy, int iz, float mm,
+                                           float fx, float fy, float fz, float qscale) {
+  long long q[8];
+  cic_q_large(mm, fx, fy, fz, qscale, q);
+  corners_to_grid(qg, G, ix, iy, iz, q);
+}
+
+__device__ __noinline__ void run_to_grid(long long *__restrict__ qg, int G, int ix, int iy, int iz, int q0, int q1,
+                                         int q2, int q3, int q4, int q5, int q6, int q7) {
+  const long long q[8] = {q0, q1, q2, q3, q4, q5, q6, q7};
+  corners_to_grid(qg, G, ix, iy, iz, q);
 }
 
 // Where finished runs go: the int64 grid, or (box != null) an int32 box of nodes
@@ -266,28 +285,26 @@ struct DepOut {
   int x0, y0, z0, ny, nz, G;
 };
 
-__device__ __forceinline__ void run_out(const DepOut &o, const DepRun &r, const long long (&q)[8]) {
+__device__ __forceinline__ void run_out(const DepOut &o, const DepRun &r, const int (&q)[8]) {
   if (o.box) {
     const int bi = ((r.ix - o.x0) * o.ny + (r.iy - o.y0)) * o.nz + (r.iz - o.z0);
 #pragma unroll
     for (int c = 0; c < 8; ++c)
-      if (q[c] != 0) atomicAdd(o.box + bi + ((c >> 2) * o.ny + ((c >> 1) & 1)) * o.nz + (c & 1), (int)q[c]);
+      if (q[c] != 0) atomicAdd(o.box + bi + ((c >> 2) * o.ny + ((c >> 1) & 1)) * o.nz + (c & 1), q[c]);
   } else {
-    run_to_grid(o.qg, o.G, r, q);
+    run_to_grid(o.qg, o.G, r.ix, r.iy, r.iz, q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7]);
   }
 }
 
 // Lanes whose run is the same cell (__match_any_sync) reduce it with redux.sync
-// and one of them adds it; runs with a large contribution are added per lane.
+// (a group's sums stay below 32 * 2^25 = 2^30) and one of them adds it.
 __device__ __forceinline__ void dep_merge(const DepRun &r, const DepOut &o, int lane) {
   const unsigned peers = __match_any_sync(0xffffffffu, r.key);
-  const unsigned large = __ballot_sync(0xffffffffu, !r.small);
   if (r.key == DEP_NONE) return;
-  if ((large & peers) == 0 && __popc(peers) > 1) {
-    // each lane's sums are below DEP_SEQ * 2^22, a group's below 2^30
-    long long tot[8];
+  if (__popc(peers) > 1) {
+    int tot[8];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) tot[t] = (long long)__reduce_add_sync(peers, (int)r.q[t]);
+    for (int t = 0; t < 8; ++t) tot[t] = __reduce_add_sync(peers, r.q[t]);
     if (lane == __ffs(peers) - 1) run_out(o, r, tot);
   } else {
     run_out(o, r, r.q);
@@ -300,7 +317,7 @@ __device__ __forceinline__ void dep_merge(const DepRun &r, const DepOut &o, int 
 // rolled loop with a two-run cache (particles that drifted into a neighbour
 // cell since the last sort do not break the run of the cell they are
 // interleaved with), and the warp merges the cached runs at the end. A first
-// pass finds the box of cells the tile touches and the tile's largest
+// pass finds the box of cells the tile touches and its largest small
 // contribution: when the box's nodes fit DEP_BOX_CAP and the tile's total stays
 // below 2^30 quanta per node, runs are added to an int32 box in shared memory
 // and the box is added to the grid with one int64 atomic per nonzero node, so
@@ -348,7 +365,7 @@ __global__ void __launch_bounds__(256, 3)
     __syncthreads();
     const int i0 = tid * DEP_SEQ;
     const int cnt = cnt_tile - i0 < 0 ? 0 : (cnt_tile - i0 > DEP_SEQ ? DEP_SEQ : cnt_tile - i0);
-    // box of the cells that receive mass and the largest |m/dx^3| in quanta
+    // box of the cells that receive mass and the largest small |m/dx^3| in quanta
     int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {-0x7fffffff, -0x7fffffff, -0x7fffffff};
     float mq = 0.0f;
 #pragma unroll 1
@@ -360,7 +377,7 @@ __global__ void __launch_bounds__(256, 3)
         lo[0] = min(lo[0], ix); lo[1] = min(lo[1], iy); lo[2] = min(lo[2], iz);
         hi[0] = max(hi[0], ix); hi[1] = max(hi[1], iy); hi[2] = max(hi[2], iz);
         const float a = __fmul_rn(fabsf(__fmul_rn(sm_[i], d.inv_vol)), qscale);
-        mq = (a > mq || a != a) ? (a == a ? a : 3.0e38f) : mq;
+        if (a < 4194304.0f) mq = fmaxf(mq, a);  // large ones bypass the box (NaN fails the test)
       }
     }
 #pragma unroll
@@ -382,7 +399,7 @@ __global__ void __launch_bounds__(256, 3)
     o.x0 = bnd[0]; o.y0 = bnd[1]; o.z0 = bnd[2];
     const int nx = bnd[3] - bnd[0] + 2, ny = bnd[4] - bnd[1] + 2, nz = bnd[5] - bnd[2] + 2;
     o.ny = ny; o.nz = nz;
-    // every contribution is at most (largest |m/dx^3| in quanta) + 1/2 after rounding
+    // every small contribution is at most (largest small |m/dx^3| in quanta) + 1/2
     const float tile_q = __fmul_rn(__uint_as_float((unsigned)bnd[6]) + 1.0f, (float)cnt_tile);
     const bool use_box = bnd[3] >= bnd[0] && (long long)nx * ny * nz <= DEP_BOX_CAP && tile_q < 1073741824.0f;
     const int vol = use_box ? nx * ny * nz : 0;
@@ -393,8 +410,7 @@ __global__ void __launch_bounds__(256, 3)
     }
     DepRun r0, r1;
     r0.key = r1.key = DEP_NONE;
-    r0.small = r1.small = true;
-    r0.base = r1.base = r0.ix = r0.iy = r0.iz = r1.ix = r1.iy = r1.iz = 0;
+    r0.ix = r0.iy = r0.iz = r1.ix = r1.iy = r1.iz = 0;
 #pragma unroll
     for (int t = 0; t < 8; ++t) r0.q[t] = r1.q[t] = 0;
 #pragma unroll 1
@@ -406,39 +422,34 @@ __global__ void __launch_bounds__(256, 3)
       float fx, fy, fz;
       if (!dep_cell<POW2>(px, py, pz, d, inv_dx, ix, iy, iz, fx, fy, fz)) continue;
       const float mm = __fmul_rn(sm_[i], d.inv_vol);
-      const bool small = __fmul_rn(fabsf(mm), qscale) < 4194304.0f;  // every |w| <= |mm| < 2^22 quanta
-      long long q[8];
-      if (small) {
-        const float wx0 = __fsub_rn(1.0f, fx), wy0 = __fsub_rn(1.0f, fy), wz0 = __fsub_rn(1.0f, fz);
-        const float a0 = __fmul_rn(mm, wx0), a1 = __fmul_rn(mm, fx);
-        const float b00 = __fmul_rn(a0, wy0), b01 = __fmul_rn(a0, fy), b10 = __fmul_rn(a1, wy0), b11 = __fmul_rn(a1, fy);
-        q[0] = rne_small(__fmul_rn(__fmul_rn(b00, wz0), qscale));
-        q[1] = rne_small(__fmul_rn(__fmul_rn(b00, fz), qscale));
-        q[2] = rne_small(__fmul_rn(__fmul_rn(b01, wz0), qscale));
-        q[3] = rne_small(__fmul_rn(__fmul_rn(b01, fz), qscale));
-        q[4] = rne_small(__fmul_rn(__fmul_rn(b10, wz0), qscale));
-        q[5] = rne_small(__fmul_rn(__fmul_rn(b10, fz), qscale));
-        q[6] = rne_small(__fmul_rn(__fmul_rn(b11, wz0), qscale));
-        q[7] = rne_small(__fmul_rn(__fmul_rn(b11, fz), qscale));
-      } else {
-        cic_q_large(mm, fx, fy, fz, qscale, q);
+      if (!(__fmul_rn(fabsf(mm), qscale) < 4194304.0f)) {  // large (or NaN): straight to the grid
+        large_to_grid(qg, d.G, ix, iy, iz, mm, fx, fy, fz, qscale);
+        continue;
       }
+      const float wx0 = __fsub_rn(1.0f, fx), wy0 = __fsub_rn(1.0f, fy), wz0 = __fsub_rn(1.0f, fz);
+      const float a0 = __fmul_rn(mm, wx0), a1 = __fmul_rn(mm, fx);
+      const float b00 = __fmul_rn(a0, wy0), b01 = __fmul_rn(a0, fy), b10 = __fmul_rn(a1, wy0), b11 = __fmul_rn(a1, fy);
+      int q[8];
+      q[0] = rne_small(__fmul_rn(__fmul_rn(b00, wz0), qscale));
+      q[1] = rne_small(__fmul_rn(__fmul_rn(b00, fz), qscale));
+      q[2] = rne_small(__fmul_rn(__fmul_rn(b01, wz0), qscale));
+      q[3] = rne_small(__fmul_rn(__fmul_rn(b01, fz), qscale));
+      q[4] = rne_small(__fmul_rn(__fmul_rn(b10, wz0), qscale));
+      q[5] = rne_small(__fmul_rn(__fmul_rn(b10, fz), qscale));
+      q[6] = rne_small(__fmul_rn(__fmul_rn(b11, wz0), qscale));
+      q[7] = rne_small(__fmul_rn(__fmul_rn(b11, fz), qscale));
       const unsigned key = (unsigned)(((ix + 1) * (d.G + 1) + (iy + 1)) * (d.G + 1) + (iz + 1));
       if (key == r0.key) {
-        r0.small = r0.small && small;
 #pragma unroll
         for (int t = 0; t < 8; ++t) r0.q[t] += q[t];
       } else if (key == r1.key) {
-        r1.small = r1.small && small;
 #pragma unroll
         for (int t = 0; t < 8; ++t) r1.q[t] += q[t];
       } else {  // evict run 1, demote run 0, start a new run 0
         if (r1.key != DEP_NONE) run_out(o, r1, r1.q);
         r1 = r0;
         r0.key = key;
-        r0.base = (ix * d.G + iy) * d.G + iz;
         r0.ix = ix; r0.iy = iy; r0.iz = iz;
-        r0.small = small;
 #pragma unroll
         for (int t = 0; t < 8; ++t) r0.q[t] = q[t];
       }

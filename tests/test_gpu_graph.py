@@ -60,10 +60,9 @@ def test_ensemble_graph_advances_every_run(cuda):
     from galaxy_collision_gb300 import ensemble
 
     ens = ensemble.Ensemble(n_runs=3, seed=11)
-    # small members keep the test short: shrink to the first three members' sizes
     assert len(ens.engines) == 3
     x0 = [e.cur["x"].clone() for e in ens.engines]
-    ens.prime()
+    ens.prime()  # first steps adaptive, then the graph
     for _ in range(5):
         ens.step()
     torch.cuda.synchronize()
