@@ -365,19 +365,35 @@ __global__ void __launch_bounds__(256, 3)
     __syncthreads();
     const int i0 = tid * DEP_SEQ;
     const int cnt = cnt_tile - i0 < 0 ? 0 : (cnt_tile - i0 > DEP_SEQ ? DEP_SEQ : cnt_tile - i0);
-    // box of the cells that receive mass and the largest small |m/dx^3| in quanta
-    int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {-0x7fffffff, -0x7fffffff, -0x7fffffff};
-    float mq = 0.0f;
+    // box of the cells that can receive mass: x/dx is monotone in x, so the
+    // cells of the tile's coordinate range (clamped to the grid range; NaN is
+    // ignored by fmin/fmax) bound every particle's cell. Also the largest small
+    // |m| (|m/dx^3| in quanta below 2^22 enter runs).
+    float xl = 3.0e38f, yl = 3.0e38f, zl = 3.0e38f, xh = -3.0e38f, yh = -3.0e38f, zh = -3.0e38f, ma = 0.0f;
+    const float lim = __fmul_rn(4194304.0f, 1.0f / qscale);  // |m/dx^3| below this is small
 #pragma unroll 1
     for (int j = 0; j < cnt; ++j) {
       const int i = DEP_PAD(i0 + j);
-      int ix, iy, iz;
-      float fx, fy, fz;
-      if (dep_cell<POW2>(sx[i], sy[i], sz[i], d, inv_dx, ix, iy, iz, fx, fy, fz)) {
-        lo[0] = min(lo[0], ix); lo[1] = min(lo[1], iy); lo[2] = min(lo[2], iz);
-        hi[0] = max(hi[0], ix); hi[1] = max(hi[1], iy); hi[2] = max(hi[2], iz);
-        const float a = __fmul_rn(fabsf(__fmul_rn(sm_[i], d.inv_vol)), qscale);
-        if (a < 4194304.0f) mq = fmaxf(mq, a);  // large ones bypass the box (NaN fails the test)
+      const float px = sx[i], py = sy[i], pz = sz[i];
+      xl = fminf(xl, px); xh = fmaxf(xh, px);
+      yl = fminf(yl, py); yh = fmaxf(yh, py);
+      zl = fminf(zl, pz); zh = fmaxf(zh, pz);
+      const float a = fabsf(__fmul_rn(sm_[i], d.inv_vol));
+      if (a < lim) ma = fmaxf(ma, a);
+    }
+    int lo[3], hi[3];
+    {
+      const float gl = -1.0f, gh = (float)d.G - 1.0f;  // cells -1 .. G-1 receive mass
+      const float cl[3] = {xl, yl, zl}, ch[3] = {xh, yh, zh};
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        float l = POW2 ? __fmul_rn(cl[a], inv_dx) : __fdiv_rn(cl[a], d.dx);
+        float h = POW2 ? __fmul_rn(ch[a], inv_dx) : __fdiv_rn(ch[a], d.dx);
+        l = fminf(fmaxf(floorf(l), gl), gh);
+        h = fminf(fmaxf(floorf(h), gl), gh);
+        const bool any_pt = cl[a] <= ch[a];
+        lo[a] = any_pt ? (int)l : 0x7fffffff;
+        hi[a] = any_pt ? (int)h : -0x7fffffff;
       }
     }
 #pragma unroll
@@ -385,7 +401,7 @@ __global__ void __launch_bounds__(256, 3)
       lo[a] = __reduce_min_sync(0xffffffffu, lo[a]);
       hi[a] = __reduce_max_sync(0xffffffffu, hi[a]);
     }
-    const unsigned mqb = __reduce_max_sync(0xffffffffu, __float_as_uint(mq));  // non-negative floats order as ints
+    const unsigned mqb = __reduce_max_sync(0xffffffffu, __float_as_uint(__fmul_rn(ma, qscale)));
     if (lane == 0) {
 #pragma unroll
       for (int a = 0; a < 3; ++a) { atomicMin(&bnd[a], lo[a]); atomicMax(&bnd[3 + a], hi[a]); }
