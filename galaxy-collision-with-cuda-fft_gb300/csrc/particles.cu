@@ -968,8 +968,16 @@ __global__ void __launch_bounds__(256)
   double dv[11];
 #pragma unroll
   for (int t = 0; t < 11; ++t) dv[t] = 0.0;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
-    const float px = x[p], py = y[p], pz = z[p], ux = vx[p], uy = vy[p], uz = vz[p];
+  // software pipelined: the next particle's state is loaded before this one's
+  // corner gather, so its DRAM latency overlaps the gather's L2 latency
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  float nx = 0.0f, ny = 0.0f, nz = 0.0f, nvx = 0.0f, nvy = 0.0f, nvz = 0.0f;
+  if (p < n) { nx = x[p]; ny = y[p]; nz = z[p]; nvx = vx[p]; nvy = vy[p]; nvz = vz[p]; }
+  for (; p < n; p += stride) {
+    const float px = nx, py = ny, pz = nz, ux = nvx, uy = nvy, uz = nvz;
+    const long long q = p + stride;
+    if (q < n) { nx = x[q]; ny = y[q]; nz = z[q]; nvx = vx[q]; nvy = vy[q]; nvz = vz[q]; }
     float ax, ay, az;
     gather_g4<POW2>(g4, px, py, pz, f, ax, ay, az);
     kd_update<DIAG>(p, px, py, pz, ux, uy, uz, ax, ay, az, x, y, z, vx, vy, vz, m, f, dv);
