@@ -65,7 +65,8 @@ ALGO_BYTES = {
 def _parse(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40,
+                    help="timed steps (default: two cell-sort periods, so the sorts are inside the timed region)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--config", default="two_disk_100M")
@@ -107,7 +108,7 @@ def _log(args, *msg):
 
 # ---------------------------------------------------------------------------- clocks
 class ClockSampler:
-    """nvidia-smi samples (200 ms) of SM clock and throttle reasons during the timed region."""
+    """nvidia-smi samples (50 ms) of SM clock and throttle reasons during the timed region."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -123,7 +124,7 @@ class ClockSampler:
         os.close(fd)
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
@@ -301,6 +302,10 @@ def run_ours(args):
     eng = make_engine()
     eng.load(icr.pos, icr.vel, icr.mass, icr.gid, sort=True)
     eng.prime(dt)
+    # the sampler starts before the warm-up steps so that it samples the loaded GPU
+    # from the first timed step on
+    sampler = ClockSampler(local)
+    sampler.start()
     for _ in range(args.warmup):
         eng.advance(dt)
     torch.cuda.synchronize()
@@ -308,8 +313,6 @@ def run_ours(args):
         torch.distributed.barrier()
 
     counts0 = {k: v[0] for k, v in eng.ctx.kernel_stats().items()}
-    sampler = ClockSampler(local)
-    sampler.start()
     stream = torch.cuda.current_stream()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()

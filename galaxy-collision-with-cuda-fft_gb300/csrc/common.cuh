@@ -111,6 +111,7 @@ struct gc_ctx {
   int ws_hist;          // solves recorded in the history (0, 1, 2+)
   void *ws_record;      // one-shot f16 [5][R^3] sample destination
   int ws_skip;          // this step leaves the history alone (PRIME after CLOSE)
+  int pending_push;     // a SOLVE_ONLY step awaits its PUSH_ONLY step
   float *ws_buf;        // rho_c, phi_c, delta_c, y (R^3 each) + scalars + partials
   size_t ws_buf_cap;
 

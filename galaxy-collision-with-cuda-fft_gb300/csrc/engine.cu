@@ -13,24 +13,10 @@
 
 #include <math.h>
 
-extern "C" int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp, gc_step_stats *st) {
-  if (!ctx) return GC_ERR_ARG;
-  GC_REQUIRE(ctx, p && sp, "gc_pm_step: NULL argument");
-  GC_REQUIRE(ctx, p->n >= 0 && p->n < (1LL << 31), "particle count out of range");
-  GC_REQUIRE(ctx, p->n == 0 || (p->x && p->y && p->z && p->vx && p->vy && p->vz && p->m),
-             "gc_pm_step: particle arrays required");
-  GC_REQUIRE(ctx, sp->mode >= GC_STEP_PRIME && sp->mode <= GC_STEP_CLOSE, "gc_pm_step: bad mode %d", sp->mode);
-  GC_REQUIRE(ctx, sp->dt == sp->dt, "gc_pm_step: dt must be finite");
-  GC_REQUIRE(ctx, sp->fixed_point_bits >= 24 && sp->fixed_point_bits <= gc_max_fixed_point_bits(ctx),
-             "fixed_point_bits must be in [24, %d] for a %d^3 grid", gc_max_fixed_point_bits(ctx), ctx->G);
-  if (sp->mode != GC_STEP_PRIME && !ctx->last_step_valid) {
-    gc_set_error(ctx, "gc_pm_step: ADVANCE/CLOSE before PRIME");
-    return GC_ERR_STATE;
-  }
-  int s = gc_mg_check_params(ctx, &sp->mg);
-  if (s) return s;
+// Phases 1-3: deposit, b0 + moments, initial guess, faces and V-cycles.
+static int pm_solve(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp, gc_mg_stats *mst) {
+  int s;
   const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
-
   // 1. deposit (the quantum is fixed at PRIME: the masses do not change)
   if (sp->mode == GC_STEP_PRIME) {
     if ((s = gc_fixed_point_setup(ctx, p->m, p->n, sp->fixed_point_bits, GC_S_MASS_PM, GC_S_QEXP_PM))) return s;
@@ -47,10 +33,14 @@ extern "C" int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_para
   // learned / extrapolated correction of the previous potential, sample recording
   if ((s = gc_ws_pre_solve(ctx, warm, sp->mode))) return s;
   if ((s = gc_faces_from_moments(ctx))) return s;
-  gc_mg_stats mst;
-  if ((s = gc_mg_run(ctx, &sp->mg, &mst))) return s;
-  if ((s = gc_ws_post_solve(ctx))) return s;
-  // 4. particle pass
+  return gc_mg_run(ctx, &sp->mg, mst);
+}
+
+// Phase 4: the particle pass, diagnostics, state and stats.
+static int pm_push(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp, const gc_mg_stats &mst,
+                   gc_step_stats *st) {
+  int s;
+  const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
   int nparts = 0;
   if ((s = gc_gather_kick_drift(ctx, p, sp->dt, sp->mode, sp->diagnostics, (sp->flags & GC_STEP_GRAD_GRID) != 0,
                                 nullptr, nullptr, nullptr, &nparts)))
@@ -73,6 +63,77 @@ extern "C" int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_para
       st->grid_pe_raw = bfac != 0.0 ? h[11] / bfac : 0.0;
     }
   }
+  return GC_OK;
+}
+
+extern "C" int gc_pm_step(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp, gc_step_stats *st) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, p && sp, "gc_pm_step: NULL argument");
+  GC_REQUIRE(ctx, p->n >= 0 && p->n < (1LL << 31), "particle count out of range");
+  GC_REQUIRE(ctx, p->n == 0 || (p->x && p->y && p->z && p->vx && p->vy && p->vz && p->m),
+             "gc_pm_step: particle arrays required");
+  GC_REQUIRE(ctx, sp->mode >= GC_STEP_PRIME && sp->mode <= GC_STEP_CLOSE, "gc_pm_step: bad mode %d", sp->mode);
+  GC_REQUIRE(ctx, sp->dt == sp->dt, "gc_pm_step: dt must be finite");
+  GC_REQUIRE(ctx, sp->fixed_point_bits >= 24 && sp->fixed_point_bits <= gc_max_fixed_point_bits(ctx),
+             "fixed_point_bits must be in [24, %d] for a %d^3 grid", gc_max_fixed_point_bits(ctx), ctx->G);
+  if (sp->mode != GC_STEP_PRIME && !ctx->last_step_valid) {
+    gc_set_error(ctx, "gc_pm_step: ADVANCE/CLOSE before PRIME");
+    return GC_ERR_STATE;
+  }
+  int s = gc_mg_check_params(ctx, &sp->mg);
+  if (s) return s;
+  const int solve_only = (sp->flags & GC_STEP_SOLVE_ONLY) != 0, push_only = (sp->flags & GC_STEP_PUSH_ONLY) != 0;
+  GC_REQUIRE(ctx, !(solve_only && push_only), "gc_pm_step: SOLVE_ONLY and PUSH_ONLY are exclusive");
+  GC_REQUIRE(ctx, push_only == ctx->pending_push, "gc_pm_step: %s",
+             push_only ? "PUSH_ONLY without a SOLVE_ONLY step before it" : "a SOLVE_ONLY step awaits its PUSH_ONLY");
+  gc_mg_stats mst;
+  memset(&mst, 0, sizeof(mst));
+  if (push_only) {
+    ctx->pending_push = 0;
+    mst = ctx->last_stats;
+  } else {
+    if ((s = pm_solve(ctx, p, sp, &mst))) return s;
+    if (solve_only) {  // the particle pass (and the history update) come with PUSH_ONLY
+      ctx->pending_push = 1;
+      if (st) {
+        memset(st, 0, sizeof(*st));
+        st->mg = mst;
+      }
+      return GC_OK;
+    }
+  }
+  if ((s = gc_ws_post_solve(ctx))) return s;
+  return pm_push(ctx, p, sp, mst, st);
+}
+
+// More V-cycles on the current potential until ||r|| < tol ||b|| (between a
+// SOLVE_ONLY and a PUSH_ONLY step); adds the cycles run to *cycles.
+extern "C" int gc_pm_refine(gc_ctx *ctx, const gc_mg_params *p, int *cycles) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, p, "gc_pm_refine: NULL params");
+  int s = gc_mg_check_params(ctx, p);
+  if (s) return s;
+  gc_mg_params q = *p;
+  q.flags &= ~GC_MG_FIXED_CYCLES;
+  q.min_cycles = 0;
+  const gc_mg_stats before = ctx->last_stats;
+  gc_mg_stats st;
+  if ((s = gc_mg_run(ctx, &q, &st))) return s;
+  ctx->last_stats = before;
+  ctx->last_stats.cycles += st.cycles;
+  ctx->last_stats.converged = st.converged;
+  ctx->last_stats.rhs_norm = st.rhs_norm;
+  ctx->last_stats.res_norm = st.res_norm;
+  if (cycles) *cycles = st.cycles;
+  return GC_OK;
+}
+
+// Relative residual of the last fixed-cycle solve from the pinned host mirror the
+// solve wrote (no copy, no synchronisation: the caller synchronised already).
+extern "C" int gc_pm_residual_host(const gc_ctx *ctx, double *rel) {
+  if (!ctx || !rel) return GC_ERR_ARG;
+  const double b2 = ctx->hsmall[GC_S_BNORM2], r2 = ctx->hsmall[GC_S_RNORM2];
+  *rel = b2 > 0.0 ? sqrt(r2) / sqrt(b2) : 0.0;
   return GC_OK;
 }
 

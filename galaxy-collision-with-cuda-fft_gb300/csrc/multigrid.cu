@@ -1003,6 +1003,9 @@ int gc_mg_run(gc_ctx *ctx, const gc_mg_params *p, gc_mg_stats *stats) {
     for (int c = 0; c < p->max_cycles && ctx->nlev > 0; ++c)
       if ((s = vcycle(ctx, p))) return s;
     if (ctx->nlev > 0 && (s = resid_norm_async(ctx))) return s;
+    // ||b0||^2 and ||r0||^2 (slots 0 and 1) to the pinned host mirror, stream
+    // ordered: after a synchronisation the caller reads them without a copy
+    GC_CUDA(ctx, cudaMemcpyAsync(ctx->hsmall, ctx->dsmall, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     st.cycles = ctx->nlev > 0 ? p->max_cycles : 0;
     st.converged = -1;
     st.rhs_norm = st.res_norm = NAN;

@@ -26,6 +26,8 @@ GC_FLAG_NONFINITE_RHO = 0x2
 GC_MG_FUSED_SWEEP = 0x1
 GC_MG_FIXED_CYCLES = 0x2
 GC_STEP_GRAD_GRID = 0x1
+GC_STEP_SOLVE_ONLY = 0x2
+GC_STEP_PUSH_ONLY = 0x4
 
 GC_WS_PLAIN = 0
 GC_WS_LEARNED = 1
@@ -124,6 +126,8 @@ _PROTOS = {
     "gc_pm_potential": (_vp, [_ctxp]),
     "gc_pm_copy_potential": (C.c_int, [_ctxp, _vp]),
     "gc_pm_last_residual": (C.c_int, [_ctxp, C.POINTER(C.c_double)]),
+    "gc_pm_residual_host": (C.c_int, [_ctxp, C.POINTER(C.c_double)]),
+    "gc_pm_refine": (C.c_int, [_ctxp, C.POINTER(MGParams), C.POINTER(C.c_int)]),
     "gc_profile_enable": (C.c_int, [_ctxp, C.c_int]),
     "gc_profile_reset": (C.c_int, [_ctxp]),
     "gc_profile_read": (C.c_int, [_ctxp, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),

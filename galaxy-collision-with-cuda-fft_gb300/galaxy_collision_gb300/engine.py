@@ -122,7 +122,7 @@ class PMEngine:
         self.steps_since_sort = 0
 
     # -- stepping ---------------------------------------------------------------
-    def _step(self, mode: int, dt: float, diagnostics: bool) -> StepResult:
+    def _step(self, mode: int, dt: float, diagnostics: bool, phase_flags: int = 0) -> StepResult:
         sp = _native.StepParams()
         sp.dt = float(dt)
         sp.mode = mode
@@ -130,7 +130,7 @@ class PMEngine:
         sp.diagnostics = int(bool(diagnostics))
         sp.mg = self.mg
         sp.fixed_point_bits = self.fixed_point_bits
-        sp.flags = _native.GC_STEP_GRAD_GRID if self.grad_grid else 0
+        sp.flags = (_native.GC_STEP_GRAD_GRID if self.grad_grid else 0) | phase_flags
         st = _native.StepStats()
         p = self._struct(self.cur)
         self.ctx.call("gc_pm_step", C.byref(p), C.byref(sp), C.byref(st), what="gc_pm_step")
@@ -189,6 +189,35 @@ class PMEngine:
         if self.fixed_cycles <= 0:
             raise RuntimeError("graph capture needs fixed_cycles > 0 (no host reads inside the step)")
         self._step(_native.GC_STEP_ADVANCE, dt, False)
+
+    def solve_kernels(self, dt: float) -> None:
+        """First half of an ADVANCE step (deposit and fixed-cycle solve), no host read."""
+        if self.fixed_cycles <= 0:
+            raise RuntimeError("split steps need fixed_cycles > 0")
+        self._step(_native.GC_STEP_ADVANCE, dt, False, _native.GC_STEP_SOLVE_ONLY)
+
+    def push_kernels(self, dt: float) -> None:
+        """Second half: the particle pass on the potential of solve_kernels."""
+        self._step(_native.GC_STEP_ADVANCE, dt, False, _native.GC_STEP_PUSH_ONLY)
+
+    def residual_host(self) -> float:
+        """Relative residual of the last fixed-cycle solve from the pinned host copy
+        it enqueued (call after synchronising; no device access)."""
+        r = C.c_double()
+        _native.check(self.ctx._lib.gc_pm_residual_host(self.ctx.handle, C.byref(r)), self.ctx.handle,
+                      "residual_host")
+        return float(r.value)
+
+    def refine(self) -> int:
+        """More V-cycles on the pending solve until it meets the tolerance; returns
+        how many were run."""
+        q = _native.MGParams()
+        C.pointer(q)[0] = self.mg
+        q.flags &= ~_native.GC_MG_FIXED_CYCLES
+        q.max_cycles, q.min_cycles = 60, 0
+        n = C.c_int()
+        self.ctx.call("gc_pm_refine", C.byref(q), C.byref(n), what="refine")
+        return int(n.value)
 
     def advance_graph(self, dt: float) -> None:
         """advance() through a CUDA graph of the whole step, captured on first use

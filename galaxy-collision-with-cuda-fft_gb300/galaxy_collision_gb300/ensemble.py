@@ -3,13 +3,15 @@
 Many small runs cannot fill a GB300 one at a time: a 64^3 or 128^3 grid step is
 a few hundred microseconds of mostly latency-bound kernels, and each solve of
 the adaptive multigrid reads its residual on the host. The ensemble advances
-all runs together: every engine solves with a fixed number of V-cycles (the
-extrapolated warm start needs one to reach 1e-6; the residual stays on the
-device and is checked at cadence), so a whole step has no host synchronisation,
-and the steps of all runs are captured into ONE CUDA graph with one stream
-branch per run. Replaying the graph launches every kernel of every run with no
+all runs together. Every engine solves with one V-cycle (enough for 1e-6 from
+the extrapolated warm start at almost every step) and writes its residual to
+pinned host memory; the solves of all runs are captured into ONE CUDA graph
+with one stream branch per run, the particle passes into a second one. Between
+the two replays the host reads every run's residual after one synchronisation
+and runs extra V-cycles for the few runs above the tolerance, so every solve
+still meets it. Replaying a graph launches every kernel of every run with no
 host gaps and lets independent runs overlap on the SMs. Runs are sorted at the
-same steps, so two graphs (one per particle-buffer parity) cover the whole run.
+same steps, so one pair of graphs per particle-buffer parity covers the run.
 
 Workload (the batched-ensemble configuration): 64 two-disk collisions with
 particle counts log-uniform in [0.25M, 4M], 64^3 grids below 1M particles and
@@ -66,6 +68,7 @@ class Ensemble:
         self._graphs = {}
         self.steps_since_sort = 0
         self.sort_every = sort_every
+        self.extra_cycles = 0
 
     @property
     def particles(self) -> int:
@@ -97,7 +100,7 @@ class Ensemble:
         e.mg.max_cycles = e.mg.min_cycles = cycles
         e.fixed_cycles = cycles
 
-    def _capture(self):
+    def _capture(self, what: str):
         g = torch.cuda.CUDAGraph()
         torch.cuda.synchronize()
         with torch.cuda.graph(g):
@@ -105,26 +108,40 @@ class Ensemble:
             for e, s in zip(self.engines, self.streams):
                 s.wait_stream(cap)
                 with torch.cuda.stream(s):
-                    e.step_kernels(self.dt)
+                    if what == "solve":
+                        e.solve_kernels(self.dt)
+                    else:
+                        e.push_kernels(self.dt)
             for s in self.streams:
                 cap.wait_stream(s)
         return g
 
-    def step(self) -> None:
-        """One KDK step of every run: the batched graph (sorting all runs together
-        every sort_every steps, outside the graph)."""
+    def step(self) -> int:
+        """One KDK step of every run: the solves of all runs as one graph (fixed
+        V-cycles), the residual of each run read from its pinned host copy after one
+        synchronisation, extra V-cycles for the runs above the tolerance, then the
+        particle passes of all runs as a second graph. Runs are sorted together every
+        sort_every steps, outside the graphs. Returns the extra V-cycles run."""
         if self.sort_every > 0 and self.steps_since_sort >= self.sort_every:
             for e in self.engines:
                 e.sort()
             self.steps_since_sort = 0
         key = tuple(e.cur["x"].data_ptr() for e in self.engines)
-        g = self._graphs.get(key)
-        if g is None:
-            g = self._graphs[key] = self._capture()
-        g.replay()
+        gs = self._graphs.get(key)
+        if gs is None:
+            gs = self._graphs[key] = (self._capture("solve"), self._capture("push"))
+        gs[0].replay()
+        torch.cuda.current_stream().synchronize()
+        extra = 0
+        for e in self.engines:
+            if e.residual_host() >= e.mg.tol:
+                extra += e.refine()
+        gs[1].replay()
         self.steps_since_sort += 1
         for e in self.engines:
             e.steps_since_sort = self.steps_since_sort
+        self.extra_cycles += extra
+        return extra
 
     def max_residual(self) -> float:
         return max(e.last_residual() for e in self.engines)
@@ -172,8 +189,10 @@ def run_comparison(n_runs: int = 64, steps: int = 300, seed: int = 5, one_by_one
     out = {
         "runs": n_runs, "particles": n, "grids": sorted({e.grid_size for e in ens.engines}),
         "batched": {"particle_steps_per_s": n * steps / (ms_batched / 1e3), "ms_per_step": ms_batched / steps,
-                    "v_cycles_per_solve": ens.fixed_cycles, "max_rel_residual_checked": resid,
-                    "residual_check": "every run, every 25 steps"},
+                    "v_cycles_per_solve": ens.fixed_cycles + ens.extra_cycles / (n_runs * (steps + 1)),
+                    "extra_v_cycles": ens.extra_cycles, "max_rel_residual_checked": resid,
+                    "residual_check": "every run after every step's fixed cycle (extra cycles below tol); the "
+                                      "final residual of every run every 25 steps"},
         "one_by_one": {"particle_steps_per_s": n * k / (ms_single / 1e3), "ms_per_step": ms_single / k,
                        "mean_v_cycles": float(np.mean(cycles))},
         "steps": steps, "one_by_one_steps": k,

@@ -109,6 +109,13 @@ typedef struct gc_step_params {
  * and gather it with one vector load per corner (same arithmetic as forming it
  * on the fly from phi; costs a G^3 float4 buffer held by the context). */
 #define GC_STEP_GRAD_GRID 0x1
+/* gc_step_params.flags: split a step in two calls. SOLVE_ONLY runs the deposit
+ * and the solve and stops; PUSH_ONLY (the next call, same mode and dt) runs the
+ * particle pass on that potential. In between, gc_pm_residual_host reads the
+ * residual of a fixed-cycle solve and gc_pm_refine adds V-cycles, so batched
+ * fixed-cycle solves can still meet the tolerance. */
+#define GC_STEP_SOLVE_ONLY 0x2
+#define GC_STEP_PUSH_ONLY 0x4
 
 typedef struct gc_step_stats {
   gc_mg_stats mg;
@@ -265,6 +272,12 @@ const float *gc_pm_potential(const gc_ctx *ctx);
 int gc_pm_copy_potential(gc_ctx *ctx, float *phi);
 /* Relative residual ||r||/||4 pi G rho|| of the engine's last solve (synchronises). */
 int gc_pm_last_residual(gc_ctx *ctx, double *rel);
+/* Same, for a fixed-cycle solve, from the pinned host copy that solve enqueued:
+ * no copy and no synchronisation (the caller has synchronised the stream). */
+int gc_pm_residual_host(const gc_ctx *ctx, double *rel);
+/* Between a SOLVE_ONLY and a PUSH_ONLY step: more V-cycles on the current
+ * potential until ||r|| < tol ||4 pi G rho|| (at least one); *cycles gets how many. */
+int gc_pm_refine(gc_ctx *ctx, const gc_mg_params *params, int *cycles);
 
 /* ---- instrumentation (no kernel counterpart in the reference: it replaces the
  * sync-bracketed per-stage wall clock of bench.py:66-73, 176-186) ---------- */

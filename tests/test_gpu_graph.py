@@ -3,8 +3,10 @@
 With a fixed number of V-cycles the engine's step makes no host read, so it
 can be captured once and replayed. Replays must give bit-identical states to
 the same steps launched eagerly (same kernels, same order), across re-sorts
-that swap the particle buffers; the ensemble's multi-stream graph must advance
-every run to the solver tolerance.
+that swap the particle buffers. A step split into its solve and push halves is
+the whole step, and extra V-cycles between the halves bring a solve that one
+cycle left above the tolerance below it; the ensemble's multi-stream graphs
+must advance every run to the solver tolerance.
 """
 
 from __future__ import annotations
@@ -62,10 +64,48 @@ def test_ensemble_graph_advances_every_run(cuda):
     ens = ensemble.Ensemble(n_runs=3, seed=11)
     assert len(ens.engines) == 3
     x0 = [e.cur["x"].clone() for e in ens.engines]
-    ens.prime()  # first steps adaptive, then the graph
+    ens.prime()  # first steps adaptive, then the graphs
     for _ in range(5):
         ens.step()
-    torch.cuda.synchronize()
-    assert ens.max_residual() < 1e-5
+        torch.cuda.synchronize()
+        # every run's solve met the tolerance (extra V-cycles where one was not enough)
+        assert ens.max_residual() < 1e-6
     for e, x in zip(ens.engines, x0):
         assert not torch.equal(e.cur["x"], x)
+
+
+def test_split_step_is_the_whole_step_and_refine_meets_tol(cuda):
+    G, dt = 32, 0.05
+    pos, vel, mass = _cluster(30000, G, 2)
+    a, b = _engine(G, "plain"), _engine(G, "plain")
+    for e in (a, b):
+        e.load(pos, vel, mass)
+        e.prime(dt)
+    for _ in range(3):
+        a.advance(dt)
+        b.solve_kernels(dt)
+        b.push_kernels(dt)
+        b.steps_since_sort += 1
+    for e in (a, b):
+        e.synchronize(dt)
+    np.testing.assert_array_equal(a.state_arrays()[0].cpu().numpy(), b.state_arrays()[0].cpu().numpy())
+    np.testing.assert_array_equal(a.state_arrays()[1].cpu().numpy(), b.state_arrays()[1].cpu().numpy())
+
+    # one fixed V-cycle from the plain start leaves the solve above 1e-6
+    c = _engine(G, "plain")
+    c.mg.max_cycles = c.mg.min_cycles = c.fixed_cycles = 1
+    c.load(pos, vel, mass)
+    c.prime(dt)
+    c.solve_kernels(dt)
+    import torch
+
+    torch.cuda.synchronize()
+    r1 = c.residual_host()
+    assert r1 > 1e-6
+    extra = c.refine()
+    assert extra >= 1
+    assert c.last_residual() < 1e-6
+    c.push_kernels(dt)
+    torch.cuda.synchronize()
+    with pytest.raises(Exception):
+        c.push_kernels(dt)  # no pending solve
