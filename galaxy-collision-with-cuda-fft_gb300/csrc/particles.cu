@@ -179,22 +179,41 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Cell-sorted particles. Each thread walks DEP_SEQ consecutive particles of the
-// array, so the particles of one cell (adjacent after the sort) are summed in
-// registers. Two runs are cached per thread, so particles that drifted into a
-// neighbouring cell since the last sort do not break the run of the cell they
-// are interleaved with; a run evicted from the cache is added to the grid with
-// one int64 atomic per in-box corner. Lanes hold consecutive slices: at the end
-// lanes whose cached runs are the same cell (__match_any_sync) reduce them with
-// redux.sync and one lane adds the sums. Correct for any particle order; the
-// sort only makes the runs long.
-#define DEP_SEQ 8
+// Cell-sorted particles, warp-contiguous. Lane L of warp w takes the particles
+// t0 + 256 w + 32 j + L (j = 0..7) of the CTA's tile of 2048, so the 32
+// particles a warp handles at once are adjacent in the array: after the cell
+// sort they share one or two cells, and the particles that drifted into a
+// neighbouring cell since the sort are scattered among them.
+//
+// Per particle the 8 corner contributions are the reference's f32 products
+// m/dx^3 * wx * wy * wz (deposit.py:69-82) scaled by the quantum (a power of
+// two: exact) and rounded to the nearest integer. The rounding adds 1.5 * 2^23
+// (the f32 spacing is 1 in [2^23, 2^24)) and keeps the bits; those biased
+// values are summed in unsigned (wrapping) arithmetic and the bias of the
+// summands is subtracted afterwards, which is exact because every true sum fits
+// in int32.
+//
+// The cells of lane 0 and lane 31 are the warp's "main" cells: all lanes in one
+// of them reduce their corners with one full-warp redux.sync per corner (lanes
+// elsewhere contribute the bias, i.e. zero), and lane 0 / lane 31 adds the
+// sums. Lanes in any other cell (drifted particles, or sparse regions where
+// every particle has its own cell) add their own corners. A redux.sync over the
+// full warp costs the same whatever the keys, unlike one per group of equal
+// keys, which serialises over the groups.
+//
+// Corners go to an int32 box of nodes in shared memory when the tile's cells
+// fit DEP_BOX (the box is the cell range of the tile's coordinate range: x/dx is
+// monotone) and the tile's total quanta bound every node below 2^31; the box is
+// added to the int64 grid with one atomic per nonzero node at the end of the
+// tile. Otherwise corners go to the grid directly. Particles whose contribution
+// reaches 2^22 quanta (point masses) are deposited out of line at the end of
+// the tile with the general int64 rounding. Correct for any particle order;
+// the sort makes it fast.
 #define DEP_NONE 0xffffffffu
-
-// Round-to-nearest-even integer of v (|v| < 2^22): the f32 add of 1.5*2^23 lands
-// in [2^23, 2^24), where the f32 spacing is 1, and the integer is read from the
-// bits. Same result as f32_to_i64_rn.
-__device__ __forceinline__ int rne_small(float v) { return __float_as_int(__fadd_rn(v, 12582912.0f)) - 0x4B400000; }
+#define DEP_PER 8
+#define DEP_TILE (256 * DEP_PER)
+#define DEP_BOX 8192
+#define DEP_BIAS 0x4B400000u
 
 // Corner contributions of a particle whose mass exceeds 2^22 quanta.
 __device__ __forceinline__ void cic_q_large(float mm, float fx, float fy, float fz, float qscale, long long (&q)[8]) {
@@ -207,37 +226,6 @@ __device__ __forceinline__ void cic_q_large(float mm, float fx, float fy, float 
     q[c] = f32_to_i64_rn(__fmul_rn(w, qscale));
   }
 }
-
-
-template <bool POW2>
-__device__ __forceinline__ bool dep_cell(float px, float py, float pz, const DepCtx &d, float inv_dx, int &ix, int &iy,
-                                         int &iz, float &fx, float &fy, float &fz) {
-  float gx, gy, gz;
-  if (POW2) {  // x / dx == x * (1/dx) exactly when dx is a power of two
-    gx = __fmul_rn(px, inv_dx); gy = __fmul_rn(py, inv_dx); gz = __fmul_rn(pz, inv_dx);
-  } else {
-    gx = __fdiv_rn(px, d.dx); gy = __fdiv_rn(py, d.dx); gz = __fdiv_rn(pz, d.dx);
-  }
-  const float hi = (float)d.G;
-  if (!(gx >= -1.0f && gx < hi && gy >= -1.0f && gy < hi && gz >= -1.0f && gz < hi)) return false;
-  const float flx = floorf(gx), fly = floorf(gy), flz = floorf(gz);
-  ix = (int)flx; iy = (int)fly; iz = (int)flz;
-  fx = __fsub_rn(gx, flx); fy = __fsub_rn(gy, fly); fz = __fsub_rn(gz, flz);
-  return true;
-}
-
-// Runs of equal cells. A run carries the linear index of its (ix, iy, iz) node
-// and whether all 8 corners are inside the grid, so adding it to the grid is 8
-// fire-and-forget atomics with constant offsets (no key decoding, no call).
-// A run of equal cells: its cell, and the int32 sums of its particles' small
-// contributions (each below 2^22 quanta, at most DEP_SEQ particles: < 2^25).
-// Particles with a larger contribution never enter a run; they are added to the
-// grid directly.
-struct DepRun {
-  unsigned key;   // cell key, DEP_NONE when empty
-  int ix, iy, iz;
-  int q[8];
-};
 
 // Add 8 corner values to the int64 grid, dropping corners outside it.
 __device__ __forceinline__ void corners_to_grid(long long *__restrict__ qg, int G, int ix, int iy, int iz,
@@ -260,8 +248,7 @@ __device__ __forceinline__ void corners_to_grid(long long *__restrict__ qg, int 
   }
 }
 
-// A particle whose contribution exceeds 2^22 quanta (rare: point masses) goes
-// to the grid on its own, out of line.
+// A particle whose contribution reaches 2^22 quanta goes to the grid on its own.
 __device__ __noinline__ void large_to_grid(long long *__restrict__ qg, int G, int ix, int iy, int iz, float mm,
                                            float fx, float fy, float fz, float qscale) {
   long long q[8];
@@ -269,122 +256,132 @@ __device__ __noinline__ void large_to_grid(long long *__restrict__ qg, int G, in
   corners_to_grid(qg, G, ix, iy, iz, q);
 }
 
-__device__ __noinline__ void run_to_grid(long long *__restrict__ qg, int G, int ix, int iy, int iz, int q0, int q1,
-                                         int q2, int q3, int q4, int q5, int q6, int q7) {
-  const long long q[8] = {q0, q1, q2, q3, q4, q5, q6, q7};
-  corners_to_grid(qg, G, ix, iy, iz, q);
-}
-
-// Where finished runs go: the int64 grid, or (box != null) an int32 box of nodes
-// [x0, x0+nx) x [y0, y0+ny) x [z0, z0+nz) in shared memory that holds every
-// corner of the CTA's current tile; the tile's bound on its total quanta keeps
-// every box value below 2^31.
-struct DepOut {
-  long long *qg;
-  int *box;
-  int x0, y0, z0, ny, nz, G;
+// The tile's box of nodes [x0, x0+nx) x [y0, y0+ny) x [z0, z0+nz) in shared memory.
+struct DepBox {
+  int *b;
+  int x0, y0, z0, ny, nz, nyz;
 };
 
-__device__ __forceinline__ void run_out(const DepOut &o, const DepRun &r, const int (&q)[8]) {
-  if (o.box) {
-    const int bi = ((r.ix - o.x0) * o.ny + (r.iy - o.y0)) * o.nz + (r.iz - o.z0);
-#pragma unroll
-    for (int c = 0; c < 8; ++c)
-      if (q[c] != 0) atomicAdd(o.box + bi + ((c >> 2) * o.ny + ((c >> 1) & 1)) * o.nz + (c & 1), q[c]);
+template <bool BOX>
+__device__ __forceinline__ void dep_out(const DepBox &bx, long long *__restrict__ qg, int G, int ix, int iy, int iz,
+                                        const int (&t)[8]) {
+  if (BOX) {
+    int *b = bx.b + ((ix - bx.x0) * bx.ny + (iy - bx.y0)) * bx.nz + (iz - bx.z0);
+    const int nz = bx.nz, nyz = bx.nyz;
+    atomicAdd(b, t[0]); atomicAdd(b + 1, t[1]); atomicAdd(b + nz, t[2]); atomicAdd(b + nz + 1, t[3]);
+    atomicAdd(b + nyz, t[4]); atomicAdd(b + nyz + 1, t[5]); atomicAdd(b + nyz + nz, t[6]);
+    atomicAdd(b + nyz + nz + 1, t[7]);
   } else {
-    run_to_grid(o.qg, o.G, r.ix, r.iy, r.iz, q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7]);
+    const long long q[8] = {t[0], t[1], t[2], t[3], t[4], t[5], t[6], t[7]};
+    corners_to_grid(qg, G, ix, iy, iz, q);
   }
 }
 
-// Lanes whose run is the same cell (__match_any_sync) reduce it with redux.sync
-// (a group's sums stay below 32 * 2^25 = 2^30) and one of them adds it.
-__device__ __forceinline__ void dep_merge(const DepRun &r, const DepOut &o, int lane) {
-  const unsigned peers = __match_any_sync(0xffffffffu, r.key);
-  if (r.key == DEP_NONE) return;
-  if (__popc(peers) > 1) {
-    int tot[8];
+// The DEP_PER particles of one lane (registers), 32 adjacent particles of the
+// warp at a time. Sets bit j of `large` for particles left to the out-of-line pass.
+template <bool POW2, bool BOX>
+__device__ __forceinline__ void dep_warp_pass(const float (&px)[DEP_PER], const float (&py)[DEP_PER],
+                                              const float (&pz)[DEP_PER], const float (&pm)[DEP_PER], long long nrem,
+                                              const DepCtx &d, float inv_dx, float qscale, const DepBox &bx,
+                                              long long *__restrict__ qg, unsigned *__restrict__ status, int lane,
+                                              unsigned &large) {
+  const int G1 = d.G + 1;
+  const float hi = (float)d.G;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) tot[t] = __reduce_add_sync(peers, r.q[t]);
-    if (lane == __ffs(peers) - 1) run_out(o, r, tot);
-  } else {
-    run_out(o, r, r.q);
+  for (int j = 0; j < DEP_PER; ++j) {
+    float gx, gy, gz;
+    if (POW2) {  // x / dx == x * (1/dx) exactly when dx is a power of two
+      gx = __fmul_rn(px[j], inv_dx); gy = __fmul_rn(py[j], inv_dx); gz = __fmul_rn(pz[j], inv_dx);
+    } else {
+      gx = __fdiv_rn(px[j], d.dx); gy = __fdiv_rn(py[j], d.dx); gz = __fdiv_rn(pz[j], d.dx);
+    }
+    const bool inr = gx >= -1.0f && gx < hi && gy >= -1.0f && gy < hi && gz >= -1.0f && gz < hi;
+    const int ix = __float2int_rd(gx), iy = __float2int_rd(gy), iz = __float2int_rd(gz);
+    const float fx = __fsub_rn(gx, __int2float_rn(ix)), fy = __fsub_rn(gy, __int2float_rn(iy)),
+                fz = __fsub_rn(gz, __int2float_rn(iz));
+    const float mmq = __fmul_rn(__fmul_rn(pm[j], d.inv_vol), qscale);
+    const bool small = fabsf(mmq) < 4194304.0f;
+    if (!inr && 32 * j < nrem && !gc_finite3(px[j], py[j], pz[j])) atomicOr(status, GC_FLAG_NONFINITE_POS);
+    if (inr && !small) large |= 1u << j;
+    const bool ok = inr && small;
+    const float s = ok ? mmq : 0.0f;
+    const float wx0 = __fsub_rn(1.0f, fx), wy0 = __fsub_rn(1.0f, fy), wz0 = __fsub_rn(1.0f, fz);
+    const float a0 = __fmul_rn(s, wx0), a1 = __fmul_rn(s, fx);
+    const float b00 = __fmul_rn(a0, wy0), b01 = __fmul_rn(a0, fy), b10 = __fmul_rn(a1, wy0), b11 = __fmul_rn(a1, fy);
+    unsigned r[8];
+    r[0] = __float_as_uint(__fadd_rn(__fmul_rn(b00, wz0), 12582912.0f));
+    r[1] = __float_as_uint(__fadd_rn(__fmul_rn(b00, fz), 12582912.0f));
+    r[2] = __float_as_uint(__fadd_rn(__fmul_rn(b01, wz0), 12582912.0f));
+    r[3] = __float_as_uint(__fadd_rn(__fmul_rn(b01, fz), 12582912.0f));
+    r[4] = __float_as_uint(__fadd_rn(__fmul_rn(b10, wz0), 12582912.0f));
+    r[5] = __float_as_uint(__fadd_rn(__fmul_rn(b10, fz), 12582912.0f));
+    r[6] = __float_as_uint(__fadd_rn(__fmul_rn(b11, wz0), 12582912.0f));
+    r[7] = __float_as_uint(__fadd_rn(__fmul_rn(b11, fz), 12582912.0f));
+    const unsigned key = ok ? (unsigned)(((ix + 1) * G1 + (iy + 1)) * G1 + (iz + 1)) : DEP_NONE;
+    const unsigned kA = __shfl_sync(0xffffffffu, key, 0), kB = __shfl_sync(0xffffffffu, key, 31);
+    const bool inA = key == kA, inB = key == kB;
+    int t[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) t[c] = (int)(__reduce_add_sync(0xffffffffu, inA ? r[c] : DEP_BIAS) - 32u * DEP_BIAS);
+    if (lane == 0 && kA != DEP_NONE) dep_out<BOX>(bx, qg, d.G, ix, iy, iz, t);
+    if (kB != kA) {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) t[c] = (int)(__reduce_add_sync(0xffffffffu, inB ? r[c] : DEP_BIAS) - 32u * DEP_BIAS);
+      if (lane == 31 && kB != DEP_NONE) dep_out<BOX>(bx, qg, d.G, ix, iy, iz, t);
+    }
+    if (!inA && !inB && key != DEP_NONE) {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) t[c] = (int)(r[c] - DEP_BIAS);
+      dep_out<BOX>(bx, qg, d.G, ix, iy, iz, t);
+    }
   }
 }
 
-// The CTA stages a tile of DEP_TILE consecutive particles in shared memory with
-// coalesced loads (one padding word per 32 keeps the per-thread reads of 8
-// consecutive particles conflict-free); each thread walks its 8 particles in a
-// rolled loop with a two-run cache (particles that drifted into a neighbour
-// cell since the last sort do not break the run of the cell they are
-// interleaved with), and the warp merges the cached runs at the end. A first
-// pass finds the box of cells the tile touches and its largest small
-// contribution: when the box's nodes fit DEP_BOX_CAP and the tile's total stays
-// below 2^30 quanta per node, runs are added to an int32 box in shared memory
-// and the box is added to the grid with one int64 atomic per nonzero node, so
-// run ends caused by drift cost shared-memory atomics only.
-#define DEP_TILE (256 * DEP_SEQ)
-#define DEP_PAD(i) ((i) + ((i) >> 5))
-#define DEP_BOX_CAP 3072
-template <bool POW2, bool VEC>
+template <bool POW2>
 __global__ void __launch_bounds__(256, 3)
     k_deposit_sorted(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
                      const float *__restrict__ m, long long n, DepCtx d, float inv_dx,
                      const double *__restrict__ qexp, long long *__restrict__ qg, unsigned *__restrict__ status) {
-  __shared__ float sx[DEP_PAD(DEP_TILE)], sy[DEP_PAD(DEP_TILE)], sz[DEP_PAD(DEP_TILE)], sm_[DEP_PAD(DEP_TILE)];
-  __shared__ int box[DEP_BOX_CAP];
-  __shared__ int bnd[7];
+  __shared__ int box[DEP_BOX];
+  __shared__ int bnd[2][8];  // per tile parity: cell min x,y,z, max x,y,z, max |m| bits
   const float qscale = ldexpf(1.0f, -(int)(*qexp));
-  const int tid = threadIdx.x, lane = tid & 31;
-  for (long long t0 = (long long)blockIdx.x * DEP_TILE; t0 < n; t0 += (long long)gridDim.x * DEP_TILE) {
-    const int cnt_tile = (int)(n - t0 < DEP_TILE ? n - t0 : DEP_TILE);
-    __syncthreads();  // the previous tile and box have been consumed
-    if (tid < 3) { bnd[tid] = 0x7fffffff; bnd[3 + tid] = -0x7fffffff; }
-    if (tid == 3) bnd[6] = 0;
-    if (VEC && cnt_tile == DEP_TILE) {
-#pragma unroll 1
-      for (int h = 0; h < DEP_SEQ / 4; ++h) {
-        const int q4 = h * 256 + tid;  // float4 index inside the tile
-        const float4 a = __ldg(reinterpret_cast<const float4 *>(x + t0) + q4);
-        const float4 b = __ldg(reinterpret_cast<const float4 *>(y + t0) + q4);
-        const float4 c = __ldg(reinterpret_cast<const float4 *>(z + t0) + q4);
-        const float4 e = __ldg(reinterpret_cast<const float4 *>(m + t0) + q4);
-        const int i = 4 * q4;
-        sx[DEP_PAD(i)] = a.x; sx[DEP_PAD(i + 1)] = a.y; sx[DEP_PAD(i + 2)] = a.z; sx[DEP_PAD(i + 3)] = a.w;
-        sy[DEP_PAD(i)] = b.x; sy[DEP_PAD(i + 1)] = b.y; sy[DEP_PAD(i + 2)] = b.z; sy[DEP_PAD(i + 3)] = b.w;
-        sz[DEP_PAD(i)] = c.x; sz[DEP_PAD(i + 1)] = c.y; sz[DEP_PAD(i + 2)] = c.z; sz[DEP_PAD(i + 3)] = c.w;
-        sm_[DEP_PAD(i)] = e.x; sm_[DEP_PAD(i + 1)] = e.y; sm_[DEP_PAD(i + 2)] = e.z; sm_[DEP_PAD(i + 3)] = e.w;
-      }
-    } else {
-      for (int i = tid; i < cnt_tile; i += 256) {
-        sx[DEP_PAD(i)] = x[t0 + i];
-        sy[DEP_PAD(i)] = y[t0 + i];
-        sz[DEP_PAD(i)] = z[t0 + i];
-        sm_[DEP_PAD(i)] = m[t0 + i];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < DEP_BOX; i += 256) box[i] = 0;  // every flush zeroes what it read
+  if (tid < 16) {
+    const int a = tid & 7;
+    bnd[tid >> 3][a] = a < 3 ? 0x7fffffff : (a < 6 ? -0x7fffffff : 0);
+  }
+  __syncthreads();
+  int par = 0;
+  for (long long t0 = (long long)blockIdx.x * DEP_TILE; t0 < n; t0 += (long long)gridDim.x * DEP_TILE, par ^= 1) {
+    const long long wb = t0 + warp * (32 * DEP_PER) + lane;
+    const long long nrem = n - wb;  // particle j of this lane exists when 32 j < nrem
+    float px[DEP_PER], py[DEP_PER], pz[DEP_PER], pm[DEP_PER];
+#pragma unroll
+    for (int j = 0; j < DEP_PER; ++j) {
+      if (32 * j < nrem) {
+        px[j] = __ldg(x + wb + 32 * j); py[j] = __ldg(y + wb + 32 * j); pz[j] = __ldg(z + wb + 32 * j);
+        pm[j] = __ldg(m + wb + 32 * j);
+      } else {  // missing: NaN position (ignored by the bounds, deposits nothing), zero mass
+        px[j] = py[j] = pz[j] = __int_as_float(0x7fc00000);
+        pm[j] = 0.0f;
       }
     }
-    __syncthreads();
-    const int i0 = tid * DEP_SEQ;
-    const int cnt = cnt_tile - i0 < 0 ? 0 : (cnt_tile - i0 > DEP_SEQ ? DEP_SEQ : cnt_tile - i0);
-    // box of the cells that can receive mass: x/dx is monotone in x, so the
-    // cells of the tile's coordinate range (clamped to the grid range; NaN is
-    // ignored by fmin/fmax) bound every particle's cell. Also the largest small
-    // |m| (|m/dx^3| in quanta below 2^22 enter runs).
-    float xl = 3.0e38f, yl = 3.0e38f, zl = 3.0e38f, xh = -3.0e38f, yh = -3.0e38f, zh = -3.0e38f, ma = 0.0f;
-    const float lim = __fmul_rn(4194304.0f, 1.0f / qscale);  // |m/dx^3| below this is small
-#pragma unroll 1
-    for (int j = 0; j < cnt; ++j) {
-      const int i = DEP_PAD(i0 + j);
-      const float px = sx[i], py = sy[i], pz = sz[i];
-      xl = fminf(xl, px); xh = fmaxf(xh, px);
-      yl = fminf(yl, py); yh = fmaxf(yh, py);
-      zl = fminf(zl, pz); zh = fmaxf(zh, pz);
-      const float a = fabsf(__fmul_rn(sm_[i], d.inv_vol));
-      if (a < lim) ma = fmaxf(ma, a);
-    }
-    int lo[3], hi[3];
+    // the tile's cell range from its coordinate range (fminf/fmaxf skip NaN),
+    // clamped to the cells -1 .. G-1 that receive mass, and its largest |m|
     {
-      const float gl = -1.0f, gh = (float)d.G - 1.0f;  // cells -1 .. G-1 receive mass
+      float xl = 3.0e38f, yl = 3.0e38f, zl = 3.0e38f, xh = -3.0e38f, yh = -3.0e38f, zh = -3.0e38f;
+      unsigned mb = 0;
+#pragma unroll
+      for (int j = 0; j < DEP_PER; ++j) {
+        xl = fminf(xl, px[j]); xh = fmaxf(xh, px[j]);
+        yl = fminf(yl, py[j]); yh = fmaxf(yh, py[j]);
+        zl = fminf(zl, pz[j]); zh = fmaxf(zh, pz[j]);
+        mb = max(mb, __float_as_uint(pm[j]) & 0x7fffffffu);
+      }
+      const float gl = -1.0f, gh = (float)d.G - 1.0f;
       const float cl[3] = {xl, yl, zl}, ch[3] = {xh, yh, zh};
+      int lo[3], hi[3];
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
         float l = POW2 ? __fmul_rn(cl[a], inv_dx) : __fdiv_rn(cl[a], d.dx);
@@ -392,95 +389,63 @@ __global__ void __launch_bounds__(256, 3)
         l = fminf(fmaxf(floorf(l), gl), gh);
         h = fminf(fmaxf(floorf(h), gl), gh);
         const bool any_pt = cl[a] <= ch[a];
-        lo[a] = any_pt ? (int)l : 0x7fffffff;
-        hi[a] = any_pt ? (int)h : -0x7fffffff;
+        lo[a] = __reduce_min_sync(0xffffffffu, any_pt ? (int)l : 0x7fffffff);
+        hi[a] = __reduce_max_sync(0xffffffffu, any_pt ? (int)h : -0x7fffffff);
       }
-    }
+      mb = __reduce_max_sync(0xffffffffu, mb);
+      if (lane == 0) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      lo[a] = __reduce_min_sync(0xffffffffu, lo[a]);
-      hi[a] = __reduce_max_sync(0xffffffffu, hi[a]);
-    }
-    const unsigned mqb = __reduce_max_sync(0xffffffffu, __float_as_uint(__fmul_rn(ma, qscale)));
-    if (lane == 0) {
-#pragma unroll
-      for (int a = 0; a < 3; ++a) { atomicMin(&bnd[a], lo[a]); atomicMax(&bnd[3 + a], hi[a]); }
-      atomicMax(&bnd[6], (int)mqb);
+        for (int a = 0; a < 3; ++a) { atomicMin(&bnd[par][a], lo[a]); atomicMax(&bnd[par][3 + a], hi[a]); }
+        atomicMax(&bnd[par][6], (int)mb);
+      }
     }
     __syncthreads();
-    DepOut o;
-    o.qg = qg;
-    o.G = d.G;
-    o.box = nullptr;
-    o.x0 = bnd[0]; o.y0 = bnd[1]; o.z0 = bnd[2];
-    const int nx = bnd[3] - bnd[0] + 2, ny = bnd[4] - bnd[1] + 2, nz = bnd[5] - bnd[2] + 2;
-    o.ny = ny; o.nz = nz;
-    // every small contribution is at most (largest small |m/dx^3| in quanta) + 1/2
-    const float tile_q = __fmul_rn(__uint_as_float((unsigned)bnd[6]) + 1.0f, (float)cnt_tile);
-    const bool use_box = bnd[3] >= bnd[0] && (long long)nx * ny * nz <= DEP_BOX_CAP && tile_q < 1073741824.0f;
-    const int vol = use_box ? nx * ny * nz : 0;
-    if (use_box) {
-      o.box = box;
-      for (int i = tid; i < vol; i += 256) box[i] = 0;
-      __syncthreads();
+    DepBox bx;
+    bx.b = box;
+    bx.x0 = bnd[par][0]; bx.y0 = bnd[par][1]; bx.z0 = bnd[par][2];
+    const int nx = bnd[par][3] - bx.x0 + 2;
+    bx.ny = bnd[par][4] - bx.y0 + 2;
+    bx.nz = bnd[par][5] - bx.z0 + 2;
+    bx.nyz = bx.ny * bx.nz;
+    // every small corner is at most min(largest |m| in quanta, 2^22) + 1/2
+    const float mq = __fmul_rn(__fmul_rn(__uint_as_float((unsigned)bnd[par][6]), d.inv_vol), qscale);
+    const int cnt_tile = (int)(n - t0 < DEP_TILE ? n - t0 : DEP_TILE);
+    const bool use_box = bnd[par][3] >= bx.x0 && (long long)nx * bx.nyz <= DEP_BOX &&
+                         __fmul_rn(fminf(mq, 4194304.0f) + 1.0f, (float)cnt_tile) < 1073741824.0f;
+    __syncthreads();  // every thread has read bnd[par]; reset it for the tile after next
+    if (tid < 8) bnd[par][tid] = tid < 3 ? 0x7fffffff : (tid < 6 ? -0x7fffffff : 0);
+    unsigned large = 0;
+    if (use_box)
+      dep_warp_pass<POW2, true>(px, py, pz, pm, nrem, d, inv_dx, qscale, bx, qg, status, lane, large);
+    else
+      dep_warp_pass<POW2, false>(px, py, pz, pm, nrem, d, inv_dx, qscale, bx, qg, status, lane, large);
+    while (large) {  // rare: point masses
+      const int j = __ffs(large) - 1;
+      large &= large - 1;
+      const long long p = wb + 32 * j;
+      const float gx = POW2 ? __fmul_rn(x[p], inv_dx) : __fdiv_rn(x[p], d.dx);
+      const float gy = POW2 ? __fmul_rn(y[p], inv_dx) : __fdiv_rn(y[p], d.dx);
+      const float gz = POW2 ? __fmul_rn(z[p], inv_dx) : __fdiv_rn(z[p], d.dx);
+      const int ix = __float2int_rd(gx), iy = __float2int_rd(gy), iz = __float2int_rd(gz);
+      large_to_grid(qg, d.G, ix, iy, iz, __fmul_rn(m[p], d.inv_vol), __fsub_rn(gx, __int2float_rn(ix)),
+                    __fsub_rn(gy, __int2float_rn(iy)), __fsub_rn(gz, __int2float_rn(iz)), qscale);
     }
-    DepRun r0, r1;
-    r0.key = r1.key = DEP_NONE;
-    r0.ix = r0.iy = r0.iz = r1.ix = r1.iy = r1.iz = 0;
-#pragma unroll
-    for (int t = 0; t < 8; ++t) r0.q[t] = r1.q[t] = 0;
-#pragma unroll 1
-    for (int j = 0; j < cnt; ++j) {
-      const int i = DEP_PAD(i0 + j);
-      const float px = sx[i], py = sy[i], pz = sz[i];
-      if (!gc_finite3(px, py, pz)) atomicOr(status, GC_FLAG_NONFINITE_POS);
-      int ix, iy, iz;
-      float fx, fy, fz;
-      if (!dep_cell<POW2>(px, py, pz, d, inv_dx, ix, iy, iz, fx, fy, fz)) continue;
-      const float mm = __fmul_rn(sm_[i], d.inv_vol);
-      if (!(__fmul_rn(fabsf(mm), qscale) < 4194304.0f)) {  // large (or NaN): straight to the grid
-        large_to_grid(qg, d.G, ix, iy, iz, mm, fx, fy, fz, qscale);
-        continue;
-      }
-      const float wx0 = __fsub_rn(1.0f, fx), wy0 = __fsub_rn(1.0f, fy), wz0 = __fsub_rn(1.0f, fz);
-      const float a0 = __fmul_rn(mm, wx0), a1 = __fmul_rn(mm, fx);
-      const float b00 = __fmul_rn(a0, wy0), b01 = __fmul_rn(a0, fy), b10 = __fmul_rn(a1, wy0), b11 = __fmul_rn(a1, fy);
-      int q[8];
-      q[0] = rne_small(__fmul_rn(__fmul_rn(b00, wz0), qscale));
-      q[1] = rne_small(__fmul_rn(__fmul_rn(b00, fz), qscale));
-      q[2] = rne_small(__fmul_rn(__fmul_rn(b01, wz0), qscale));
-      q[3] = rne_small(__fmul_rn(__fmul_rn(b01, fz), qscale));
-      q[4] = rne_small(__fmul_rn(__fmul_rn(b10, wz0), qscale));
-      q[5] = rne_small(__fmul_rn(__fmul_rn(b10, fz), qscale));
-      q[6] = rne_small(__fmul_rn(__fmul_rn(b11, wz0), qscale));
-      q[7] = rne_small(__fmul_rn(__fmul_rn(b11, fz), qscale));
-      const unsigned key = (unsigned)(((ix + 1) * (d.G + 1) + (iy + 1)) * (d.G + 1) + (iz + 1));
-      if (key == r0.key) {
-#pragma unroll
-        for (int t = 0; t < 8; ++t) r0.q[t] += q[t];
-      } else if (key == r1.key) {
-#pragma unroll
-        for (int t = 0; t < 8; ++t) r1.q[t] += q[t];
-      } else {  // evict run 1, demote run 0, start a new run 0
-        if (r1.key != DEP_NONE) run_out(o, r1, r1.q);
-        r1 = r0;
-        r0.key = key;
-        r0.ix = ix; r0.iy = iy; r0.iz = iz;
-#pragma unroll
-        for (int t = 0; t < 8; ++t) r0.q[t] = q[t];
-      }
-    }
-    dep_merge(r0, o, lane);
-    dep_merge(r1, o, lane);
     if (use_box) {
       __syncthreads();
-      for (int i = tid; i < vol; i += 256) {
-        const int v = box[i];
-        if (v == 0) continue;
-        const int bx = i / (ny * nz), rem = i - bx * ny * nz, by = rem / nz, bz = rem - by * nz;
-        const int jx = o.x0 + bx, jy = o.y0 + by, jz = o.z0 + bz;
-        if ((unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G && (unsigned)jz < (unsigned)d.G)
-          atomicAdd((unsigned long long *)(qg + ((size_t)jx * d.G + jy) * d.G + jz), (unsigned long long)(long long)v);
+      // rows (bx, by) over the warps, z over the lanes; every entry read is zeroed
+      for (int row = warp; row < nx * bx.ny; row += 8) {
+        const int rx = row / bx.ny, ry = row - rx * bx.ny;
+        const int jx = bx.x0 + rx, jy = bx.y0 + ry;
+        const bool rin = (unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G;
+        int *b = box + row * bx.nz;
+        for (int bz = lane; bz < bx.nz; bz += 32) {
+          const int v = b[bz];
+          if (v == 0) continue;
+          b[bz] = 0;
+          const int jz = bx.z0 + bz;
+          if (rin && (unsigned)jz < (unsigned)d.G)
+            atomicAdd((unsigned long long *)(qg + ((size_t)jx * d.G + jy) * d.G + jz), (unsigned long long)(long long)v);
+        }
       }
     }
   }
@@ -494,23 +459,16 @@ int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, co
   d.inv_vol = 1.0f / ((d.dx * d.dx) * d.dx);
   d.G = ctx->G;
   const long long ntiles = (n + DEP_TILE - 1) / DEP_TILE;
-  unsigned nb = (unsigned)(ntiles < 152LL * 8 ? ntiles : 152LL * 8);
+  const unsigned nb = (unsigned)(ntiles < 152LL * 3 ? ntiles : 152LL * 3);  // 3 CTAs per SM, persistent
   int fe = 0;
   const bool pow2 = std::frexp(d.dx, &fe) == 0.5f;
   const float inv_dx = pow2 ? std::ldexp(1.0f, 1 - fe) : 0.0f;
-  const bool vec = ((((uintptr_t)x) | ((uintptr_t)y) | ((uintptr_t)z) | ((uintptr_t)m)) & 15u) == 0;
-  if (pow2 && vec)
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true, true>, dim3(nb), dim3(256), 0, x, y, z, m,
-              (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
-  else if (pow2)
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true, false>, dim3(nb), dim3(256), 0, x, y, z, m,
-              (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
-  else if (vec)
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false, true>, dim3(nb), dim3(256), 0, x, y, z, m,
-              (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
+  if (pow2)
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<true>, dim3(nb), dim3(256), 0, x, y, z, m, (long long)n, d,
+              inv_dx, qexp, ctx->q, ctx->dstatus);
   else
-    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false, false>, dim3(nb), dim3(256), 0, x, y, z, m,
-              (long long)n, d, inv_dx, qexp, ctx->q, ctx->dstatus);
+    gc_launch(ctx, GK_DEPOSIT_RUNS, k_deposit_sorted<false>, dim3(nb), dim3(256), 0, x, y, z, m, (long long)n, d,
+              inv_dx, qexp, ctx->q, ctx->dstatus);
   GC_LAUNCH_CHECK(ctx, "deposit");
   return GC_OK;
 }
