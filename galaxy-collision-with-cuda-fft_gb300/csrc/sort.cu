@@ -14,6 +14,7 @@
 #define RS_WARPS (RS_THREADS / 32)
 #define RS_IPT 16                          // items per thread
 #define RS_TILE (RS_THREADS * RS_IPT)      // 4096 items per tile
+static_assert(RS_THREADS == RS_RADIX, "the scatter's per-digit phase has one thread per digit");
 
 __global__ void __launch_bounds__(256)
     k_cell_keys(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z, long long n,
@@ -121,16 +122,24 @@ __global__ void __launch_bounds__(SC_THREADS) k_scan_apply(unsigned *__restrict_
 
 // Stable scatter. Warp w of a tile owns items [w*32*IPT, (w+1)*32*IPT) of the
 // tile; round r handles item r*32+lane of that range, so (round, lane) order is
-// input order.
+// input order. Ranks within the tile (per-warp digit counts, then across warps
+// and digits) place every item at its slot of the tile's digit-sorted order in
+// shared memory; the items are then written out from there, so consecutive
+// threads write consecutive addresses of one digit's output segment.
 __global__ void __launch_bounds__(RS_THREADS)
     k_rs_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, long long n, int shift,
                  const unsigned *__restrict__ hist, int ntiles, uint32_t *__restrict__ kout,
                  uint32_t *__restrict__ vout) {
   __shared__ unsigned whist[RS_WARPS][RS_RADIX];
+  __shared__ unsigned dstart[RS_RADIX];  // first slot of each digit in the tile's sorted order
+  __shared__ unsigned gofs[RS_RADIX];    // output index of the tile's first item of each digit
+  __shared__ uint32_t sk[RS_TILE], sv[RS_TILE];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int t = threadIdx.x; t < RS_WARPS * RS_RADIX; t += RS_THREADS) (&whist[0][0])[t] = 0;
   __syncthreads();
-  const long long seg = (long long)blockIdx.x * RS_TILE + (long long)w * 32 * RS_IPT;
+  const long long tile0 = (long long)blockIdx.x * RS_TILE;
+  const int cnt = (int)(n - tile0 < RS_TILE ? n - tile0 : RS_TILE);
+  const long long seg = tile0 + (long long)w * 32 * RS_IPT;
   uint32_t k[RS_IPT], v[RS_IPT];
   unsigned rank[RS_IPT];
   const unsigned lt = (1u << lane) - 1u;
@@ -150,14 +159,32 @@ __global__ void __launch_bounds__(RS_THREADS)
     rank[r] = old + __popc(peers & lt);
   }
   __syncthreads();
-  // exclusive scan over warps per digit, plus the tile's global offset
-  for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) {
-    unsigned run = hist[(size_t)d * ntiles + blockIdx.x];
+  // per digit: exclusive prefix over the warps, the digit's tile total, and the
+  // tile's global offset for it
+  unsigned tot = 0;
+  {
+    const int d = threadIdx.x;  // RS_THREADS == RS_RADIX
     for (int ww = 0; ww < RS_WARPS; ++ww) {
       const unsigned c = whist[ww][d];
-      whist[ww][d] = run;
-      run += c;
+      whist[ww][d] = tot;
+      tot += c;
     }
+    gofs[d] = hist[(size_t)d * ntiles + blockIdx.x];
+  }
+  // exclusive scan of the digit totals over the block
+  {
+    unsigned x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    __shared__ unsigned wsum[RS_WARPS];
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    unsigned before = 0;
+    for (int ww = 0; ww < w; ++ww) before += wsum[ww];
+    dstart[threadIdx.x] = before + x - tot;
   }
   __syncthreads();
 #pragma unroll
@@ -165,10 +192,18 @@ __global__ void __launch_bounds__(RS_THREADS)
     const long long p = seg + r * 32 + lane;
     if (p < n) {
       const unsigned d = (k[r] >> shift) & (RS_RADIX - 1);
-      const unsigned dst = whist[w][d] + rank[r];
-      kout[dst] = k[r];
-      vout[dst] = v[r];
+      const unsigned slot = dstart[d] + whist[w][d] + rank[r];
+      sk[slot] = k[r];
+      sv[slot] = v[r];
     }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < cnt; i += RS_THREADS) {
+    const uint32_t kk = sk[i];
+    const unsigned d = (kk >> shift) & (RS_RADIX - 1);
+    const unsigned dst = gofs[d] + (unsigned)i - dstart[d];
+    kout[dst] = kk;
+    vout[dst] = sv[i];
   }
 }
 
@@ -182,12 +217,12 @@ static int exclusive_scan(gc_ctx *ctx, unsigned *a, long long n) {
   return GC_OK;
 }
 
-int gc_radix_sort_pairs(gc_ctx *ctx, const uint32_t *keys_in, const uint32_t *vals_in, int64_t n, int bits,
-                        uint32_t **keys_out, uint32_t **vals_out) {
+// Key/value ping-pong buffers and digit histograms for n items (grown, never shrunk).
+static int ensure_sort_scratch(gc_ctx *ctx, int64_t n) {
   int s = gc_ensure_particle_scratch(ctx, (size_t)n);
   if (s) return s;
-  const int ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
-  const size_t hn = (size_t)ntiles * RS_RADIX;
+  const size_t ntiles = (ctx->pcap + RS_TILE - 1) / RS_TILE;  // sized for the scratch capacity
+  const size_t hn = ntiles * RS_RADIX;
   if (ctx->hist_cap < hn) {
     GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     cudaFree(ctx->hist);
@@ -198,6 +233,21 @@ int gc_radix_sort_pairs(gc_ctx *ctx, const uint32_t *keys_in, const uint32_t *va
     GC_CUDA(ctx, cudaMalloc(&ctx->hist_aux, ((hn + SC_TILE - 1) / SC_TILE + 32) * sizeof(unsigned)));
     ctx->hist_cap = hn;
   }
+  return GC_OK;
+}
+
+extern "C" int gc_pm_reserve(gc_ctx *ctx, int64_t n) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  return n > 0 ? ensure_sort_scratch(ctx, n) : GC_OK;
+}
+
+int gc_radix_sort_pairs(gc_ctx *ctx, const uint32_t *keys_in, const uint32_t *vals_in, int64_t n, int bits,
+                        uint32_t **keys_out, uint32_t **vals_out) {
+  int s = ensure_sort_scratch(ctx, n);
+  if (s) return s;
+  const int ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
+  const size_t hn = (size_t)ntiles * RS_RADIX;
   const uint32_t *kin = keys_in, *vin = vals_in;
   // ping-pong between (keys, vals) and (keys2, vals2); never write into the caller's input
   uint32_t *ka = ctx->keys, *va = ctx->vals, *kb = ctx->keys2, *vb = ctx->vals2;
@@ -269,11 +319,26 @@ extern "C" int gc_sort_keys(gc_ctx *ctx, const uint32_t *keys, int64_t n, uint32
   return GC_OK;
 }
 
-template <typename T>
-__global__ void k_gather_perm(const T *__restrict__ in, T *__restrict__ out, const uint32_t *__restrict__ perm,
-                              long long n) {
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
-    out[p] = in[perm[p]];
+// All arrays of a particle set permuted in one pass: perm is read once and the
+// nine gathers of a particle are independent loads.
+struct PermSet {
+  const float *fin[7];
+  float *fout[7];
+  const int32_t *iin[2];
+  int32_t *iout[2];
+};
+
+__global__ void __launch_bounds__(256)
+    k_permute_set(PermSet s, const uint32_t *__restrict__ perm, long long n) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const uint32_t q = perm[p];
+#pragma unroll
+    for (int a = 0; a < 7; ++a)
+      if (s.fin[a]) s.fout[a][p] = __ldg(s.fin[a] + q);
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+      if (s.iin[a]) s.iout[a][p] = __ldg(s.iin[a] + q);
+  }
 }
 
 extern "C" int gc_pm_sort(gc_ctx *ctx, const gc_particles *in, const gc_particles *out) {
@@ -293,20 +358,100 @@ extern "C" int gc_pm_sort(gc_ctx *ctx, const gc_particles *in, const gc_particle
   GC_LAUNCH_CHECK(ctx, "cell keys");
   uint32_t *ko, *vo;
   if ((s = gc_radix_sort_pairs(ctx, ctx->keys2, ctx->vals2, n, key_bits(ctx->G), &ko, &vo))) return s;
+  PermSet ps;
   const float *fin[7] = {in->x, in->y, in->z, in->vx, in->vy, in->vz, in->m};
   float *fout[7] = {out->x, out->y, out->z, out->vx, out->vy, out->vz, out->m};
   for (int a = 0; a < 7; ++a) {
-    if (!fin[a]) continue;
-    GC_REQUIRE(ctx, fout[a] && fout[a] != fin[a], "gc_pm_sort: output array %d missing or aliases its input", a);
-    gc_launch(ctx, GK_PERMUTE, k_gather_perm<float>, dim3(nb), dim3(256), 0, fin[a], fout[a], vo, (long long)n);
+    GC_REQUIRE(ctx, !fin[a] || (fout[a] && fout[a] != fin[a]), "gc_pm_sort: output array %d missing or aliases its input", a);
+    ps.fin[a] = fin[a];
+    ps.fout[a] = fin[a] ? fout[a] : nullptr;
   }
   const int32_t *iin[2] = {in->gid, in->pid};
   int32_t *iout[2] = {out->gid, out->pid};
   for (int a = 0; a < 2; ++a) {
-    if (!iin[a]) continue;
-    GC_REQUIRE(ctx, iout[a] && iout[a] != iin[a], "gc_pm_sort: id array %d missing or aliases its input", a);
-    gc_launch(ctx, GK_PERMUTE, k_gather_perm<int32_t>, dim3(nb), dim3(256), 0, iin[a], iout[a], vo, (long long)n);
+    GC_REQUIRE(ctx, !iin[a] || (iout[a] && iout[a] != iin[a]), "gc_pm_sort: id array %d missing or aliases its input", a);
+    ps.iin[a] = iin[a];
+    ps.iout[a] = iin[a] ? iout[a] : nullptr;
   }
+  gc_launch(ctx, GK_PERMUTE, k_permute_set, dim3(nb), dim3(256), 0, ps, vo, (long long)n);
   GC_LAUNCH_CHECK(ctx, "permute");
+  return GC_OK;
+}
+
+// ---- reference layout <-> engine layout ---------------------------------------
+__global__ void __launch_bounds__(256)
+    k_pm_import(const float *__restrict__ pos, const float *__restrict__ vel, const float *__restrict__ m,
+                const int32_t *__restrict__ gid, double ox, double oy, double oz, gc_particles o, long long n) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    o.x[p] = (float)((double)pos[3 * p] - ox);
+    o.y[p] = (float)((double)pos[3 * p + 1] - oy);
+    o.z[p] = (float)((double)pos[3 * p + 2] - oz);
+    o.vx[p] = vel[3 * p];
+    o.vy[p] = vel[3 * p + 1];
+    o.vz[p] = vel[3 * p + 2];
+    o.m[p] = m[p];
+    if (o.gid) o.gid[p] = gid ? gid[p] : 0;
+    if (o.pid) o.pid[p] = (int32_t)p;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_pm_export(gc_particles s, double ox, double oy, double oz, float *__restrict__ pos, float *__restrict__ vel,
+                float *__restrict__ m, int32_t *__restrict__ gid, long long n, unsigned *__restrict__ status) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const long long q = s.pid[p];
+    if (q < 0 || q >= n) {
+      atomicOr(status, GC_FLAG_BAD_PID);
+      continue;
+    }
+    if (pos) {
+      pos[3 * q] = (float)((double)s.x[p] + ox);
+      pos[3 * q + 1] = (float)((double)s.y[p] + oy);
+      pos[3 * q + 2] = (float)((double)s.z[p] + oz);
+    }
+    if (vel) {
+      vel[3 * q] = s.vx[p];
+      vel[3 * q + 1] = s.vy[p];
+      vel[3 * q + 2] = s.vz[p];
+    }
+    if (m) m[q] = s.m[p];
+    if (gid) gid[q] = s.gid ? s.gid[p] : 0;
+  }
+}
+
+extern "C" int gc_pm_import(gc_ctx *ctx, const float *pos, const float *vel, const float *m, const int32_t *gid,
+                            const double origin[3], const gc_particles *out) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, out && origin, "gc_pm_import: NULL particle set or origin");
+  const int64_t n = out->n;
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  if (n == 0) return GC_OK;
+  GC_REQUIRE(ctx, pos && vel && m, "gc_pm_import: NULL input");
+  GC_REQUIRE(ctx, out->x && out->y && out->z && out->vx && out->vy && out->vz && out->m,
+             "gc_pm_import: output arrays required");
+  unsigned nb = gc_blocks(n, 256);
+  if (nb > 152u * 32u) nb = 152u * 32u;
+  gc_launch(ctx, GK_COPY, k_pm_import, dim3(nb), dim3(256), 0, pos, vel, m, gid, origin[0], origin[1], origin[2], *out,
+            (long long)n);
+  GC_LAUNCH_CHECK(ctx, "import");
+  return GC_OK;
+}
+
+extern "C" int gc_pm_export(gc_ctx *ctx, const gc_particles *p, const double origin[3], float *pos, float *vel,
+                            float *m_out, int32_t *gid_out) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, p && origin, "gc_pm_export: NULL particle set or origin");
+  const int64_t n = p->n;
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  if (n == 0) return GC_OK;
+  GC_REQUIRE(ctx, p->pid, "gc_pm_export: pid required");
+  GC_REQUIRE(ctx, !pos || (p->x && p->y && p->z), "gc_pm_export: positions missing");
+  GC_REQUIRE(ctx, !vel || (p->vx && p->vy && p->vz), "gc_pm_export: velocities missing");
+  GC_REQUIRE(ctx, !m_out || p->m, "gc_pm_export: masses missing");
+  unsigned nb = gc_blocks(n, 256);
+  if (nb > 152u * 32u) nb = 152u * 32u;
+  gc_launch(ctx, GK_COPY, k_pm_export, dim3(nb), dim3(256), 0, *p, origin[0], origin[1], origin[2], pos, vel, m_out,
+            gid_out, (long long)n, ctx->dstatus);
+  GC_LAUNCH_CHECK(ctx, "export");
   return GC_OK;
 }

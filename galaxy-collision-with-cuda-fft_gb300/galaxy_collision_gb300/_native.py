@@ -23,6 +23,7 @@ GC_ERR_STATE = -6
 
 GC_FLAG_NONFINITE_POS = 0x1
 GC_FLAG_NONFINITE_RHO = 0x2
+GC_FLAG_BAD_PID = 0x4
 GC_MG_FUSED_SWEEP = 0x1
 GC_MG_FIXED_CYCLES = 0x2
 GC_STEP_GRAD_GRID = 0x1
@@ -122,6 +123,9 @@ _PROTOS = {
     "gc_project_ngp": (C.c_int, [_ctxp, _vp, _vp, _vp, _i64, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_int, _vp]),
     "gc_pm_sort": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(Particles)]),
+    "gc_pm_reserve": (C.c_int, [_ctxp, _i64]),
+    "gc_pm_import": (C.c_int, [_ctxp, _vp, _vp, _vp, _vp, C.POINTER(C.c_double), C.POINTER(Particles)]),
+    "gc_pm_export": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(C.c_double), _vp, _vp, _vp, _vp]),
     "gc_pm_step": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(StepParams), C.POINTER(StepStats)]),
     "gc_pm_potential": (_vp, [_ctxp]),
     "gc_pm_copy_potential": (C.c_int, [_ctxp, _vp]),

@@ -40,7 +40,8 @@ class StepResult:
 class PMEngine:
     def __init__(self, grid_size: int, dx: float, grav: float = 1.0, *, origin=(0.0, 0.0, 0.0), tol: float = 1e-6,
                  max_cycles: int = 50, pre_sweeps: int = 2, post_sweeps: int = 2, coarse_sweeps: int = 40,
-                 fixed_point_bits: int = 52, sort_every: int = 20, grad_grid: bool = True, fixed_cycles: int = 0):
+                 fixed_point_bits: int = 52, sort_every: int = 20, grad_grid: bool = True, fixed_cycles: int = 0,
+                 max_particles: int = 0):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
         self.grav = float(grav)
@@ -71,41 +72,120 @@ class PMEngine:
         self.alt = None
         self.last = None
         self._graphs = {}
+        if max_particles > 0:  # allocate the particle sets and sort scratch now, not in load
+            self.reserve(max_particles)
+
+    def reserve(self, n: int) -> None:
+        """Allocate both particle sets for n particles and the context's sort
+        scratch, so that load(n particles) allocates nothing."""
+        n = int(n)
+        if self.cur is None or self.cur["x"].numel() != n:
+            self.cur = self._alloc(n)
+            self.alt = self._alloc(n)
+        self.ctx.call("gc_pm_reserve", n, what="gc_pm_reserve")
 
     # -- state ------------------------------------------------------------------
+    @staticmethod
+    def _stride(n: int) -> int:
+        return (n + 63) // 64 * 64  # every array of a set starts on a 256-byte boundary
+
     def _alloc(self, n: int):
+        """One particle set: the 9 arrays as slices of one device block (so the
+        block can also stage interleaved N x 3 arrays for import and export)."""
         dev = torch.device("cuda", torch.cuda.current_device())
-        f = {k: torch.empty(n, dtype=torch.float32, device=dev) for k in _FLOAT_FIELDS}
-        f.update({k: torch.empty(n, dtype=torch.int32, device=dev) for k in _INT_FIELDS})
+        st = self._stride(n)
+        blk = torch.empty(9 * st, dtype=torch.float32, device=dev)
+        f = {k: blk[i * st:i * st + n] for i, k in enumerate(_FLOAT_FIELDS)}
+        f.update({k: blk[(7 + i) * st:(7 + i) * st + n].view(torch.int32) for i, k in enumerate(_INT_FIELDS)})
+        f["_block"] = blk
         return f
 
+    def _origin_c(self):
+        return (C.c_double * 3)(*[float(v) for v in self.origin])
+
     def load(self, pos, vel, mass, gid=None, *, sort: bool = True, non_blocking: bool = False) -> None:
-        """Load particles (host or device arrays, physical coordinates) into the engine."""
+        """Load particles in the reference's layout (pos and vel N x 3 in physical
+        coordinates, mass N, gid N or None; host or device arrays) into the engine.
+        Host arrays are copied into the spare particle set (asynchronously when
+        they are pinned) and split on the device by gc_pm_import."""
         pos_t = torch.as_tensor(pos)
         n = int(pos_t.shape[0])
         if n <= 0:
             raise ValueError("need at least one particle")
+        if tuple(pos_t.shape) != (n, 3):
+            raise ValueError(f"pos must be N x 3, got {tuple(pos_t.shape)}")
         self.n = n
-        self.cur = self._alloc(n)
-        self.alt = self._alloc(n)
+        if self.cur is None or self.cur["x"].numel() != n:
+            self.cur = self._alloc(n)
+            self.alt = self._alloc(n)
         dev = self.cur["x"].device
-        pos64 = torch.as_tensor(pos, dtype=torch.float64) if not torch.is_tensor(pos) else pos
-        org = torch.as_tensor(self.origin, dtype=pos64.dtype, device=pos64.device)
-        rel = (pos64 - org).to(torch.float32)
-        vel_t = torch.as_tensor(vel).to(torch.float32)
-        for i, k in enumerate(("x", "y", "z")):
-            self.cur[k].copy_(rel[:, i].contiguous().to(dev, non_blocking=non_blocking))
-        for i, k in enumerate(("vx", "vy", "vz")):
-            self.cur[k].copy_(vel_t[:, i].contiguous().to(dev, non_blocking=non_blocking))
-        self.cur["m"].copy_(torch.as_tensor(mass).to(torch.float32).to(dev, non_blocking=non_blocking))
-        if gid is None:
-            self.cur["gid"].zero_()
-        else:
-            self.cur["gid"].copy_(torch.as_tensor(gid).to(torch.int32).to(dev, non_blocking=non_blocking))
-        self.cur["pid"].copy_(torch.arange(n, dtype=torch.int32, device=dev))
+        st = self._stride(n)
+        stage = self.alt["_block"]
+        origin = self._origin_c()
+        if pos_t.dtype == torch.float64:  # subtract the origin in f64 first, as the reference's f64 inputs allow
+            pos_t = (pos_t - torch.as_tensor(self.origin, dtype=torch.float64, device=pos_t.device)).to(torch.float32)
+            origin = (C.c_double * 3)(0.0, 0.0, 0.0)
+
+        def staged(a, off, shape, dtype):
+            t = torch.as_tensor(a)
+            if t.device == dev and t.dtype == dtype and t.is_contiguous():
+                return t
+            dst = stage[off:off + t.numel()].view(dtype).view(shape)
+            if t.device.type == "cpu":
+                t = t.to(dtype)
+                dst.copy_(t, non_blocking=non_blocking or t.is_pinned())
+            else:
+                dst.copy_(t.to(dtype))
+            return dst
+
+        pos_d = staged(pos_t, 0, (n, 3), torch.float32)
+        vel_d = staged(vel, 3 * st, (n, 3), torch.float32)
+        m_d = staged(mass, 6 * st, (n,), torch.float32)
+        gid_d = None if gid is None else staged(gid, 7 * st, (n,), torch.int32)
+        out = self._struct(self.cur)
+        self.ctx.call("gc_pm_import", pos_d.data_ptr(), vel_d.data_ptr(), m_d.data_ptr(),
+                      None if gid_d is None else gid_d.data_ptr(), origin, C.byref(out), what="gc_pm_import")
         self.state = "synced"
+        self.steps_since_sort = 0
+        self._graphs = {}
         if sort:
             self.sort()
+
+    def export(self, pos=None, vel=None, mass=None, gid=None):
+        """The state in the original particle order and the reference's layout:
+        pos (N x 3 f32, physical coordinates), vel (N x 3 f32), mass, gid, written
+        into the given tensors (host, pinned host or device); only the given ones
+        are written, or all four into new host tensors when none is given.
+        gc_pm_export scatters by pid into the spare particle set (or straight into
+        device outputs); host outputs are filled by one copy each, asynchronous
+        when pinned. Velocities are those of the current state (staggered by half
+        a step while the engine is open)."""
+        n = self.n
+        st = self._stride(n)
+        stage = self.alt["_block"]
+        dev = self.cur["x"].device
+        spec = [(pos, 0, (n, 3), torch.float32), (vel, 3 * st, (n, 3), torch.float32),
+                (mass, 6 * st, (n,), torch.float32), (gid, 7 * st, (n,), torch.int32)]
+        want_all = all(t is None for t, _, _, _ in spec)
+        outs, ptrs = [], []
+        for t, off, shape, dtype in spec:
+            if t is None:
+                if not want_all:
+                    outs.append((None, None))
+                    ptrs.append(None)
+                    continue
+                t = torch.empty(shape, dtype=dtype)
+            if tuple(t.shape) != shape or t.dtype != dtype:
+                raise ValueError(f"export output must be {shape} {dtype}, got {tuple(t.shape)} {t.dtype}")
+            direct = t.device == dev and t.is_contiguous()
+            outs.append((t, None if direct else stage[off:off + t.numel()].view(dtype).view(shape)))
+            ptrs.append(t.data_ptr() if direct else outs[-1][1].data_ptr())
+        src = self._struct(self.cur)
+        self.ctx.call("gc_pm_export", C.byref(src), self._origin_c(), *ptrs, what="gc_pm_export")
+        for t, s in outs:
+            if t is not None and s is not None:
+                t.copy_(s, non_blocking=t.is_pinned())
+        return tuple(t for t, _ in outs)
 
     def _struct(self, f) -> _native.Particles:
         p = _native.Particles()

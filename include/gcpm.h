@@ -45,6 +45,7 @@ enum gc_status_code {
 /* Device status bits, OR-ed by kernels into a per-context word (gc_status). */
 #define GC_FLAG_NONFINITE_POS 0x1u  /* a particle position was NaN/Inf: it deposited nothing */
 #define GC_FLAG_NONFINITE_RHO 0x2u  /* the density handed to the solver had NaN/Inf */
+#define GC_FLAG_BAD_PID 0x4u        /* gc_pm_export met a pid outside [0, n): that particle was skipped */
 
 /* gc_mg_params.flags: relax the finest level with the streaming sweep (one
  * red+black sweep per pass through shared memory, ping-pong buffers, the
@@ -257,6 +258,28 @@ int gc_project_ngp(gc_ctx *ctx, const float *pa, const float *pb, const float *m
 /* Stable-sort the particles by cell key and write the permuted set to out
  * (every non-NULL array of in is permuted into the matching array of out). */
 int gc_pm_sort(gc_ctx *ctx, const gc_particles *in, const gc_particles *out);
+
+/* Allocate the sort scratch of the context for n particles now (keys, values,
+ * digit histograms), so that the first gc_pm_sort allocates nothing. Optional. */
+int gc_pm_reserve(gc_ctx *ctx, int64_t n);
+
+/* Fill the engine's particle arrays from the reference's interleaved layout:
+ * pos and vel are N x 3 f32 in physical coordinates, as ParticleState holds them
+ * after from_numpy (data.py:84-113, ic.py:386-405); m is N f32; gid may be NULL
+ * (zeros). Writes out->x = f32((double)pos[3i] - origin[0]) (grid-origin
+ * coordinates), the velocities and masses as given, out->pid = i. All pointers
+ * are device pointers; stream-ordered, no synchronisation. */
+int gc_pm_import(gc_ctx *ctx, const float *pos, const float *vel, const float *m, const int32_t *gid,
+                 const double origin[3], const gc_particles *out);
+
+/* The inverse, in the original particle order: for every i, with q = p->pid[i],
+ * pos[3q+c] = f32((double)x_c[i] + origin[c]), vel[3q+c] = v_c[i], m_out[q],
+ * gid_out[q] (each output may be NULL; p->pid is required). Replaces
+ * ParticleState.to_numpy (data.py:84-113) on the engine's sorted state. A pid
+ * outside [0, n) is skipped and raises GC_FLAG_BAD_PID. Device pointers;
+ * stream-ordered. */
+int gc_pm_export(gc_ctx *ctx, const gc_particles *p, const double origin[3], float *pos, float *vel, float *m_out,
+                 int32_t *gid_out);
 
 /* One force evaluation of the fused chain plus the kicks/drift of the mode:
  * int64 fixed-point deposit, moments and 4 pi G h^2 rho in one pass, FP64

@@ -95,7 +95,7 @@ def test_pm_sort_permutes_all_arrays(cuda):
     eng = PMEngine(G, dx, sort_every=0)
     eng.load(pos, vel, mass, gid, sort=True)
     perm = pm.stable_sort_perm(pm.cell_keys(pos, dx, G))
-    cur = {k: v.cpu().numpy() for k, v in eng.cur.items()}
+    cur = {k: v.cpu().numpy() for k, v in eng.cur.items() if not k.startswith("_")}
     np.testing.assert_array_equal(cur["pid"], perm.astype(np.int32))
     np.testing.assert_array_equal(cur["x"], pos[perm, 0])
     np.testing.assert_array_equal(cur["vz"], vel[perm, 2])
@@ -324,3 +324,48 @@ def test_kdk_step_bit_identical_to_inline_loop(cuda):  # tests/test_integrator.p
         kick(p2.vel_x, p2.vel_y, p2.vel_z, *acc2, n, dt / 2)
     for a, b in zip(p1.fields()[:6], p2.fields()[:6]):
         np.testing.assert_array_equal(a.to_numpy(), b.to_numpy())
+
+
+def test_import_export_round_trip(cuda):
+    """gc_pm_import splits the reference's N x 3 layout into the engine's arrays
+    (origin subtracted in f64); gc_pm_export writes them back in the original
+    order after sorts and steps, equal to state_arrays."""
+    from galaxy_collision_gb300.engine import PMEngine
+
+    G, dx = 32, 0.5
+    origin = (-8.0, -8.0, -8.0)
+    rng = np.random.default_rng(12)
+    n = 20011
+    pos = rng.uniform(-7.0, 7.0, size=(n, 3)).astype(np.float32)
+    vel = rng.normal(size=(n, 3)).astype(np.float32)
+    mass = rng.uniform(0.5, 1.5, size=n).astype(np.float32) / n
+    gid = rng.integers(0, 3, size=n).astype(np.int32)
+    eng = PMEngine(G, dx, origin=origin, sort_every=3)
+    eng.load(pos, vel, mass, gid, sort=True)
+    rel = (pos.astype(np.float64) - np.asarray(origin)).astype(np.float32)
+    cur = {k: eng.cur[k].cpu().numpy() for k in ("x", "y", "z", "vx", "m", "gid", "pid")}
+    pid = cur["pid"]
+    np.testing.assert_array_equal(np.sort(pid), np.arange(n))
+    np.testing.assert_array_equal(cur["x"], rel[pid, 0])
+    np.testing.assert_array_equal(cur["z"], rel[pid, 2])
+    np.testing.assert_array_equal(cur["vx"], vel[pid, 0])
+    np.testing.assert_array_equal(cur["m"], mass[pid])
+    np.testing.assert_array_equal(cur["gid"], gid[pid])
+    p, v, m, g = eng.export()
+    back = (rel.astype(np.float64) + np.asarray(origin)).astype(np.float32)
+    np.testing.assert_array_equal(p.numpy(), back)
+    np.testing.assert_array_equal(v.numpy(), vel)
+    np.testing.assert_array_equal(m.numpy(), mass)
+    np.testing.assert_array_equal(g.numpy(), gid)
+    eng.prime(0.01)
+    for _ in range(7):  # crosses two re-sorts
+        eng.advance(0.01)
+    eng.synchronize(0.01)
+    pp = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+    vd = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    eng.export(pp, vd)
+    torch.cuda.synchronize()
+    ps, vs, _, _ = eng.state_arrays(physical=True)
+    np.testing.assert_array_equal(pp.numpy(), ps.to(torch.float32).cpu().numpy())
+    np.testing.assert_array_equal(vd.cpu().numpy(), vs.cpu().numpy())
+    assert eng.ctx.status() & 0x4 == 0
