@@ -36,7 +36,8 @@ enum {
   GC_S_GRIDPE = 6,   // Sum b0*phi (engine grid energy, h^2 4 pi G units)
   GC_S_MASS_PM = 7,  // engine: total density-mass of its particles
   GC_S_QEXP_PM = 8,  // engine: quantum exponent
-  GC_S_NSLOTS = 64
+  GC_S_FIN_TMP = 128, // [128, 256): chunk partials of gc_finalize
+  GC_S_NSLOTS = 256
 };
 
 // Kernel ids for launch counting and event timing (gc_profile_*).
@@ -85,7 +86,7 @@ struct gc_ctx {
   double *red;          // reduction scratch (block partials)
   size_t red_cap;       // doubles in red
   double *dmom;         // 10 moments
-  double *dsmall;       // 64 device scalars, see GC_S_* below
+  double *dsmall;       // GC_S_NSLOTS device scalars, see GC_S_* below
   double *hsmall;       // pinned host mirror of dsmall
   unsigned *dstatus;    // device status word
   double *ddiag;        // 16 doubles for diagnostics
@@ -107,7 +108,8 @@ struct gc_ctx {
   // warm-start hook (coarse history of the potential on the (G/2)^3 grid)
   struct gc_ws *ws;     // attached network (learned mode), not owned
   int ws_mode;          // GC_WS_PLAIN / GC_WS_LEARNED / GC_WS_EXTRAPOLATE
-  int ws_track;         // maintain the coarse history
+  int ws_track;         // maintain the warm-start history (previous potential)
+  int ws_coarse;        // also the coarse history and network features (learned mode or track = 1)
   int ws_hist;          // solves recorded in the history (0, 1, 2+)
   void *ws_record;      // one-shot f16 [5][R^3] sample destination
   int ws_skip;          // this step leaves the history alone (PRIME after CLOSE)

@@ -128,22 +128,37 @@ void gc_mg_free(gc_ctx *ctx) {
 // ------------------------------------------------------------------------------
 // reductions: per-block partials written in a fixed order, then one block sums them
 // ------------------------------------------------------------------------------
-// Sum nparts rows of NV partials into dst[0..NV) (single block, fixed order).
-__global__ void k_finalize(const double *__restrict__ parts, int nparts, int nv, double *__restrict__ dst,
-                           int accumulate) {
-  __shared__ double sh[32];
-  for (int v = 0; v < nv; ++v) {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += parts[(size_t)i * nv + v];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      double x = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-      if (threadIdx.x == 0) dst[v] = accumulate ? dst[v] + x : x;
-    }
-    __syncthreads();
+// Sum nparts rows of nv partials into dst[0..nv), deterministically (a fixed
+// association for given nparts and nv). FP64 runs at a small fraction of the
+// f32 rate on this GPU, so the adds are spread: warp w of one block sums value
+// w (lanes take rows lane, lane + 32, ...); a long single-value list is first
+// cut into GC_FIN_CHUNKS contiguous chunks summed by as many blocks.
+#define GC_FIN_NV 32
+#define GC_FIN_CHUNKS 128
+__global__ void __launch_bounds__(1024)
+    k_fin_warps(const double *__restrict__ parts, int nparts, int nv, double *__restrict__ dst) {
+  const int lane = threadIdx.x & 31, v = threadIdx.x >> 5;
+  if (v >= nv) return;
+  double s = 0.0;
+  for (int i = lane; i < nparts; i += 32) s += parts[(size_t)i * nv + v];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) dst[v] = s;
+}
+
+__global__ void __launch_bounds__(256)
+    k_fin_chunks(const double *__restrict__ parts, int nparts, double *__restrict__ out) {
+  __shared__ double sh[8];
+  const int per = (nparts + gridDim.x - 1) / gridDim.x;
+  const int i0 = blockIdx.x * per, i1 = min(nparts, i0 + per);
+  double s = 0.0;
+  for (int i = i0 + (int)threadIdx.x; i < i1; i += 256) s += parts[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0.0;
+    for (int w = 0; w < 8; ++w) x += sh[w];
+    out[blockIdx.x] = x;
   }
 }
 
@@ -944,7 +959,14 @@ static int vcycle(gc_ctx *ctx, const gc_mg_params *p) {
 }
 
 int gc_finalize(gc_ctx *ctx, const double *parts, int nparts, int nv, double *dst) {
-  gc_launch(ctx, GK_REDUCE, k_finalize, dim3(1), dim3(1024), 0, parts, nparts, nv, dst, 0);
+  GC_REQUIRE(ctx, nv >= 1 && nv <= GC_FIN_NV, "gc_finalize: %d values per row (at most %d)", nv, GC_FIN_NV);
+  if (nv == 1 && nparts > 32 * GC_FIN_CHUNKS) {
+    double *tmp = ctx->dsmall + GC_S_FIN_TMP;
+    gc_launch(ctx, GK_REDUCE, k_fin_chunks, dim3(GC_FIN_CHUNKS), dim3(256), 0, parts, nparts, tmp);
+    gc_launch(ctx, GK_REDUCE, k_fin_warps, dim3(1), dim3(32), 0, (const double *)tmp, GC_FIN_CHUNKS, 1, dst);
+  } else {
+    gc_launch(ctx, GK_REDUCE, k_fin_warps, dim3(1), dim3(32 * nv), 0, parts, nparts, nv, dst);
+  }
   GC_LAUNCH_CHECK(ctx, "finalize");
   return GC_OK;
 }
@@ -1070,7 +1092,7 @@ static int moments_rho_async(gc_ctx *ctx, const float *rho) {
   if (s) return s;
   gc_launch(ctx, GK_MOMENTS, k_moments_rho, dim3(nb), dim3(256), 0, rho, ctx->G, ctx->dx, ctx->red, ctx->dstatus);
   GC_LAUNCH_CHECK(ctx, "moments");
-  gc_launch(ctx, GK_REDUCE, k_finalize, dim3(1), dim3(1024), 0, ctx->red, (int)nb, 10, ctx->dmom, 0);
+  if ((s = gc_finalize(ctx, ctx->red, (int)nb, 10, ctx->dmom))) return s;
   GC_LAUNCH_CHECK(ctx, "moments finalize");
   return GC_OK;
 }

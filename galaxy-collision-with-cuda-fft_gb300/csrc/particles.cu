@@ -476,23 +476,25 @@ int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, co
 // ------------------------------------------------------------------------------
 // q -> rho / b, zero q, exact integer column moments, ||b||^2
 // ------------------------------------------------------------------------------
-// One warp per (i,j) column. Column sums S0 = sum q, S1 = sum q k and
-// S2 = sum q k^2 are exact in integers (S2 split at bit 32), combined across
-// columns in FP64. Partials per block: 10 moments + ||b||^2.
+// One warp per (i,j) column, persistent over the columns. Column sums S0 = sum q,
+// S1 = sum q k and S2 = sum q k^2 are exact in integers (S2 split at bit 32),
+// combined across columns in FP64 in a fixed order. Partials per block: 10
+// moments + ||b||^2.
 __global__ void __launch_bounds__(256)
     k_convert_q(long long *__restrict__ qg, int G, double dx, const double *__restrict__ qexp, float *__restrict__ rho,
                 float *__restrict__ b, double bfac, double *__restrict__ parts) {
   __shared__ double wsum[8][11];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const long long col = (long long)blockIdx.x * 8 + wid;
   const int E = (int)(*qexp);
   const float qinv = ldexpf(1.0f, E);
   const float bscale = (float)(ldexp(1.0, E) * bfac);
+  const double msc = ldexp(1.0, E) * dx * dx * dx;  // mass of one quantum
   double v[11];
 #pragma unroll
   for (int t = 0; t < 11; ++t) v[t] = 0.0;
-  if (col < (long long)G * G) {
-    const int i = (int)(col / G), j = (int)(col % G);
+  const long long ncols = (long long)G * G;
+  for (long long col = (long long)blockIdx.x * 8 + wid; col < ncols; col += (long long)gridDim.x * 8) {
+    const int i = (int)(col / G), j = (int)(col - (long long)i * G);
     long long *p = qg + (size_t)col * G;
     float *rp = rho ? rho + (size_t)col * G : nullptr;
     float *bp = b ? b + (size_t)col * G : nullptr;
@@ -531,18 +533,17 @@ __global__ void __launch_bounds__(256)
       S2l += __shfl_down_sync(0xffffffffu, S2l, o);
       bb += __shfl_down_sync(0xffffffffu, bb, o);
     }
-    if (lane == 0) {
+    if (lane == 0) v[10] += (double)bb;
+    if (lane == 0 && (S0 | S1 | S2h | (long long)S2l) != 0) {
       const double d0 = (double)S0, d1 = (double)S1, d2 = (double)S2h * 4294967296.0 + (double)S2l;
-      const double msc = ldexp(1.0, E) * dx * dx * dx;  // mass of one quantum
       const double x = i * dx, y = j * dx;
       const double m0 = d0 * msc, m1 = d1 * msc * dx, m2 = d2 * msc * dx * dx;
-      v[0] = m0; v[1] = m0 * x; v[2] = m0 * y; v[3] = m1;
-      v[4] = m0 * x * x; v[5] = m0 * y * y; v[6] = m2;
-      v[7] = m0 * x * y; v[8] = m1 * x; v[9] = m1 * y;
-      v[10] = (double)bb;
+      v[0] += m0; v[1] += m0 * x; v[2] += m0 * y; v[3] += m1;
+      v[4] += m0 * x * x; v[5] += m0 * y * y; v[6] += m2;
+      v[7] += m0 * x * y; v[8] += m1 * x; v[9] += m1 * y;
     }
   }
-  // only lane 0 of each warp holds a column total: sum the 8 warps directly
+  // lane 0 of each warp holds the warp's totals: sum the 8 warps in order
   if (lane == 0) {
 #pragma unroll
     for (int t = 0; t < 11; ++t) wsum[wid][t] = v[t];
@@ -564,7 +565,8 @@ int gc_max_fixed_point_bits(const gc_ctx *ctx) {
 
 int gc_convert_q(gc_ctx *ctx, const double *qexp, float *rho_out, float *b_out) {
   const long long cols = (long long)ctx->G * ctx->G;
-  const unsigned nb = gc_blocks(cols, 8);
+  unsigned nb = gc_blocks(cols, 8);
+  if (nb > 152u * 3u) nb = 152u * 3u;  // persistent: 3 CTAs per SM (80 registers)
   int s = gc_ensure_red(ctx, (size_t)nb * 11);
   if (s) return s;
   const double bfac = 4.0 * M_PI * ctx->grav * ctx->dx * ctx->dx;

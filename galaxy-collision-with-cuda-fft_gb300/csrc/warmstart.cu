@@ -1418,10 +1418,10 @@ __global__ void __launch_bounds__(256) k_ws_features(const float *__restrict__ r
 }
 
 // Initial guess on every fine node: prev holds phi(n-2) on entry and phi(n-1)
-// on exit; hi/lo (phi(n-1) on entry) get + d(n-1) when extrapolating (and the
-// history allows it) and + s * trilinear(yc) when yc is given.
+// on exit; hi/lo (phi(n-1) on entry) get + d(n-1) when use_d (extrapolating,
+// with two solves in the history) and + s * trilinear(yc) when yc is given.
 __global__ void __launch_bounds__(128) k_ws_apply(const float *__restrict__ yc, const float *__restrict__ scal,
-                                                  int extrap, int G, float *__restrict__ hi, float *__restrict__ lo,
+                                                  int use_d, int G, float *__restrict__ hi, float *__restrict__ lo,
                                                   float *__restrict__ prev) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
   if (k >= G) return;
@@ -1429,7 +1429,7 @@ __global__ void __launch_bounds__(128) k_ws_apply(const float *__restrict__ yc, 
   const size_t v = ((size_t)i * G + j) * G + k;
   const float h = hi[v], l = lo[v];
   float corr = 0.0f;
-  if (extrap && scal[3] != 0.0f) corr = __fsub_rn(h, prev[v]);
+  if (use_d) corr = __fsub_rn(h, prev[v]);
   if (yc && scal[5] != 0.0f) {
     int i0[3];
     float f[3];
@@ -1536,6 +1536,10 @@ int gc_ws_pre_solve(gc_ctx *ctx, int warm, int mode) {
   const int R = ctx->G / 2;
   const size_t R3 = (size_t)R * R * R;
   unsigned nb = (unsigned)std::min<size_t>((R3 + 255) / 256, 1024);
+  // the coarse history and the network features: for the learned guess, for
+  // recording, or when tracking was asked for (the extrapolation needs neither)
+  const bool coarse = ctx->ws_coarse || ctx->ws_record;
+  if (coarse) {
   gc_launch(ctx, GK_WARMSTART, k_ws_coarsen, dim3((R + 63) / 64, R, R), dim3(64), 0, (const float *)ctx->b0, ctx->G,
             w.rho);
   gc_launch(ctx, GK_WARMSTART, k_ws_stats, dim3(nb), dim3(256), 0, (const float *)w.rho, (const float *)w.phi,
@@ -1546,6 +1550,7 @@ int gc_ws_pre_solve(gc_ctx *ctx, int warm, int mode) {
             (const float *)w.dlt, (const float *)w.ddl, (const float *)w.scal, ctx->ws_hist, R3, w.feat,
             (__half *)ctx->ws_record);
   GC_LAUNCH_CHECK(ctx, "warm-start features");
+  }
   if (!warm || ctx->ws_hist < 1) return GC_OK;
   const float *yc = nullptr;
   if (ctx->ws_mode == GC_WS_LEARNED && ctx->ws_hist >= 3) {
@@ -1562,9 +1567,9 @@ int gc_ws_pre_solve(gc_ctx *ctx, int warm, int mode) {
     ctx->prof.launches[GK_WARMSTART] += 18;
     yc = w.y;
   }
-  const int extrap = ctx->ws_mode != GC_WS_PLAIN;
+  const int use_d = ctx->ws_mode != GC_WS_PLAIN && ctx->ws_hist >= 2;
   gc_launch(ctx, GK_WARMSTART, k_ws_apply, dim3((ctx->G + 127) / 128, ctx->G, ctx->G), dim3(128), 0, yc,
-            (const float *)w.scal, extrap, ctx->G, ctx->hi, ctx->lo, w.prev);
+            (const float *)w.scal, use_d, ctx->G, ctx->hi, ctx->lo, w.prev);
   GC_LAUNCH_CHECK(ctx, "warm-start apply");
   return GC_OK;
 }
@@ -1572,6 +1577,10 @@ int gc_ws_pre_solve(gc_ctx *ctx, int warm, int mode) {
 int gc_ws_post_solve(gc_ctx *ctx) {
   if (!ctx->ws_track && !ctx->ws_record) return GC_OK;
   if (ctx->G % 2 || ctx->ws_skip) return GC_OK;
+  if (!ctx->ws_coarse && !ctx->ws_record) {
+    ctx->ws_hist = ctx->ws_hist < 3 ? ctx->ws_hist + 1 : 3;
+    return GC_OK;
+  }
   const WsViews w = ws_views(ctx);
   const int R = ctx->G / 2;
   gc_launch(ctx, GK_WARMSTART, k_ws_post, dim3((R + 63) / 64, R, R), dim3(64), 0, (const float *)ctx->hi, ctx->G,
@@ -1591,17 +1600,21 @@ extern "C" int gc_pm_set_warmstart(gc_ctx *ctx, gc_ws *ws, int mode, int track) 
              "gc_pm_set_warmstart: the coarse history needs an even grid size");
   GC_REQUIRE(ctx, !ws || ws->R == ctx->G / 2, "gc_pm_set_warmstart: network R=%d, grid needs R=%d", ws ? ws->R : 0,
              ctx->G / 2);
+  const int tr = (track || mode != GC_WS_PLAIN) ? 1 : 0;
+  const int coarse = (track || mode == GC_WS_LEARNED) ? 1 : 0;
+  // the history restarts when what it holds changes
+  if ((tr && !ctx->ws_track) || (coarse && !ctx->ws_coarse) || mode != ctx->ws_mode) ctx->ws_hist = 0;
   ctx->ws = ws;
   ctx->ws_mode = mode;
-  const int tr = (track || mode != GC_WS_PLAIN) ? 1 : 0;
-  if (tr && !ctx->ws_track) ctx->ws_hist = 0;
   ctx->ws_track = tr;
+  ctx->ws_coarse = coarse;
   return GC_OK;
 }
 
 extern "C" int gc_pm_record_sample(gc_ctx *ctx, void *out) {
   if (!ctx) return GC_ERR_ARG;
   GC_REQUIRE(ctx, ctx->G % 2 == 0, "gc_pm_record_sample: the coarse grid needs an even grid size");
+  GC_REQUIRE(ctx, ctx->ws_coarse, "gc_pm_record_sample: set the warm start with track = 1 first");
   ctx->ws_record = out;
   return GC_OK;
 }

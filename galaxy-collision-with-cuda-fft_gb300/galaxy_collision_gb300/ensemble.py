@@ -60,7 +60,7 @@ class Ensemble:
             icr = random_collision(rng, n, box / grid)
             e = PMEngine(grid, box / grid, grav=1.0, origin=(-box / 2.0,) * 3, tol=tol, sort_every=sort_every,
                          fixed_point_bits=40, fixed_cycles=fixed_cycles)
-            e.set_warmstart(warmstart, net=net if warmstart == "learned" else None, track=True)
+            e.set_warmstart(warmstart, net=net if warmstart == "learned" else None)
             e.load(icr.pos, icr.vel, icr.mass, icr.gid)
             self.engines.append(e)
             self.counts.append(n)

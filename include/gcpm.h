@@ -370,8 +370,10 @@ int gc_ws_plan_info(const gc_ws *ws, int layer, int kind, int *out);
  *   GC_WS_LEARNED     the extrapolation + the network's prediction of the next
  *                     second difference of the potential (R = G/2 grid, trilinear).
  * The multigrid always iterates to the same residual: only the start changes.
- * With track != 0 (implied by the non-plain modes) the context keeps the
- * history the extrapolation and the features need. G even. */
+ * The non-plain modes keep the previous potential; the learned mode, and any
+ * mode with track != 0, also keep the coarse (G/2) history and build the
+ * network features every solve (gc_pm_record_sample needs track != 0). A
+ * change of mode restarts the history. G even. */
 #define GC_WS_PLAIN 0
 #define GC_WS_LEARNED 1
 #define GC_WS_EXTRAPOLATE 2
