@@ -545,10 +545,8 @@ def _e2e(args, icr, make_engine, dt):
         eng.ctx.profile_reset()
         eng.ctx.profile(True)
     t0 = time.perf_counter()
-    eng.load(pos, vel, mass, gid, sort=False)  # pinned host arrays: staged H2D + gc_pm_import
-    mark("load")
-    eng.sort()
-    mark("sort")
+    eng.load(pos, vel, mass, gid, sort=True)  # pinned host arrays: staged H2D + gc_pm_import_sorted
+    mark("load+sort")
     if args.verbose:
         _log(args, "e2e load kernels (ms): " + ", ".join(f"{k} {v[2]:.2f}" for k, v in eng.ctx.kernel_stats().items()
                                                        if v[2] > 0))
@@ -572,7 +570,7 @@ def _e2e(args, icr, make_engine, dt):
     n = icr.n
     return {"value": n * args.steps / t, "unit": UNIT, "h2d_bytes_per_step": int(n * 32 / args.steps),
             "d2h_bytes_per_step": int((n * 24 + 12 * 8) / args.steps),
-            "note": "wall clock around load (pinned H2D of the reference layout + device split + cell sort), "
+            "note": "wall clock around load (pinned H2D of the reference layout, cell sort and gather into cell order), "
                     "prime, steps-1 advances, close with FP64 diagnostics, export in the original order + "
                     "pinned D2H of positions and velocities (the pinned buffers are mapped by one untimed transfer "
                     "before, as part of pinning)"}

@@ -739,14 +739,27 @@ __global__ void __launch_bounds__(1024) k_tail(const float *__restrict__ b_in, f
 // ------------------------------------------------------------------------------
 // Multipole Dirichlet faces (multigrid.py:261-295) evaluated in FP64 from the raw
 // moments (multigrid.py:378-389), written as double-float pairs.
-__global__ void k_faces(float *__restrict__ hi, float *__restrict__ lo, float *__restrict__ hi2,
-                        float *__restrict__ lo2, int G, double dx, double grav, const double *__restrict__ mom) {
-  const long long tot = 6LL * G * G;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= tot) return;
-  const int face = (int)(t / ((long long)G * G));
-  const int rem = (int)(t % ((long long)G * G));
-  const int u = rem / G, v = rem % G;
+__global__ void __launch_bounds__(256)
+    k_faces(float *__restrict__ hi, float *__restrict__ lo, float *__restrict__ hi2, float *__restrict__ lo2, int G,
+            double dx, double grav, const double *__restrict__ mom) {
+  // centre of mass and second moments about it, once per block (FP64 runs at a
+  // small fraction of the f32 rate: each face node keeps only its own terms)
+  __shared__ double sm[11];
+  if (threadIdx.x == 0) {
+    const double M = mom[0];
+    const double cx = M > 0.0 ? mom[1] / M : 0.0, cy = M > 0.0 ? mom[2] / M : 0.0, cz = M > 0.0 ? mom[3] / M : 0.0;
+    sm[0] = M; sm[1] = cx; sm[2] = cy; sm[3] = cz;
+    sm[4] = mom[4] - M * cx * cx; sm[5] = mom[5] - M * cy * cy; sm[6] = mom[6] - M * cz * cz;
+    sm[7] = mom[7] - M * cx * cy; sm[8] = mom[8] - M * cx * cz; sm[9] = mom[9] - M * cy * cz;
+    sm[10] = sm[4] + sm[5] + sm[6];
+  }
+  __syncthreads();
+  const int GG = G * G;  // 6 G^2 < 2^31 for G <= 1024
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 6 * GG) return;
+  const int face = t / GG;
+  const int rem = t - face * GG;
+  const int u = rem / G, v = rem - u * G;
   int i, j, k;
   switch (face) {
     case 0: i = 0; j = u; k = v; break;
@@ -756,20 +769,18 @@ __global__ void k_faces(float *__restrict__ hi, float *__restrict__ lo, float *_
     case 4: k = 0; i = u; j = v; break;
     default: k = G - 1; i = u; j = v; break;
   }
-  const double M = mom[0];
+  const double M = sm[0];
   double phi = 0.0;
   if (M > 0.0) {
-    const double cx = mom[1] / M, cy = mom[2] / M, cz = mom[3] / M;
-    const double sxx = mom[4] - M * cx * cx, syy = mom[5] - M * cy * cy, szz = mom[6] - M * cz * cz;
-    const double sxy = mom[7] - M * cx * cy, sxz = mom[8] - M * cx * cz, syz = mom[9] - M * cy * cz;
-    const double trs = sxx + syy + szz;
-    const double rx = i * dx - cx, ry = j * dx - cy, rz = k * dx - cz;
+    const double rx = i * dx - sm[1], ry = j * dx - sm[2], rz = k * dx - sm[3];
     const double d2 = rx * rx + ry * ry + rz * rz + 1e-12;
-    const double dd = sqrt(d2);
-    const double nx = rx / dd, ny = ry / dd, nz = rz / dd;
-    const double nsn = nx * nx * sxx + ny * ny * syy + nz * nz * szz + 2.0 * (nx * ny * sxy + nx * nz * sxz + ny * nz * syz);
-    const double quad = 3.0 * nsn - trs;
-    phi = -grav * (M / dd + quad / (2.0 * d2 * dd));
+    const double inv = 1.0 / sqrt(d2);
+    const double nx = rx * inv, ny = ry * inv, nz = rz * inv;
+    const double nsn = nx * nx * sm[4] + ny * ny * sm[5] + nz * nz * sm[6] +
+                       2.0 * (nx * ny * sm[7] + nx * nz * sm[8] + ny * nz * sm[9]);
+    const double quad = 3.0 * nsn - sm[10];
+    // Phi = -G (M/d + (3 n.S.n - tr S) / (2 d^3)), multigrid.py:261-295
+    phi = -grav * (M * inv + quad * (0.5 * inv * inv * inv));
   }
   const size_t c = ((size_t)i * G + j) * G + k;
   const float h = (float)phi;

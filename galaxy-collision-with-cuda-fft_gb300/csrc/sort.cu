@@ -455,3 +455,72 @@ extern "C" int gc_pm_export(gc_ctx *ctx, const gc_particles *p, const double ori
   GC_LAUNCH_CHECK(ctx, "export");
   return GC_OK;
 }
+
+// ---- import straight into cell order ---------------------------------------------
+// Keys from the interleaved physical positions (the origin subtracted in f64,
+// as gc_pm_import does), then every particle gathered from the interleaved
+// arrays at its sorted slot: one random read of 12 contiguous bytes per vector
+// instead of one per component, and no intermediate unsorted copy.
+__global__ void __launch_bounds__(256)
+    k_cell_keys_aos(const float *__restrict__ pos, double ox, double oy, double oz, long long n, float dx, int G,
+                    uint32_t *__restrict__ keys, uint32_t *__restrict__ iota) {
+  const uint32_t sentinel = (uint32_t)(G + 1) * (uint32_t)(G + 1) * (uint32_t)(G + 1);
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const float x = (float)((double)pos[3 * p] - ox);
+    const float y = (float)((double)pos[3 * p + 1] - oy);
+    const float z = (float)((double)pos[3 * p + 2] - oz);
+    CellPos c;
+    uint32_t key = sentinel;
+    if (gc_cell_of(x, y, z, dx, G, c))
+      key = ((uint32_t)(c.ix + 1) * (uint32_t)(G + 1) + (uint32_t)(c.iy + 1)) * (uint32_t)(G + 1) + (uint32_t)(c.iz + 1);
+    keys[p] = key;
+    iota[p] = (uint32_t)p;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_import_gather(const float *__restrict__ pos, const float *__restrict__ vel, const float *__restrict__ m,
+                    const int32_t *__restrict__ gid, double ox, double oy, double oz,
+                    const uint32_t *__restrict__ perm, gc_particles o, long long n) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const long long q = perm[p];
+    const float px = __ldg(pos + 3 * q), py = __ldg(pos + 3 * q + 1), pz = __ldg(pos + 3 * q + 2);
+    const float vx = __ldg(vel + 3 * q), vy = __ldg(vel + 3 * q + 1), vz = __ldg(vel + 3 * q + 2);
+    const float mm = __ldg(m + q);
+    const int32_t g = gid ? __ldg(gid + q) : 0;
+    o.x[p] = (float)((double)px - ox);
+    o.y[p] = (float)((double)py - oy);
+    o.z[p] = (float)((double)pz - oz);
+    o.vx[p] = vx;
+    o.vy[p] = vy;
+    o.vz[p] = vz;
+    o.m[p] = mm;
+    if (o.gid) o.gid[p] = g;
+    if (o.pid) o.pid[p] = (int32_t)q;
+  }
+}
+
+extern "C" int gc_pm_import_sorted(gc_ctx *ctx, const float *pos, const float *vel, const float *m, const int32_t *gid,
+                                   const double origin[3], const gc_particles *out) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, out && origin, "gc_pm_import_sorted: NULL particle set or origin");
+  const int64_t n = out->n;
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  if (n == 0) return GC_OK;
+  GC_REQUIRE(ctx, pos && vel && m, "gc_pm_import_sorted: NULL input");
+  GC_REQUIRE(ctx, out->x && out->y && out->z && out->vx && out->vy && out->vz && out->m,
+             "gc_pm_import_sorted: output arrays required");
+  int s = ensure_sort_scratch(ctx, n);
+  if (s) return s;
+  unsigned nb = gc_blocks(n, 256);
+  if (nb > 152u * 32u) nb = 152u * 32u;
+  gc_launch(ctx, GK_KEYS, k_cell_keys_aos, dim3(nb), dim3(256), 0, pos, origin[0], origin[1], origin[2], (long long)n,
+            (float)ctx->dx, ctx->G, ctx->keys2, ctx->vals2);
+  GC_LAUNCH_CHECK(ctx, "cell keys");
+  uint32_t *ko, *vo;
+  if ((s = gc_radix_sort_pairs(ctx, ctx->keys2, ctx->vals2, n, key_bits(ctx->G), &ko, &vo))) return s;
+  gc_launch(ctx, GK_PERMUTE, k_import_gather, dim3(nb), dim3(256), 0, pos, vel, m, gid, origin[0], origin[1],
+            origin[2], (const uint32_t *)vo, *out, (long long)n);
+  GC_LAUNCH_CHECK(ctx, "import gather");
+  return GC_OK;
+}

@@ -107,7 +107,8 @@ class PMEngine:
         """Load particles in the reference's layout (pos and vel N x 3 in physical
         coordinates, mass N, gid N or None; host or device arrays) into the engine.
         Host arrays are copied into the spare particle set (asynchronously when
-        they are pinned) and split on the device by gc_pm_import."""
+        they are pinned) and split on the device by gc_pm_import, or with sort
+        by gc_pm_import_sorted, which gathers them straight into cell order."""
         pos_t = torch.as_tensor(pos)
         n = int(pos_t.shape[0])
         if n <= 0:
@@ -143,13 +144,14 @@ class PMEngine:
         m_d = staged(mass, 6 * st, (n,), torch.float32)
         gid_d = None if gid is None else staged(gid, 7 * st, (n,), torch.int32)
         out = self._struct(self.cur)
-        self.ctx.call("gc_pm_import", pos_d.data_ptr(), vel_d.data_ptr(), m_d.data_ptr(),
-                      None if gid_d is None else gid_d.data_ptr(), origin, C.byref(out), what="gc_pm_import")
+        # with sort, keys come from the staged positions and the particles are
+        # gathered straight into cell order (same result as import + sort)
+        self.ctx.call("gc_pm_import_sorted" if sort else "gc_pm_import", pos_d.data_ptr(), vel_d.data_ptr(),
+                      m_d.data_ptr(), None if gid_d is None else gid_d.data_ptr(), origin, C.byref(out),
+                      what="gc_pm_import")
         self.state = "synced"
         self.steps_since_sort = 0
         self._graphs = {}
-        if sort:
-            self.sort()
 
     def export(self, pos=None, vel=None, mass=None, gid=None):
         """The state in the original particle order and the reference's layout:

@@ -272,6 +272,13 @@ int gc_pm_reserve(gc_ctx *ctx, int64_t n);
 int gc_pm_import(gc_ctx *ctx, const float *pos, const float *vel, const float *m, const int32_t *gid,
                  const double origin[3], const gc_particles *out);
 
+/* gc_pm_import followed by gc_pm_sort in one: the cell keys are computed from
+ * the interleaved positions and the particles are gathered from the interleaved
+ * arrays straight into cell order (out->pid = original index). The result is
+ * identical to gc_pm_import + gc_pm_sort. */
+int gc_pm_import_sorted(gc_ctx *ctx, const float *pos, const float *vel, const float *m, const int32_t *gid,
+                        const double origin[3], const gc_particles *out);
+
 /* The inverse, in the original particle order: for every i, with q = p->pid[i],
  * pos[3q+c] = f32((double)x_c[i] + origin[c]), vel[3q+c] = v_c[i], m_out[q],
  * gid_out[q] (each output may be NULL; p->pid is required). Replaces

@@ -351,6 +351,13 @@ def test_import_export_round_trip(cuda):
     np.testing.assert_array_equal(cur["vx"], vel[pid, 0])
     np.testing.assert_array_equal(cur["m"], mass[pid])
     np.testing.assert_array_equal(cur["gid"], gid[pid])
+    # the sorted import equals import + sort
+    e2 = PMEngine(G, dx, origin=origin, sort_every=3)
+    e2.load(pos, vel, mass, gid, sort=False)
+    np.testing.assert_array_equal(e2.cur["pid"].cpu().numpy(), np.arange(n, dtype=np.int32))
+    e2.sort()
+    for k in ("x", "y", "z", "vx", "vy", "vz", "m", "gid", "pid"):
+        np.testing.assert_array_equal(e2.cur[k].cpu().numpy(), eng.cur[k].cpu().numpy())
     p, v, m, g = eng.export()
     back = (rel.astype(np.float64) + np.asarray(origin)).astype(np.float32)
     np.testing.assert_array_equal(p.numpy(), back)
