@@ -201,11 +201,12 @@ __global__ void __launch_bounds__(256)
 // full warp costs the same whatever the keys, unlike one per group of equal
 // keys, which serialises over the groups.
 //
-// Corners go to an int32 box of nodes in shared memory when the tile's cells
-// fit DEP_BOX (the box is the cell range of the tile's coordinate range: x/dx is
-// monotone) and the tile's total quanta bound every node below 2^31; the box is
-// added to the int64 grid with one atomic per nonzero node at the end of the
-// tile. Otherwise corners go to the grid directly. Particles whose contribution
+// Each warp owns an int32 box of nodes in shared memory (no block-wide
+// barriers: warps never wait for each other). Corners go to it when the cells
+// of the warp's 256 particles fit DEP_WBOX nodes (the box is the cell range of
+// their coordinate range: x/dx is monotone) and their total quanta bound every
+// node below 2^31; the box is added to the int64 grid with one atomic per
+// nonzero node when the warp moves on. Otherwise corners go to the grid directly. Particles whose contribution
 // reaches 2^22 quanta (point masses) are deposited out of line at the end of
 // the tile with the general int64 rounding. Correct for any particle order;
 // the sort makes it fast.
@@ -213,6 +214,7 @@ __global__ void __launch_bounds__(256)
 #define DEP_PER 8
 #define DEP_TILE (256 * DEP_PER)
 #define DEP_BOX 8192
+#define DEP_WBOX (DEP_BOX / 8)  // nodes of one warp's box
 #define DEP_BIAS 0x4B400000u
 
 // Corner contributions of a particle whose mass exceeds 2^22 quanta.
@@ -343,19 +345,15 @@ __global__ void __launch_bounds__(256, 3)
                      const float *__restrict__ m, long long n, DepCtx d, float inv_dx,
                      const double *__restrict__ qexp, long long *__restrict__ qg, unsigned *__restrict__ status) {
   __shared__ int box[DEP_BOX];
-  __shared__ int bnd[2][8];  // per tile parity: cell min x,y,z, max x,y,z, max |m| bits
   const float qscale = ldexpf(1.0f, -(int)(*qexp));
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i = tid; i < DEP_BOX; i += 256) box[i] = 0;  // every flush zeroes what it read
-  if (tid < 16) {
-    const int a = tid & 7;
-    bnd[tid >> 3][a] = a < 3 ? 0x7fffffff : (a < 6 ? -0x7fffffff : 0);
-  }
-  __syncthreads();
-  int par = 0;
-  for (long long t0 = (long long)blockIdx.x * DEP_TILE; t0 < n; t0 += (long long)gridDim.x * DEP_TILE, par ^= 1) {
+  int *wbox = box + warp * DEP_WBOX;  // each warp owns a box: no block-wide barriers
+  for (int i = lane; i < DEP_WBOX; i += 32) wbox[i] = 0;  // every flush zeroes what it read
+  __syncwarp();
+  for (long long t0 = (long long)blockIdx.x * DEP_TILE; t0 < n; t0 += (long long)gridDim.x * DEP_TILE) {
     const long long wb = t0 + warp * (32 * DEP_PER) + lane;
     const long long nrem = n - wb;  // particle j of this lane exists when 32 j < nrem
+    if (nrem + lane <= 0) continue;  // this warp's part of the last tile is empty (warp-uniform)
     float px[DEP_PER], py[DEP_PER], pz[DEP_PER], pm[DEP_PER];
 #pragma unroll
     for (int j = 0; j < DEP_PER; ++j) {
@@ -367,8 +365,12 @@ __global__ void __launch_bounds__(256, 3)
         pm[j] = 0.0f;
       }
     }
-    // the tile's cell range from its coordinate range (fminf/fmaxf skip NaN),
+    // the warp's cell range from its coordinate range (fminf/fmaxf skip NaN),
     // clamped to the cells -1 .. G-1 that receive mass, and its largest |m|
+    DepBox bx;
+    bx.b = wbox;
+    bool use_box;
+    int nx;
     {
       float xl = 3.0e38f, yl = 3.0e38f, zl = 3.0e38f, xh = -3.0e38f, yh = -3.0e38f, zh = -3.0e38f;
       unsigned mb = 0;
@@ -393,27 +395,16 @@ __global__ void __launch_bounds__(256, 3)
         hi[a] = __reduce_max_sync(0xffffffffu, any_pt ? (int)h : -0x7fffffff);
       }
       mb = __reduce_max_sync(0xffffffffu, mb);
-      if (lane == 0) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) { atomicMin(&bnd[par][a], lo[a]); atomicMax(&bnd[par][3 + a], hi[a]); }
-        atomicMax(&bnd[par][6], (int)mb);
-      }
+      bx.x0 = lo[0]; bx.y0 = lo[1]; bx.z0 = lo[2];
+      nx = hi[0] - lo[0] + 2;
+      bx.ny = hi[1] - lo[1] + 2;
+      bx.nz = hi[2] - lo[2] + 2;
+      bx.nyz = bx.ny * bx.nz;
+      // every small corner is at most min(largest |m| in quanta, 2^22) + 1/2
+      const float mq = __fmul_rn(__fmul_rn(__uint_as_float(mb), d.inv_vol), qscale);
+      use_box = hi[0] >= lo[0] && (long long)nx * bx.nyz <= DEP_WBOX &&
+                __fmul_rn(fminf(mq, 4194304.0f) + 1.0f, (float)(32 * DEP_PER)) < 1073741824.0f;
     }
-    __syncthreads();
-    DepBox bx;
-    bx.b = box;
-    bx.x0 = bnd[par][0]; bx.y0 = bnd[par][1]; bx.z0 = bnd[par][2];
-    const int nx = bnd[par][3] - bx.x0 + 2;
-    bx.ny = bnd[par][4] - bx.y0 + 2;
-    bx.nz = bnd[par][5] - bx.z0 + 2;
-    bx.nyz = bx.ny * bx.nz;
-    // every small corner is at most min(largest |m| in quanta, 2^22) + 1/2
-    const float mq = __fmul_rn(__fmul_rn(__uint_as_float((unsigned)bnd[par][6]), d.inv_vol), qscale);
-    const int cnt_tile = (int)(n - t0 < DEP_TILE ? n - t0 : DEP_TILE);
-    const bool use_box = bnd[par][3] >= bx.x0 && (long long)nx * bx.nyz <= DEP_BOX &&
-                         __fmul_rn(fminf(mq, 4194304.0f) + 1.0f, (float)cnt_tile) < 1073741824.0f;
-    __syncthreads();  // every thread has read bnd[par]; reset it for the tile after next
-    if (tid < 8) bnd[par][tid] = tid < 3 ? 0x7fffffff : (tid < 6 ? -0x7fffffff : 0);
     unsigned large = 0;
     if (use_box)
       dep_warp_pass<POW2, true>(px, py, pz, pm, nrem, d, inv_dx, qscale, bx, qg, status, lane, large);
@@ -431,22 +422,19 @@ __global__ void __launch_bounds__(256, 3)
                     __fsub_rn(gy, __int2float_rn(iy)), __fsub_rn(gz, __int2float_rn(iz)), qscale);
     }
     if (use_box) {
-      __syncthreads();
-      // rows (bx, by) over the warps, z over the lanes; every entry read is zeroed
-      for (int row = warp; row < nx * bx.ny; row += 8) {
-        const int rx = row / bx.ny, ry = row - rx * bx.ny;
-        const int jx = bx.x0 + rx, jy = bx.y0 + ry;
-        const bool rin = (unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G;
-        int *b = box + row * bx.nz;
-        for (int bz = lane; bz < bx.nz; bz += 32) {
-          const int v = b[bz];
-          if (v == 0) continue;
-          b[bz] = 0;
-          const int jz = bx.z0 + bz;
-          if (rin && (unsigned)jz < (unsigned)d.G)
-            atomicAdd((unsigned long long *)(qg + ((size_t)jx * d.G + jy) * d.G + jz), (unsigned long long)(long long)v);
-        }
+      __syncwarp();
+      // the warp's box to the grid, one atomic per nonzero node; zeroed as read
+      const int vol = nx * bx.nyz;
+      for (int i = lane; i < vol; i += 32) {
+        const int v = wbox[i];
+        if (v == 0) continue;
+        wbox[i] = 0;
+        const int rx = i / bx.nyz, rem = i - rx * bx.nyz, ry = rem / bx.nz, rz = rem - ry * bx.nz;
+        const int jx = bx.x0 + rx, jy = bx.y0 + ry, jz = bx.z0 + rz;
+        if ((unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G && (unsigned)jz < (unsigned)d.G)
+          atomicAdd((unsigned long long *)(qg + ((size_t)jx * d.G + jy) * d.G + jz), (unsigned long long)(long long)v);
       }
+      __syncwarp();
     }
   }
 }
