@@ -340,7 +340,7 @@ __device__ __forceinline__ void dep_warp_pass(const float (&px)[DEP_PER], const 
 }
 
 template <bool POW2>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(256, 4)
     k_deposit_sorted(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
                      const float *__restrict__ m, long long n, DepCtx d, float inv_dx,
                      const double *__restrict__ qexp, long long *__restrict__ qg, unsigned *__restrict__ status) {
@@ -447,7 +447,7 @@ int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, co
   d.inv_vol = 1.0f / ((d.dx * d.dx) * d.dx);
   d.G = ctx->G;
   const long long ntiles = (n + DEP_TILE - 1) / DEP_TILE;
-  const unsigned nb = (unsigned)(ntiles < 152LL * 3 ? ntiles : 152LL * 3);  // 3 CTAs per SM, persistent
+  const unsigned nb = (unsigned)(ntiles < 152LL * 4 ? ntiles : 152LL * 4);  // 4 CTAs per SM, persistent
   int fe = 0;
   const bool pow2 = std::frexp(d.dx, &fe) == 0.5f;
   const float inv_dx = pow2 ? std::ldexp(1.0f, 1 - fe) : 0.0f;

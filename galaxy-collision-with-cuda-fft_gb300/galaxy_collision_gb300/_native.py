@@ -122,6 +122,13 @@ _PROTOS = {
                                       C.c_double, C.c_int, _vp]),
     "gc_project_ngp": (C.c_int, [_ctxp, _vp, _vp, _vp, _i64, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_int, _vp]),
+    "gc_max_f32": (C.c_int, [_ctxp, _vp, _i64, _vp]),
+    "gc_colormap_log": (C.c_int, [_ctxp, _vp, _i64, _vp, C.c_float, C.c_float, _vp]),
+    "gc_pack_positions": (C.c_int, [_ctxp, _vp, _vp, _vp, _i64, C.c_float, _i64, _vp]),
+    "gc_density_color": (C.c_int, [_ctxp, _vp, _vp, _vp, _vp, C.c_int, _i64, _i64, C.c_float, _vp, C.c_float,
+                                   C.c_float, _vp]),
+    "gc_splat_points": (C.c_int, [_ctxp, _vp, _vp, _i64, C.POINTER(C.c_float), C.c_int, C.c_int, C.c_float,
+                                  C.POINTER(C.c_float), _vp, _vp]),
     "gc_pm_sort": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(Particles)]),
     "gc_pm_reserve": (C.c_int, [_ctxp, _i64]),
     "gc_pm_import": (C.c_int, [_ctxp, _vp, _vp, _vp, _vp, C.POINTER(C.c_double), C.POINTER(Particles)]),

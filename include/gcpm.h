@@ -253,6 +253,35 @@ int gc_radial_histogram(gc_ctx *ctx, const float *x, const float *y, const float
 int gc_project_ngp(gc_ctx *ctx, const float *pa, const float *pb, const float *m, int64_t n, double lo_a,
                    double lo_b, double binw_a, double binw_b, int bins, float *img);
 
+/* ---- headless views (viz/viewer.py; the GGUI window and scene are replaced by
+ * device buffers) ------------------------------------------------------------ */
+
+/* *out = max(0, max of a[0..n)) (device scalar; _max_field / _max_grid3,
+ * viewer.py:68-73, 98-101). */
+int gc_max_f32(gc_ctx *ctx, const float *a, int64_t n, float *out);
+/* rgb[3i..3i+2] = lut[idx], idx = int(clamp01((ln img[i] - log_vmin) * inv_logspan)
+ * * 255 + 0.5) (0 where img <= 0); lut is 256 x 3 f32 (_colormap_log,
+ * viewer.py:76-93). */
+int gc_colormap_log(gc_ctx *ctx, const float *img, int64_t n, const float *lut, float log_vmin, float inv_logspan,
+                    float *rgb);
+/* out[3i+c] = pos_c[i*stride] * inv_box - 0.5 for i < m (_pack_positions, viewer.py:50-65). */
+int gc_pack_positions(gc_ctx *ctx, const float *x, const float *y, const float *z, int64_t stride, float inv_box,
+                      int64_t m, float *out);
+/* col[3i..] = lut colour of rho at the nearest node of particle i*stride
+ * (clamp(int(x * inv_dx + 0.5)) per axis), as gc_colormap_log (_density_color,
+ * viewer.py:104-121). */
+int gc_density_color(gc_ctx *ctx, const float *x, const float *y, const float *z, const float *rho, int grid,
+                     int64_t stride, int64_t m, float inv_dx, const float *lut, float log_vmin, float inv_logspan,
+                     float *col);
+/* Draw m points (unit-cube coordinates pos[3i..], colours col[3i..] in [0,1]) as
+ * flat discs of radius_px pixels into rgba (width x height x 4, row 0 at the
+ * top), nearest point per pixel (ties to the lower index), bg elsewhere; the 3-D
+ * view's scene.particles (viewer.py:258-272) without a graphics API. view_proj
+ * is a row-major 4 x 4 matrix to clip space; points with w <= 0 or depth
+ * outside [0, 1] are skipped. zbuf is width x height u64 scratch. */
+int gc_splat_points(gc_ctx *ctx, const float *pos, const float *col, int64_t m, const float view_proj[16], int width,
+                    int height, float radius_px, const float bg[3], unsigned long long *zbuf, unsigned char *rgba);
+
 /* ---- fused engine (callers: bench.py:145-152, sim.py:320-325) ------------ */
 
 /* Stable-sort the particles by cell key and write the permuted set to out
