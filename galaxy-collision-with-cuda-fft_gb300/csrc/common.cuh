@@ -45,7 +45,7 @@ enum gc_kernel_id {
   GK_DEPOSIT = 0, GK_DEPOSIT_RUNS, GK_CONVERT_Q, GK_MASS, GK_SMOOTH0, GK_RESID0, GK_RESTRICT, GK_SMOOTH,
   GK_RESID, GK_PROLONG, GK_PROLONG0, GK_TAIL, GK_FACES, GK_MOMENTS, GK_RHS, GK_REDUCE, GK_GATHER_KD,
   GK_GRAD, GK_GATHER, GK_AXPY, GK_KEYS, GK_SORT, GK_PERMUTE, GK_DIAG, GK_HIST, GK_RESID64, GK_COPY,
-  GK_SWEEP0, GK_PROJECT, GK_WARMSTART, GK_VIZ, GK_COUNT
+  GK_SWEEP0, GK_PROJECT, GK_WARMSTART, GK_VIZ, GK_IC, GK_COUNT
 };
 extern const char *const gc_kernel_names[GK_COUNT];
 

@@ -9,7 +9,7 @@ const char *const gc_kernel_names[GK_COUNT] = {
     "deposit", "deposit_runs", "convert_q", "mass_setup", "smooth0", "resid0", "restrict", "smooth",
     "resid", "prolong", "prolong0", "tail", "faces", "moments", "rhs", "reduce", "gather_kick_drift",
     "grad", "gather", "axpy", "cell_keys", "radix_sort", "permute", "diag", "radial_hist", "resid64", "copy",
-    "sweep0", "project_ngp", "warmstart", "viz"};
+    "sweep0", "project_ngp", "warmstart", "viz", "ic"};
 
 int gc_prof_slot(gc_ctx *ctx, int kid) {
   gc_profiler &p = ctx->prof;

@@ -21,7 +21,7 @@ INCLUDE = PKG_DIR.parent.parent / "include"
 BUILD_DIR = PKG_DIR / "_build"
 LIB_PATH = PKG_DIR / "libgcpm.so"
 
-SOURCES = ("ctx.cu", "multigrid.cu", "particles.cu", "sort.cu", "engine.cu", "noalloc.cu", "warmstart.cu", "viz.cu")
+SOURCES = ("ctx.cu", "multigrid.cu", "particles.cu", "sort.cu", "engine.cu", "noalloc.cu", "warmstart.cu", "viz.cu", "ic.cu")
 ARCH_FLAGS = ("-gencode", "arch=compute_103a,code=sm_103a")
 NVCC_FLAGS = ("-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2")
 

@@ -24,6 +24,7 @@ GC_ERR_STATE = -6
 GC_FLAG_NONFINITE_POS = 0x1
 GC_FLAG_NONFINITE_RHO = 0x2
 GC_FLAG_BAD_PID = 0x4
+GC_FLAG_IC_REJECT = 0x8
 GC_MG_FUSED_SWEEP = 0x1
 GC_MG_FIXED_CYCLES = 0x2
 GC_STEP_GRAD_GRID = 0x1
@@ -122,6 +123,11 @@ _PROTOS = {
                                       C.c_double, C.c_int, _vp]),
     "gc_project_ngp": (C.c_int, [_ctxp, _vp, _vp, _vp, _i64, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_int, _vp]),
+    "gc_rng_uniform": (C.c_int, [_ctxp, C.c_uint64, C.c_uint32, _i64, _vp]),
+    "gc_ic_plummer": (C.c_int, [_ctxp, _i64, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_double, _vp, _vp,
+                                _vp, _vp]),
+    "gc_ic_disk": (C.c_int, [_ctxp, _i64, C.c_uint64, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                             C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double), _vp, _vp, _vp, _vp]),
     "gc_max_f32": (C.c_int, [_ctxp, _vp, _i64, _vp]),
     "gc_colormap_log": (C.c_int, [_ctxp, _vp, _i64, _vp, C.c_float, C.c_float, _vp]),
     "gc_pack_positions": (C.c_int, [_ctxp, _vp, _vp, _vp, _i64, C.c_float, _i64, _vp]),

@@ -46,6 +46,7 @@ enum gc_status_code {
 #define GC_FLAG_NONFINITE_POS 0x1u  /* a particle position was NaN/Inf: it deposited nothing */
 #define GC_FLAG_NONFINITE_RHO 0x2u  /* the density handed to the solver had NaN/Inf */
 #define GC_FLAG_BAD_PID 0x4u        /* gc_pm_export met a pid outside [0, n): that particle was skipped */
+#define GC_FLAG_IC_REJECT 0x8u      /* a device IC rejection loop reached its attempt limit */
 
 /* gc_mg_params.flags: relax the finest level with the streaming sweep (one
  * red+black sweep per pass through shared memory, ping-pong buffers, the
@@ -252,6 +253,28 @@ int gc_radial_histogram(gc_ctx *ctx, const float *x, const float *y, const float
  * Replaces viz/project.py _project / scatter_density (viz/project.py:26-70). */
 int gc_project_ngp(gc_ctx *ctx, const float *pa, const float *pb, const float *m, int64_t n, double lo_a,
                    double lo_b, double binw_a, double binw_b, int bins, float *img);
+
+/* ---- initial conditions on the device (the reference samples on the host:
+ * _sample_plummer / _sample_plummer_q, ic.py:296-384, and _sample_disk /
+ * build_ic, ic.py:145-285; these follow the benchmark configurations' spec
+ * with counter-based random numbers, so particle i depends only on (seed, i)) */
+
+/* out[4i..4i+3]: the four uniforms in (0, 1) of Philox4x32-10 with counter
+ * (i, 0, stream) and key seed (24-bit resolution, centred in their bins). */
+int gc_rng_uniform(gc_ctx *ctx, uint64_t seed, uint32_t stream, int64_t n, float *out);
+/* n-particle Plummer sphere of mass `mass`, scale a, truncated at rmax*a;
+ * speeds from the isotropic distribution function (rejection sampling).
+ * pos, vel: n x 3 f32; m: n f32 (mass/n); gid: n (0). */
+int gc_ic_plummer(gc_ctx *ctx, int64_t n, uint64_t seed, double mass, double a, double rmax, double grav, float *pos,
+                  float *vel, float *m, int32_t *gid);
+/* One galaxy of the two-disk collision: n_disk particles of an exponential
+ * sech^2 disk (scale rd, cut at 5 rd, height 0.1 rd) plus its central point mass
+ * (1 % of m_disk) as particle n_disk, circular speeds from the enclosed mass
+ * (softened by soft) with 10 % dispersion, inclined about x by incline_deg,
+ * shifted by off and boosted by bulk. Writes n_disk + 1 particles (gid = galaxy). */
+int gc_ic_disk(gc_ctx *ctx, int64_t n_disk, uint64_t seed, int galaxy, double m_disk, double rd, double grav,
+               double soft, double incline_deg, const double off[3], const double bulk[3], float *pos, float *vel,
+               float *m, int32_t *gid);
 
 /* ---- headless views (viz/viewer.py; the GGUI window and scene are replaced by
  * device buffers) ------------------------------------------------------------ */
