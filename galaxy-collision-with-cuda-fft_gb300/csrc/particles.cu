@@ -8,6 +8,7 @@
 // is associative, so the density is bit-identical whatever the particle order or
 // atomic interleaving.
 #include "common.cuh"
+#include "umma.cuh"
 
 #include <math.h>
 
@@ -933,6 +934,124 @@ __global__ void __launch_bounds__(256)
   if (DIAG) block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
 }
 
+// The same particle pass with the particle state streamed by the TMA engine: a
+// CTA owns tiles of GT_TILE particles (round robin); one thread arms an
+// mbarrier and issues six 1-D bulk copies (x, y, z, vx, vy, vz) of the next
+// tile into the other half of a double buffer while all threads work on the
+// current one, reading the state from shared memory, gathering the corners
+// from the float4 grid, and writing the new state back in place; the tile then
+// leaves with six bulk stores. The DRAM streams never wait for the gather's
+// dependent loads. Full tiles only; the remainder goes through plain loads.
+// Waits are bounded (clock budget): a timeout raises GC_FLAG_TIMEOUT and the
+// CTA stops issuing.
+#define GT_TILE 992  // 6 arrays x 2 buffers x 992 x 4 B = 47,616 B of shared memory; 992 x 4 B = 248 x 16 B
+#define GT_BUDGET 2000000000LL
+
+template <bool POW2>
+__device__ __forceinline__ void gt_particle(float *s0, float *s1, float *s2, float *s3, float *s4, float *s5, int i,
+                                            const float4 *__restrict__ g4, const FusedCtx &f) {
+  const float px = s0[i], py = s1[i], pz = s2[i];
+  float ux = s3[i], uy = s4[i], uz = s5[i];
+  float ax, ay, az;
+  gather_g4<POW2>(g4, px, py, pz, f, ax, ay, az);
+  if (f.mode != GC_STEP_PRIME) {
+    ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
+    uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
+    uz = __fadd_rn(uz, __fmul_rn(az, f.h));
+  }
+  if (f.mode != GC_STEP_CLOSE) {
+    ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
+    uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
+    uz = __fadd_rn(uz, __fmul_rn(az, f.h));
+    s0[i] = __fadd_rn(px, __fmul_rn(ux, f.dt));
+    s1[i] = __fadd_rn(py, __fmul_rn(uy, f.dt));
+    s2[i] = __fadd_rn(pz, __fmul_rn(uz, f.dt));
+  }
+  s3[i] = ux;
+  s4[i] = uy;
+  s5[i] = uz;
+}
+
+template <bool POW2>
+__global__ void __launch_bounds__(256)
+    k_gather4_tma(float *__restrict__ x, float *__restrict__ y, float *__restrict__ z, float *__restrict__ vx,
+                  float *__restrict__ vy, float *__restrict__ vz, long long n, const float4 *__restrict__ g4, FusedCtx f,
+                  unsigned *__restrict__ status) {
+  using namespace umma;
+  __shared__ __align__(128) float buf[2][6][GT_TILE];
+  __shared__ __align__(8) uint64_t bar[2];
+  float *const arr[6] = {x, y, z, vx, vy, vz};
+  const int tid = threadIdx.x;
+  const long long ntiles = n / GT_TILE;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const uint32_t tile_bytes = GT_TILE * 4;
+  long long t = blockIdx.x;
+  if (tid == 0 && t < ntiles) {
+    mbar_arrive_expect_tx(&bar[0], 6 * tile_bytes);
+#pragma unroll
+    for (int a = 0; a < 6; ++a) bulk_g2s(buf[0][a], arr[a] + t * GT_TILE, tile_bytes, &bar[0]);
+  }
+  for (int it = 0; t < ntiles; ++it, t += gridDim.x) {
+    const int b = it & 1;
+    const long long tn = t + gridDim.x;
+    if (tid == 0 && tn < ntiles) {  // prefetch the next tile into the other buffer
+      bulk_wait_read_all();          // its previous tile's stores have read it
+      mbar_arrive_expect_tx(&bar[b ^ 1], 6 * tile_bytes);
+#pragma unroll
+      for (int a = 0; a < 6; ++a) bulk_g2s(buf[b ^ 1][a], arr[a] + tn * GT_TILE, tile_bytes, &bar[b ^ 1]);
+    }
+    const bool got = mbar_wait(&bar[b], (uint32_t)(it >> 1) & 1u, GT_BUDGET);
+    if (!__syncthreads_and(got)) {  // the block leaves together
+      if (tid == 0) {  // record it, and give the copies still in flight a bounded time to land
+        atomicOr(status, GC_FLAG_TIMEOUT);
+        mbar_wait(&bar[b], (uint32_t)(it >> 1) & 1u, GT_BUDGET);
+        if (tn < ntiles) mbar_wait(&bar[b ^ 1], (uint32_t)((it + 1) >> 1) & 1u, GT_BUDGET);
+        bulk_wait_all();
+      }
+      return;
+    }
+    float *s0 = buf[b][0], *s1 = buf[b][1], *s2 = buf[b][2], *s3 = buf[b][3], *s4 = buf[b][4], *s5 = buf[b][5];
+#pragma unroll 4
+    for (int i = tid; i < GT_TILE; i += 256) gt_particle<POW2>(s0, s1, s2, s3, s4, s5, i, g4, f);
+    fence_async_smem();  // this thread's shared-memory writes -> visible to the bulk stores
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+      for (int a = 0; a < 6; ++a) bulk_s2g(arr[a] + t * GT_TILE, buf[b][a], tile_bytes);
+      bulk_commit();
+    }
+  }
+  if (tid == 0) bulk_wait_all();
+  // the remainder after the full tiles: plain loads, every CTA a slice
+  const long long r0 = ntiles * GT_TILE;
+  for (long long p = r0 + blockIdx.x * (long long)blockDim.x + tid; p < n; p += (long long)gridDim.x * blockDim.x) {
+    float px = x[p], py = y[p], pz = z[p], ux = vx[p], uy = vy[p], uz = vz[p];
+    float ax, ay, az;
+    gather_g4<POW2>(g4, px, py, pz, f, ax, ay, az);
+    if (f.mode != GC_STEP_PRIME) {
+      ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
+      uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
+      uz = __fadd_rn(uz, __fmul_rn(az, f.h));
+    }
+    if (f.mode != GC_STEP_CLOSE) {
+      ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
+      uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
+      uz = __fadd_rn(uz, __fmul_rn(az, f.h));
+      x[p] = __fadd_rn(px, __fmul_rn(ux, f.dt));
+      y[p] = __fadd_rn(py, __fmul_rn(uy, f.dt));
+      z[p] = __fadd_rn(pz, __fmul_rn(uz, f.dt));
+    }
+    vx[p] = ux;
+    vy[p] = uy;
+    vz[p] = uz;
+  }
+}
+
 int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode, int diag, int grad_grid,
                          float *axo, float *ayo, float *azo, int *nparts_out) {
   FusedCtx f;
@@ -956,10 +1075,20 @@ int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode,
               (float4 *)ctx->g4, g);
     int fe = 0;
     const bool pow2 = std::frexp(f.dx, &fe) == 0.5f;  // then inv_dx is exact
-    auto k = diag ? (pow2 ? k_gather4_kick_drift<true, true> : k_gather4_kick_drift<true, false>)
-                  : (pow2 ? k_gather4_kick_drift<false, true> : k_gather4_kick_drift<false, false>);
-    gc_launch(ctx, GK_GATHER_KD, k, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx, p->vy, p->vz, p->m,
-              (long long)p->n, (const float4 *)ctx->g4, f, ctx->red);
+    const uintptr_t al = (uintptr_t)p->x | (uintptr_t)p->y | (uintptr_t)p->z | (uintptr_t)p->vx | (uintptr_t)p->vy |
+                         (uintptr_t)p->vz;
+    if (!diag && (al & 15u) == 0 && p->n >= GT_TILE) {
+      // bulk-streamed state: 4 CTAs of 47.6 KB shared memory per SM, persistent
+      const long long ntiles = p->n / GT_TILE;
+      const unsigned nbt = (unsigned)(ntiles < 152LL * 4 ? ntiles : 152LL * 4);
+      gc_launch(ctx, GK_GATHER_KD, pow2 ? k_gather4_tma<true> : k_gather4_tma<false>, dim3(nbt), dim3(256), 0,
+                p->x, p->y, p->z, p->vx, p->vy, p->vz, (long long)p->n, (const float4 *)ctx->g4, f, ctx->dstatus);
+    } else {
+      auto k = diag ? (pow2 ? k_gather4_kick_drift<true, true> : k_gather4_kick_drift<true, false>)
+                    : (pow2 ? k_gather4_kick_drift<false, true> : k_gather4_kick_drift<false, false>);
+      gc_launch(ctx, GK_GATHER_KD, k, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx, p->vy, p->vz, p->m,
+                (long long)p->n, (const float4 *)ctx->g4, f, ctx->red);
+    }
   } else if (diag) {
     gc_launch(ctx, GK_GATHER_KD, k_gather_kick_drift<true>, dim3(nb), dim3(256), 0, p->x, p->y, p->z, p->vx, p->vy,
               p->vz, p->m, (long long)p->n, ctx->hi, f, axo, ayo, azo, ctx->red);

@@ -25,6 +25,7 @@ GC_FLAG_NONFINITE_POS = 0x1
 GC_FLAG_NONFINITE_RHO = 0x2
 GC_FLAG_BAD_PID = 0x4
 GC_FLAG_IC_REJECT = 0x8
+GC_FLAG_TIMEOUT = 0x10
 GC_MG_FUSED_SWEEP = 0x1
 GC_MG_FIXED_CYCLES = 0x2
 GC_STEP_GRAD_GRID = 0x1

@@ -47,6 +47,7 @@ enum gc_status_code {
 #define GC_FLAG_NONFINITE_RHO 0x2u  /* the density handed to the solver had NaN/Inf */
 #define GC_FLAG_BAD_PID 0x4u        /* gc_pm_export met a pid outside [0, n): that particle was skipped */
 #define GC_FLAG_IC_REJECT 0x8u      /* a device IC rejection loop reached its attempt limit */
+#define GC_FLAG_TIMEOUT 0x10u       /* a bounded wait inside a kernel ran out; that kernel stopped early */
 
 /* gc_mg_params.flags: relax the finest level with the streaming sweep (one
  * red+black sweep per pass through shared memory, ping-pong buffers, the
