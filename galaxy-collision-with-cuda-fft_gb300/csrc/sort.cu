@@ -12,8 +12,8 @@
 #define RS_RADIX 256
 #define RS_THREADS 256
 #define RS_WARPS (RS_THREADS / 32)
-#define RS_IPT 16                          // items per thread
-#define RS_TILE (RS_THREADS * RS_IPT)      // 4096 items per tile
+#define RS_IPT 4                           // items per thread (small tiles: more CTAs in flight)
+#define RS_TILE (RS_THREADS * RS_IPT)      // 1024 items per tile
 static_assert(RS_THREADS == RS_RADIX, "the scatter's per-digit phase has one thread per digit");
 
 __global__ void __launch_bounds__(256)
