@@ -100,6 +100,8 @@ struct gc_ctx {
 
   double mass_sum_cache; // sum of masses for the engine's fixed-point quantum
   int last_step_valid;
+  int q_next_ready;     // q holds the deposit of the current positions (made by the last particle pass)
+  int gt_smem_set;      // the TMA particle-pass kernels' dynamic shared-memory limit has been raised
   int solved_once;
   gc_mg_stats last_stats;
 
@@ -342,8 +344,10 @@ int gc_mg_check_params(gc_ctx *ctx, const gc_mg_params *p);
 int gc_max_fixed_point_bits(const gc_ctx *ctx);
 // Fused gather(-grad phi of ctx->hi) + kicks + drift over p (mode: gc_step_mode).
 // With diag, writes nparts rows of 11 FP64 partials into ctx->red.
+// With deposit_next (and a drifting mode) the bulk-streamed pass also deposits
+// the new positions into ctx->q; *deposited tells whether it did.
 int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode, int diag, int grad_grid,
-                         float *axo, float *ayo, float *azo, int *nparts_out);
+                         int deposit_next, float *axo, float *ayo, float *azo, int *nparts_out, int *deposited);
 // dst = sum a*b in FP64 (async).
 int gc_dot_async(gc_ctx *ctx, const float *a, const float *b, size_t n, double *dst);
 // Stable LSD radix sort of (keys, vals) pairs on the low `bits` bits; results in

@@ -21,7 +21,10 @@ static int pm_solve(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp
   if (sp->mode == GC_STEP_PRIME) {
     if ((s = gc_fixed_point_setup(ctx, p->m, p->n, sp->fixed_point_bits, GC_S_MASS_PM, GC_S_QEXP_PM))) return s;
   }
-  if ((s = gc_deposit_q(ctx, p->x, p->y, p->z, p->m, p->n, ctx->dsmall + GC_S_QEXP_PM))) return s;
+  // the previous particle pass may have deposited these positions already
+  const bool have_q = ctx->q_next_ready && sp->mode != GC_STEP_PRIME && (sp->flags & GC_STEP_DEPOSIT_NEXT);
+  ctx->q_next_ready = 0;
+  if (!have_q && (s = gc_deposit_q(ctx, p->x, p->y, p->z, p->m, p->n, ctx->dsmall + GC_S_QEXP_PM))) return s;
   // 2. b0, moments, ||b0||
   if ((s = gc_convert_q(ctx, ctx->dsmall + GC_S_QEXP_PM, nullptr, ctx->b0))) return s;
   // 3. initial guess and faces, then V-cycles
@@ -42,9 +45,12 @@ static int pm_push(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp,
   int s;
   const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
   int nparts = 0;
+  int deposited = 0;
   if ((s = gc_gather_kick_drift(ctx, p, sp->dt, sp->mode, sp->diagnostics, (sp->flags & GC_STEP_GRAD_GRID) != 0,
-                                nullptr, nullptr, nullptr, &nparts)))
+                                (sp->flags & GC_STEP_DEPOSIT_NEXT) != 0, nullptr, nullptr, nullptr, &nparts,
+                                &deposited)))
     return s;
+  ctx->q_next_ready = deposited;
   if (sp->diagnostics) {
     if ((s = gc_finalize(ctx, ctx->red, nparts, 11, ctx->ddiag))) return s;
     if ((s = gc_dot_async(ctx, ctx->b0, ctx->hi, g3, ctx->ddiag + 11))) return s;

@@ -282,16 +282,16 @@ __device__ __forceinline__ void dep_out(const DepBox &bx, long long *__restrict_
 
 // The DEP_PER particles of one lane (registers), 32 adjacent particles of the
 // warp at a time. Sets bit j of `large` for particles left to the out-of-line pass.
-template <bool POW2, bool BOX>
-__device__ __forceinline__ void dep_warp_pass(const float (&px)[DEP_PER], const float (&py)[DEP_PER],
-                                              const float (&pz)[DEP_PER], const float (&pm)[DEP_PER], long long nrem,
+template <bool POW2, bool BOX, int NJ = DEP_PER>
+__device__ __forceinline__ void dep_warp_pass(const float (&px)[NJ], const float (&py)[NJ],
+                                              const float (&pz)[NJ], const float (&pm)[NJ], long long nrem,
                                               const DepCtx &d, float inv_dx, float qscale, const DepBox &bx,
                                               long long *__restrict__ qg, unsigned *__restrict__ status, int lane,
                                               unsigned &large) {
   const int G1 = d.G + 1;
   const float hi = (float)d.G;
 #pragma unroll
-  for (int j = 0; j < DEP_PER; ++j) {
+  for (int j = 0; j < NJ; ++j) {
     float gx, gy, gz;
     if (POW2) {  // x / dx == x * (1/dx) exactly when dx is a power of two
       gx = __fmul_rn(px[j], inv_dx); gy = __fmul_rn(py[j], inv_dx); gz = __fmul_rn(pz[j], inv_dx);
@@ -936,16 +936,28 @@ __global__ void __launch_bounds__(256)
 
 // The same particle pass with the particle state streamed by the TMA engine: a
 // CTA owns tiles of GT_TILE particles (round robin); one thread arms an
-// mbarrier and issues six 1-D bulk copies (x, y, z, vx, vy, vz) of the next
-// tile into the other half of a double buffer while all threads work on the
-// current one, reading the state from shared memory, gathering the corners
-// from the float4 grid, and writing the new state back in place; the tile then
-// leaves with six bulk stores. The DRAM streams never wait for the gather's
-// dependent loads. Full tiles only; the remainder goes through plain loads.
-// Waits are bounded (clock budget): a timeout raises GC_FLAG_TIMEOUT and the
-// CTA stops issuing.
-#define GT_TILE 992  // 6 arrays x 2 buffers x 992 x 4 B = 47,616 B of shared memory; 992 x 4 B = 248 x 16 B
+// mbarrier and issues 1-D bulk copies (x, y, z, vx, vy, vz, and m when
+// depositing) of the next tile into the other half of a double buffer while all
+// threads work on the current one, reading the state from shared memory,
+// gathering the corners from the float4 grid, and writing the new state back in
+// place; the tile then leaves with six bulk stores. The DRAM streams never wait
+// for the gather's dependent loads.
+//
+// With DEP the pass also deposits the drifted positions (the next step's
+// density) into the int64 grid while the stores drain: warp w takes the tile's
+// particles [128 w, 128 w + 128) 32 at a time, exactly as k_deposit_sorted does
+// (two full-warp reductions for the main cells, direct adds for the others, a
+// per-warp shared-memory box), so the density is the one k_deposit_sorted
+// would produce from the stored positions, bit for bit.
+//
+// Full tiles only; the remainder goes through plain loads (and per-particle
+// deposits). Waits are bounded (clock budget): a timeout raises
+// GC_FLAG_TIMEOUT and the CTA stops issuing.
+#define GT_TILE 1024
 #define GT_BUDGET 2000000000LL
+#define GT_WBOX 512  // nodes of one warp's deposit box
+// dynamic shared memory: two buffers of 7 arrays, the warps' boxes
+#define GT_SMEM(dep) (2 * ((dep) ? 7 : 6) * GT_TILE * 4 + ((dep) ? 8 * GT_WBOX * 4 : 0))
 
 template <bool POW2>
 __device__ __forceinline__ void gt_particle(float *s0, float *s1, float *s2, float *s3, float *s4, float *s5, int i,
@@ -972,17 +984,129 @@ __device__ __forceinline__ void gt_particle(float *s0, float *s1, float *s2, flo
   s5[i] = uz;
 }
 
+// Deposit of 128 staged particles (warp-contiguous, the k_deposit_sorted rules)
+// into the warp's box or the grid.
 template <bool POW2>
+__device__ __forceinline__ void gt_deposit_warp(const float *s0, const float *s1, const float *s2, const float *s6,
+                                                int base, int *wbox, const DepCtx &d, float inv_dx, float qscale,
+                                                long long *__restrict__ qg, unsigned *__restrict__ status, int lane) {
+  float px[4], py[4], pz[4], pm[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int i = base + 32 * j + lane;
+    px[j] = s0[i]; py[j] = s1[i]; pz[j] = s2[i]; pm[j] = s6[i];
+  }
+  DepBox bx;
+  bx.b = wbox;
+  bool use_box;
+  int nx;
+  {
+    float xl = 3.0e38f, yl = 3.0e38f, zl = 3.0e38f, xh = -3.0e38f, yh = -3.0e38f, zh = -3.0e38f;
+    unsigned mb = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      xl = fminf(xl, px[j]); xh = fmaxf(xh, px[j]);
+      yl = fminf(yl, py[j]); yh = fmaxf(yh, py[j]);
+      zl = fminf(zl, pz[j]); zh = fmaxf(zh, pz[j]);
+      mb = max(mb, __float_as_uint(pm[j]) & 0x7fffffffu);
+    }
+    const float gl = -1.0f, gh = (float)d.G - 1.0f;
+    const float cl[3] = {xl, yl, zl}, ch[3] = {xh, yh, zh};
+    int lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      float l = POW2 ? __fmul_rn(cl[a], inv_dx) : __fdiv_rn(cl[a], d.dx);
+      float h = POW2 ? __fmul_rn(ch[a], inv_dx) : __fdiv_rn(ch[a], d.dx);
+      l = fminf(fmaxf(floorf(l), gl), gh);
+      h = fminf(fmaxf(floorf(h), gl), gh);
+      const bool any_pt = cl[a] <= ch[a];
+      lo[a] = __reduce_min_sync(0xffffffffu, any_pt ? (int)l : 0x7fffffff);
+      hi[a] = __reduce_max_sync(0xffffffffu, any_pt ? (int)h : -0x7fffffff);
+    }
+    mb = __reduce_max_sync(0xffffffffu, mb);
+    bx.x0 = lo[0]; bx.y0 = lo[1]; bx.z0 = lo[2];
+    nx = hi[0] - lo[0] + 2;
+    bx.ny = hi[1] - lo[1] + 2;
+    bx.nz = hi[2] - lo[2] + 2;
+    bx.nyz = bx.ny * bx.nz;
+    const float mq = __fmul_rn(__fmul_rn(__uint_as_float(mb), d.inv_vol), qscale);
+    use_box = hi[0] >= lo[0] && (long long)nx * bx.nyz <= GT_WBOX &&
+              __fmul_rn(fminf(mq, 4194304.0f) + 1.0f, 128.0f) < 1073741824.0f;
+  }
+  unsigned large = 0;
+  const long long nrem = 1LL << 40;  // all 128 particles exist
+  if (use_box)
+    dep_warp_pass<POW2, true, 4>(px, py, pz, pm, nrem, d, inv_dx, qscale, bx, qg, status, lane, large);
+  else
+    dep_warp_pass<POW2, false, 4>(px, py, pz, pm, nrem, d, inv_dx, qscale, bx, qg, status, lane, large);
+  while (large) {  // rare: point masses
+    const int j = __ffs(large) - 1;
+    large &= large - 1;
+    const int i = base + 32 * j + lane;
+    const float gx = POW2 ? __fmul_rn(s0[i], inv_dx) : __fdiv_rn(s0[i], d.dx);
+    const float gy = POW2 ? __fmul_rn(s1[i], inv_dx) : __fdiv_rn(s1[i], d.dx);
+    const float gz = POW2 ? __fmul_rn(s2[i], inv_dx) : __fdiv_rn(s2[i], d.dx);
+    const int ix = __float2int_rd(gx), iy = __float2int_rd(gy), iz = __float2int_rd(gz);
+    large_to_grid(qg, d.G, ix, iy, iz, __fmul_rn(s6[i], d.inv_vol), __fsub_rn(gx, __int2float_rn(ix)),
+                  __fsub_rn(gy, __int2float_rn(iy)), __fsub_rn(gz, __int2float_rn(iz)), qscale);
+  }
+  if (use_box) {
+    __syncwarp();
+    const int vol = nx * bx.nyz;
+    for (int i = lane; i < vol; i += 32) {
+      const int v = wbox[i];
+      if (v == 0) continue;
+      wbox[i] = 0;
+      const int rx = i / bx.nyz, rem = i - rx * bx.nyz, ry = rem / bx.nz, rz = rem - ry * bx.nz;
+      const int jx = bx.x0 + rx, jy = bx.y0 + ry, jz = bx.z0 + rz;
+      if ((unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G && (unsigned)jz < (unsigned)d.G)
+        atomicAdd((unsigned long long *)(qg + ((size_t)jx * d.G + jy) * d.G + jz), (unsigned long long)(long long)v);
+    }
+    __syncwarp();
+  }
+}
+
+// One particle of the remainder: its corners straight to the grid.
+template <bool POW2>
+__device__ __forceinline__ void gt_deposit_one(float px, float py, float pz, float pm, const DepCtx &d, float inv_dx,
+                                               float qscale, long long *__restrict__ qg,
+                                               unsigned *__restrict__ status) {
+  float gx, gy, gz;
+  if (POW2) {
+    gx = __fmul_rn(px, inv_dx); gy = __fmul_rn(py, inv_dx); gz = __fmul_rn(pz, inv_dx);
+  } else {
+    gx = __fdiv_rn(px, d.dx); gy = __fdiv_rn(py, d.dx); gz = __fdiv_rn(pz, d.dx);
+  }
+  const float hi = (float)d.G;
+  if (!(gx >= -1.0f && gx < hi && gy >= -1.0f && gy < hi && gz >= -1.0f && gz < hi)) {
+    if (!gc_finite3(px, py, pz)) atomicOr(status, GC_FLAG_NONFINITE_POS);
+    return;
+  }
+  const int ix = __float2int_rd(gx), iy = __float2int_rd(gy), iz = __float2int_rd(gz);
+  const float fx = __fsub_rn(gx, __int2float_rn(ix)), fy = __fsub_rn(gy, __int2float_rn(iy)),
+              fz = __fsub_rn(gz, __int2float_rn(iz));
+  large_to_grid(qg, d.G, ix, iy, iz, __fmul_rn(pm, d.inv_vol), fx, fy, fz, qscale);
+}
+
+template <bool POW2, bool DEP>
 __global__ void __launch_bounds__(256)
     k_gather4_tma(float *__restrict__ x, float *__restrict__ y, float *__restrict__ z, float *__restrict__ vx,
-                  float *__restrict__ vy, float *__restrict__ vz, long long n, const float4 *__restrict__ g4, FusedCtx f,
-                  unsigned *__restrict__ status) {
+                  float *__restrict__ vy, float *__restrict__ vz, const float *__restrict__ m, long long n,
+                  const float4 *__restrict__ g4, FusedCtx f, DepCtx d, float inv_dx, const double *__restrict__ qexp,
+                  long long *__restrict__ qg, unsigned *__restrict__ status) {
   using namespace umma;
-  __shared__ __align__(128) float buf[2][6][GT_TILE];
+  constexpr int NA = DEP ? 7 : 6;
+  extern __shared__ __align__(128) float gt_smem[];
+  float *buf = gt_smem;                               // [2][NA][GT_TILE]
+  int *wboxes = reinterpret_cast<int *>(gt_smem + 2 * NA * GT_TILE);  // [8][GT_WBOX] when DEP
   __shared__ __align__(8) uint64_t bar[2];
-  float *const arr[6] = {x, y, z, vx, vy, vz};
-  const int tid = threadIdx.x;
+  const float *src[7] = {x, y, z, vx, vy, vz, m};
+  float *const dst[6] = {x, y, z, vx, vy, vz};
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long ntiles = n / GT_TILE;
+  const float qscale = DEP ? ldexpf(1.0f, -(int)(*qexp)) : 1.0f;
+  if (DEP)
+    for (int i = tid; i < 8 * GT_WBOX; i += 256) wboxes[i] = 0;  // every flush zeroes what it read
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -992,18 +1116,19 @@ __global__ void __launch_bounds__(256)
   const uint32_t tile_bytes = GT_TILE * 4;
   long long t = blockIdx.x;
   if (tid == 0 && t < ntiles) {
-    mbar_arrive_expect_tx(&bar[0], 6 * tile_bytes);
+    mbar_arrive_expect_tx(&bar[0], NA * tile_bytes);
 #pragma unroll
-    for (int a = 0; a < 6; ++a) bulk_g2s(buf[0][a], arr[a] + t * GT_TILE, tile_bytes, &bar[0]);
+    for (int a = 0; a < NA; ++a) bulk_g2s(buf + a * GT_TILE, src[a] + t * GT_TILE, tile_bytes, &bar[0]);
   }
   for (int it = 0; t < ntiles; ++it, t += gridDim.x) {
     const int b = it & 1;
+    float *cur = buf + b * NA * GT_TILE, *nxt = buf + (b ^ 1) * NA * GT_TILE;
     const long long tn = t + gridDim.x;
     if (tid == 0 && tn < ntiles) {  // prefetch the next tile into the other buffer
       bulk_wait_read_all();          // its previous tile's stores have read it
-      mbar_arrive_expect_tx(&bar[b ^ 1], 6 * tile_bytes);
+      mbar_arrive_expect_tx(&bar[b ^ 1], NA * tile_bytes);
 #pragma unroll
-      for (int a = 0; a < 6; ++a) bulk_g2s(buf[b ^ 1][a], arr[a] + tn * GT_TILE, tile_bytes, &bar[b ^ 1]);
+      for (int a = 0; a < NA; ++a) bulk_g2s(nxt + a * GT_TILE, src[a] + tn * GT_TILE, tile_bytes, &bar[b ^ 1]);
     }
     const bool got = mbar_wait(&bar[b], (uint32_t)(it >> 1) & 1u, GT_BUDGET);
     if (!__syncthreads_and(got)) {  // the block leaves together
@@ -1015,15 +1140,22 @@ __global__ void __launch_bounds__(256)
       }
       return;
     }
-    float *s0 = buf[b][0], *s1 = buf[b][1], *s2 = buf[b][2], *s3 = buf[b][3], *s4 = buf[b][4], *s5 = buf[b][5];
+    float *s0 = cur, *s1 = cur + GT_TILE, *s2 = cur + 2 * GT_TILE, *s3 = cur + 3 * GT_TILE, *s4 = cur + 4 * GT_TILE,
+          *s5 = cur + 5 * GT_TILE;
 #pragma unroll 4
     for (int i = tid; i < GT_TILE; i += 256) gt_particle<POW2>(s0, s1, s2, s3, s4, s5, i, g4, f);
     fence_async_smem();  // this thread's shared-memory writes -> visible to the bulk stores
     __syncthreads();
     if (tid == 0) {
 #pragma unroll
-      for (int a = 0; a < 6; ++a) bulk_s2g(arr[a] + t * GT_TILE, buf[b][a], tile_bytes);
+      for (int a = 0; a < 6; ++a) bulk_s2g(dst[a] + t * GT_TILE, cur + a * GT_TILE, tile_bytes);
       bulk_commit();
+    }
+    if (DEP) {  // the drifted positions' density while the stores drain
+      gt_deposit_warp<POW2>(s0, s1, s2, cur + 6 * GT_TILE, 128 * warp, wboxes + warp * GT_WBOX, d, inv_dx, qscale,
+                            qg, status, lane);
+      fence_async_smem();
+      __syncthreads();  // the buffer is free for the prefetch of the tile after next
     }
   }
   if (tid == 0) bulk_wait_all();
@@ -1042,18 +1174,23 @@ __global__ void __launch_bounds__(256)
       ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
       uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
       uz = __fadd_rn(uz, __fmul_rn(az, f.h));
-      x[p] = __fadd_rn(px, __fmul_rn(ux, f.dt));
-      y[p] = __fadd_rn(py, __fmul_rn(uy, f.dt));
-      z[p] = __fadd_rn(pz, __fmul_rn(uz, f.dt));
+      px = __fadd_rn(px, __fmul_rn(ux, f.dt));
+      py = __fadd_rn(py, __fmul_rn(uy, f.dt));
+      pz = __fadd_rn(pz, __fmul_rn(uz, f.dt));
+      x[p] = px;
+      y[p] = py;
+      z[p] = pz;
     }
     vx[p] = ux;
     vy[p] = uy;
     vz[p] = uz;
+    if (DEP) gt_deposit_one<POW2>(px, py, pz, m[p], d, inv_dx, qscale, qg, status);
   }
 }
 
 int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode, int diag, int grad_grid,
-                         float *axo, float *ayo, float *azo, int *nparts_out) {
+                         int deposit_next, float *axo, float *ayo, float *azo, int *nparts_out, int *deposited) {
+  if (deposited) *deposited = 0;
   FusedCtx f;
   f.dx = (float)ctx->dx;
   f.inv_dx = 1.0f / f.dx;
@@ -1077,12 +1214,30 @@ int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode,
     const bool pow2 = std::frexp(f.dx, &fe) == 0.5f;  // then inv_dx is exact
     const uintptr_t al = (uintptr_t)p->x | (uintptr_t)p->y | (uintptr_t)p->z | (uintptr_t)p->vx | (uintptr_t)p->vy |
                          (uintptr_t)p->vz;
+    const bool dep = deposit_next && mode != GC_STEP_CLOSE && ((uintptr_t)p->m & 15u) == 0;
     if (!diag && (al & 15u) == 0 && p->n >= GT_TILE) {
-      // bulk-streamed state: 4 CTAs of 47.6 KB shared memory per SM, persistent
+      if (!ctx->gt_smem_set) {  // opt in to more than 48 KB of dynamic shared memory (once per context)
+        GC_CUDA(ctx, cudaFuncSetAttribute(k_gather4_tma<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, GT_SMEM(false)));
+        GC_CUDA(ctx, cudaFuncSetAttribute(k_gather4_tma<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, GT_SMEM(false)));
+        GC_CUDA(ctx, cudaFuncSetAttribute(k_gather4_tma<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GT_SMEM(true)));
+        GC_CUDA(ctx, cudaFuncSetAttribute(k_gather4_tma<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, GT_SMEM(true)));
+        ctx->gt_smem_set = 1;
+      }
+      // bulk-streamed state, persistent: 4 CTAs per SM (3 when depositing: 72 KB each)
       const long long ntiles = p->n / GT_TILE;
-      const unsigned nbt = (unsigned)(ntiles < 152LL * 4 ? ntiles : 152LL * 4);
-      gc_launch(ctx, GK_GATHER_KD, pow2 ? k_gather4_tma<true> : k_gather4_tma<false>, dim3(nbt), dim3(256), 0,
-                p->x, p->y, p->z, p->vx, p->vy, p->vz, (long long)p->n, (const float4 *)ctx->g4, f, ctx->dstatus);
+      const long long per_sm = dep ? 3 : 4;
+      const unsigned nbt = (unsigned)(ntiles < 152LL * per_sm ? ntiles : 152LL * per_sm);
+      DepCtx d;
+      d.dx = (float)ctx->dx;
+      d.inv_vol = 1.0f / ((d.dx * d.dx) * d.dx);
+      d.G = ctx->G;
+      const float inv_dx_dep = pow2 ? std::ldexp(1.0f, 1 - fe) : 0.0f;
+      auto k = dep ? (pow2 ? k_gather4_tma<true, true> : k_gather4_tma<false, true>)
+                   : (pow2 ? k_gather4_tma<true, false> : k_gather4_tma<false, false>);
+      gc_launch(ctx, GK_GATHER_KD, k, dim3(nbt), dim3(256), GT_SMEM(dep), p->x, p->y, p->z, p->vx, p->vy, p->vz, p->m,
+                (long long)p->n, (const float4 *)ctx->g4, f, d, inv_dx_dep, (const double *)(ctx->dsmall + GC_S_QEXP_PM),
+                ctx->q, ctx->dstatus);
+      if (dep && deposited) *deposited = 1;
     } else {
       auto k = diag ? (pow2 ? k_gather4_kick_drift<true, true> : k_gather4_kick_drift<true, false>)
                     : (pow2 ? k_gather4_kick_drift<false, true> : k_gather4_kick_drift<false, false>);

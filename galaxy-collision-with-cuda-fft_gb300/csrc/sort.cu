@@ -431,6 +431,7 @@ extern "C" int gc_pm_import(gc_ctx *ctx, const float *pos, const float *vel, con
              "gc_pm_import: output arrays required");
   unsigned nb = gc_blocks(n, 256);
   if (nb > 152u * 32u) nb = 152u * 32u;
+  ctx->q_next_ready = 0;  // new positions: no deposit is pending
   gc_launch(ctx, GK_COPY, k_pm_import, dim3(nb), dim3(256), 0, pos, vel, m, gid, origin[0], origin[1], origin[2], *out,
             (long long)n);
   GC_LAUNCH_CHECK(ctx, "import");
@@ -512,6 +513,7 @@ extern "C" int gc_pm_import_sorted(gc_ctx *ctx, const float *pos, const float *v
              "gc_pm_import_sorted: output arrays required");
   int s = ensure_sort_scratch(ctx, n);
   if (s) return s;
+  ctx->q_next_ready = 0;  // new positions: no deposit is pending
   unsigned nb = gc_blocks(n, 256);
   if (nb > 152u * 32u) nb = 152u * 32u;
   gc_launch(ctx, GK_KEYS, k_cell_keys_aos, dim3(nb), dim3(256), 0, pos, origin[0], origin[1], origin[2], (long long)n,

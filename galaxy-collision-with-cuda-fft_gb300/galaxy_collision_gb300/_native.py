@@ -31,6 +31,7 @@ GC_MG_FIXED_CYCLES = 0x2
 GC_STEP_GRAD_GRID = 0x1
 GC_STEP_SOLVE_ONLY = 0x2
 GC_STEP_PUSH_ONLY = 0x4
+GC_STEP_DEPOSIT_NEXT = 0x8
 
 GC_WS_PLAIN = 0
 GC_WS_LEARNED = 1

@@ -41,7 +41,7 @@ class PMEngine:
     def __init__(self, grid_size: int, dx: float, grav: float = 1.0, *, origin=(0.0, 0.0, 0.0), tol: float = 1e-6,
                  max_cycles: int = 50, pre_sweeps: int = 2, post_sweeps: int = 2, coarse_sweeps: int = 40,
                  fixed_point_bits: int = 52, sort_every: int = 20, grad_grid: bool = True, fixed_cycles: int = 0,
-                 max_particles: int = 0):
+                 max_particles: int = 0, deposit_next: bool = False):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
         self.grav = float(grav)
@@ -65,6 +65,11 @@ class PMEngine:
         self.fixed_point_bits = int(fixed_point_bits)
         self.sort_every = int(sort_every)
         self.grad_grid = bool(grad_grid)  # gather from a float4 -grad(phi) grid (same results)
+        # the particle pass deposits the drifted positions for the next step (same
+        # density, one pass fewer); off by default: at 100M particles on GB300 the
+        # fused pass (1.33 ms after a sort, 1.92 ms 20 steps later) is no faster
+        # than the gather and deposit passes it replaces (1.37 / 1.86 ms)
+        self.deposit_next = bool(deposit_next)
         self.n = 0
         self.state = "empty"   # empty -> synced -> open -> synced ...
         self.steps_since_sort = 0
@@ -213,6 +218,8 @@ class PMEngine:
         sp.mg = self.mg
         sp.fixed_point_bits = self.fixed_point_bits
         sp.flags = (_native.GC_STEP_GRAD_GRID if self.grad_grid else 0) | phase_flags
+        if self.deposit_next:
+            sp.flags |= _native.GC_STEP_DEPOSIT_NEXT
         st = _native.StepStats()
         p = self._struct(self.cur)
         self.ctx.call("gc_pm_step", C.byref(p), C.byref(sp), C.byref(st), what="gc_pm_step")

@@ -119,6 +119,12 @@ typedef struct gc_step_params {
  * fixed-cycle solves can still meet the tolerance. */
 #define GC_STEP_SOLVE_ONLY 0x2
 #define GC_STEP_PUSH_ONLY 0x4
+/* gc_step_params.flags: the particle pass also deposits the drifted positions
+ * (the next step's density) into the context's fixed-point grid, and the next
+ * step given this flag skips its own deposit. PRIME always deposits; a CLOSE,
+ * gc_pm_import or gc_pm_import_sorted drops the pending deposit. Same density,
+ * bit for bit, one pass over the particles fewer. */
+#define GC_STEP_DEPOSIT_NEXT 0x8
 
 typedef struct gc_step_stats {
   gc_mg_stats mg;
