@@ -492,16 +492,28 @@ __global__ void __launch_bounds__(256)
     float bb = 0.0f;
     for (int k0 = 0; k0 < G; k0 += 32 * 8) {
       long long qv[8];
+      bool nz = false;
 #pragma unroll
       for (int t = 0; t < 8; ++t) {  // all loads of the lane in flight together
         const int k = k0 + 32 * t + lane;
         qv[t] = k < G ? p[k] : 0;
+        nz |= qv[t] != 0;
+      }
+      if (!__any_sync(0xffffffffu, nz)) {  // an empty stretch (most of a disk's box): zeros out, q stays 0
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          const int k = k0 + 32 * t + lane;
+          if (k >= G) continue;
+          if (rp) rp[k] = 0.0f;
+          if (bp) bp[k] = 0.0f;
+        }
+        continue;
       }
 #pragma unroll
       for (int t = 0; t < 8; ++t) {
         const int k = k0 + 32 * t + lane;
         if (k >= G) continue;
-        p[k] = 0;
+        if (qv[t] != 0) p[k] = 0;  // clear for the next deposit (zeros need no store)
         const float qf = i64_to_f32_rn(qv[t]);  // one rounding, as (float)q
         if (rp) rp[k] = __fmul_rn(qf, qinv);
         const float bv = __fmul_rn(qf, bscale);
