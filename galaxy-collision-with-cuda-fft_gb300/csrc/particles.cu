@@ -102,6 +102,84 @@ int gc_fixed_point_setup(gc_ctx *ctx, const float *m, int64_t n, int bits, int m
 // ------------------------------------------------------------------------------
 // deposit (deposit.py:47-82)
 // ------------------------------------------------------------------------------
+// Per-corner int64 contributions of one particle; corners outside the box are 0.
+// Returns false when the particle deposits nothing.
+__device__ __forceinline__ bool cic_contrib(float x, float y, float z, float mass, const DepCtx &d, float qscale,
+                                            CellPos &c, long long (&q)[8]) {
+  if (!gc_cell_of(x, y, z, d.dx, d.G, c)) return false;
+  const float mm = __fmul_rn(mass, d.inv_vol);
+  const float wx[2] = {__fsub_rn(1.0f, c.fx), c.fx};
+  const float wy[2] = {__fsub_rn(1.0f, c.fy), c.fy};
+  const float wz[2] = {__fsub_rn(1.0f, c.fz), c.fz};
+#pragma unroll
+  for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+      for (int cz = 0; cz < 2; ++cz) {
+        const int jx = c.ix + cx, jy = c.iy + cy, jz = c.iz + cz;
+        const bool in = (unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G && (unsigned)jz < (unsigned)d.G;
+        const float w = __fmul_rn(__fmul_rn(__fmul_rn(mm, wx[cx]), wy[cy]), wz[cz]);
+        q[(cx * 2 + cy) * 2 + cz] = in ? f32_to_i64_rn(__fmul_rn(w, qscale)) : 0LL;
+      }
+  return true;
+}
+
+__device__ __forceinline__ void flush_corners(long long *__restrict__ qg, int ix, int iy, int iz, int G,
+                                              const long long (&q)[8]) {
+#pragma unroll
+  for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+      for (int cz = 0; cz < 2; ++cz) {
+        const long long v = q[(cx * 2 + cy) * 2 + cz];
+        const int jx = ix + cx, jy = iy + cy, jz = iz + cz;
+        if (v != 0 && (unsigned)jx < (unsigned)G && (unsigned)jy < (unsigned)G && (unsigned)jz < (unsigned)G) {
+          const size_t idx = ((size_t)jx * G + jy) * G + jz;
+          atomicAdd((unsigned long long *)(qg + idx), (unsigned long long)v);
+        }
+      }
+}
+
+// One particle per thread; when a whole warp shares one cell its 8 corner sums
+// are reduced in registers and flushed by one lane.
+__global__ void __launch_bounds__(256)
+    k_deposit(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
+              const float *__restrict__ m, long long n, DepCtx d, const double *__restrict__ qexp,
+              long long *__restrict__ qg, unsigned *__restrict__ status) {
+  const float qscale = ldexpf(1.0f, -(int)(*qexp));
+  const int lane = threadIdx.x & 31;
+  const long long warp0 = (blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31));
+  const long long wstride = (long long)gridDim.x * blockDim.x;
+  for (long long base = warp0; base < n; base += wstride) {
+    const long long p = base + lane;
+    CellPos c;
+    long long q[8];
+    bool ok = false;
+    if (p < n) {
+      const float px = x[p], py = y[p], pz = z[p];
+      if (!gc_finite3(px, py, pz)) atomicOr(status, GC_FLAG_NONFINITE_POS);
+      ok = cic_contrib(px, py, pz, m[p], d, qscale, c, q);
+    }
+    const unsigned key = ok ? (unsigned)(((c.ix + 1) * (d.G + 1) + (c.iy + 1)) * (d.G + 1) + (c.iz + 1))
+                            : (0x80000000u | (unsigned)lane);
+    int all_same = 0;
+    __match_all_sync(0xffffffffu, key, &all_same);
+    if (all_same) {
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        long long v = q[t];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        q[t] = v;
+      }
+      if (lane == 0) flush_corners(qg, c.ix, c.iy, c.iz, d.G, q);
+    } else if (ok) {
+      flush_corners(qg, c.ix, c.iy, c.iz, d.G, q);
+    }
+  }
+}
+
 // Cell-sorted particles, warp-contiguous. Lane L of warp w takes the particles
 // t0 + 256 w + 32 j + L (j = 0..7) of the CTA's tile of 2048, so the 32
 // particles a warp handles at once are adjacent in the array: after the cell
