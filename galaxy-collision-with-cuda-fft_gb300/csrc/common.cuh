@@ -102,6 +102,7 @@ struct gc_ctx {
   int last_step_valid;
   int q_next_ready;     // q holds the deposit of the current positions (made by the last particle pass)
   int gt_smem_set;      // the TMA particle-pass kernels' dynamic shared-memory limit has been raised
+  int sw_smem_set;      // the streaming sweep's dynamic shared-memory limit has been raised
   int solved_once;
   gc_mg_stats last_stats;
 

@@ -438,31 +438,45 @@ __global__ void __launch_bounds__(256)
 // finest level, fused: one red-black sweep per pass, streamed along i
 // ------------------------------------------------------------------------------
 // A CTA owns a SW_TJ x SW_TK tile of (j,k) columns and a chunk of i planes. It
-// streams the planes through a 4-slot shared-memory ring (hi, lo, b with a halo
-// of 2 in j and k): after loading plane p it relaxes the red nodes of plane p-1
-// on the tile plus a 1-node halo (from old black values only) and then the black
-// nodes of plane p-2 on the tile (from the new red values), and stores plane p-2.
-// Reading from one potential buffer and writing to the other keeps every CTA on
-// old values outside its own tile, so the result is exactly the two in-place
-// half-sweeps of k_smooth0, with each datum read and written once per sweep.
-// With `corr` set, the level-1 correction is prolongated into every loaded node
-// first (the prolongation kernel fused into the first post-smoothing sweep).
+// streams the planes through a ring in shared memory (hi, lo with a halo of 2
+// in j and k; b likewise), loading plane p+1 with cp.async while it works on
+// plane p: it relaxes the red nodes of plane p-1 on the tile plus a one-node
+// ring (from old black values only), then the black nodes of plane p-2 on the
+// tile (from the new red values), and stores plane p-2. Reading one potential
+// buffer and writing the other keeps every CTA on old values outside its own
+// tile, so the result is exactly the two in-place half-sweeps of k_smooth0,
+// with each datum read and written once per sweep. Thread t relaxes one red
+// node of the tile (plus one of the ring for the first 50 threads) and one
+// black node per plane.
 #define SW_TJ 16
 #define SW_TK 32
-#define SW_H 2
+#define SW_H 2                   // halo in j
+#define SW_KO 5                  // smem column of k0 (rows start 16-byte aligned at k0 - 5)
 #define SW_EJ (SW_TJ + 2 * SW_H)
-#define SW_EK (SW_TK + 2 * SW_H)
+#define SW_EK 40                 // k0 - 5 .. k0 + 34: the halo of 2 plus alignment
 #define SW_THREADS 256
+#define SW_NS 6  // potential planes in flight: p-3 .. p+2
+#define SW_NB 5  // right-hand-side planes in flight: p-2 .. p+2
 
 struct SweepSmem {
-  float hi[4][SW_EJ][SW_EK];
-  float lo[4][SW_EJ][SW_EK];
-  float b[4][SW_EJ][SW_EK];
+  float hi[SW_NS][SW_EJ][SW_EK];
+  float lo[SW_NS][SW_EJ][SW_EK];
+  float b[SW_NB][SW_EJ][SW_EK];
 };
+
+__device__ __forceinline__ int sw_slot(int p) { return (p + 10 * SW_NS) % SW_NS; }
+__device__ __forceinline__ int sw_bslot(int p) { return (p + 10 * SW_NB) % SW_NB; }
+
+// 16-byte asynchronous copy global -> shared; zero-filled (and no global read) when !valid.
+__device__ __forceinline__ void sw_cp16(float *smem, const float *gmem, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem), "r"(valid ? 16 : 0)
+               : "memory");
+}
 
 // The red-black Gauss-Seidel update of one node from the ring (same arithmetic
 // order as df_residual + k_smooth0).
-__device__ __forceinline__ void sw_update(SweepSmem &S, int sm, int sc, int sp, int jj, int kk) {
+__device__ __forceinline__ void sw_update(SweepSmem &S, int sm, int sc, int sp, int bs, int jj, int kk) {
   const float hc = S.hi[sc][jj][kk];
   const float d0 = __fsub_rn(S.hi[sp][jj][kk], hc);
   const float d1 = __fsub_rn(S.hi[sm][jj][kk], hc);
@@ -481,7 +495,7 @@ __device__ __forceinline__ void sw_update(SweepSmem &S, int sm, int sc, int sp, 
                     S.lo[sc][jj][kk + 1]) + S.lo[sc][jj][kk - 1];
   const float ll = __fsub_rn(ln, __fmul_rn(6.0f, lc));
   float r1, r1e;
-  df_two_sum(S.b[sc][jj][kk], -s, r1, r1e);
+  df_two_sum(S.b[bs][jj][kk], -s, r1, r1e);
   const float r = __fadd_rn(r1, __fsub_rn(r1e, __fadd_rn(e, ll)));
   const float delta = __fmul_rn(r, -0.16666667f);
   float s2, e2, h3, l3;
@@ -492,10 +506,11 @@ __device__ __forceinline__ void sw_update(SweepSmem &S, int sm, int sc, int sp, 
   S.lo[sc][jj][kk] = l3;
 }
 
+// G must be a multiple of 4 (rows 16-byte aligned; a 16-byte group is wholly
+// inside or outside the grid).
 __global__ void __launch_bounds__(SW_THREADS)
     k_sweep0(const float *__restrict__ hi_in, const float *__restrict__ lo_in, const float *__restrict__ b,
-             float *__restrict__ hi_out, float *__restrict__ lo_out, int G, int chunk,
-             const float *__restrict__ corr, LevelGeom gc, LevelGeom gf) {
+             float *__restrict__ hi_out, float *__restrict__ lo_out, int G, int chunk) {
   extern __shared__ __align__(16) unsigned char sw_raw[];
   SweepSmem &S = *reinterpret_cast<SweepSmem *>(sw_raw);
   const int tid = threadIdx.x;
@@ -504,60 +519,60 @@ __global__ void __launch_bounds__(SW_THREADS)
   const int i0 = 1 + blockIdx.z * chunk;
   const int i1 = min(i0 + chunk, G - 1);  // planes [i0, i1) are relaxed and stored
   const size_t sj = (size_t)G, si = (size_t)G * G;
+  auto load_plane = [&](int p) {  // issue the copies of plane p into its slots (16-byte groups)
+    const int s = sw_slot(p), bs = sw_bslot(p);
+    for (int t = tid; t < SW_EJ * (SW_EK / 4); t += SW_THREADS) {
+      const int jj = t / (SW_EK / 4), q4 = t - jj * (SW_EK / 4);
+      const int j = j0 - SW_H + jj, k = k0 - SW_KO + 4 * q4;
+      const bool v = p >= 0 && p < G && j >= 0 && j < G && k >= 0 && k < G;
+      const size_t c = v ? (size_t)p * si + (size_t)j * sj + k : 0;
+      sw_cp16(&S.hi[s][jj][4 * q4], hi_in + c, v);
+      sw_cp16(&S.lo[s][jj][4 * q4], lo_in + c, v);
+      sw_cp16(&S.b[bs][jj][4 * q4], b + c, v);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  load_plane(i0 - 2);
+  load_plane(i0 - 1);
   for (int p = i0 - 2; p <= i1 + 1; ++p) {
-    const int s = (p + 4) & 3;
-    for (int t = tid; t < SW_EJ * SW_EK; t += SW_THREADS) {
-      const int jj = t / SW_EK, kk = t - jj * SW_EK;
-      const int j = j0 - SW_H + jj, k = k0 - SW_H + kk;
-      float h = 0.f, l = 0.f, bb = 0.f;
-      if (p >= 0 && p < G && j >= 0 && j < G && k >= 0 && k < G) {
-        const size_t c = (size_t)p * si + (size_t)j * sj + k;
-        h = hi_in[c];
-        l = lo_in[c];
-        bb = b[c];
-        if (corr && p >= 1 && p <= G - 2 && j >= 1 && j <= G - 2 && k >= 1 && k <= G - 2) {
-          const float v = prolong_value(corr, p, j, k, gf, gc);
-          float s1, e1, h1, l1;
-          df_two_sum(h, v, s1, e1);
-          const float ln1 = __fadd_rn(l, e1);
-          df_fast_two_sum(s1, ln1, h1, l1);
-          h = h1;
-          l = l1;
-        }
-      }
-      S.hi[s][jj][kk] = h;
-      S.lo[s][jj][kk] = l;
-      S.b[s][jj][kk] = bb;
+    if (p + 2 <= i1 + 1) {
+      load_plane(p + 2);
+      asm volatile("cp.async.wait_group 2;" ::: "memory");  // plane p has landed
+    } else if (p + 1 <= i1 + 1) {
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
     }
     __syncthreads();
     const int q = p - 1;  // red on plane q, tile + 1 halo
     if (q >= i0 - 1 && q <= i1 && q >= 1 && q <= G - 2) {
-      const int sc = (q + 4) & 3, sm = (q + 3) & 3, sp = (q + 5) & 3;
-      for (int t = tid; t < (SW_EJ - 2) * (SW_EK - 2); t += SW_THREADS) {
-        const int jj = 1 + t / (SW_EK - 2), kk = 1 + t % (SW_EK - 2);
-        const int j = j0 - SW_H + jj, k = k0 - SW_H + kk;
-        if (((q + j + k) & 1) != 0 || j < 1 || j > G - 2 || k < 1 || k > G - 2) continue;
-        sw_update(S, sm, sc, sp, jj, kk);
+      const int sc = sw_slot(q), sm = sw_slot(q - 1), sp = sw_slot(q + 1), bs = sw_bslot(q);
+      for (int idx = tid; idx < (SW_EJ - 2) * 17; idx += SW_THREADS) {
+        const int row = idx / 17, m = idx - row * 17;
+        const int jj = 1 + row, j = j0 - SW_H + jj;
+        const int kk = SW_KO - 1 + 2 * m + ((q + j + k0 - 1) & 1), k = k0 - SW_KO + kk;
+        if (j < 1 || j > G - 2 || k < 1 || k > G - 2) continue;
+        sw_update(S, sm, sc, sp, bs, jj, kk);
       }
     }
     __syncthreads();
     const int r = p - 2;  // black on plane r, tile only; then store plane r
     if (r >= i0 && r < i1) {
-      const int sc = (r + 4) & 3, sm = (r + 3) & 3, sp = (r + 5) & 3;
-      for (int t = tid; t < SW_TJ * SW_TK; t += SW_THREADS) {
-        const int jj = SW_H + t / SW_TK, kk = SW_H + t % SW_TK;
-        const int j = j0 - SW_H + jj, k = k0 - SW_H + kk;
-        if (((r + j + k) & 1) != 1 || j > G - 2 || k > G - 2) continue;
-        sw_update(S, sm, sc, sp, jj, kk);
+      const int sc = sw_slot(r), sm = sw_slot(r - 1), sp = sw_slot(r + 1), bs = sw_bslot(r);
+      {
+        const int row = tid >> 4, m = tid & 15;
+        const int jj = SW_H + row, j = j0 + row;
+        const int kk = SW_KO + 2 * m + (((r + j + k0) & 1) ? 0 : 1), k = k0 - SW_KO + kk;
+        if (j <= G - 2 && k <= G - 2) sw_update(S, sm, sc, sp, bs, jj, kk);
       }
       __syncthreads();
-      for (int t = tid; t < SW_TJ * SW_TK; t += SW_THREADS) {
-        const int jj = SW_H + t / SW_TK, kk = SW_H + t % SW_TK;
-        const int j = j0 - SW_H + jj, k = k0 - SW_H + kk;
+      for (int idx = tid; idx < SW_TJ * SW_TK; idx += SW_THREADS) {
+        const int row = idx >> 5, col = idx & 31;
+        const int j = j0 + row, k = k0 + col;
         if (j > G - 2 || k > G - 2) continue;
         const size_t c = (size_t)r * si + (size_t)j * sj + k;
-        hi_out[c] = S.hi[sc][jj][kk];
-        lo_out[c] = S.lo[sc][jj][kk];
+        hi_out[c] = S.hi[sc][SW_H + row][SW_KO + col];
+        lo_out[c] = S.lo[sc][SW_H + row][SW_KO + col];
       }
     }
     __syncthreads();
@@ -878,7 +893,7 @@ static dim3 node_grid(const LevelGeom &g) { return dim3(gc_blocks(g.J, 32), gc_b
 static int launch_smooth0(gc_ctx *ctx, int sweeps, int with_corr, int flags) {
   const LevelGeom &g = ctx->lev[0];
   const int G = ctx->G;
-  if (!(flags & GC_MG_FUSED_SWEEP) || sweeps == 0) {
+  if (!(flags & GC_MG_FUSED_SWEEP) || sweeps == 0 || G % 4 != 0) {
     if (with_corr) {
       gc_launch(ctx, GK_PROLONG0, k_prolong0, dim3(node_grid(g)), dim3(dim3(32, 8)), 0, ctx->e[1], ctx->lev[1],
                 ctx->hi, ctx->lo, g);
@@ -890,20 +905,32 @@ static int launch_smooth0(gc_ctx *ctx, int sweeps, int with_corr, int flags) {
     GC_LAUNCH_CHECK(ctx, "smooth0");
     return GC_OK;
   }
+  if (with_corr)  // the coarse correction first (the streaming sweep starts from the corrected potential)
+    gc_launch(ctx, GK_PROLONG0, k_prolong0, dim3(node_grid(g)), dim3(dim3(32, 8)), 0, ctx->e[1], ctx->lev[1],
+              ctx->hi, ctx->lo, g);
+  if (!ctx->sw_smem_set) {  // 54 KB of dynamic shared memory: opt in once per context
+    GC_CUDA(ctx, cudaFuncSetAttribute(k_sweep0, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem)));
+    ctx->sw_smem_set = 1;
+  }
   const int tk = (G - 2 + SW_TK - 1) / SW_TK, tj = (G - 2 + SW_TJ - 1) / SW_TJ;
-  int nchunks = (640 + tk * tj - 1) / (tk * tj);
-  const int max_chunks = (G - 2 + 7) / 8;
+  int nchunks = (152 * 4 + tk * tj - 1) / (tk * tj);  // ~4 CTAs per SM
+  const int max_chunks = (G - 2 + 15) / 16;            // chunks of at least 16 planes
   if (nchunks > max_chunks) nchunks = max_chunks;
   if (nchunks < 1) nchunks = 1;
   const int chunk = (G - 2 + nchunks - 1) / nchunks;
   nchunks = (G - 2 + chunk - 1) / chunk;
-  for (int s = 0; s < sweeps; ++s) {
-    const float *corr = (with_corr && s == 0) ? ctx->e[1] : nullptr;
+  // pairs of streaming sweeps (each swaps the buffers, so a pair leaves the
+  // potential where it started); an odd last sweep as two half-sweeps
+  for (int s = 0; s < (sweeps & ~1); ++s) {
     gc_launch(ctx, GK_SWEEP0, k_sweep0, dim3(tk, tj, nchunks), dim3(SW_THREADS), sizeof(SweepSmem), ctx->hi,
-              ctx->lo, ctx->b0, ctx->hi2, ctx->lo2, G, chunk, corr, ctx->nlev > 1 ? ctx->lev[1] : g, g);
+              ctx->lo, ctx->b0, ctx->hi2, ctx->lo2, G, chunk);
     float *t = ctx->hi; ctx->hi = ctx->hi2; ctx->hi2 = t;
     t = ctx->lo; ctx->lo = ctx->lo2; ctx->lo2 = t;
   }
+  if (sweeps & 1)
+    for (int color = 0; color < 2; ++color)
+      gc_launch(ctx, GK_SMOOTH0, k_smooth0, dim3(rb_grid(g)), dim3(dim3(RB_TX, RB_TY)), 0, ctx->hi, ctx->lo,
+                ctx->b0, ctx->G, color);
   GC_LAUNCH_CHECK(ctx, "sweep0");
   return GC_OK;
 }
