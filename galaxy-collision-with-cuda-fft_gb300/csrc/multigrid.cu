@@ -434,6 +434,62 @@ __global__ void __launch_bounds__(256)
   lo[c] = l;
 }
 
+// The same, two nodes (k, k+1), k even, per thread: the pair shares its coarse
+// loads (the even node reads coarse column k/2, the odd one k/2 and k/2 + 1)
+// and moves hi/lo as float2. Each node's sum is formed exactly as in
+// prolong_value (same weights, same order), so the result is identical.
+__global__ void __launch_bounds__(256)
+    k_prolong0x2(const float *__restrict__ ec, LevelGeom cg, float *__restrict__ hi, float *__restrict__ lo,
+                 LevelGeom f) {
+  const int k = 2 * (blockIdx.x * 32 + threadIdx.x);
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  if (j > f.J || k > f.J) return;  // k + 1 <= f.J + 1 = n - 1 stays inside the row (n even: c is even)
+  const size_t n = f.n;
+  const size_t c = ((size_t)i * n + j) * n + k;
+  const bool u0 = k >= 1, u1 = k + 1 <= f.J;  // interior nodes of the pair
+  int ci, cj, ck0, ck1;
+  float wi0, wi1, wj0, wj1, a0, a1, b0, b1;
+  const int ni = prolong_w(i, f, cg, ci, wi0, wi1);
+  const int nj = prolong_w(j, f, cg, cj, wj0, wj1);
+  const int nk0 = prolong_w(k, f, cg, ck0, a0, a1);      // even: one coarse column, weight 1
+  const int nk1 = prolong_w(k + 1, f, cg, ck1, b0, b1);  // odd: ck1 == ck0, one or two columns
+  const size_t m = cg.n;
+  float v0 = 0.0f, v1 = 0.0f;
+  for (int a = 0; a < ni; ++a) {
+    const float wa = a ? wi1 : wi0;
+    for (int bb = 0; bb < nj; ++bb) {
+      const float wb = bb ? wj1 : wj0;
+      const size_t row = ((size_t)(ci + a) * m + (cj + bb)) * m;
+      const float wab = wa * wb;
+      const float e0 = ec[row + ck0];
+      const float e1 = (nk0 == 2 || nk1 == 2) ? ec[row + ck0 + 1] : 0.0f;
+      v0 += wab * a0 * e0;
+      if (nk0 == 2) v0 += wab * a1 * e1;
+      v1 += wab * b0 * (ck1 == ck0 ? e0 : e1);
+      if (nk1 == 2) v1 += wab * b1 * ec[row + ck1 + 1];
+    }
+  }
+  float2 h = *reinterpret_cast<const float2 *>(hi + c);
+  float2 l = *reinterpret_cast<const float2 *>(lo + c);
+  if (u0) {
+    float s1, e1, hh, ll;
+    df_two_sum(h.x, v0, s1, e1);
+    df_fast_two_sum(s1, __fadd_rn(l.x, e1), hh, ll);
+    h.x = hh;
+    l.x = ll;
+  }
+  if (u1) {
+    float s1, e1, hh, ll;
+    df_two_sum(h.y, v1, s1, e1);
+    df_fast_two_sum(s1, __fadd_rn(l.y, e1), hh, ll);
+    h.y = hh;
+    l.y = ll;
+  }
+  *reinterpret_cast<float2 *>(hi + c) = h;
+  *reinterpret_cast<float2 *>(lo + c) = l;
+}
+
 // ------------------------------------------------------------------------------
 // finest level, fused: one red-black sweep per pass, streamed along i
 // ------------------------------------------------------------------------------
@@ -885,6 +941,22 @@ static dim3 rb_grid(const LevelGeom &g) {
   return dim3(gc_blocks(nkk, RB_TX), gc_blocks(g.J, RB_TY), (unsigned)g.J);
 }
 static dim3 node_grid(const LevelGeom &g) { return dim3(gc_blocks(g.J, 32), gc_blocks(g.J, 8), (unsigned)g.J); }
+// pairs (k, k+1), k = 0, 2, ..., J: J/2 + 1 pairs per row
+static dim3 pair_grid(const LevelGeom &g) {
+  return dim3(gc_blocks(g.J / 2 + 1, 32), gc_blocks(g.J, 8), (unsigned)g.J);
+}
+
+// Add the level-1 correction into the finest double-float potential: pairs of
+// nodes per thread when rows have an even length (so every pair starts on an
+// 8-byte boundary), one node per thread otherwise.
+static void launch_prolong0(gc_ctx *ctx, const LevelGeom &g) {
+  if (g.n % 2 == 0)
+    gc_launch(ctx, GK_PROLONG0, k_prolong0x2, dim3(pair_grid(g)), dim3(dim3(32, 8)), 0, ctx->e[1], ctx->lev[1],
+              ctx->hi, ctx->lo, g);
+  else
+    gc_launch(ctx, GK_PROLONG0, k_prolong0, dim3(node_grid(g)), dim3(dim3(32, 8)), 0, ctx->e[1], ctx->lev[1],
+              ctx->hi, ctx->lo, g);
+}
 
 // Finest-level smoothing: `sweeps` red-black sweeps, the first one preceded by
 // the prolongation of the level-1 correction when `with_corr` is set. Default:
@@ -895,8 +967,7 @@ static int launch_smooth0(gc_ctx *ctx, int sweeps, int with_corr, int flags) {
   const int G = ctx->G;
   if (!(flags & GC_MG_FUSED_SWEEP) || sweeps == 0 || G % 4 != 0) {
     if (with_corr) {
-      gc_launch(ctx, GK_PROLONG0, k_prolong0, dim3(node_grid(g)), dim3(dim3(32, 8)), 0, ctx->e[1], ctx->lev[1],
-                ctx->hi, ctx->lo, g);
+      launch_prolong0(ctx, g);
     }
     for (int s = 0; s < sweeps; ++s)
       for (int color = 0; color < 2; ++color)
@@ -906,8 +977,7 @@ static int launch_smooth0(gc_ctx *ctx, int sweeps, int with_corr, int flags) {
     return GC_OK;
   }
   if (with_corr)  // the coarse correction first (the streaming sweep starts from the corrected potential)
-    gc_launch(ctx, GK_PROLONG0, k_prolong0, dim3(node_grid(g)), dim3(dim3(32, 8)), 0, ctx->e[1], ctx->lev[1],
-              ctx->hi, ctx->lo, g);
+    launch_prolong0(ctx, g);
   if (!ctx->sw_smem_set) {  // 54 KB of dynamic shared memory: opt in once per context
     GC_CUDA(ctx, cudaFuncSetAttribute(k_sweep0, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem)));
     ctx->sw_smem_set = 1;
