@@ -103,6 +103,8 @@ struct gc_ctx {
   int q_next_ready;     // q holds the deposit of the current positions (made by the last particle pass)
   int gt_smem_set;      // the TMA particle-pass kernels' dynamic shared-memory limit has been raised
   int sw_smem_set;      // the streaming sweep's dynamic shared-memory limit has been raised
+  const uint32_t *import_perm;  // gc_pm_import_order's permutation (in the sort scratch) ...
+  int64_t import_n;             // ... for this many particles (0: none pending)
   int solved_once;
   gc_mg_stats last_stats;
 

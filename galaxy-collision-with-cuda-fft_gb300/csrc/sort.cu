@@ -244,6 +244,8 @@ extern "C" int gc_pm_reserve(gc_ctx *ctx, int64_t n) {
 
 int gc_radix_sort_pairs(gc_ctx *ctx, const uint32_t *keys_in, const uint32_t *vals_in, int64_t n, int bits,
                         uint32_t **keys_out, uint32_t **vals_out) {
+  ctx->import_n = 0;  // the scratch is about to be reused: a kept import order is gone
+  ctx->import_perm = nullptr;
   int s = ensure_sort_scratch(ctx, n);
   if (s) return s;
   const int ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
@@ -501,16 +503,14 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-extern "C" int gc_pm_import_sorted(gc_ctx *ctx, const float *pos, const float *vel, const float *m, const int32_t *gid,
-                                   const double origin[3], const gc_particles *out) {
+// Phase 1 of gc_pm_import_sorted: keys from the interleaved positions and the
+// stable sort; the permutation stays in the context's scratch for phase 2.
+extern "C" int gc_pm_import_order(gc_ctx *ctx, const float *pos, const double origin[3], int64_t n) {
   if (!ctx) return GC_ERR_ARG;
-  GC_REQUIRE(ctx, out && origin, "gc_pm_import_sorted: NULL particle set or origin");
-  const int64_t n = out->n;
-  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  GC_REQUIRE(ctx, origin && n >= 0 && n < (1LL << 31), "gc_pm_import_order: bad arguments");
+  ctx->import_n = 0;
   if (n == 0) return GC_OK;
-  GC_REQUIRE(ctx, pos && vel && m, "gc_pm_import_sorted: NULL input");
-  GC_REQUIRE(ctx, out->x && out->y && out->z && out->vx && out->vy && out->vz && out->m,
-             "gc_pm_import_sorted: output arrays required");
+  GC_REQUIRE(ctx, pos, "gc_pm_import_order: NULL positions");
   int s = ensure_sort_scratch(ctx, n);
   if (s) return s;
   ctx->q_next_ready = 0;  // new positions: no deposit is pending
@@ -521,8 +521,39 @@ extern "C" int gc_pm_import_sorted(gc_ctx *ctx, const float *pos, const float *v
   GC_LAUNCH_CHECK(ctx, "cell keys");
   uint32_t *ko, *vo;
   if ((s = gc_radix_sort_pairs(ctx, ctx->keys2, ctx->vals2, n, key_bits(ctx->G), &ko, &vo))) return s;
-  gc_launch(ctx, GK_PERMUTE, k_import_gather, dim3(nb), dim3(256), 0, pos, vel, m, gid, origin[0], origin[1],
-            origin[2], (const uint32_t *)vo, *out, (long long)n);
-  GC_LAUNCH_CHECK(ctx, "import gather");
+  ctx->import_perm = vo;
+  ctx->import_n = n;
   return GC_OK;
+}
+
+// Phase 2: every particle gathered from the interleaved arrays into cell order.
+extern "C" int gc_pm_import_gather(gc_ctx *ctx, const float *pos, const float *vel, const float *m, const int32_t *gid,
+                                   const double origin[3], const gc_particles *out) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, out && origin, "gc_pm_import_gather: NULL particle set or origin");
+  const int64_t n = out->n;
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  if (n == 0) return GC_OK;
+  GC_REQUIRE(ctx, ctx->import_n == n && ctx->import_perm,
+             "gc_pm_import_gather: no gc_pm_import_order of %lld particles before it", (long long)n);
+  GC_REQUIRE(ctx, pos && vel && m, "gc_pm_import_gather: NULL input");
+  GC_REQUIRE(ctx, out->x && out->y && out->z && out->vx && out->vy && out->vz && out->m,
+             "gc_pm_import_gather: output arrays required");
+  unsigned nb = gc_blocks(n, 256);
+  if (nb > 152u * 32u) nb = 152u * 32u;
+  gc_launch(ctx, GK_PERMUTE, k_import_gather, dim3(nb), dim3(256), 0, pos, vel, m, gid, origin[0], origin[1],
+            origin[2], ctx->import_perm, *out, (long long)n);
+  GC_LAUNCH_CHECK(ctx, "import gather");
+  ctx->import_n = 0;
+  ctx->import_perm = nullptr;
+  return GC_OK;
+}
+
+extern "C" int gc_pm_import_sorted(gc_ctx *ctx, const float *pos, const float *vel, const float *m, const int32_t *gid,
+                                   const double origin[3], const gc_particles *out) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, out && origin, "gc_pm_import_sorted: NULL particle set or origin");
+  int s = gc_pm_import_order(ctx, pos, origin, out->n);
+  if (s) return s;
+  return gc_pm_import_gather(ctx, pos, vel, m, gid, origin, out);
 }

@@ -88,6 +88,7 @@ class PMEngine:
             self.cur = self._alloc(n)
             self.alt = self._alloc(n)
         self.ctx.call("gc_pm_reserve", n, what="gc_pm_reserve")
+        self._side_stream()  # the copy stream of load and export
 
     # -- state ------------------------------------------------------------------
     @staticmethod
@@ -145,15 +146,28 @@ class PMEngine:
             return dst
 
         pos_d = staged(pos_t, 0, (n, 3), torch.float32)
-        vel_d = staged(vel, 3 * st, (n, 3), torch.float32)
-        m_d = staged(mass, 6 * st, (n,), torch.float32)
-        gid_d = None if gid is None else staged(gid, 7 * st, (n,), torch.int32)
         out = self._struct(self.cur)
-        # with sort, keys come from the staged positions and the particles are
-        # gathered straight into cell order (same result as import + sort)
-        self.ctx.call("gc_pm_import_sorted" if sort else "gc_pm_import", pos_d.data_ptr(), vel_d.data_ptr(),
-                      m_d.data_ptr(), None if gid_d is None else gid_d.data_ptr(), origin, C.byref(out),
-                      what="gc_pm_import")
+        main = torch.cuda.current_stream()
+        if sort:
+            # the positions are keyed and sorted while the other arrays are still
+            # being copied (on a side stream); then everything is gathered into
+            # cell order (same result as import + sort)
+            side = self._side_stream()
+            side.wait_stream(main)
+            with torch.cuda.stream(side):
+                vel_d = staged(vel, 3 * st, (n, 3), torch.float32)
+                m_d = staged(mass, 6 * st, (n,), torch.float32)
+                gid_d = None if gid is None else staged(gid, 7 * st, (n,), torch.int32)
+            self.ctx.call("gc_pm_import_order", pos_d.data_ptr(), origin, n, what="gc_pm_import_order")
+            main.wait_stream(side)
+            self.ctx.call("gc_pm_import_gather", pos_d.data_ptr(), vel_d.data_ptr(), m_d.data_ptr(),
+                          None if gid_d is None else gid_d.data_ptr(), origin, C.byref(out), what="gc_pm_import")
+        else:
+            vel_d = staged(vel, 3 * st, (n, 3), torch.float32)
+            m_d = staged(mass, 6 * st, (n,), torch.float32)
+            gid_d = None if gid is None else staged(gid, 7 * st, (n,), torch.int32)
+            self.ctx.call("gc_pm_import", pos_d.data_ptr(), vel_d.data_ptr(), m_d.data_ptr(),
+                          None if gid_d is None else gid_d.data_ptr(), origin, C.byref(out), what="gc_pm_import")
         self.state = "synced"
         self.steps_since_sort = 0
         self._graphs = {}
@@ -188,11 +202,27 @@ class PMEngine:
             outs.append((t, None if direct else stage[off:off + t.numel()].view(dtype).view(shape)))
             ptrs.append(t.data_ptr() if direct else outs[-1][1].data_ptr())
         src = self._struct(self.cur)
-        self.ctx.call("gc_pm_export", C.byref(src), self._origin_c(), *ptrs, what="gc_pm_export")
-        for t, s in outs:
-            if t is not None and s is not None:
-                t.copy_(s, non_blocking=t.is_pinned())
+        main = torch.cuda.current_stream()
+        side = self._side_stream()
+        # one array at a time: each staged host copy runs on the side stream
+        # while the next array is being written (the scatters are independent)
+        for a, (t, stg) in enumerate(outs):
+            if t is None:
+                continue
+            one = [None] * 4
+            one[a] = ptrs[a]
+            self.ctx.call("gc_pm_export", C.byref(src), self._origin_c(), *one, what="gc_pm_export")
+            if stg is not None:
+                side.wait_stream(main)
+                with torch.cuda.stream(side):
+                    t.copy_(stg, non_blocking=t.is_pinned())
+        main.wait_stream(side)
         return tuple(t for t, _ in outs)
+
+    def _side_stream(self):
+        if getattr(self, "_side", None) is None:
+            self._side = torch.cuda.Stream()
+        return self._side
 
     def _struct(self, f) -> _native.Particles:
         p = _native.Particles()

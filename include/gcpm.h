@@ -337,6 +337,14 @@ int gc_pm_import(gc_ctx *ctx, const float *pos, const float *vel, const float *m
  * identical to gc_pm_import + gc_pm_sort. */
 int gc_pm_import_sorted(gc_ctx *ctx, const float *pos, const float *vel, const float *m, const int32_t *gid,
                         const double origin[3], const gc_particles *out);
+/* gc_pm_import_sorted in two phases, so that the copies of vel, m and gid can
+ * still be in flight (on another stream) while the positions are keyed and
+ * sorted: gc_pm_import_order reads only pos and keeps the permutation in the
+ * context; gc_pm_import_gather (n must match; no other sort in between) then
+ * gathers every array into cell order. */
+int gc_pm_import_order(gc_ctx *ctx, const float *pos, const double origin[3], int64_t n);
+int gc_pm_import_gather(gc_ctx *ctx, const float *pos, const float *vel, const float *m, const int32_t *gid,
+                        const double origin[3], const gc_particles *out);
 
 /* The inverse, in the original particle order: for every i, with q = p->pid[i],
  * pos[3q+c] = f32((double)x_c[i] + origin[c]), vel[3q+c] = v_c[i], m_out[q],
