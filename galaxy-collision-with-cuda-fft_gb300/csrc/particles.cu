@@ -773,15 +773,84 @@ __device__ __forceinline__ void gather_grad(const float *__restrict__ phi, float
       }
 }
 
+// Per-thread diagnostic sums (diagnostics_device.py:56-74: M, KE, P, L, M x) in
+// double-float: every product of f32 state is formed exactly (TwoProduct with an
+// FMA) or to ~2^-46, and accumulated as an unevaluated sum hi + lo (Knuth's
+// TwoSum), all in FP32 instructions; the per-thread totals go to FP64 for the
+// block and grid reductions. FP64 arithmetic per particle would run at a small
+// fraction of the FP32 rate on this part (it cost ~4 ms per 100M particles).
+struct DiagAcc {
+  float h[11], l[11];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int t = 0; t < 11; ++t) h[t] = l[t] = 0.0f;
+  }
+  // exact a*b = p + e
+  static __device__ __forceinline__ void tp(float a, float b, float &p, float &e) {
+    p = __fmul_rn(a, b);
+    e = __fmaf_rn(a, b, -p);
+  }
+  // exact a+b = s + e
+  static __device__ __forceinline__ void ts(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  }
+  __device__ __forceinline__ void add(int t, float ph, float pl) {
+    float s, e;
+    ts(h[t], ph, s, e);
+    h[t] = s;
+    l[t] = __fadd_rn(l[t], __fadd_rn(e, pl));
+  }
+  // m (a*b - c*d) to ~2^-46 relative
+  static __device__ __forceinline__ void cross(float m, float a, float b, float c, float d, float &q, float &ql) {
+    float p1, e1, p2, e2, s, r, qe;
+    tp(a, b, p1, e1);
+    tp(c, d, p2, e2);
+    ts(p1, -p2, s, r);
+    const float sl = __fadd_rn(r, __fsub_rn(e1, e2));
+    tp(s, m, q, qe);
+    ql = __fmaf_rn(sl, m, qe);
+  }
+  __device__ __forceinline__ void particle(float m, float X, float Y, float Z, float VX, float VY, float VZ) {
+    float p, e, q, ql;
+    add(0, m, 0.0f);
+    {  // 0.5 m |v|^2
+      float a1, e1, a2, e2, a3, e3, s1, r1, s2, r2, qe;
+      tp(VX, VX, a1, e1);
+      tp(VY, VY, a2, e2);
+      tp(VZ, VZ, a3, e3);
+      ts(a1, a2, s1, r1);
+      ts(s1, a3, s2, r2);
+      const float sl = __fadd_rn(__fadd_rn(__fadd_rn(e1, e2), e3), __fadd_rn(r1, r2));
+      tp(s2, m, q, qe);
+      ql = __fmaf_rn(sl, m, qe);
+      add(1, __fmul_rn(0.5f, q), __fmul_rn(0.5f, ql));
+    }
+    tp(m, VX, p, e); add(2, p, e);
+    tp(m, VY, p, e); add(3, p, e);
+    tp(m, VZ, p, e); add(4, p, e);
+    cross(m, Y, VZ, Z, VY, q, ql); add(5, q, ql);
+    cross(m, Z, VX, X, VZ, q, ql); add(6, q, ql);
+    cross(m, X, VY, Y, VX, q, ql); add(7, q, ql);
+    tp(m, X, p, e); add(8, p, e);
+    tp(m, Y, p, e); add(9, p, e);
+    tp(m, Z, p, e); add(10, p, e);
+  }
+  __device__ __forceinline__ void to_double(double (&dv)[11]) const {
+#pragma unroll
+    for (int t = 0; t < 11; ++t) dv[t] = (double)h[t] + (double)l[t];
+  }
+};
+
 template <bool DIAG>
 __global__ void __launch_bounds__(256)
     k_gather_kick_drift(float *__restrict__ x, float *__restrict__ y, float *__restrict__ z, float *__restrict__ vx,
                         float *__restrict__ vy, float *__restrict__ vz, const float *__restrict__ m, long long n,
                         const float *__restrict__ phi, FusedCtx f, float *__restrict__ axo, float *__restrict__ ayo,
                         float *__restrict__ azo, double *__restrict__ parts) {
-  double dv[11];
-#pragma unroll
-  for (int t = 0; t < 11; ++t) dv[t] = 0.0;
+  DiagAcc acc;
+  acc.zero();
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     float px = x[p], py = y[p], pz = z[p];
     float ux = vx[p], uy = vy[p], uz = vz[p];
@@ -798,19 +867,7 @@ __global__ void __launch_bounds__(256)
       uz = __fadd_rn(uz, __fmul_rn(az, f.h));
     }
     if (DIAG) {  // synchronised state (diagnostics_device.py:56-74)
-      const double mm = m[p];
-      const double X = px, Y = py, Z = pz, VX = ux, VY = uy, VZ = uz;
-      dv[0] += mm;
-      dv[1] += 0.5 * mm * (VX * VX + VY * VY + VZ * VZ);
-      dv[2] += mm * VX;
-      dv[3] += mm * VY;
-      dv[4] += mm * VZ;
-      dv[5] += mm * (Y * VZ - Z * VY);
-      dv[6] += mm * (Z * VX - X * VZ);
-      dv[7] += mm * (X * VY - Y * VX);
-      dv[8] += mm * X;
-      dv[9] += mm * Y;
-      dv[10] += mm * Z;
+      acc.particle(m[p], px, py, pz, ux, uy, uz);
     }
     if (f.mode != GC_STEP_CLOSE) {  // opening half-kick + drift (integrator.py:128-129)
       ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
@@ -824,7 +881,11 @@ __global__ void __launch_bounds__(256)
     vy[p] = uy;
     vz[p] = uz;
   }
-  if (DIAG) block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
+  if (DIAG) {
+    double dv[11];
+    acc.to_double(dv);
+    block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
+  }
 }
 
 // Variant with the node field g = -grad(phi) precomputed as float4 (x, y, z, 0):
@@ -887,26 +948,14 @@ __device__ __forceinline__ void kd_update(long long p, float px, float py, float
                                           float ax, float ay, float az, float *__restrict__ x, float *__restrict__ y,
                                           float *__restrict__ z, float *__restrict__ vx, float *__restrict__ vy,
                                           float *__restrict__ vz, const float *__restrict__ m, const FusedCtx &f,
-                                          double (&dv)[11]) {
+                                          DiagAcc &acc) {
   if (f.mode != GC_STEP_PRIME) {
     ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
     uy = __fadd_rn(uy, __fmul_rn(ay, f.h));
     uz = __fadd_rn(uz, __fmul_rn(az, f.h));
   }
   if (DIAG) {
-    const double mm = m[p];
-    const double X = px, Y = py, Z = pz, VX = ux, VY = uy, VZ = uz;
-    dv[0] += mm;
-    dv[1] += 0.5 * mm * (VX * VX + VY * VY + VZ * VZ);
-    dv[2] += mm * VX;
-    dv[3] += mm * VY;
-    dv[4] += mm * VZ;
-    dv[5] += mm * (Y * VZ - Z * VY);
-    dv[6] += mm * (Z * VX - X * VZ);
-    dv[7] += mm * (X * VY - Y * VX);
-    dv[8] += mm * X;
-    dv[9] += mm * Y;
-    dv[10] += mm * Z;
+    acc.particle(m[p], px, py, pz, ux, uy, uz);
   }
   if (f.mode != GC_STEP_CLOSE) {
     ux = __fadd_rn(ux, __fmul_rn(ax, f.h));
@@ -926,9 +975,8 @@ __global__ void __launch_bounds__(256)
     k_gather4_kick_drift(float *__restrict__ x, float *__restrict__ y, float *__restrict__ z, float *__restrict__ vx,
                          float *__restrict__ vy, float *__restrict__ vz, const float *__restrict__ m, long long n,
                          const float4 *__restrict__ g4, FusedCtx f, double *__restrict__ parts) {
-  double dv[11];
-#pragma unroll
-  for (int t = 0; t < 11; ++t) dv[t] = 0.0;
+  DiagAcc acc;
+  acc.zero();
   // software pipelined: the next particle's state is loaded before this one's
   // corner gather, so its DRAM latency overlaps the gather's L2 latency
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -941,9 +989,13 @@ __global__ void __launch_bounds__(256)
     if (q < n) { nx = x[q]; ny = y[q]; nz = z[q]; nvx = vx[q]; nvy = vy[q]; nvz = vz[q]; }
     float ax, ay, az;
     gather_g4<POW2>(g4, px, py, pz, f, ax, ay, az);
-    kd_update<DIAG>(p, px, py, pz, ux, uy, uz, ax, ay, az, x, y, z, vx, vy, vz, m, f, dv);
+    kd_update<DIAG>(p, px, py, pz, ux, uy, uz, ax, ay, az, x, y, z, vx, vy, vz, m, f, acc);
   }
-  if (DIAG) block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
+  if (DIAG) {
+    double dv[11];
+    acc.to_double(dv);
+    block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
+  }
 }
 
 // The same particle pass with the particle state streamed by the TMA engine: a
@@ -1275,24 +1327,13 @@ __global__ void __launch_bounds__(256)
     k_diag_particles(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
                      const float *__restrict__ vx, const float *__restrict__ vy, const float *__restrict__ vz,
                      const float *__restrict__ m, long long n, double *__restrict__ parts) {
-  double dv[11];
-#pragma unroll
-  for (int t = 0; t < 11; ++t) dv[t] = 0.0;
+  DiagAcc acc;
+  acc.zero();
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
-    const double mm = m[p];
-    const double X = x[p], Y = y[p], Z = z[p], VX = vx[p], VY = vy[p], VZ = vz[p];
-    dv[0] += mm;
-    dv[1] += 0.5 * mm * (VX * VX + VY * VY + VZ * VZ);
-    dv[2] += mm * VX;
-    dv[3] += mm * VY;
-    dv[4] += mm * VZ;
-    dv[5] += mm * (Y * VZ - Z * VY);
-    dv[6] += mm * (Z * VX - X * VZ);
-    dv[7] += mm * (X * VY - Y * VX);
-    dv[8] += mm * X;
-    dv[9] += mm * Y;
-    dv[10] += mm * Z;
+    acc.particle(m[p], x[p], y[p], z[p], vx[p], vy[p], vz[p]);
   }
+  double dv[11];
+  acc.to_double(dv);
   block_partials<11>(dv, parts + (size_t)blockIdx.x * 11);
 }
 
