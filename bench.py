@@ -571,7 +571,7 @@ def _e2e(args, icr, make_engine, dt):
     return {"value": n * args.steps / t, "unit": UNIT, "h2d_bytes_per_step": int(n * 32 / args.steps),
             "d2h_bytes_per_step": int((n * 24 + 12 * 8) / args.steps),
             "note": "wall clock around load (pinned H2D of the reference layout, cell sort and gather into cell order), "
-                    "prime, steps-1 advances, close with FP64 diagnostics, export in the original order + "
+                    "prime, steps-1 advances, close with diagnostics, export in the original order + "
                     "pinned D2H of positions and velocities (the pinned buffers are mapped by one untimed transfer "
                     "before, as part of pinning)"}
 

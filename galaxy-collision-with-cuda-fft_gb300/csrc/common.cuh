@@ -105,6 +105,7 @@ struct gc_ctx {
   int sw_smem_set;      // the streaming sweep's dynamic shared-memory limit has been raised
   const uint32_t *import_perm;  // gc_pm_import_order's permutation (in the sort scratch) ...
   int64_t import_n;             // ... for this many particles (0: none pending)
+  int64_t export_n;             // gc_pm_export_order's ranks (in ctx->keys) are for this many particles (0: none)
   int solved_once;
   gc_mg_stats last_stats;
 

@@ -102,6 +102,9 @@ int gc_ensure_red(gc_ctx *ctx, size_t ndoubles) {
 
 int gc_ensure_particle_scratch(gc_ctx *ctx, size_t n) {
   if (ctx->pcap >= n) return GC_OK;
+  ctx->import_n = 0;  // a kept import order or export rank lives in these buffers
+  ctx->import_perm = nullptr;
+  ctx->export_n = 0;
   GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   cudaFree(ctx->keys); cudaFree(ctx->keys2); cudaFree(ctx->vals); cudaFree(ctx->vals2);
   ctx->keys = ctx->keys2 = ctx->vals = ctx->vals2 = nullptr;

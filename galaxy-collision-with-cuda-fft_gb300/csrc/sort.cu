@@ -246,6 +246,7 @@ int gc_radix_sort_pairs(gc_ctx *ctx, const uint32_t *keys_in, const uint32_t *va
                         uint32_t **keys_out, uint32_t **vals_out) {
   ctx->import_n = 0;  // the scratch is about to be reused: a kept import order is gone
   ctx->import_perm = nullptr;
+  ctx->export_n = 0;  // ... and so are kept export ranks
   int s = ensure_sort_scratch(ctx, n);
   if (s) return s;
   const int ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
@@ -459,6 +460,94 @@ extern "C" int gc_pm_export(gc_ctx *ctx, const gc_particles *p, const double ori
   return GC_OK;
 }
 
+// ---- export as a gather over the original order ---------------------------------
+// gc_pm_export scatters (random writes, the whole output at once); this pair
+// first inverts pid (rank[pid[i]] = i, in the sort scratch), then writes any
+// range [q0, q1) of the original order with coalesced stores, so that a caller
+// can copy each finished range to the host while the next one is written.
+__global__ void __launch_bounds__(256)
+    k_export_rank(const int32_t *__restrict__ pid, long long n, uint32_t *__restrict__ rank,
+                  unsigned *__restrict__ status) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const long long q = pid[p];
+    if (q < 0 || q >= n) {
+      atomicOr(status, GC_FLAG_BAD_PID);
+      continue;
+    }
+    rank[q] = (uint32_t)p;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_export_range(gc_particles s, const uint32_t *__restrict__ rank, double ox, double oy, double oz,
+                   float *__restrict__ pos, float *__restrict__ vel, float *__restrict__ m, int32_t *__restrict__ gid,
+                   long long q0, long long q1, unsigned *__restrict__ status) {
+  for (long long q = q0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; q < q1;
+       q += (long long)gridDim.x * blockDim.x) {
+    const uint32_t r = rank[q];
+    if (r == 0xffffffffu) {  // no particle claims this original index
+      atomicOr(status, GC_FLAG_BAD_PID);
+      continue;
+    }
+    if (pos) {
+      pos[3 * q] = (float)((double)s.x[r] + ox);
+      pos[3 * q + 1] = (float)((double)s.y[r] + oy);
+      pos[3 * q + 2] = (float)((double)s.z[r] + oz);
+    }
+    if (vel) {
+      vel[3 * q] = s.vx[r];
+      vel[3 * q + 1] = s.vy[r];
+      vel[3 * q + 2] = s.vz[r];
+    }
+    if (m) m[q] = s.m[r];
+    if (gid) gid[q] = s.gid ? s.gid[r] : 0;
+  }
+}
+
+extern "C" int gc_pm_export_order(gc_ctx *ctx, const gc_particles *p) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, p, "gc_pm_export_order: NULL particle set");
+  const int64_t n = p->n;
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  ctx->export_n = 0;
+  if (n == 0) return GC_OK;
+  GC_REQUIRE(ctx, p->pid, "gc_pm_export_order: pid required");
+  int s = gc_ensure_particle_scratch(ctx, (size_t)n);
+  if (s) return s;
+  ctx->import_n = 0;  // the ranks take the scratch
+  ctx->import_perm = nullptr;
+  GC_CUDA(ctx, cudaMemsetAsync(ctx->keys, 0xff, (size_t)n * sizeof(uint32_t), ctx->stream));
+  unsigned nb = gc_blocks(n, 256);
+  if (nb > 152u * 32u) nb = 152u * 32u;
+  gc_launch(ctx, GK_COPY, k_export_rank, dim3(nb), dim3(256), 0, (const int32_t *)p->pid, (long long)n, ctx->keys,
+            ctx->dstatus);
+  GC_LAUNCH_CHECK(ctx, "export rank");
+  ctx->export_n = n;
+  return GC_OK;
+}
+
+extern "C" int gc_pm_export_range(gc_ctx *ctx, const gc_particles *p, const double origin[3], float *pos, float *vel,
+                                  float *m_out, int32_t *gid_out, int64_t q0, int64_t q1) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, p && origin, "gc_pm_export_range: NULL particle set or origin");
+  const int64_t n = p->n;
+  GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
+  GC_REQUIRE(ctx, q0 >= 0 && q0 <= q1 && q1 <= n, "gc_pm_export_range: range [%lld, %lld) outside [0, %lld)",
+             (long long)q0, (long long)q1, (long long)n);
+  if (q0 == q1) return GC_OK;
+  GC_REQUIRE(ctx, ctx->export_n == n, "gc_pm_export_range: no gc_pm_export_order of %lld particles before it",
+             (long long)n);
+  GC_REQUIRE(ctx, !pos || (p->x && p->y && p->z), "gc_pm_export_range: positions missing");
+  GC_REQUIRE(ctx, !vel || (p->vx && p->vy && p->vz), "gc_pm_export_range: velocities missing");
+  GC_REQUIRE(ctx, !m_out || p->m, "gc_pm_export_range: masses missing");
+  unsigned nb = gc_blocks(q1 - q0, 256);
+  if (nb > 152u * 32u) nb = 152u * 32u;
+  gc_launch(ctx, GK_COPY, k_export_range, dim3(nb), dim3(256), 0, *p, (const uint32_t *)ctx->keys, origin[0],
+            origin[1], origin[2], pos, vel, m_out, gid_out, (long long)q0, (long long)q1, ctx->dstatus);
+  GC_LAUNCH_CHECK(ctx, "export range");
+  return GC_OK;
+}
+
 // ---- import straight into cell order ---------------------------------------------
 // Keys from the interleaved physical positions (the origin subtracted in f64,
 // as gc_pm_import does), then every particle gathered from the interleaved
@@ -483,23 +572,26 @@ __global__ void __launch_bounds__(256)
 
 __global__ void __launch_bounds__(256)
     k_import_gather(const float *__restrict__ pos, const float *__restrict__ vel, const float *__restrict__ m,
-                    const int32_t *__restrict__ gid, double ox, double oy, double oz,
+                    const int32_t *__restrict__ gid, bool zero_gid, double ox, double oy, double oz,
                     const uint32_t *__restrict__ perm, gc_particles o, long long n) {
+  // each given input is one uniform branch: a call may gather any subset
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     const long long q = perm[p];
-    const float px = __ldg(pos + 3 * q), py = __ldg(pos + 3 * q + 1), pz = __ldg(pos + 3 * q + 2);
-    const float vx = __ldg(vel + 3 * q), vy = __ldg(vel + 3 * q + 1), vz = __ldg(vel + 3 * q + 2);
-    const float mm = __ldg(m + q);
-    const int32_t g = gid ? __ldg(gid + q) : 0;
-    o.x[p] = (float)((double)px - ox);
-    o.y[p] = (float)((double)py - oy);
-    o.z[p] = (float)((double)pz - oz);
-    o.vx[p] = vx;
-    o.vy[p] = vy;
-    o.vz[p] = vz;
-    o.m[p] = mm;
-    if (o.gid) o.gid[p] = g;
-    if (o.pid) o.pid[p] = (int32_t)q;
+    if (pos) {
+      const float px = __ldg(pos + 3 * q), py = __ldg(pos + 3 * q + 1), pz = __ldg(pos + 3 * q + 2);
+      o.x[p] = (float)((double)px - ox);
+      o.y[p] = (float)((double)py - oy);
+      o.z[p] = (float)((double)pz - oz);
+      if (o.pid) o.pid[p] = (int32_t)q;
+    }
+    if (vel) {
+      const float vx = __ldg(vel + 3 * q), vy = __ldg(vel + 3 * q + 1), vz = __ldg(vel + 3 * q + 2);
+      o.vx[p] = vx;
+      o.vy[p] = vy;
+      o.vz[p] = vz;
+    }
+    if (m) o.m[p] = __ldg(m + q);
+    if (o.gid && (gid || zero_gid)) o.gid[p] = gid ? __ldg(gid + q) : 0;
   }
 }
 
@@ -536,16 +628,15 @@ extern "C" int gc_pm_import_gather(gc_ctx *ctx, const float *pos, const float *v
   if (n == 0) return GC_OK;
   GC_REQUIRE(ctx, ctx->import_n == n && ctx->import_perm,
              "gc_pm_import_gather: no gc_pm_import_order of %lld particles before it", (long long)n);
-  GC_REQUIRE(ctx, pos && vel && m, "gc_pm_import_gather: NULL input");
-  GC_REQUIRE(ctx, out->x && out->y && out->z && out->vx && out->vy && out->vz && out->m,
-             "gc_pm_import_gather: output arrays required");
+  GC_REQUIRE(ctx, !pos || (out->x && out->y && out->z), "gc_pm_import_gather: position outputs required");
+  GC_REQUIRE(ctx, !vel || (out->vx && out->vy && out->vz), "gc_pm_import_gather: velocity outputs required");
+  GC_REQUIRE(ctx, !m || out->m, "gc_pm_import_gather: mass output required");
+  if (!pos && !vel && !m && !(gid && out->gid)) return GC_OK;
   unsigned nb = gc_blocks(n, 256);
   if (nb > 152u * 32u) nb = 152u * 32u;
-  gc_launch(ctx, GK_PERMUTE, k_import_gather, dim3(nb), dim3(256), 0, pos, vel, m, gid, origin[0], origin[1],
-            origin[2], ctx->import_perm, *out, (long long)n);
+  gc_launch(ctx, GK_PERMUTE, k_import_gather, dim3(nb), dim3(256), 0, pos, vel, m, gid, pos != nullptr, origin[0],
+            origin[1], origin[2], ctx->import_perm, *out, (long long)n);
   GC_LAUNCH_CHECK(ctx, "import gather");
-  ctx->import_n = 0;
-  ctx->import_perm = nullptr;
   return GC_OK;
 }
 

@@ -144,6 +144,9 @@ _PROTOS = {
     "gc_pm_import_order": (C.c_int, [_ctxp, _vp, C.POINTER(C.c_double), _i64]),
     "gc_pm_import_gather": (C.c_int, [_ctxp, _vp, _vp, _vp, _vp, C.POINTER(C.c_double), C.POINTER(Particles)]),
     "gc_pm_export": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(C.c_double), _vp, _vp, _vp, _vp]),
+    "gc_pm_export_order": (C.c_int, [_ctxp, C.POINTER(Particles)]),
+    "gc_pm_export_range": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(C.c_double), _vp, _vp, _vp, _vp, _i64,
+                                     _i64]),
     "gc_pm_step": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(StepParams), C.POINTER(StepStats)]),
     "gc_pm_potential": (_vp, [_ctxp]),
     "gc_pm_copy_potential": (C.c_int, [_ctxp, _vp]),

@@ -114,7 +114,9 @@ class PMEngine:
         coordinates, mass N, gid N or None; host or device arrays) into the engine.
         Host arrays are copied into the spare particle set (asynchronously when
         they are pinned) and split on the device by gc_pm_import, or with sort
-        by gc_pm_import_sorted, which gathers them straight into cell order."""
+        by gc_pm_import_order (keys and sort of the positions) and one
+        gc_pm_import_gather per array as its copy lands, which gathers them
+        straight into cell order."""
         pos_t = torch.as_tensor(pos)
         n = int(pos_t.shape[0])
         if n <= 0:
@@ -150,18 +152,32 @@ class PMEngine:
         main = torch.cuda.current_stream()
         if sort:
             # the positions are keyed and sorted while the other arrays are still
-            # being copied (on a side stream); then everything is gathered into
-            # cell order (same result as import + sort)
+            # being copied (on a side stream); each array is then gathered into
+            # cell order as soon as its copy has landed (same result as import + sort)
             side = self._side_stream()
             side.wait_stream(main)
+            landed = []
             with torch.cuda.stream(side):
-                vel_d = staged(vel, 3 * st, (n, 3), torch.float32)
-                m_d = staged(mass, 6 * st, (n,), torch.float32)
-                gid_d = None if gid is None else staged(gid, 7 * st, (n,), torch.int32)
+                for a, off, shape, dtype in ((vel, 3 * st, (n, 3), torch.float32), (mass, 6 * st, (n,), torch.float32),
+                                             (gid, 7 * st, (n,), torch.int32)):
+                    if a is None:
+                        landed.append((None, None))
+                        continue
+                    d = staged(a, off, shape, dtype)
+                    ev = torch.cuda.Event()
+                    ev.record(side)
+                    landed.append((d, ev))
             self.ctx.call("gc_pm_import_order", pos_d.data_ptr(), origin, n, what="gc_pm_import_order")
+            self.ctx.call("gc_pm_import_gather", pos_d.data_ptr(), None, None, None, origin, C.byref(out),
+                          what="gc_pm_import")
+            for slot, (d, ev) in enumerate(landed):
+                if d is None:
+                    continue
+                main.wait_event(ev)
+                one = [None, None, None]
+                one[slot] = d.data_ptr()
+                self.ctx.call("gc_pm_import_gather", None, *one, origin, C.byref(out), what="gc_pm_import")
             main.wait_stream(side)
-            self.ctx.call("gc_pm_import_gather", pos_d.data_ptr(), vel_d.data_ptr(), m_d.data_ptr(),
-                          None if gid_d is None else gid_d.data_ptr(), origin, C.byref(out), what="gc_pm_import")
         else:
             vel_d = staged(vel, 3 * st, (n, 3), torch.float32)
             m_d = staged(mass, 6 * st, (n,), torch.float32)
@@ -177,10 +193,12 @@ class PMEngine:
         pos (N x 3 f32, physical coordinates), vel (N x 3 f32), mass, gid, written
         into the given tensors (host, pinned host or device); only the given ones
         are written, or all four into new host tensors when none is given.
-        gc_pm_export scatters by pid into the spare particle set (or straight into
-        device outputs); host outputs are filled by one copy each, asynchronous
-        when pinned. Velocities are those of the current state (staggered by half
-        a step while the engine is open)."""
+        gc_pm_export_order inverts pid, gc_pm_export_range writes each array in
+        the original order into the spare particle set (or straight into device
+        outputs); host outputs are filled range by range on a side stream while
+        later ranges are written, asynchronously when pinned. Velocities are
+        those of the current state (staggered by half a step while the engine is
+        open)."""
         n = self.n
         st = self._stride(n)
         stage = self.alt["_block"]
@@ -202,22 +220,35 @@ class PMEngine:
             outs.append((t, None if direct else stage[off:off + t.numel()].view(dtype).view(shape)))
             ptrs.append(t.data_ptr() if direct else outs[-1][1].data_ptr())
         src = self._struct(self.cur)
+        origin = self._origin_c()
         main = torch.cuda.current_stream()
         side = self._side_stream()
-        # one array at a time: each staged host copy runs on the side stream
-        # while the next array is being written (the scatters are independent)
+        # pid inverted once; then each array is written in the original order a
+        # range at a time, and every finished range of a host output goes to
+        # the host on the side stream while the next one is being written
+        self.ctx.call("gc_pm_export_order", C.byref(src), what="gc_pm_export_order")
         for a, (t, stg) in enumerate(outs):
             if t is None:
                 continue
             one = [None] * 4
             one[a] = ptrs[a]
-            self.ctx.call("gc_pm_export", C.byref(src), self._origin_c(), *one, what="gc_pm_export")
-            if stg is not None:
-                side.wait_stream(main)
-                with torch.cuda.stream(side):
-                    t.copy_(stg, non_blocking=t.is_pinned())
+            ranges = [(0, n)] if stg is None else self._export_ranges(n)
+            for q0, q1 in ranges:
+                self.ctx.call("gc_pm_export_range", C.byref(src), origin, *one, q0, q1, what="gc_pm_export_range")
+                if stg is not None:
+                    side.wait_stream(main)
+                    with torch.cuda.stream(side):
+                        t[q0:q1].copy_(stg[q0:q1], non_blocking=t.is_pinned())
         main.wait_stream(side)
         return tuple(t for t, _ in outs)
+
+    @staticmethod
+    def _export_ranges(n: int, per: int = 1 << 23):
+        """Ranges of about `per` particles (8M: ~100 MB of positions, ~0.5 ms on
+        the host link) for the overlapped export."""
+        k = max(1, -(-n // per))
+        b = [n * i // k for i in range(k + 1)]
+        return list(zip(b[:-1], b[1:]))
 
     def _side_stream(self):
         if getattr(self, "_side", None) is None:

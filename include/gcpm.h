@@ -341,7 +341,13 @@ int gc_pm_import_sorted(gc_ctx *ctx, const float *pos, const float *vel, const f
  * still be in flight (on another stream) while the positions are keyed and
  * sorted: gc_pm_import_order reads only pos and keeps the permutation in the
  * context; gc_pm_import_gather (n must match; no other sort in between) then
- * gathers every array into cell order. */
+ * gathers the arrays into cell order. Any of pos, vel, m, gid may be NULL, so
+ * that each array can be gathered as soon as its copy has landed: pos writes
+ * out->x, y, z and out->pid, vel out->vx, vy, vz, m out->m, gid out->gid (zeros
+ * when gid is NULL and pos is given). The permutation stays valid for further
+ * gathers until the next call on this context that sorts (gc_pm_import_order,
+ * gc_pm_import_sorted, gc_pm_sort, gc_sort_keys) or grows its particle scratch
+ * (gc_pm_reserve). */
 int gc_pm_import_order(gc_ctx *ctx, const float *pos, const double origin[3], int64_t n);
 int gc_pm_import_gather(gc_ctx *ctx, const float *pos, const float *vel, const float *m, const int32_t *gid,
                         const double origin[3], const gc_particles *out);
@@ -354,6 +360,18 @@ int gc_pm_import_gather(gc_ctx *ctx, const float *pos, const float *vel, const f
  * stream-ordered. */
 int gc_pm_export(gc_ctx *ctx, const gc_particles *p, const double origin[3], float *pos, float *vel, float *m_out,
                  int32_t *gid_out);
+/* gc_pm_export in two phases, written in the original order (coalesced
+ * stores) so that finished ranges can go to the host while later ones are
+ * written: gc_pm_export_order inverts p->pid into the context's scratch
+ * (a pid outside [0, n) raises GC_FLAG_BAD_PID); gc_pm_export_range then
+ * writes the outputs of original indices [q0, q1) exactly as gc_pm_export does
+ * (outputs are whole arrays indexed by the original index; an index that no
+ * particle claims is left untouched and raises GC_FLAG_BAD_PID). The ranks stay
+ * valid until the next call on this context that sorts or grows its particle
+ * scratch, or the next gc_pm_import_order. */
+int gc_pm_export_order(gc_ctx *ctx, const gc_particles *p);
+int gc_pm_export_range(gc_ctx *ctx, const gc_particles *p, const double origin[3], float *pos, float *vel,
+                       float *m_out, int32_t *gid_out, int64_t q0, int64_t q1);
 
 /* One force evaluation of the fused chain plus the kicks/drift of the mode:
  * int64 fixed-point deposit, moments and 4 pi G h^2 rho in one pass, FP64

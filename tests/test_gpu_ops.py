@@ -330,6 +330,8 @@ def test_import_export_round_trip(cuda):
     """gc_pm_import splits the reference's N x 3 layout into the engine's arrays
     (origin subtracted in f64); gc_pm_export writes them back in the original
     order after sorts and steps, equal to state_arrays."""
+    import ctypes as C
+
     from galaxy_collision_gb300.engine import PMEngine
 
     G, dx = 32, 0.5
@@ -358,6 +360,29 @@ def test_import_export_round_trip(cuda):
     e2.sort()
     for k in ("x", "y", "z", "vx", "vy", "vz", "m", "gid", "pid"):
         np.testing.assert_array_equal(e2.cur[k].cpu().numpy(), eng.cur[k].cpu().numpy())
+    # pinned host arrays (each gathered as its copy lands), no gid: gid zeros
+    e3 = PMEngine(G, dx, origin=origin, sort_every=3)
+    e3.cur = e3._alloc(n)
+    e3.cur["gid"].fill_(7)
+    e3.alt = e3._alloc(n)
+    e3.load(torch.from_numpy(pos).pin_memory(), torch.from_numpy(vel).pin_memory(),
+            torch.from_numpy(mass).pin_memory(), None, sort=True)
+    for k in ("x", "y", "z", "vx", "vy", "vz", "m", "pid"):
+        np.testing.assert_array_equal(e3.cur[k].cpu().numpy(), eng.cur[k].cpu().numpy())
+    assert not e3.cur["gid"].any()
+    # the kept order serves gathers of any subset, in any order, until the next sort
+    o = e3._struct(e3.alt)
+    posd, veld, md = (torch.from_numpy(a).cuda() for a in (pos, vel, mass))
+    oc = e3._origin_c()
+    e3.ctx.call("gc_pm_import_order", posd.data_ptr(), oc, n, what="order")
+    e3.ctx.call("gc_pm_import_gather", None, None, md.data_ptr(), None, oc, C.byref(o), what="gather m")
+    e3.ctx.call("gc_pm_import_gather", None, veld.data_ptr(), None, None, oc, C.byref(o), what="gather vel")
+    e3.ctx.call("gc_pm_import_gather", posd.data_ptr(), None, None, None, oc, C.byref(o), what="gather pos")
+    for k in ("x", "y", "z", "vx", "vy", "vz", "m", "pid"):
+        np.testing.assert_array_equal(e3.alt[k].cpu().numpy(), eng.cur[k].cpu().numpy())
+    e3.sort()  # the sort reuses the scratch: the kept order is gone
+    with pytest.raises(Exception, match="gc_pm_import_order"):
+        e3.ctx.call("gc_pm_import_gather", posd.data_ptr(), None, None, None, oc, C.byref(o), what="gather pos")
     p, v, m, g = eng.export()
     back = (rel.astype(np.float64) + np.asarray(origin)).astype(np.float32)
     np.testing.assert_array_equal(p.numpy(), back)
@@ -375,4 +400,34 @@ def test_import_export_round_trip(cuda):
     ps, vs, _, _ = eng.state_arrays(physical=True)
     np.testing.assert_array_equal(pp.numpy(), ps.to(torch.float32).cpu().numpy())
     np.testing.assert_array_equal(vd.cpu().numpy(), vs.cpu().numpy())
+    # many overlapped ranges (pinned and pageable host outputs) == gc_pm_export's scatter
+    eng._export_ranges = lambda k: PMEngine._export_ranges(k, per=3000)
+    assert len(eng._export_ranges(n)) == 7
+    pp2 = torch.zeros((n, 3), dtype=torch.float32).pin_memory()
+    mm2, gg2 = torch.zeros(n, dtype=torch.float32), torch.zeros(n, dtype=torch.int32).pin_memory()
+    eng.export(pp2, None, mm2, gg2)
+    torch.cuda.synchronize()
+    ref = [torch.zeros((n, 3), dtype=torch.float32, device="cuda"), torch.zeros(n, dtype=torch.float32, device="cuda"),
+           torch.zeros(n, dtype=torch.int32, device="cuda")]
+    eng.ctx.call("gc_pm_export", C.byref(eng._struct(eng.cur)), eng._origin_c(), ref[0].data_ptr(), None,
+                 ref[1].data_ptr(), ref[2].data_ptr(), what="gc_pm_export")
+    np.testing.assert_array_equal(pp2.numpy(), ref[0].cpu().numpy())
+    np.testing.assert_array_equal(mm2.numpy(), ref[1].cpu().numpy())
+    np.testing.assert_array_equal(gg2.numpy(), ref[2].cpu().numpy())
+    np.testing.assert_array_equal(gg2.numpy(), gid)
+    with pytest.raises(Exception, match=r"range \[0, 20012\) outside"):
+        eng.ctx.call("gc_pm_export_range", C.byref(eng._struct(eng.cur)), eng._origin_c(), ref[0].data_ptr(), None,
+                     None, None, 0, n + 1, what="gc_pm_export_range")
     assert eng.ctx.status() & 0x4 == 0
+    # a pid outside [0, n): flagged at the inversion, its original index left untouched and flagged
+    q = int(eng.cur["pid"][0])
+    eng.cur["pid"][0] = -1
+    out = torch.full((n,), -5.0, dtype=torch.float32, device="cuda")
+    src = eng._struct(eng.cur)
+    eng.ctx.call("gc_pm_export_order", C.byref(src), what="gc_pm_export_order")
+    eng.ctx.call("gc_pm_export_range", C.byref(src), eng._origin_c(), None, None, out.data_ptr(), None, 0, n,
+                 what="gc_pm_export_range")
+    assert eng.ctx.status(clear=True) & 0x4
+    o = out.cpu().numpy()
+    assert o[q] == -5.0
+    np.testing.assert_array_equal(np.delete(o, q), np.delete(mass, q))
