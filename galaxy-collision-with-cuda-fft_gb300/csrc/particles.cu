@@ -280,6 +280,22 @@ __device__ __forceinline__ void dep_out(const DepBox &bx, long long *__restrict_
   }
 }
 
+// dep_out with the lane's box node already located.
+template <bool BOX>
+__device__ __forceinline__ void dep_put(int bo, const DepBox &bx, long long *__restrict__ qg, int G, int ix, int iy,
+                                        int iz, const int (&t)[8]) {
+  if (BOX) {
+    int *bp = bx.b + bo;
+    const int nz = bx.nz, nyz = bx.nyz;
+    atomicAdd(bp, t[0]); atomicAdd(bp + 1, t[1]); atomicAdd(bp + nz, t[2]); atomicAdd(bp + nz + 1, t[3]);
+    atomicAdd(bp + nyz, t[4]); atomicAdd(bp + nyz + 1, t[5]); atomicAdd(bp + nyz + nz, t[6]);
+    atomicAdd(bp + nyz + nz + 1, t[7]);
+  } else {
+    const long long q[8] = {t[0], t[1], t[2], t[3], t[4], t[5], t[6], t[7]};
+    corners_to_grid(qg, G, ix, iy, iz, q);
+  }
+}
+
 // The DEP_PER particles of one lane (registers), 32 adjacent particles of the
 // warp at a time. Sets bit j of `large` for particles left to the out-of-line pass.
 template <bool POW2, bool BOX, int NJ = DEP_PER>
@@ -323,20 +339,27 @@ __device__ __forceinline__ void dep_warp_pass(const float (&px)[NJ], const float
     const unsigned key = ok ? (unsigned)(((ix + 1) * G1 + (iy + 1)) * G1 + (iz + 1)) : DEP_NONE;
     const unsigned kA = __shfl_sync(0xffffffffu, key, 0), kB = __shfl_sync(0xffffffffu, key, 31);
     const bool inA = key == kA, inB = key == kB;
+    // the lane's corner values, unbiased once for every use below (lanes without
+    // a key are never summed into an output: their products may be NaN)
+    int v[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v[c] = (int)(r[c] - DEP_BIAS);
+    // the lane's node in the box, shared by the three outputs (unsigned: a lane
+    // without a key may hold any cell)
+    const int bo = BOX ? (int)((((unsigned)ix - (unsigned)bx.x0) * (unsigned)bx.ny + ((unsigned)iy - (unsigned)bx.y0)) *
+                                   (unsigned)bx.nz +
+                               ((unsigned)iz - (unsigned)bx.z0))
+                       : 0;
     int t[8];
 #pragma unroll
-    for (int c = 0; c < 8; ++c) t[c] = (int)(__reduce_add_sync(0xffffffffu, inA ? r[c] : DEP_BIAS) - 32u * DEP_BIAS);
-    if (lane == 0 && kA != DEP_NONE) dep_out<BOX>(bx, qg, d.G, ix, iy, iz, t);
+    for (int c = 0; c < 8; ++c) t[c] = __reduce_add_sync(0xffffffffu, inA ? v[c] : 0);
+    if (lane == 0 && kA != DEP_NONE) dep_put<BOX>(bo, bx, qg, d.G, ix, iy, iz, t);
     if (kB != kA) {
 #pragma unroll
-      for (int c = 0; c < 8; ++c) t[c] = (int)(__reduce_add_sync(0xffffffffu, inB ? r[c] : DEP_BIAS) - 32u * DEP_BIAS);
-      if (lane == 31 && kB != DEP_NONE) dep_out<BOX>(bx, qg, d.G, ix, iy, iz, t);
+      for (int c = 0; c < 8; ++c) t[c] = __reduce_add_sync(0xffffffffu, inB ? v[c] : 0);
+      if (lane == 31 && kB != DEP_NONE) dep_put<BOX>(bo, bx, qg, d.G, ix, iy, iz, t);
     }
-    if (!inA && !inB && key != DEP_NONE) {
-#pragma unroll
-      for (int c = 0; c < 8; ++c) t[c] = (int)(r[c] - DEP_BIAS);
-      dep_out<BOX>(bx, qg, d.G, ix, iy, iz, t);
-    }
+    if (!inA && !inB && key != DEP_NONE) dep_put<BOX>(bo, bx, qg, d.G, ix, iy, iz, v);
   }
 }
 
