@@ -363,6 +363,100 @@ __device__ __forceinline__ void dep_warp_pass(const float (&px)[NJ], const float
   }
 }
 
+// The box path with warp runs: after the cell sort the warp's 32 particles
+// of one step mostly share one cell with those of the next steps, so the warp
+// keeps a run cell K (warp-uniform) and each lane adds its corner values for K
+// in registers; the run's 8 sums are reduced across the warp (redux.sync) and
+// added to the box only when no lane is in K any more, and at the end. Lane 31's
+// cell, when it differs from K (the warp reaching the next cell), is reduced at
+// once; particles in any other cell (drifted since the sort) add their own
+// corners. The sums are those of dep_warp_pass regrouped: integer, exact
+// (every partial sum of the warp's 256 particles is below 2^30 on this path).
+template <bool POW2, int NJ = DEP_PER>
+__device__ __forceinline__ void dep_warp_runs(const float (&px)[NJ], const float (&py)[NJ], const float (&pz)[NJ],
+                                              const float (&pm)[NJ], long long nrem, const DepCtx &d, float inv_dx,
+                                              float qscale, const DepBox &bx, unsigned *__restrict__ status, int lane,
+                                              unsigned &large) {
+  const int G1 = d.G + 1;
+  const float hi = (float)d.G;
+  unsigned K = DEP_NONE;  // the run's cell (warp-uniform) ...
+  int Kbo = 0;            // ... and its node in the box
+  int acc[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) acc[c] = 0;
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    float gx, gy, gz;
+    if (POW2) {  // x / dx == x * (1/dx) exactly when dx is a power of two
+      gx = __fmul_rn(px[j], inv_dx); gy = __fmul_rn(py[j], inv_dx); gz = __fmul_rn(pz[j], inv_dx);
+    } else {
+      gx = __fdiv_rn(px[j], d.dx); gy = __fdiv_rn(py[j], d.dx); gz = __fdiv_rn(pz[j], d.dx);
+    }
+    const bool inr = gx >= -1.0f && gx < hi && gy >= -1.0f && gy < hi && gz >= -1.0f && gz < hi;
+    const int ix = __float2int_rd(gx), iy = __float2int_rd(gy), iz = __float2int_rd(gz);
+    const float fx = __fsub_rn(gx, __int2float_rn(ix)), fy = __fsub_rn(gy, __int2float_rn(iy)),
+                fz = __fsub_rn(gz, __int2float_rn(iz));
+    const float mmq = __fmul_rn(__fmul_rn(pm[j], d.inv_vol), qscale);
+    const bool small = fabsf(mmq) < 4194304.0f;
+    if (!inr && 32 * j < nrem && !gc_finite3(px[j], py[j], pz[j])) atomicOr(status, GC_FLAG_NONFINITE_POS);
+    if (inr && !small) large |= 1u << j;
+    const bool ok = inr && small;
+    const float s = ok ? mmq : 0.0f;
+    const float wx0 = __fsub_rn(1.0f, fx), wy0 = __fsub_rn(1.0f, fy), wz0 = __fsub_rn(1.0f, fz);
+    const float a0 = __fmul_rn(s, wx0), a1 = __fmul_rn(s, fx);
+    const float b00 = __fmul_rn(a0, wy0), b01 = __fmul_rn(a0, fy), b10 = __fmul_rn(a1, wy0), b11 = __fmul_rn(a1, fy);
+    int v[8];
+    v[0] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b00, wz0), 12582912.0f)) - DEP_BIAS);
+    v[1] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b00, fz), 12582912.0f)) - DEP_BIAS);
+    v[2] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b01, wz0), 12582912.0f)) - DEP_BIAS);
+    v[3] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b01, fz), 12582912.0f)) - DEP_BIAS);
+    v[4] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b10, wz0), 12582912.0f)) - DEP_BIAS);
+    v[5] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b10, fz), 12582912.0f)) - DEP_BIAS);
+    v[6] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b11, wz0), 12582912.0f)) - DEP_BIAS);
+    v[7] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b11, fz), 12582912.0f)) - DEP_BIAS);
+    const unsigned key = ok ? (unsigned)(((ix + 1) * G1 + (iy + 1)) * G1 + (iz + 1)) : DEP_NONE;
+    // the lane's node in the box (unsigned: a lane without a key may hold any cell)
+    const int bo = (int)((((unsigned)ix - (unsigned)bx.x0) * (unsigned)bx.ny + ((unsigned)iy - (unsigned)bx.y0)) *
+                             (unsigned)bx.nz +
+                         ((unsigned)iz - (unsigned)bx.z0));
+    if (!__any_sync(0xffffffffu, K != DEP_NONE && key == K)) {  // the run has ended (warp-uniform)
+      if (K != DEP_NONE) {
+        int t[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) t[c] = __reduce_add_sync(0xffffffffu, acc[c]);
+        if (lane == 0) dep_put<true>(Kbo, bx, nullptr, d.G, 0, 0, 0, t);
+      }
+      const unsigned have = __ballot_sync(0xffffffffu, key != DEP_NONE);
+      const int src = have ? __ffs(have) - 1 : 0;
+      K = have ? __shfl_sync(0xffffffffu, key, src) : DEP_NONE;
+      Kbo = __shfl_sync(0xffffffffu, bo, src);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc[c] = 0;
+    }
+    const bool inK = K != DEP_NONE && key == K;
+    if (inK) {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc[c] += v[c];
+    }
+    const unsigned kB = __shfl_sync(0xffffffffu, key, 31);
+    const bool bnext = kB != K && kB != DEP_NONE;  // lane 31 already in another cell (warp-uniform)
+    const bool inB = bnext && key == kB;
+    if (bnext) {
+      int t[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) t[c] = __reduce_add_sync(0xffffffffu, inB ? v[c] : 0);
+      if (lane == 31) dep_put<true>(bo, bx, nullptr, d.G, 0, 0, 0, t);
+    }
+    if (key != DEP_NONE && !inK && !inB) dep_put<true>(bo, bx, nullptr, d.G, 0, 0, 0, v);
+  }
+  if (K != DEP_NONE) {
+    int t[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) t[c] = __reduce_add_sync(0xffffffffu, acc[c]);
+    if (lane == 0) dep_put<true>(Kbo, bx, nullptr, d.G, 0, 0, 0, t);
+  }
+}
+
 template <bool POW2>
 __global__ void __launch_bounds__(256, 4)
     k_deposit_sorted(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
@@ -431,7 +525,7 @@ __global__ void __launch_bounds__(256, 4)
     }
     unsigned large = 0;
     if (use_box)
-      dep_warp_pass<POW2, true>(px, py, pz, pm, nrem, d, inv_dx, qscale, bx, qg, status, lane, large);
+      dep_warp_runs<POW2>(px, py, pz, pm, nrem, d, inv_dx, qscale, bx, status, lane, large);
     else
       dep_warp_pass<POW2, false>(px, py, pz, pm, nrem, d, inv_dx, qscale, bx, qg, status, lane, large);
     while (large) {  // rare: point masses
