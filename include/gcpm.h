@@ -102,7 +102,7 @@ typedef struct gc_step_params {
   float dt;          /* full step; the kicks use dt/2 as in kdk_step */
   int mode;          /* gc_step_mode */
   int warm_start;    /* reuse the previous potential (hi+lo) as the initial guess */
-  int diagnostics;   /* 1: accumulate FP64 particle diagnostics at the synchronised time */
+  int diagnostics;   /* 1: accumulate the particle diagnostics (as gc_diag_particles) at the synchronised time */
   gc_mg_params mg;
   int fixed_point_bits; /* deposit quantum = 2^-bits of the total mass; 24 <= bits <= 62 - ceil(log2 G) */
   int flags;         /* GC_STEP_* bits */
@@ -240,7 +240,10 @@ int gc_moments(gc_ctx *ctx, const float *rho, double out[10]);
 
 /* ---- diagnostics (reference diagnostics_device.py) ---------------------- */
 
-/* FP64 sums [M, KE, P(3), L about the origin (3), Sum m r (3)].
+/* Sums [M, KE, P(3), L about the origin (3), Sum m r (3)] returned as FP64: each
+ * thread forms its particles' products exactly or to ~2^-46 and sums them in
+ * double-float (FP32 hi + lo), the threads' totals are added in FP64 (relative
+ * error ~1e-14 of the sum of magnitudes).
  * Replaces _reduce_particle_scalars (diagnostics_device.py:42-74). Synchronises. */
 int gc_diag_particles(gc_ctx *ctx, const float *x, const float *y, const float *z,
                       const float *vx, const float *vy, const float *vz, const float *m,
