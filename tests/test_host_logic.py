@@ -138,6 +138,19 @@ def test_two_disk_sampler_properties():
     assert tilt == pytest.approx(30.0, abs=1.5)
 
 
+# ---- engine host logic -------------------------------------------------------
+@pytest.mark.parametrize("n,per", [(1, 8), (7, 8), (8, 8), (9, 8), (100_000_000, 1 << 23), (20011, 3000)])
+def test_export_ranges_partition(n, per):
+    """The overlapped export's ranges tile [0, n) in order, at most `per` each."""
+    from galaxy_collision_gb300.engine import PMEngine
+
+    r = PMEngine._export_ranges(n, per=per)
+    assert r[0][0] == 0 and r[-1][1] == n
+    assert all(a[1] == b[0] for a, b in zip(r[:-1], r[1:]))
+    assert all(0 < q1 - q0 <= per for q0, q1 in r)
+    assert len(r) == -(-n // per)
+
+
 # ---- benchmark bookkeeping ----------------------------------------------------
 def test_bench_roofline_and_traffic_parse(tmp_path):
     import bench
