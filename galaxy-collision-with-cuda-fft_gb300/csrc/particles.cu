@@ -189,27 +189,29 @@ __global__ void __launch_bounds__(256)
 // Per particle the 8 corner contributions are the reference's f32 products
 // m/dx^3 * wx * wy * wz (deposit.py:69-82) scaled by the quantum (a power of
 // two: exact) and rounded to the nearest integer. The rounding adds 1.5 * 2^23
-// (the f32 spacing is 1 in [2^23, 2^24)) and keeps the bits; those biased
-// values are summed in unsigned (wrapping) arithmetic and the bias of the
-// summands is subtracted afterwards, which is exact because every true sum fits
-// in int32.
+// (the f32 spacing is 1 in [2^23, 2^24)) and keeps the bits; the bias is
+// subtracted in integer arithmetic, and the corner values are summed in int32,
+// which is exact because every partial sum fits.
 //
-// The cells of lane 0 and lane 31 are the warp's "main" cells: all lanes in one
-// of them reduce their corners with one full-warp redux.sync per corner (lanes
-// elsewhere contribute the bias, i.e. zero), and lane 0 / lane 31 adds the
-// sums. Lanes in any other cell (drifted particles, or sparse regions where
-// every particle has its own cell) add their own corners. A redux.sync over the
-// full warp costs the same whatever the keys, unlike one per group of equal
-// keys, which serialises over the groups.
+// Into the shared-memory box (below) the warp keeps a run cell (dep_warp_runs):
+// lanes in it add their corners in registers, and the run is reduced across the
+// warp with one redux.sync per corner when the warp leaves the cell. Directly
+// into the grid (dep_warp_pass) the cells of lane 0 and lane 31 are the warp's
+// "main" cells, each reduced with one full-warp redux.sync per corner. In both,
+// lanes in any other cell (drifted particles, or sparse regions where every
+// particle has its own cell) add their own corners. A redux.sync over the full
+// warp costs the same whatever the keys, unlike one per group of equal keys,
+// which serialises over the groups.
 //
 // Each warp owns an int32 box of nodes in shared memory (no block-wide
 // barriers: warps never wait for each other). Corners go to it when the cells
 // of the warp's 256 particles fit DEP_WBOX nodes (the box is the cell range of
 // their coordinate range: x/dx is monotone) and their total quanta bound every
 // node below 2^31; the box is added to the int64 grid with one atomic per
-// nonzero node when the warp moves on. Otherwise corners go to the grid directly. Particles whose contribution
-// reaches 2^22 quanta (point masses) are deposited out of line at the end of
-// the tile with the general int64 rounding. Correct for any particle order;
+// nonzero node when the warp moves on. Otherwise corners go to the grid
+// directly. Particles whose contribution reaches 2^22 quanta (point masses) are
+// deposited out of line at the end of the tile with the general int64
+// rounding. Correct for any particle order;
 // the sort makes it fast.
 #define DEP_NONE 0xffffffffu
 #define DEP_PER 8
