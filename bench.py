@@ -373,7 +373,7 @@ def run_ours(args):
         if not args.no_accuracy:
             eng.synchronize(dt)
             acc = force_chain_errors(eng)
-            line["accuracy"] = {k: (round(v, 9) if isinstance(v, float) else v) for k, v in acc.items()}
+            line["accuracy"] = {k: (float(f"{v:.4e}") if isinstance(v, float) else v) for k, v in acc.items()}
             line["accuracy"]["note"] = ("relative L2 over the grid (phi) and over all particles and components "
                                         "(CIC-gathered -grad phi) of the engine's synchronised state after the "
                                         "timed and profiled steps, against the FP64 zero-padded FFT of the same "

@@ -106,6 +106,7 @@ struct gc_ctx {
   const uint32_t *import_perm;  // gc_pm_import_order's permutation (in the sort scratch) ...
   int64_t import_n;             // ... for this many particles (0: none pending)
   int64_t export_n;             // gc_pm_export_order's ranks (in ctx->keys) are for this many particles (0: none)
+  const int32_t *export_pid;    // ... and for the particle set with this pid array
   int solved_once;
   gc_mg_stats last_stats;
 
@@ -172,6 +173,10 @@ int gc_check_launch(gc_ctx *ctx, const char *what);
 
 int gc_ensure_red(gc_ctx *ctx, size_t ndoubles);
 int gc_ensure_particle_scratch(gc_ctx *ctx, size_t n);
+
+// Streaming multiprocessors of the current device (queried once per device and
+// cached); persistent and grid-capped launches size their grids from it.
+unsigned gc_sms(void);
 
 static inline unsigned gc_blocks(long long n, int threads) {
   long long b = (n + threads - 1) / threads;

@@ -70,6 +70,18 @@ extern "C" int gc_profile_reset(gc_ctx *ctx) {
   return GC_OK;
 }
 
+unsigned gc_sms(void) {
+  static int cache[64];  // 0: not queried yet
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+  int v = __atomic_load_n(&cache[dev], __ATOMIC_RELAXED);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 1;
+    __atomic_store_n(&cache[dev], v, __ATOMIC_RELAXED);
+  }
+  return (unsigned)v;
+}
+
 void gc_set_error(gc_ctx *ctx, const char *fmt, ...) {
   char *dst = ctx ? ctx->err : g_create_err;
   va_list ap;

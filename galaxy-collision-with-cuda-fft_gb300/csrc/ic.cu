@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(256)
 
 static unsigned ic_grid(long long n) {
   unsigned nb = gc_blocks(n, 256);
-  return nb > 152u * 16u ? 152u * 16u : (nb == 0 ? 1u : nb);
+  return nb > gc_sms() * 16u ? gc_sms() * 16u : (nb == 0 ? 1u : nb);
 }
 
 extern "C" int gc_rng_uniform(gc_ctx *ctx, uint64_t seed, uint32_t stream, int64_t n, float *out) {

@@ -983,7 +983,7 @@ static int launch_smooth0(gc_ctx *ctx, int sweeps, int with_corr, int flags) {
     ctx->sw_smem_set = 1;
   }
   const int tk = (G - 2 + SW_TK - 1) / SW_TK, tj = (G - 2 + SW_TJ - 1) / SW_TJ;
-  int nchunks = (152 * 4 + tk * tj - 1) / (tk * tj);  // ~4 CTAs per SM
+  int nchunks = ((int)gc_sms() * 4 + tk * tj - 1) / (tk * tj);  // ~4 CTAs per SM
   const int max_chunks = (G - 2 + 15) / 16;            // chunks of at least 16 planes
   if (nchunks > max_chunks) nchunks = max_chunks;
   if (nchunks < 1) nchunks = 1;

@@ -15,9 +15,17 @@
 // array is only a stand-in, never a device address; the device address is looked
 // up once per device with cudaGetSymbolAddress on the first call made with that
 // device current. That first call should therefore be made before any stream
-// capture begins. All calls share the one array: calls whose work overlaps on
-// the GPU (different streams, or different host threads on one device) race on
-// it and must be serialised by the caller.
+// capture begins. The cached address is per device ordinal: after
+// cudaDeviceReset on a device this entry point must not be called again on it
+// in the same process (the array would be mapped anew at another address). All
+// calls share the one array: calls whose work overlaps on the GPU (different
+// streams, or different host threads on one device) race on it and must be
+// serialised by the caller.
+//
+// A position that is NaN or Inf deposits nothing and raises
+// GC_FLAG_NONFINITE_POS. The status word the kernels raise it in is part of the
+// shared array and is cleared by the next call, so callers that want to know
+// pass their own device word (flags) and the bit is OR-ed into it instead.
 #include "common.cuh"
 
 #include <mutex>
@@ -83,7 +91,8 @@ static int noalloc_scratch(unsigned char **out) {
 }
 
 extern "C" int gc_deposit_cic_noalloc(const float *x, const float *y, const float *z, const float *m, int64_t n,
-                                      int grid_size, double dx, int fixed_point_bits, float *rho, void *stream) {
+                                      int grid_size, double dx, int fixed_point_bits, float *rho,
+                                      uint32_t *flags, void *stream) {
   if (grid_size < 2 || grid_size > GC_NOALLOC_MAX_GRID) {
     gc_set_error(nullptr, "gc_deposit_cic_noalloc: grid_size must be in [2, %d], got %d", GC_NOALLOC_MAX_GRID,
                  grid_size);
@@ -120,7 +129,8 @@ extern "C" int gc_deposit_cic_noalloc(const float *x, const float *y, const floa
   double *small = (double *)(base + NA_OFF_SMALL);
   unsigned *maxbits = (unsigned *)(small + 4);
   unsigned long long *isum = (unsigned long long *)(small + 5);
-  unsigned *status = (unsigned *)(small + 6);
+  // the caller's status word when given (it outlives the call), else a scratch slot
+  unsigned *status = flags ? (unsigned *)flags : (unsigned *)(small + 6);
   // the array keeps the previous call's contents: clear what must start at zero
   cudaError_t e = cudaMemsetAsync(q, 0, g3 * sizeof(long long), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(small, 0, NA_SMALL_BYTES, st);
@@ -135,14 +145,14 @@ extern "C" int gc_deposit_cic_noalloc(const float *x, const float *y, const floa
   d.G = G;
   if (n > 0) {
     unsigned nb = gc_blocks(n, 256);
-    if (nb > 152u * 8u) nb = 152u * 8u;
+    if (nb > gc_sms() * 8u) nb = gc_sms() * 8u;
     int L = 0;
     while ((1LL << L) < n) ++L;
     k_mass_max<<<nb, 256, 0, st>>>(m, (long long)n, d.inv_vol, maxbits);
     k_mass_isum<<<nb, 256, 0, st>>>(m, (long long)n, d.inv_vol, maxbits, L, isum);
     k_qexp<<<1, 32, 0, st>>>(maxbits, isum, L, small, 0, 1, fixed_point_bits);
     unsigned nd = gc_blocks(n, 256);
-    if (nd > 152u * 32u) nd = 152u * 32u;
+    if (nd > gc_sms() * 32u) nd = gc_sms() * 32u;
     k_deposit<<<nd, 256, 0, st>>>(x, y, z, m, (long long)n, d, small + 1, q, status);
   }
   // rho from q (q is cleared again by the conversion); the moments land in parts

@@ -90,7 +90,7 @@ int gc_fixed_point_setup(gc_ctx *ctx, const float *m, int64_t n, int bits, int m
   unsigned long long *isum = (unsigned long long *)(ctx->red + 1);
   GC_CUDA(ctx, cudaMemsetAsync(ctx->red, 0, 2 * sizeof(double), ctx->stream));
   unsigned nb = gc_blocks(n, 256);
-  if (nb > 152u * 8u) nb = 152u * 8u;
+  if (nb > gc_sms() * 8u) nb = gc_sms() * 8u;
   const int L = ceil_log2((long long)n);
   gc_launch(ctx, GK_MASS, k_mass_max, dim3(nb), dim3(256), 0, m, (long long)n, inv_vol, maxbits);
   gc_launch(ctx, GK_MASS, k_mass_isum, dim3(nb), dim3(256), 0, m, (long long)n, inv_vol, maxbits, L, isum);
@@ -567,7 +567,7 @@ int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, co
   d.inv_vol = 1.0f / ((d.dx * d.dx) * d.dx);
   d.G = ctx->G;
   const long long ntiles = (n + DEP_TILE - 1) / DEP_TILE;
-  const unsigned nb = (unsigned)(ntiles < 152LL * 4 ? ntiles : 152LL * 4);  // 4 CTAs per SM, persistent
+  const unsigned nb = (unsigned)(ntiles < (long long)gc_sms() * 4 ? ntiles : (long long)gc_sms() * 4);  // 4 CTAs per SM, persistent
   int fe = 0;
   const bool pow2 = std::frexp(d.dx, &fe) == 0.5f;
   const float inv_dx = pow2 ? std::ldexp(1.0f, 1 - fe) : 0.0f;
@@ -686,7 +686,7 @@ int gc_max_fixed_point_bits(const gc_ctx *ctx) {
 int gc_convert_q(gc_ctx *ctx, const double *qexp, float *rho_out, float *b_out) {
   const long long cols = (long long)ctx->G * ctx->G;
   unsigned nb = gc_blocks(cols, 8);
-  if (nb > 152u * 3u) nb = 152u * 3u;  // persistent: 3 CTAs per SM (80 registers)
+  if (nb > gc_sms() * 3u) nb = gc_sms() * 3u;  // persistent: 3 CTAs per SM (80 registers)
   int s = gc_ensure_red(ctx, (size_t)nb * 11);
   if (s) return s;
   const double bfac = 4.0 * M_PI * ctx->grav * ctx->dx * ctx->dx;
@@ -805,7 +805,7 @@ extern "C" int gc_gather_accel(gc_ctx *ctx, const float *x, const float *y, cons
   if (n == 0) return GC_OK;
   GC_REQUIRE(ctx, x && y && z && ax_g && ay_g && az_g && acc_x && acc_y && acc_z, "gc_gather_accel: NULL pointer");
   unsigned nb = gc_blocks(n, 256);
-  if (nb > 152u * 32u) nb = 152u * 32u;
+  if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
   gc_launch(ctx, GK_GATHER, k_gather, dim3(nb), dim3(256), 0, x, y, z, (long long)n, ax_g, ay_g, az_g, acc_x, acc_y, acc_z,
                                         (float)ctx->dx, ctx->G);
   GC_LAUNCH_CHECK(ctx, "gather");
@@ -831,7 +831,7 @@ static int axpy3(gc_ctx *ctx, float *u, float *v, float *w, const float *a, cons
   if (n == 0) return GC_OK;
   GC_REQUIRE(ctx, u && v && w && a && b && c, "%s: NULL pointer", what);
   unsigned nb = gc_blocks(n, 256);
-  if (nb > 152u * 32u) nb = 152u * 32u;
+  if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
   gc_launch(ctx, GK_AXPY, k_axpy3, dim3(nb), dim3(256), 0, u, v, w, a, b, c, (long long)n, dt);
   GC_LAUNCH_CHECK(ctx, what);
   return GC_OK;
@@ -1384,7 +1384,7 @@ int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode,
   f.mode = mode;
   f.diag = diag;
   unsigned nb = gc_blocks(p->n, 256);
-  if (nb > 152u * 16u) nb = 152u * 16u;
+  if (nb > gc_sms() * 16u) nb = gc_sms() * 16u;
   int s = gc_ensure_red(ctx, (size_t)nb * 11);
   if (s) return s;
   if (grad_grid && !axo) {
@@ -1409,7 +1409,7 @@ int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode,
       // bulk-streamed state, persistent: 4 CTAs per SM (3 when depositing: 72 KB each)
       const long long ntiles = p->n / GT_TILE;
       const long long per_sm = dep ? 3 : 4;
-      const unsigned nbt = (unsigned)(ntiles < 152LL * per_sm ? ntiles : 152LL * per_sm);
+      const unsigned nbt = (unsigned)(ntiles < (long long)gc_sms() * per_sm ? ntiles : (long long)gc_sms() * per_sm);
       DepCtx d;
       d.dx = (float)ctx->dx;
       d.inv_vol = 1.0f / ((d.dx * d.dx) * d.dx);
@@ -1535,7 +1535,7 @@ extern "C" int gc_radial_histogram(gc_ctx *ctx, const float *x, const float *y, 
   if (smem > 48 * 1024)
     GC_CUDA(ctx, cudaFuncSetAttribute(k_radial_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   unsigned nb = gc_blocks(n, 256);
-  if (nb > 152u * 4u) nb = 152u * 4u;
+  if (nb > gc_sms() * 4u) nb = gc_sms() * 4u;
   gc_launch(ctx, GK_HIST, k_radial_hist, dim3(nb), dim3(256), smem, x, y, z, m, (long long)n, cx, cy, cz, inv_binw, nbins, hist);
   GC_LAUNCH_CHECK(ctx, "radial hist");
   return GC_OK;
@@ -1568,7 +1568,7 @@ extern "C" int gc_project_ngp(gc_ctx *ctx, const float *pa, const float *pb, con
   if (n == 0) return GC_OK;
   GC_REQUIRE(ctx, pa && pb && m, "gc_project_ngp: NULL particle array");
   unsigned nb = gc_blocks(n, 256);
-  if (nb > 152u * 16u) nb = 152u * 16u;
+  if (nb > gc_sms() * 16u) nb = gc_sms() * 16u;
   gc_launch(ctx, GK_PROJECT, k_project_ngp, dim3(nb), dim3(256), 0, pa, pb, m, (long long)n, (float)lo_a, (float)lo_b,
             (float)binw_a, (float)binw_b, bins, img);
   GC_LAUNCH_CHECK(ctx, "project");

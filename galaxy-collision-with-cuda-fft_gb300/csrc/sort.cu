@@ -292,7 +292,7 @@ extern "C" int gc_cell_keys(gc_ctx *ctx, const float *x, const float *y, const f
   GC_REQUIRE(ctx, (unsigned long long)(ctx->G + 1) * (ctx->G + 1) * (ctx->G + 1) < 0xffffffffULL,
              "grid too large for 32-bit cell keys");
   unsigned nb = gc_blocks(n, 256);
-  if (nb > 152u * 32u) nb = 152u * 32u;
+  if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
   gc_launch(ctx, GK_KEYS, k_cell_keys, dim3(nb), dim3(256), 0, x, y, z, (long long)n, (float)ctx->dx, ctx->G, keys, nullptr);
   GC_LAUNCH_CHECK(ctx, "cell keys");
   return GC_OK;
@@ -355,7 +355,7 @@ extern "C" int gc_pm_sort(gc_ctx *ctx, const gc_particles *in, const gc_particle
   int s = gc_ensure_particle_scratch(ctx, (size_t)n);
   if (s) return s;
   unsigned nb = gc_blocks(n, 256);
-  if (nb > 152u * 32u) nb = 152u * 32u;
+  if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
   gc_launch(ctx, GK_KEYS, k_cell_keys, dim3(nb), dim3(256), 0, in->x, in->y, in->z, (long long)n, (float)ctx->dx, ctx->G, ctx->keys2,
                                            ctx->vals2);
   GC_LAUNCH_CHECK(ctx, "cell keys");
@@ -433,7 +433,7 @@ extern "C" int gc_pm_import(gc_ctx *ctx, const float *pos, const float *vel, con
   GC_REQUIRE(ctx, out->x && out->y && out->z && out->vx && out->vy && out->vz && out->m,
              "gc_pm_import: output arrays required");
   unsigned nb = gc_blocks(n, 256);
-  if (nb > 152u * 32u) nb = 152u * 32u;
+  if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
   ctx->q_next_ready = 0;  // new positions: no deposit is pending
   gc_launch(ctx, GK_COPY, k_pm_import, dim3(nb), dim3(256), 0, pos, vel, m, gid, origin[0], origin[1], origin[2], *out,
             (long long)n);
@@ -453,7 +453,7 @@ extern "C" int gc_pm_export(gc_ctx *ctx, const gc_particles *p, const double ori
   GC_REQUIRE(ctx, !vel || (p->vx && p->vy && p->vz), "gc_pm_export: velocities missing");
   GC_REQUIRE(ctx, !m_out || p->m, "gc_pm_export: masses missing");
   unsigned nb = gc_blocks(n, 256);
-  if (nb > 152u * 32u) nb = 152u * 32u;
+  if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
   gc_launch(ctx, GK_COPY, k_pm_export, dim3(nb), dim3(256), 0, *p, origin[0], origin[1], origin[2], pos, vel, m_out,
             gid_out, (long long)n, ctx->dstatus);
   GC_LAUNCH_CHECK(ctx, "export");
@@ -518,11 +518,12 @@ extern "C" int gc_pm_export_order(gc_ctx *ctx, const gc_particles *p) {
   ctx->import_perm = nullptr;
   GC_CUDA(ctx, cudaMemsetAsync(ctx->keys, 0xff, (size_t)n * sizeof(uint32_t), ctx->stream));
   unsigned nb = gc_blocks(n, 256);
-  if (nb > 152u * 32u) nb = 152u * 32u;
+  if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
   gc_launch(ctx, GK_COPY, k_export_rank, dim3(nb), dim3(256), 0, (const int32_t *)p->pid, (long long)n, ctx->keys,
             ctx->dstatus);
   GC_LAUNCH_CHECK(ctx, "export rank");
   ctx->export_n = n;
+  ctx->export_pid = p->pid;
   return GC_OK;
 }
 
@@ -537,11 +538,13 @@ extern "C" int gc_pm_export_range(gc_ctx *ctx, const gc_particles *p, const doub
   if (q0 == q1) return GC_OK;
   GC_REQUIRE(ctx, ctx->export_n == n, "gc_pm_export_range: no gc_pm_export_order of %lld particles before it",
              (long long)n);
+  GC_REQUIRE(ctx, ctx->export_pid == p->pid,
+             "gc_pm_export_range: the ranks were made by gc_pm_export_order for another particle set (pid array)");
   GC_REQUIRE(ctx, !pos || (p->x && p->y && p->z), "gc_pm_export_range: positions missing");
   GC_REQUIRE(ctx, !vel || (p->vx && p->vy && p->vz), "gc_pm_export_range: velocities missing");
   GC_REQUIRE(ctx, !m_out || p->m, "gc_pm_export_range: masses missing");
   unsigned nb = gc_blocks(q1 - q0, 256);
-  if (nb > 152u * 32u) nb = 152u * 32u;
+  if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
   gc_launch(ctx, GK_COPY, k_export_range, dim3(nb), dim3(256), 0, *p, (const uint32_t *)ctx->keys, origin[0],
             origin[1], origin[2], pos, vel, m_out, gid_out, (long long)q0, (long long)q1, ctx->dstatus);
   GC_LAUNCH_CHECK(ctx, "export range");
@@ -607,7 +610,7 @@ extern "C" int gc_pm_import_order(gc_ctx *ctx, const float *pos, const double or
   if (s) return s;
   ctx->q_next_ready = 0;  // new positions: no deposit is pending
   unsigned nb = gc_blocks(n, 256);
-  if (nb > 152u * 32u) nb = 152u * 32u;
+  if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
   gc_launch(ctx, GK_KEYS, k_cell_keys_aos, dim3(nb), dim3(256), 0, pos, origin[0], origin[1], origin[2], (long long)n,
             (float)ctx->dx, ctx->G, ctx->keys2, ctx->vals2);
   GC_LAUNCH_CHECK(ctx, "cell keys");
@@ -633,7 +636,7 @@ extern "C" int gc_pm_import_gather(gc_ctx *ctx, const float *pos, const float *v
   GC_REQUIRE(ctx, !m || out->m, "gc_pm_import_gather: mass output required");
   if (!pos && !vel && !m && !(gid && out->gid)) return GC_OK;
   unsigned nb = gc_blocks(n, 256);
-  if (nb > 152u * 32u) nb = 152u * 32u;
+  if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
   gc_launch(ctx, GK_PERMUTE, k_import_gather, dim3(nb), dim3(256), 0, pos, vel, m, gid, pos != nullptr, origin[0],
             origin[1], origin[2], ctx->import_perm, *out, (long long)n);
   GC_LAUNCH_CHECK(ctx, "import gather");

@@ -156,7 +156,7 @@ __global__ void k_fill_u64(unsigned long long *__restrict__ a, long long n, unsi
 
 static unsigned grid_of(long long n) {
   unsigned nb = gc_blocks(n, 256);
-  return nb > 152u * 16u ? 152u * 16u : (nb == 0 ? 1u : nb);
+  return nb > gc_sms() * 16u ? gc_sms() * 16u : (nb == 0 ? 1u : nb);
 }
 
 extern "C" int gc_max_f32(gc_ctx *ctx, const float *a, int64_t n, float *out) {

@@ -955,7 +955,7 @@ extern "C" int gc_ws_create(gc_ws **out, int R) {
   ws->R = R;
   cudaGetDevice(&ws->device);
   cudaDeviceGetAttribute(&ws->sm_count, cudaDevAttrMultiProcessorCount, ws->device);
-  if (ws->sm_count <= 0) ws->sm_count = 152;
+  if (ws->sm_count <= 0) ws->sm_count = (int)gc_sms();
   size_t off = 0;
   for (int l = 0; l < WS_NL; ++l) {
     ws->w_off[l] = off;

@@ -173,10 +173,15 @@ int gc_deposit_cic(gc_ctx *ctx, const float *x, const float *y, const float *z, 
  * device looks the array's address up (make it before any stream capture);
  * every call clears the part it needs. All calls share the array: calls whose
  * work overlaps on the GPU race and must be serialised by the caller. On failure
- * the message is gc_last_error(NULL). Same result, bit for bit, as
- * gc_deposit_cic with the same fixed_point_bits. */
+ * the message is gc_last_error(NULL). The device address of the array is
+ * cached per device ordinal: after cudaDeviceReset do not call it again on that
+ * device in the same process. flags (device, may be NULL): a NaN/Inf position
+ * deposits nothing and GC_FLAG_NONFINITE_POS is OR-ed into *flags (the caller
+ * clears it); without flags that status is not reported. Same result, bit for
+ * bit, as gc_deposit_cic with the same fixed_point_bits. */
 int gc_deposit_cic_noalloc(const float *x, const float *y, const float *z, const float *m, int64_t n,
-                           int grid_size, double dx, int fixed_point_bits, float *rho, void *stream);
+                           int grid_size, double dx, int fixed_point_bits, float *rho, uint32_t *flags,
+                           void *stream);
 
 /* g = -grad(phi) at every node: central differences inside, one-sided on faces.
  * Replaces _potential_to_accel / potential_to_accel (deposit.py:132-174, 204-207). */
@@ -371,7 +376,10 @@ int gc_pm_export(gc_ctx *ctx, const gc_particles *p, const double origin[3], flo
  * (outputs are whole arrays indexed by the original index; an index that no
  * particle claims is left untouched and raises GC_FLAG_BAD_PID). The ranks stay
  * valid until the next call on this context that sorts or grows its particle
- * scratch, or the next gc_pm_import_order. */
+ * scratch, or the next gc_pm_import_order; gc_pm_export_range returns
+ * GC_ERR_ARG for a particle set whose count or pid array differs from the one
+ * the ranks were made from (a pid array rewritten in place in between is not
+ * detected). */
 int gc_pm_export_order(gc_ctx *ctx, const gc_particles *p);
 int gc_pm_export_range(gc_ctx *ctx, const gc_particles *p, const double origin[3], float *pos, float *vel,
                        float *m_out, int32_t *gid_out, int64_t q0, int64_t q1);

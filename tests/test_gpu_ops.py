@@ -419,6 +419,11 @@ def test_import_export_round_trip(cuda):
         eng.ctx.call("gc_pm_export_range", C.byref(eng._struct(eng.cur)), eng._origin_c(), ref[0].data_ptr(), None,
                      None, None, 0, n + 1, what="gc_pm_export_range")
     assert eng.ctx.status() & 0x4 == 0
+    # ranks made for one particle set are refused for another of the same size
+    eng.ctx.call("gc_pm_export_order", C.byref(eng._struct(eng.cur)), what="gc_pm_export_order")
+    with pytest.raises(Exception, match=r"another particle set"):
+        eng.ctx.call("gc_pm_export_range", C.byref(eng._struct(eng.alt)), eng._origin_c(), ref[0].data_ptr(), None,
+                     None, None, 0, n, what="gc_pm_export_range")
     # a pid outside [0, n): flagged at the inversion, its original index left untouched and flagged
     q = int(eng.cur["pid"][0])
     eng.cur["pid"][0] = -1

@@ -54,7 +54,7 @@ def test_noalloc_deposit_matches_context_deposit_twice(cuda):
         (x, y, z), m = _arrays(pos, mass)
         rho = torch.full((G, G, G), float("nan"), dtype=torch.float32, device="cuda")
         st = lib.gc_deposit_cic_noalloc(x.data_ptr(), y.data_ptr(), z.data_ptr(), m.data_ptr(), n, G, dx, bits,
-                                        rho.data_ptr(), stream)
+                                        rho.data_ptr(), None, stream)
         assert st == 0, lib.gc_last_error(None)
         torch.cuda.synchronize()
         np.testing.assert_array_equal(rho.cpu().numpy(), _reference_density(pos, mass, G, dx, bits))
@@ -67,6 +67,41 @@ def test_noalloc_deposit_rejects_grids_beyond_its_scratch(cuda):
     x = torch.zeros(4, dtype=torch.float32, device="cuda")
     rho = torch.zeros((65, 65, 65), dtype=torch.float32, device="cuda")
     st = lib.gc_deposit_cic_noalloc(x.data_ptr(), x.data_ptr(), x.data_ptr(), x.data_ptr(), 4, 65, 1.0, 52,
-                                    rho.data_ptr(), None)
+                                    rho.data_ptr(), None, None)
     assert st == _native.GC_ERR_ARG
     assert b"grid_size" in lib.gc_last_error(None)
+
+
+def test_noalloc_deposit_reports_nonfinite_positions(cuda):
+    """A NaN position deposits nothing; the caller's device status word gets
+    GC_FLAG_NONFINITE_POS (the scratch array's own word is cleared by the next
+    call, so the caller passes one of its own), and the rest of the density is
+    gc_deposit_cic's."""
+    from galaxy_collision_gb300 import _native
+
+    lib = _native.load()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rng = np.random.default_rng(7)
+    G, dx, bits, n = 16, 1.0, 52, 5000
+    pos = rng.uniform(0.0, G - 1.0, size=(n, 3)).astype(np.float32)
+    mass = np.full(n, 1.0 / n, np.float32)
+    pos[123, 1] = np.nan
+    (x, y, z), m = _arrays(pos, mass)
+    rho = torch.empty((G, G, G), dtype=torch.float32, device="cuda")
+    flags = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = lib.gc_deposit_cic_noalloc(x.data_ptr(), y.data_ptr(), z.data_ptr(), m.data_ptr(), n, G, dx, bits,
+                                    rho.data_ptr(), flags.data_ptr(), stream)
+    assert st == 0, lib.gc_last_error(None)
+    torch.cuda.synchronize()
+    assert int(flags.item()) & _native.GC_FLAG_NONFINITE_POS
+    # the context deposit skips the same particle (and its mass still sets the quantum)
+    np.testing.assert_array_equal(rho.cpu().numpy(), _reference_density(pos, mass, G, dx, bits))
+    # finite positions leave the caller's word alone
+    flags.zero_()
+    pos[123, 1] = 1.0
+    (x, y, z), m = _arrays(pos, mass)
+    st = lib.gc_deposit_cic_noalloc(x.data_ptr(), y.data_ptr(), z.data_ptr(), m.data_ptr(), n, G, dx, bits,
+                                    rho.data_ptr(), flags.data_ptr(), stream)
+    assert st == 0, lib.gc_last_error(None)
+    torch.cuda.synchronize()
+    assert int(flags.item()) == 0
