@@ -1574,3 +1574,33 @@ extern "C" int gc_project_ngp(gc_ctx *ctx, const float *pa, const float *pb, con
   GC_LAUNCH_CHECK(ctx, "project");
   return GC_OK;
 }
+
+// ------------------------------------------------------------------------------
+// self-test of the bounded mbarrier wait (the wait of the TMA particle pass and
+// of the tensor-core kernels): one thread arms an mbarrier for one arrival and,
+// unless `arrive` is set, nobody arrives; the wait must give up after `budget`
+// SM clocks and raise GC_FLAG_TIMEOUT instead of spinning on.
+// ------------------------------------------------------------------------------
+__global__ void k_selftest_wait(unsigned *__restrict__ status, long long budget, int arrive) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  umma::mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  if (arrive) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(umma::smem_u32(&bar)) : "memory");
+  if (!umma::mbar_wait(&bar, 0u, budget)) atomicOr(status, GC_FLAG_TIMEOUT);
+}
+
+extern "C" int gc_selftest_wait_timeout(void *stream, uint32_t *status, int64_t budget_cycles, int arrive) {
+  if (!status || budget_cycles < 1 || budget_cycles > GT_BUDGET) {
+    gc_set_error(nullptr, "gc_selftest_wait_timeout: status required, budget in [1, %lld] clocks",
+                 (long long)GT_BUDGET);
+    return GC_ERR_ARG;
+  }
+  k_selftest_wait<<<1, 32, 0, (cudaStream_t)stream>>>((unsigned *)status, (long long)budget_cycles, arrive ? 1 : 0);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    gc_set_error(nullptr, "gc_selftest_wait_timeout: launch failed: %s", cudaGetErrorString(e));
+    return GC_ERR_CUDA;
+  }
+  return GC_OK;
+}

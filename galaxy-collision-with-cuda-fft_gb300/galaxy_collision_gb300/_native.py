@@ -108,6 +108,7 @@ _PROTOS = {
     "gc_num_levels": (C.c_int, [_ctxp]),
     "gc_level_info": (C.c_int, [_ctxp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "gc_deposit_cic": (C.c_int, [_ctxp, _vp, _vp, _vp, _vp, _i64, C.c_int, _vp]),
+    "gc_selftest_wait_timeout": (C.c_int, [_vp, _vp, _i64, C.c_int]),
     "gc_deposit_cic_noalloc": (C.c_int, [_vp, _vp, _vp, _vp, _i64, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp]),
     "gc_potential_to_accel": (C.c_int, [_ctxp, _vp, _vp, _vp, _vp]),
     "gc_gather_accel": (C.c_int, [_ctxp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp]),

@@ -418,6 +418,14 @@ int gc_profile_read(gc_ctx *ctx, int kid, long long *launches, long long *timed,
 int gc_num_kernel_ids(void);
 const char *gc_kernel_name(int kid);
 
+/* Self-test of the bounded device waits (no reference counterpart): one thread
+ * arms an mbarrier for one arrival and waits on it with the library's bounded
+ * wait for budget_cycles SM clocks (1 <= budget_cycles <= 2e9, about a second).
+ * With arrive = 0 nobody arrives, the wait gives up and GC_FLAG_TIMEOUT is OR-ed
+ * into *status (device word); with arrive = 1 the wait succeeds and *status is
+ * left alone. Stream-ordered; the context stays usable either way. */
+int gc_selftest_wait_timeout(void *stream, uint32_t *status, int64_t budget_cycles, int arrive);
+
 /* ---- learned warm start (new: replaces the previous-step initial guess of the
  * multigrid, solver/multigrid.py:464-467, by a convolutional prediction) ----- */
 

@@ -16,31 +16,41 @@ from scipy.fft import dstn, idstn
 
 def multipole_faces64(rho, dx, grav):
     """Monopole + quadrupole faces of rho about its centre of mass, in FP64
-    (the formula of multigrid.py:261-295 and the moments of :364-389)."""
+    (the formula of multigrid.py:261-295 and the moments of :364-389). The
+    moments come from marginal sums of m = rho dx^3 (exact rearrangements of the
+    triple sums), and the formula is evaluated on the 6 G^2 face nodes only."""
     rho = np.asarray(rho, dtype=np.float64)
     G = rho.shape[0]
     m = rho * dx**3
     ax = np.arange(G) * dx
-    M = m.sum()
     phi = np.zeros((G, G, G))
+    M = m.sum()
     if M <= 0:
         return phi
-    X, Y, Z = np.meshgrid(ax, ax, ax, indexing="ij")
-    c = np.array([(m * X).sum(), (m * Y).sum(), (m * Z).sum()]) / M
-    S = np.empty((3, 3))
-    R = (X - c[0], Y - c[1], Z - c[2])
-    for a in range(3):
-        for b in range(3):
-            S[a, b] = (m * R[a] * R[b]).sum()
+    m_i, m_j, m_k = m.sum(axis=(1, 2)), m.sum(axis=(0, 2)), m.sum(axis=(0, 1))
+    m_ij, m_ik, m_jk = m.sum(axis=2), m.sum(axis=1), m.sum(axis=0)
+    c = np.array([ax @ m_i, ax @ m_j, ax @ m_k]) / M
+    # raw second moments, then the parallel-axis shift to the centre of mass
+    raw = np.empty((3, 3))
+    raw[0, 0], raw[1, 1], raw[2, 2] = (ax * ax) @ m_i, (ax * ax) @ m_j, (ax * ax) @ m_k
+    raw[0, 1] = raw[1, 0] = ax @ m_ij @ ax
+    raw[0, 2] = raw[2, 0] = ax @ m_ik @ ax
+    raw[1, 2] = raw[2, 1] = ax @ m_jk @ ax
+    S = raw - M * np.outer(c, c)
     tr = np.trace(S)
-    mask = np.zeros((G, G, G), bool)
-    mask[0], mask[-1], mask[:, 0], mask[:, -1], mask[:, :, 0], mask[:, :, -1] = (True,) * 6
-    rx, ry, rz = R[0][mask], R[1][mask], R[2][mask]
-    d2 = rx * rx + ry * ry + rz * rz + 1e-12
-    d = np.sqrt(d2)
-    nv = np.stack([rx / d, ry / d, rz / d])
-    nsn = np.einsum("ip,ij,jp->p", nv, S, nv)
-    phi[mask] = -grav * (M / d + (3.0 * nsn - tr) / (2.0 * d2 * d))
+    u, v = np.meshgrid(ax, ax, indexing="ij")
+    e0, e1 = np.zeros_like(u), np.full_like(u, ax[-1])
+    # (face slice, x, y, z of its nodes)
+    faces = [((0, slice(None), slice(None)), e0, u, v), ((G - 1, slice(None), slice(None)), e1, u, v),
+             ((slice(None), 0, slice(None)), u, e0, v), ((slice(None), G - 1, slice(None)), u, e1, v),
+             ((slice(None), slice(None), 0), u, v, e0), ((slice(None), slice(None), G - 1), u, v, e1)]
+    for sl, X, Y, Z in faces:
+        rx, ry, rz = X - c[0], Y - c[1], Z - c[2]
+        d2 = rx * rx + ry * ry + rz * rz + 1e-12
+        d = np.sqrt(d2)
+        nv = (rx / d, ry / d, rz / d)
+        nsn = sum(nv[a] * S[a, b] * nv[b] for a in range(3) for b in range(3))
+        phi[sl] = -grav * (M / d + (3.0 * nsn - tr) / (2.0 * d2 * d))
     return phi
 
 
@@ -59,8 +69,8 @@ def solve_dirichlet(rhs, faces, dx):
     k = np.arange(1, n + 1)
     lam1 = (2.0 * np.cos(np.pi * k / (n + 1)) - 2.0) * inv
     lam = lam1[:, None, None] + lam1[None, :, None] + lam1[None, None, :]
-    bh = dstn(b, type=1)
-    u = idstn(bh / lam, type=1)
+    bh = dstn(b, type=1, workers=-1)
+    u = idstn(bh / lam, type=1, workers=-1)
     phi[1:-1, 1:-1, 1:-1] = u
     return phi
 
