@@ -54,12 +54,16 @@ ALGO_BYTES = {
     "grad": ("cell", 20.0),                   # read phi, write the float4 node field
     "deposit_runs": ("particle", 16.0),       # read x,y,z,m
     "deposit": ("particle", 16.0),
-    "smooth0": ("cell", 10.0),                # one colour: half of (read hi,lo,b + write hi,lo)
-    "sweep0": ("cell", 20.0),                 # one full sweep: read hi,lo,b + write hi,lo
+    "smooth0": ("cell", 6.0),                 # colour-split half-sweep: other colour's e, own r, own e (2 B each)
+    "update0": ("cell", 20.0),                # last half-sweep + phi += e: red e, black r, read/write hi,lo
+    "resid0": ("cell", 18.0),                 # read hi,lo,b0; write r and the first red half-sweep
+    "resid0e": ("cell", 12.0),                # read e, r; write the correction residual
     "convert_q": ("cell", 20.0),              # read q, clear q, write b
-    "resid0": ("cell", 14.0),                 # read hi,lo,b; write r (restriction launches)
-    "prolong0": ("cell", 16.0),               # read/write hi,lo
+    "prolong0": ("cell", 4.0),                # read/write the black correction
 }
+# Kernels of the Poisson solve (the multigrid, its faces and norms, and the b0 conversion).
+MG_KERNELS = ("smooth0", "update0", "resid0", "resid0e", "restrict", "smooth", "resid", "prolong", "prolong0",
+              "tail", "faces", "reduce", "convert_q")
 
 
 def _parse(argv=None):
@@ -364,9 +368,7 @@ def run_ours(args):
                                           sorted(stats.items(), key=lambda kv: -kv[1][2])}
         line["kernel_share"] = {k: round(v[2] / tot, 4) for k, v in sorted(stats.items(), key=lambda kv: -kv[1][2])}
         line["roofline"] = _roofline(stats, n, G, hbm, _load_traffic())
-        poisson_ms = sum(v[2] for k, v in stats.items() if k in (
-            "smooth0", "sweep0", "resid0", "restrict", "smooth", "resid", "prolong", "prolong0", "tail", "faces", "reduce",
-            "convert_q")) / args.profile_steps
+        poisson_ms = sum(v[2] for k, v in stats.items() if k in MG_KERNELS) / args.profile_steps
         line["poisson"]["ms_per_solve"] = round(poisson_ms, 4)
         line["poisson"]["warm_start"] = args.warmstart
 
@@ -435,9 +437,7 @@ def _compare_warm_starts(icr, make_engine, dt, steps, warm=4):
         torch.cuda.synchronize()
         stats = eng.ctx.kernel_stats()
         eng.ctx.profile(False)
-        solve = sum(v[2] for k, v in stats.items() if k in (
-            "smooth0", "sweep0", "resid0", "restrict", "smooth", "resid", "prolong", "prolong0", "tail", "faces",
-            "reduce", "warmstart")) / steps
+        solve = sum(v[2] for k, v in stats.items() if k in MG_KERNELS + ("warmstart",)) / steps
         out[mode] = {"mean_vcycles": float(np.mean([r.cycles for r in res])),
                      "max_rel_residual": float(max(r.rel_residual for r in res)),
                      "ms_per_solve": round(solve, 4),

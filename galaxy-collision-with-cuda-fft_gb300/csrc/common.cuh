@@ -29,13 +29,17 @@ struct LevelGeom {
 enum {
   GC_S_BNORM2 = 0,   // ||b0||^2 (h^2-scaled rhs, all nodes)
   GC_S_RNORM2 = 1,   // ||r0||^2 (interior) of the last residual evaluation
-  GC_S_MASS = 2,     // total deposited density-mass used for the fixed-point quantum
-  GC_S_QEXP = 3,     // quantum exponent E: quantum = 2^E (density units)
   GC_S_RHO_BAD = 4,  // count of non-finite density values (as double)
   GC_S_RNORM64 = 5,  // FP64 residual norm^2 (verification kernel)
   GC_S_GRIDPE = 6,   // Sum b0*phi (engine grid energy, h^2 4 pi G units)
   GC_S_MASS_PM = 7,  // engine: total density-mass of its particles
   GC_S_QEXP_PM = 8,  // engine: quantum exponent
+  GC_S_CYCLES = 2,   // V-cycles of the last device-decided (graph-captured) solve
+  GC_S_CONVERGED = 3,// 1 if that solve met its tolerance
+  GC_S_MIRROR = 4,   // slots [0, 4) are copied to the pinned mirror by captured solves
+  GC_S_GRIDBAR = 10, // [10, 12): grid-barrier words of the persistent coarse launches
+  GC_S_MASS = 12,    // total deposited density-mass used for the fixed-point quantum
+  GC_S_QEXP = 13,    // quantum exponent E: quantum = 2^E (density units)
   GC_S_FIN_TMP = 128, // [128, 256): chunk partials of gc_finalize
   GC_S_NSLOTS = 256
 };
@@ -45,7 +49,7 @@ enum gc_kernel_id {
   GK_DEPOSIT = 0, GK_DEPOSIT_RUNS, GK_CONVERT_Q, GK_MASS, GK_SMOOTH0, GK_RESID0, GK_RESTRICT, GK_SMOOTH,
   GK_RESID, GK_PROLONG, GK_PROLONG0, GK_TAIL, GK_FACES, GK_MOMENTS, GK_RHS, GK_REDUCE, GK_GATHER_KD,
   GK_GRAD, GK_GATHER, GK_AXPY, GK_KEYS, GK_SORT, GK_PERMUTE, GK_DIAG, GK_HIST, GK_RESID64, GK_COPY,
-  GK_SWEEP0, GK_PROJECT, GK_WARMSTART, GK_VIZ, GK_IC, GK_COUNT
+  GK_UPDATE0, GK_PROJECT, GK_WARMSTART, GK_VIZ, GK_IC, GK_RESIDE, GK_COARSE, GK_COUNT
 };
 extern const char *const gc_kernel_names[GK_COUNT];
 
@@ -69,13 +73,23 @@ struct gc_ctx {
   cudaStream_t stream;
   int device;
 
+  int coarse_blocks;    // CTAs of the persistent coarse-level launches (0: not sized yet)
+  int capturing;        // a gc_pm_graph_create capture is in progress (no host reads, no events)
+  cudaStream_t side;    // stream the V-cycle body of a captured solve is recorded on
+  long long cap_body_launches;  // kernel launches in that body (one V-cycle)
   int nlev;             // multigrid levels (0 = finest)
   int tail;             // first level handled by the single-CTA tail kernel (== nlev if none)
   LevelGeom lev[GC_MAX_LEVELS];
 
-  // finest level: double-float potential (current hi/lo and the ping-pong
-  // buffers hi2/lo2 of the streaming sweep), h^2-scaled right-hand side, residual scratch
-  float *hi, *lo, *hi2, *lo2, *b0, *r0;
+  // finest level: double-float potential hi + lo, h^2-scaled right-hand side b0,
+  // natural-layout scratch r0 (residual of the correction, the restriction's
+  // input); colour-split correction e0s and potential residual r0s (two halves
+  // of half0 = G*G*H0 nodes, H0 = (G+1)/2); natural-layout correction and
+  // residual e0n, r0n of the validation path (GC_MG_NATURAL_LAYOUT, lazily)
+  float *hi, *lo, *b0, *r0;
+  float *e0s, *r0s, *e0n, *r0n;
+  size_t half0;
+  int H0;
   // coarse levels (index >= 1): correction e and h^2-scaled right-hand side b
   float *e[GC_MAX_LEVELS];
   float *b[GC_MAX_LEVELS];
@@ -102,7 +116,6 @@ struct gc_ctx {
   int last_step_valid;
   int q_next_ready;     // q holds the deposit of the current positions (made by the last particle pass)
   int gt_smem_set;      // the TMA particle-pass kernels' dynamic shared-memory limit has been raised
-  int sw_smem_set;      // the streaming sweep's dynamic shared-memory limit has been raised
   const uint32_t *import_perm;  // gc_pm_import_order's permutation (in the sort scratch) ...
   int64_t import_n;             // ... for this many particles (0: none pending)
   int64_t export_n;             // gc_pm_export_order's ranks (in ctx->keys) are for this many particles (0: none)
@@ -137,10 +150,17 @@ template <typename... KArgs, typename... Args>
 static inline void gc_launch(gc_ctx *ctx, int kid, void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
                              Args &&...args) {
   ctx->prof.launches[kid]++;
-  const int slot = ctx->prof.enabled ? gc_prof_slot(ctx, kid) : -1;
+  const int slot = ctx->prof.enabled && !ctx->capturing ? gc_prof_slot(ctx, kid) : -1;
   if (slot >= 0) cudaEventRecord(ctx->prof.ev[2 * slot], ctx->stream);
   k<<<grid, block, smem, ctx->stream>>>(std::forward<Args>(args)...);
   if (slot >= 0) cudaEventRecord(ctx->prof.ev[2 * slot + 1], ctx->stream);
+}
+
+// Kernel launches counted on ctx so far (all ids).
+static inline long long gc_launch_total(const gc_ctx *ctx) {
+  long long t = 0;
+  for (int k = 0; k < GK_COUNT; ++k) t += ctx->prof.launches[k];
+  return t;
 }
 
 // ---- error helpers -----------------------------------------------------------

@@ -9,7 +9,7 @@ const char *const gc_kernel_names[GK_COUNT] = {
     "deposit", "deposit_runs", "convert_q", "mass_setup", "smooth0", "resid0", "restrict", "smooth",
     "resid", "prolong", "prolong0", "tail", "faces", "moments", "rhs", "reduce", "gather_kick_drift",
     "grad", "gather", "axpy", "cell_keys", "radix_sort", "permute", "diag", "radial_hist", "resid64", "copy",
-    "sweep0", "project_ngp", "warmstart", "viz", "ic"};
+    "update0", "project_ngp", "warmstart", "viz", "ic", "resid0e", "coarse"};
 
 int gc_prof_slot(gc_ctx *ctx, int kid) {
   gc_profiler &p = ctx->prof;
@@ -219,6 +219,7 @@ extern "C" int gc_ctx_destroy(gc_ctx *ctx) {
   cudaFree(ctx->keys); cudaFree(ctx->keys2); cudaFree(ctx->vals); cudaFree(ctx->vals2);
   cudaFree(ctx->hist); cudaFree(ctx->hist_aux);
   for (int i = 0; i < 2 * ctx->prof.nev_created; ++i) cudaEventDestroy(ctx->prof.ev[i]);
+  if (ctx->side) cudaStreamDestroy(ctx->side);
   free(ctx);
   return GC_OK;
 }

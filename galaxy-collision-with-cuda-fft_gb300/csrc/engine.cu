@@ -13,6 +13,8 @@
 
 #include <math.h>
 
+#include <new>
+
 // Phases 1-3: deposit, b0 + moments, initial guess, faces and V-cycles.
 static int pm_solve(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp, gc_mg_stats *mst) {
   int s;
@@ -159,5 +161,109 @@ extern "C" int gc_pm_copy_potential(gc_ctx *ctx, float *phi) {
   GC_REQUIRE(ctx, phi, "gc_pm_copy_potential: NULL phi");
   const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
   GC_CUDA(ctx, cudaMemcpyAsync(phi, ctx->hi, g3 * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+  return GC_OK;
+}
+
+// ---- the whole step as one CUDA graph ------------------------------------------
+// One ADVANCE step (deposit, conversion, initial guess, faces, the adaptive
+// multigrid with its stopping rule decided on the device by a conditional while
+// node, the particle pass) captured from the context's stream and instantiated.
+// A replay makes no host synchronisation and runs exactly the kernels of an
+// eager gc_pm_step, so the state is the same bit for bit. Host-side state that
+// a step advances (warm-start history depth, pending deposit) must be stationary:
+// capture after at least three steps with the same flags.
+struct gc_graph {
+  gc_ctx *ctx;
+  cudaGraphExec_t exec;
+  long long fixed_launches;  // kernels outside the V-cycle loop
+  long long body_launches;   // kernels per V-cycle
+};
+
+extern "C" int gc_pm_graph_create(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp, gc_graph **out) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, p && sp && out, "gc_pm_graph_create: NULL argument");
+  *out = nullptr;
+  GC_REQUIRE(ctx, sp->mode == GC_STEP_ADVANCE, "gc_pm_graph_create: only ADVANCE steps are captured");
+  GC_REQUIRE(ctx, !(sp->flags & (GC_STEP_SOLVE_ONLY | GC_STEP_PUSH_ONLY)), "gc_pm_graph_create: split steps");
+  GC_REQUIRE(ctx, !sp->diagnostics, "gc_pm_graph_create: diagnostics steps read the host");
+  GC_REQUIRE(ctx, ctx->stream != nullptr, "gc_pm_graph_create: set a non-default stream (gc_set_stream) first");
+  GC_REQUIRE(ctx, ctx->last_step_valid && ctx->solved_once && !ctx->pending_push,
+             "gc_pm_graph_create: needs an open engine that has stepped");
+  GC_REQUIRE(ctx, p->n > 0 && p->n < (1LL << 31) && p->x && p->y && p->z && p->vx && p->vy && p->vz && p->m,
+             "gc_pm_graph_create: particle arrays required");
+  int s = gc_mg_check_params(ctx, &sp->mg);
+  if (s) return s;
+  if (!ctx->side) GC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+  GC_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+  ctx->capturing = 1;
+  ctx->cap_body_launches = 0;
+  const long long before = gc_launch_total(ctx);
+  gc_mg_stats mst;
+  memset(&mst, 0, sizeof(mst));
+  s = pm_solve(ctx, p, sp, &mst);
+  if (!s) s = gc_ws_post_solve(ctx);
+  if (!s) s = pm_push(ctx, p, sp, mst, nullptr);
+  const long long total = gc_launch_total(ctx) - before;
+  ctx->capturing = 0;
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (s || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    if (!s) {
+      gc_set_error(ctx, "gc_pm_graph_create: capture failed: %s", cudaGetErrorString(e));
+      s = GC_ERR_CUDA;
+    }
+    return s;
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess) {
+    gc_set_error(ctx, "gc_pm_graph_create: instantiate failed: %s", cudaGetErrorString(ei));
+    return GC_ERR_CUDA;
+  }
+  gc_graph *gr = new (std::nothrow) gc_graph();
+  if (!gr) {
+    cudaGraphExecDestroy(exec);
+    return GC_ERR_CUDA;
+  }
+  gr->ctx = ctx;
+  gr->exec = exec;
+  gr->body_launches = ctx->cap_body_launches;
+  gr->fixed_launches = total - ctx->cap_body_launches;
+  *out = gr;
+  return GC_OK;
+}
+
+extern "C" int gc_pm_graph_launch(gc_graph *g) {
+  if (!g) return GC_ERR_ARG;
+  gc_ctx *ctx = g->ctx;
+  GC_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
+  return GC_OK;
+}
+
+extern "C" int gc_pm_graph_info(const gc_graph *g, long long *fixed_launches, long long *body_launches) {
+  if (!g) return GC_ERR_ARG;
+  if (fixed_launches) *fixed_launches = g->fixed_launches;
+  if (body_launches) *body_launches = g->body_launches;
+  return GC_OK;
+}
+
+extern "C" int gc_pm_graph_destroy(gc_graph *g) {
+  if (!g) return GC_OK;
+  cudaGraphExecDestroy(g->exec);
+  delete g;
+  return GC_OK;
+}
+
+// V-cycles, converged flag and relative residual of the last graph-replayed
+// solve, from the pinned mirror its graph wrote (no copy, no synchronisation:
+// the caller has synchronised the stream).
+extern "C" int gc_pm_graph_stats(const gc_ctx *ctx, int *cycles, int *converged, double *rel) {
+  if (!ctx) return GC_ERR_ARG;
+  const double b2 = ctx->hsmall[GC_S_BNORM2], r2 = ctx->hsmall[GC_S_RNORM2];
+  if (cycles) *cycles = (int)ctx->hsmall[GC_S_CYCLES];
+  if (converged) *converged = ctx->hsmall[GC_S_CONVERGED] != 0.0;
+  if (rel) *rel = b2 > 0.0 ? sqrt(r2) / sqrt(b2) : 0.0;
   return GC_OK;
 }

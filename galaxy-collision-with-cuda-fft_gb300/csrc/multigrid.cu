@@ -86,18 +86,21 @@ static size_t tail_smem_bytes(const gc_ctx *ctx) {
 int gc_mg_alloc(gc_ctx *ctx) {
   const size_t G = ctx->G;
   const size_t g3 = G * G * G;
+  ctx->H0 = (ctx->G + 1) / 2;
+  ctx->half0 = G * G * (size_t)ctx->H0;
   GC_CUDA(ctx, cudaMalloc(&ctx->hi, g3 * sizeof(float)));
   GC_CUDA(ctx, cudaMalloc(&ctx->lo, g3 * sizeof(float)));
-  GC_CUDA(ctx, cudaMalloc(&ctx->hi2, g3 * sizeof(float)));
-  GC_CUDA(ctx, cudaMalloc(&ctx->lo2, g3 * sizeof(float)));
-  GC_CUDA(ctx, cudaMemset(ctx->hi2, 0, g3 * sizeof(float)));
-  GC_CUDA(ctx, cudaMemset(ctx->lo2, 0, g3 * sizeof(float)));
   GC_CUDA(ctx, cudaMalloc(&ctx->b0, g3 * sizeof(float)));
   GC_CUDA(ctx, cudaMalloc(&ctx->r0, g3 * sizeof(float)));
   GC_CUDA(ctx, cudaMemset(ctx->hi, 0, g3 * sizeof(float)));
   GC_CUDA(ctx, cudaMemset(ctx->lo, 0, g3 * sizeof(float)));
   GC_CUDA(ctx, cudaMemset(ctx->b0, 0, g3 * sizeof(float)));
   GC_CUDA(ctx, cudaMemset(ctx->r0, 0, g3 * sizeof(float)));
+  // colour-split correction and residual of the finest level (faces stay zero)
+  GC_CUDA(ctx, cudaMalloc(&ctx->e0s, 2 * ctx->half0 * sizeof(float)));
+  GC_CUDA(ctx, cudaMalloc(&ctx->r0s, 2 * ctx->half0 * sizeof(float)));
+  GC_CUDA(ctx, cudaMemset(ctx->e0s, 0, 2 * ctx->half0 * sizeof(float)));
+  GC_CUDA(ctx, cudaMemset(ctx->r0s, 0, 2 * ctx->half0 * sizeof(float)));
   size_t rc_n = 0;
   for (int l = 1; l < ctx->nlev; ++l) {
     size_t n3 = (size_t)ctx->lev[l].n * ctx->lev[l].n * ctx->lev[l].n;
@@ -114,15 +117,29 @@ int gc_mg_alloc(gc_ctx *ctx) {
   return GC_OK;
 }
 
+// Natural-layout correction and residual of the finest level, for
+// GC_MG_NATURAL_LAYOUT (allocated on first use).
+static int mg_alloc_natural(gc_ctx *ctx) {
+  if (ctx->e0n) return GC_OK;
+  const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
+  GC_CUDA(ctx, cudaMalloc(&ctx->e0n, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMalloc(&ctx->r0n, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMemset(ctx->e0n, 0, g3 * sizeof(float)));
+  GC_CUDA(ctx, cudaMemset(ctx->r0n, 0, g3 * sizeof(float)));
+  return GC_OK;
+}
+
 void gc_mg_free(gc_ctx *ctx) {
-  cudaFree(ctx->hi); cudaFree(ctx->lo); cudaFree(ctx->hi2); cudaFree(ctx->lo2);
+  cudaFree(ctx->hi); cudaFree(ctx->lo);
   cudaFree(ctx->b0); cudaFree(ctx->r0);
+  cudaFree(ctx->e0s); cudaFree(ctx->r0s); cudaFree(ctx->e0n); cudaFree(ctx->r0n);
   for (int l = 1; l < GC_MAX_LEVELS; ++l) {
     cudaFree(ctx->e[l]); cudaFree(ctx->b[l]);
     ctx->e[l] = ctx->b[l] = nullptr;
   }
   cudaFree(ctx->rc);
-  ctx->hi = ctx->lo = ctx->hi2 = ctx->lo2 = ctx->b0 = ctx->r0 = ctx->rc = nullptr;
+  ctx->hi = ctx->lo = ctx->b0 = ctx->r0 = ctx->rc = nullptr;
+  ctx->e0s = ctx->r0s = ctx->e0n = ctx->r0n = nullptr;
 }
 
 // ------------------------------------------------------------------------------
@@ -190,50 +207,6 @@ __device__ __forceinline__ float df_residual(const float *__restrict__ hi, const
   hc_out = hc;
   lc_out = lc;
   return __fadd_rn(r1, __fsub_rn(r1e, __fadd_rn(e, ll)));
-}
-
-__global__ void __launch_bounds__(RB_TX *RB_TY)
-    k_smooth0(float *__restrict__ hi, float *__restrict__ lo, const float *__restrict__ b, int G, int color) {
-  const int kk = blockIdx.x * RB_TX + threadIdx.x;
-  const int j = blockIdx.y * RB_TY + threadIdx.y + 1;
-  const int i = blockIdx.z + 1;
-  if (j > G - 2) return;
-  const int k = 2 * kk + ((color + i + j) & 1);
-  if (k < 1 || k > G - 2) return;
-  const size_t sj = (size_t)G, si = (size_t)G * G;
-  const size_t c = (size_t)i * si + (size_t)j * sj + k;
-  float hc, lc;
-  const float r = df_residual(hi, lo, b[c], c, sj, si, hc, lc);
-  // Gauss-Seidel: phi_new = (sum6 - h^2 rhs)/6 = phi - r/6
-  const float delta = __fmul_rn(r, -0.16666667f);
-  float s2, e2, h3, l3;
-  df_two_sum(hc, delta, s2, e2);
-  const float ln = __fadd_rn(lc, e2);
-  df_fast_two_sum(s2, ln, h3, l3);
-  hi[c] = h3;
-  lo[c] = l3;
-}
-
-// Residual on the finest interior (r may be NULL) and per-block partial of sum r^2.
-__global__ void __launch_bounds__(256)
-    k_resid0(const float *__restrict__ hi, const float *__restrict__ lo, const float *__restrict__ b,
-             float *__restrict__ r, double *__restrict__ parts, int G) {
-  const int k = blockIdx.x * 32 + threadIdx.x + 1;
-  const int j = blockIdx.y * 8 + threadIdx.y + 1;
-  const int i = blockIdx.z + 1;
-  float acc = 0.0f;
-  if (k <= G - 2 && j <= G - 2) {
-    const size_t sj = (size_t)G, si = (size_t)G * G;
-    const size_t c = (size_t)i * si + (size_t)j * sj + k;
-    float hc, lc;
-    const float rv = df_residual(hi, lo, b[c], c, sj, si, hc, lc);
-    if (r) r[c] = rv;
-    acc = rv * rv;
-  }
-  if (parts) {
-    const size_t bid = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    block_sum_f32(acc, parts + bid);
-  }
 }
 
 // FP64 verification residual: phi = (double)hi + (double)lo, or hi alone when lo is NULL.
@@ -327,13 +300,9 @@ __device__ __forceinline__ float restrict_w(int Jc, int o, const LevelGeom &f, c
   return 0.5f * (f.p - (float)i) / (f.p - (float)(2 * Jc));
 }
 
-// b_c = 4 * R(r_f): full weighting (transpose of trilinear prolongation).
-__global__ void __launch_bounds__(256)
-    k_restrict(const float *__restrict__ rf, LevelGeom f, float *__restrict__ bc, LevelGeom cg) {
-  const int K = blockIdx.x * 32 + threadIdx.x + 1;
-  const int Jj = blockIdx.y * 8 + threadIdx.y + 1;
-  const int I = blockIdx.z + 1;
-  if (K > cg.J || Jj > cg.J) return;
+// b_c = 4 * R(r_f) at coarse node (I, Jj, K): full weighting (transpose of trilinear prolongation).
+__device__ __forceinline__ void restrict_node(const float *__restrict__ rf, const LevelGeom &f,
+                                              float *__restrict__ bc, const LevelGeom &cg, int I, int Jj, int K) {
   float wi[3], wj[3], wk[3];
 #pragma unroll
   for (int o = -1; o <= 1; ++o) {
@@ -362,6 +331,15 @@ __global__ void __launch_bounds__(256)
   }
   const size_t m = cg.n;
   bc[((size_t)I * m + Jj) * m + K] = 4.0f * acc;
+}
+
+__global__ void __launch_bounds__(256)
+    k_restrict(const float *__restrict__ rf, LevelGeom f, float *__restrict__ bc, LevelGeom cg) {
+  const int K = blockIdx.x * 32 + threadIdx.x + 1;
+  const int Jj = blockIdx.y * 8 + threadIdx.y + 1;
+  const int I = blockIdx.z + 1;
+  if (K > cg.J || Jj > cg.J) return;
+  restrict_node(rf, f, bc, cg, I, Jj, K);
 }
 
 // 1-D prolongation weights of fine node i from the coarse level.
@@ -415,223 +393,361 @@ __global__ void __launch_bounds__(256)
   ef[((size_t)i * n + j) * n + k] += prolong_value(ec, i, j, k, f, cg);
 }
 
-// Finest level: add the coarse correction into the double-float pair.
+// ------------------------------------------------------------------------------
+// coarse levels in two persistent launches
+// ------------------------------------------------------------------------------
+// Levels 1 .. tail-1 are relaxed grid-wide by one cooperative launch on the way
+// down (pre-smoothing, residual, restriction per level) and one on the way up
+// (prolongation, post-smoothing), with a grid barrier between phases instead of
+// a kernel boundary. The arithmetic per node is that of k_smooth / k_resid /
+// k_restrict / k_prolong, so the result equals the per-phase launches bit for
+// bit. The first half-sweep of a level starts from a zero correction and reads
+// no neighbour, so the level needs no clearing.
+struct GridBar {
+  unsigned count;  // arrivals at the current barrier
+  unsigned gen;    // barriers completed
+  unsigned abort;  // set by a CTA that gave up waiting
+  unsigned pad;
+};
+
+struct CoarseDesc {
+  int l0, l1;  // levels l0 .. l1-1
+  int pre, post;
+  long long budget;  // SM clocks a CTA waits at one barrier before it gives up
+  GridBar *bar;
+  unsigned *status;
+  float *rc;
+  LevelGeom g[GC_MAX_LEVELS];
+  float *e[GC_MAX_LEVELS];
+  float *b[GC_MAX_LEVELS];
+};
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier of a cooperative launch. Thread 0 of each CTA reads the
+// generation, arrives, and the last arrival resets the count and advances the
+// generation; the others wait for it for at most `budget` clocks. A CTA that
+// gives up raises GC_FLAG_TIMEOUT and the abort word (so the others stop
+// waiting too) and the kernel returns; the barrier word is reset before every
+// solve.
+__device__ __forceinline__ bool grid_barrier(GridBar *gb, unsigned *status, long long budget) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned gen = ld_acquire_u32(&gb->gen);
+    __threadfence();
+    const unsigned arrived = atomicAdd(&gb->count, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&gb->count, 0u);
+      __threadfence();
+      atomicAdd(&gb->gen, 1u);
+    } else {
+      const long long t0 = clock64();
+      while (ld_acquire_u32(&gb->gen) == gen) {
+        if (ld_acquire_u32(&gb->abort) || clock64() - t0 > budget) {
+          ok = 0;
+          atomicOr(status, GC_FLAG_TIMEOUT);
+          atomicExch(&gb->abort, 1u);
+          break;
+        }
+        __nanosleep(20);
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// Work of a phase is split by rows: warp w of the grid takes rows (i, j)
+// w, w + W, ... (one integer division per row), its lanes the nodes of the row.
+__device__ __forceinline__ int p_warp() { return (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); }
+__device__ __forceinline__ int p_nwarps() { return (int)((gridDim.x * blockDim.x) >> 5); }
+__device__ __forceinline__ int p_lane() { return (int)(threadIdx.x & 31); }
+
+// One red-black half-sweep of level g (k_smooth's arithmetic): row (i, j) has
+// the nodes k = 2 kk + ((color + i + j) & 1), kk = 0 .. J/2.
+__device__ void p_smooth(float *__restrict__ e, const float *__restrict__ b, const LevelGeom &g, int color,
+                         bool first) {
+  const int J = g.J, n = g.n, nkk = J / 2 + 1, rows = J * J;
+  for (int row = p_warp(); row < rows; row += p_nwarps()) {
+    const int i = row / J + 1, j = row - (i - 1) * J + 1;
+    const int par = (color + i + j) & 1;
+    const size_t base = ((size_t)i * n + j) * n;
+    for (int kk = p_lane(); kk < nkk; kk += 32) {
+      const int k = 2 * kk + par;
+      if (k < 1 || k > J) continue;
+      const size_t c = base + k;
+      float sum, diag;
+      if (first) {  // zero neighbours: the diagonal alone
+        sum = 0.0f;
+        diag = ((i == J ? g.dB : 2.0f) + (j == J ? g.dB : 2.0f)) + (k == J ? g.dB : 2.0f);
+      } else {
+        sw_stencil(e, c, i, j, k, g, sum, diag);
+      }
+      e[c] = (sum - b[c]) / diag;
+    }
+  }
+}
+
+__device__ void p_zero(float *__restrict__ e, const LevelGeom &g) {
+  const long long tot = (long long)g.n * g.n * g.n;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x)
+    e[t] = 0.0f;
+}
+
+__device__ void p_resid(const float *__restrict__ e, const float *__restrict__ b, float *__restrict__ r,
+                        const LevelGeom &g) {
+  const int J = g.J, n = g.n, rows = J * J;
+  for (int row = p_warp(); row < rows; row += p_nwarps()) {
+    const int i = row / J + 1, j = row - (i - 1) * J + 1;
+    const size_t base = ((size_t)i * n + j) * n;
+    for (int k = p_lane() + 1; k <= J; k += 32) {
+      const size_t c = base + k;
+      float sum, diag;
+      sw_stencil(e, c, i, j, k, g, sum, diag);
+      r[c] = b[c] - (sum - diag * e[c]);
+    }
+  }
+}
+
+__device__ void p_restrict(const float *__restrict__ rf, const LevelGeom &f, float *__restrict__ bc,
+                           const LevelGeom &cg) {
+  const int J = cg.J, rows = J * J;
+  for (int row = p_warp(); row < rows; row += p_nwarps()) {
+    const int I = row / J + 1, Jj = row - (I - 1) * J + 1;
+    for (int K = p_lane() + 1; K <= J; K += 32) restrict_node(rf, f, bc, cg, I, Jj, K);
+  }
+}
+
+__device__ void p_prolong(const float *__restrict__ ec, const LevelGeom &cg, float *__restrict__ ef,
+                          const LevelGeom &f) {
+  const int J = f.J, n = f.n, rows = J * J;
+  for (int row = p_warp(); row < rows; row += p_nwarps()) {
+    const int i = row / J + 1, j = row - (i - 1) * J + 1;
+    const size_t base = ((size_t)i * n + j) * n;
+    for (int k = p_lane() + 1; k <= J; k += 32) ef[base + k] += prolong_value(ec, i, j, k, f, cg);
+  }
+}
+
+#define COARSE_THREADS 512
+
+// Down: for each level, pre-smoothing, residual, restriction into b[l+1].
+__global__ void __launch_bounds__(COARSE_THREADS) k_coarse_down(CoarseDesc d) {
+  for (int l = d.l0; l < d.l1; ++l) {
+    const LevelGeom &g = d.g[l];
+    if (d.pre == 0) {
+      p_zero(d.e[l], g);
+      if (!grid_barrier(d.bar, d.status, d.budget)) return;
+    }
+    for (int h = 0; h < 2 * d.pre; ++h) {
+      p_smooth(d.e[l], d.b[l], g, h & 1, h == 0);
+      if (!grid_barrier(d.bar, d.status, d.budget)) return;
+    }
+    p_resid(d.e[l], d.b[l], d.rc, g);
+    if (!grid_barrier(d.bar, d.status, d.budget)) return;
+    p_restrict(d.rc, g, d.b[l + 1], d.g[l + 1]);
+    if (l + 1 < d.l1 && !grid_barrier(d.bar, d.status, d.budget)) return;
+  }
+}
+
+// Up: for each level from l1-1 down to l0, prolongation of e[l+1], post-smoothing.
+__global__ void __launch_bounds__(COARSE_THREADS) k_coarse_up(CoarseDesc d) {
+  for (int l = d.l1 - 1; l >= d.l0; --l) {
+    const LevelGeom &g = d.g[l];
+    p_prolong(d.e[l + 1], d.g[l + 1], d.e[l], g);
+    for (int h = 0; h < 2 * d.post; ++h) {
+      if (!grid_barrier(d.bar, d.status, d.budget)) return;
+      p_smooth(d.e[l], d.b[l], g, h & 1, false);
+    }
+    if (l > d.l0 && !grid_barrier(d.bar, d.status, d.budget)) return;
+  }
+}
+
+// ------------------------------------------------------------------------------
+// finest level: defect correction with FP32 corrections in colour-split storage
+// ------------------------------------------------------------------------------
+// Each V-cycle solves L e = r for a correction e of the current potential
+// (phi = hi + lo, double-float) with FP32 red-black Gauss-Seidel, then adds it:
+// phi += e, and forms the new residual r = b - L phi accurately from the pair.
+// The correction and the residual are stored colour-split: node (i,j,k) of
+// colour c = (i+j+k)&1 lives in half c at s = (i*G + j)*H + (k>>1), H = (G+1)/2
+// (the same-colour nodes of a row are every other k, so k>>1 is unique). A
+// half-sweep of colour c then reads only the other colour's half and its own
+// right-hand side and writes its own half: a Gauss-Seidel update does not use
+// the node's old value. Neighbours of node s of colour c in the other half:
+// i +- 1 at s +- G*H, j +- 1 at s +- H, k +- 1 at s + p and s + p - 1 with
+// p = k & 1. Face nodes are never written and stay zero (homogeneous
+// correction). The arithmetic is that of k_smooth / k_resid / k_prolong on the
+// level-0 geometry in natural layout (GC_MG_NATURAL_LAYOUT runs those), term for
+// term, so both layouts give identical potentials.
+struct Split0 {
+  int G, H;
+  size_t half;  // nodes per colour half: G * G * H
+};
+
+__device__ __forceinline__ float split_nbr_sum(const float *__restrict__ o, size_t s, size_t GH, int H, int p) {
+  const float ax = o[s + GH] + o[s - GH];
+  const float ay = o[s + H] + o[s - H];
+  const float az = o[s + p] + o[s + p - 1];
+  return (ax + ay) + az;
+}
+
+// One half-sweep of colour `color` on the interior; FIRST: the correction
+// starts at zero, so e = (0 - r)/6 and nothing is read but r.
+template <bool FIRST>
 __global__ void __launch_bounds__(256)
-    k_prolong0(const float *__restrict__ ec, LevelGeom cg, float *__restrict__ hi, float *__restrict__ lo,
-               LevelGeom f) {
+    k_rb0(float *__restrict__ e, const float *__restrict__ r, Split0 d, int color) {
+  const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  if (kk >= d.H || j > d.G - 2) return;
+  const int p = (color + i + j) & 1;
+  const int k = 2 * kk + p;
+  if (k < 1 || k > d.G - 2) return;
+  const size_t s = ((size_t)i * d.G + j) * d.H + kk;
+  float *own = e + (size_t)color * d.half;
+  const float *oth = e + (size_t)(color ^ 1) * d.half;
+  const float rv = r[(size_t)color * d.half + s];
+  const float sum = FIRST ? 0.0f : split_nbr_sum(oth, s, (size_t)d.G * d.H, d.H, p);
+  own[s] = (sum - rv) / 6.0f;
+}
+
+// phi += e at natural node c: double-float add (or a plain f32 add).
+template <bool PLAIN>
+__device__ __forceinline__ void phi_add(float *__restrict__ hi, float *__restrict__ lo, size_t c, float ev) {
+  if (PLAIN) {
+    hi[c] = hi[c] + ev;
+  } else {
+    float s1, e1, h, l;
+    df_two_sum(hi[c], ev, s1, e1);
+    const float ln = __fadd_rn(lo[c], e1);
+    df_fast_two_sum(s1, ln, h, l);
+    hi[c] = h;
+    lo[c] = l;
+  }
+}
+
+// The last half-sweep (black) fused with the update phi += e: thread kk of row
+// (i,j) relaxes the black node 2kk + pb and adds the final corrections of that
+// node and of the red node 2kk + (1 - pb) into the potential. The correction is
+// dead afterwards, so the black value is not stored.
+template <bool PLAIN>
+__global__ void __launch_bounds__(256)
+    k_rb0_last(const float *__restrict__ e, const float *__restrict__ r, float *__restrict__ hi,
+               float *__restrict__ lo, Split0 d) {
+  const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  if (kk >= d.H || j > d.G - 2) return;
+  const int pb = (1 + i + j) & 1;
+  const int kb = 2 * kk + pb, kr = 2 * kk + (pb ^ 1);
+  const size_t s = ((size_t)i * d.G + j) * d.H + kk;
+  const size_t row = ((size_t)i * d.G + j) * d.G;
+  if (kb >= 1 && kb <= d.G - 2) {
+    const float sum = split_nbr_sum(e, s, (size_t)d.G * d.H, d.H, pb);
+    const float eb = (sum - r[d.half + s]) / 6.0f;
+    phi_add<PLAIN>(hi, lo, row + kb, eb);
+  }
+  if (kr >= 1 && kr <= d.G - 2) phi_add<PLAIN>(hi, lo, row + kr, e[s]);
+}
+
+// phi += e at every interior node (natural-layout correction), the update of
+// the natural-layout path and of cycles without post-smoothing.
+template <bool PLAIN, bool SPLIT>
+__global__ void __launch_bounds__(256)
+    k_update0(const float *__restrict__ e, float *__restrict__ hi, float *__restrict__ lo, Split0 d) {
   const int k = blockIdx.x * 32 + threadIdx.x + 1;
   const int j = blockIdx.y * 8 + threadIdx.y + 1;
   const int i = blockIdx.z + 1;
-  if (k > f.J || j > f.J) return;
-  const size_t n = f.n;
-  const size_t c = ((size_t)i * n + j) * n + k;
-  const float v = prolong_value(ec, i, j, k, f, cg);
-  float s, e, h, l;
-  df_two_sum(hi[c], v, s, e);
-  const float ln = __fadd_rn(lo[c], e);
-  df_fast_two_sum(s, ln, h, l);
-  hi[c] = h;
-  lo[c] = l;
+  if (k > d.G - 2 || j > d.G - 2) return;
+  const size_t c = ((size_t)i * d.G + j) * d.G + k;
+  const float ev = SPLIT ? e[(size_t)((i + j + k) & 1) * d.half + ((size_t)i * d.G + j) * d.H + (k >> 1)] : e[c];
+  phi_add<PLAIN>(hi, lo, c, ev);
 }
 
-// The same, two nodes (k, k+1), k even, per thread: the pair shares its coarse
-// loads (the even node reads coarse column k/2, the odd one k/2 and k/2 + 1)
-// and moves hi/lo as float2. Each node's sum is formed exactly as in
-// prolong_value (same weights, same order), so the result is identical.
+// Plain FP32 residual b - L(hi) (the reference's left-to-right neighbour sum).
+__device__ __forceinline__ float f32_residual(const float *__restrict__ hi, float bc, size_t c, size_t sj, size_t si) {
+  const float s6 = ((((hi[c + si] + hi[c - si]) + hi[c + sj]) + hi[c - sj]) + hi[c + 1]) + hi[c - 1];
+  return bc - (s6 - 6.0f * hi[c]);
+}
+
+// Residual r = b - L phi of the potential (double-float, or f32 when PLAIN) at
+// every interior node, stored colour-split (SPLIT) or natural; block partials of
+// sum r^2. With e_first (split only), the first half-sweep of the next cycle's
+// pre-smoothing (red, from a zero correction) is written as well.
+template <bool PLAIN, bool SPLIT>
 __global__ void __launch_bounds__(256)
-    k_prolong0x2(const float *__restrict__ ec, LevelGeom cg, float *__restrict__ hi, float *__restrict__ lo,
-                 LevelGeom f) {
-  const int k = 2 * (blockIdx.x * 32 + threadIdx.x);
+    k_resid0(const float *__restrict__ hi, const float *__restrict__ lo, const float *__restrict__ b,
+             float *__restrict__ rout, float *__restrict__ e_first, double *__restrict__ parts, Split0 d) {
+  const int G = d.G;
+  const int k = blockIdx.x * 32 + threadIdx.x + 1;
   const int j = blockIdx.y * 8 + threadIdx.y + 1;
   const int i = blockIdx.z + 1;
-  if (j > f.J || k > f.J) return;  // k + 1 <= f.J + 1 = n - 1 stays inside the row (n even: c is even)
-  const size_t n = f.n;
-  const size_t c = ((size_t)i * n + j) * n + k;
-  const bool u0 = k >= 1, u1 = k + 1 <= f.J;  // interior nodes of the pair
-  int ci, cj, ck0, ck1;
-  float wi0, wi1, wj0, wj1, a0, a1, b0, b1;
-  const int ni = prolong_w(i, f, cg, ci, wi0, wi1);
-  const int nj = prolong_w(j, f, cg, cj, wj0, wj1);
-  const int nk0 = prolong_w(k, f, cg, ck0, a0, a1);      // even: one coarse column, weight 1
-  const int nk1 = prolong_w(k + 1, f, cg, ck1, b0, b1);  // odd: ck1 == ck0, one or two columns
-  const size_t m = cg.n;
-  float v0 = 0.0f, v1 = 0.0f;
-  for (int a = 0; a < ni; ++a) {
-    const float wa = a ? wi1 : wi0;
-    for (int bb = 0; bb < nj; ++bb) {
-      const float wb = bb ? wj1 : wj0;
-      const size_t row = ((size_t)(ci + a) * m + (cj + bb)) * m;
-      const float wab = wa * wb;
-      const float e0 = ec[row + ck0];
-      const float e1 = (nk0 == 2 || nk1 == 2) ? ec[row + ck0 + 1] : 0.0f;
-      v0 += wab * a0 * e0;
-      if (nk0 == 2) v0 += wab * a1 * e1;
-      v1 += wab * b0 * (ck1 == ck0 ? e0 : e1);
-      if (nk1 == 2) v1 += wab * b1 * ec[row + ck1 + 1];
-    }
-  }
-  float2 h = *reinterpret_cast<const float2 *>(hi + c);
-  float2 l = *reinterpret_cast<const float2 *>(lo + c);
-  if (u0) {
-    float s1, e1, hh, ll;
-    df_two_sum(h.x, v0, s1, e1);
-    df_fast_two_sum(s1, __fadd_rn(l.x, e1), hh, ll);
-    h.x = hh;
-    l.x = ll;
-  }
-  if (u1) {
-    float s1, e1, hh, ll;
-    df_two_sum(h.y, v1, s1, e1);
-    df_fast_two_sum(s1, __fadd_rn(l.y, e1), hh, ll);
-    h.y = hh;
-    l.y = ll;
-  }
-  *reinterpret_cast<float2 *>(hi + c) = h;
-  *reinterpret_cast<float2 *>(lo + c) = l;
-}
-
-// ------------------------------------------------------------------------------
-// finest level, fused: one red-black sweep per pass, streamed along i
-// ------------------------------------------------------------------------------
-// A CTA owns a SW_TJ x SW_TK tile of (j,k) columns and a chunk of i planes. It
-// streams the planes through a ring in shared memory (hi, lo with a halo of 2
-// in j and k; b likewise), loading plane p+1 with cp.async while it works on
-// plane p: it relaxes the red nodes of plane p-1 on the tile plus a one-node
-// ring (from old black values only), then the black nodes of plane p-2 on the
-// tile (from the new red values), and stores plane p-2. Reading one potential
-// buffer and writing the other keeps every CTA on old values outside its own
-// tile, so the result is exactly the two in-place half-sweeps of k_smooth0,
-// with each datum read and written once per sweep. Thread t relaxes one red
-// node of the tile (plus one of the ring for the first 50 threads) and one
-// black node per plane.
-#define SW_TJ 16
-#define SW_TK 32
-#define SW_H 2                   // halo in j
-#define SW_KO 5                  // smem column of k0 (rows start 16-byte aligned at k0 - 5)
-#define SW_EJ (SW_TJ + 2 * SW_H)
-#define SW_EK 40                 // k0 - 5 .. k0 + 34: the halo of 2 plus alignment
-#define SW_THREADS 256
-#define SW_NS 6  // potential planes in flight: p-3 .. p+2
-#define SW_NB 5  // right-hand-side planes in flight: p-2 .. p+2
-
-struct SweepSmem {
-  float hi[SW_NS][SW_EJ][SW_EK];
-  float lo[SW_NS][SW_EJ][SW_EK];
-  float b[SW_NB][SW_EJ][SW_EK];
-};
-
-__device__ __forceinline__ int sw_slot(int p) { return (p + 10 * SW_NS) % SW_NS; }
-__device__ __forceinline__ int sw_bslot(int p) { return (p + 10 * SW_NB) % SW_NB; }
-
-// 16-byte asynchronous copy global -> shared; zero-filled (and no global read) when !valid.
-__device__ __forceinline__ void sw_cp16(float *smem, const float *gmem, bool valid) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
-               "l"(gmem), "r"(valid ? 16 : 0)
-               : "memory");
-}
-
-// The red-black Gauss-Seidel update of one node from the ring (same arithmetic
-// order as df_residual + k_smooth0).
-__device__ __forceinline__ void sw_update(SweepSmem &S, int sm, int sc, int sp, int bs, int jj, int kk) {
-  const float hc = S.hi[sc][jj][kk];
-  const float d0 = __fsub_rn(S.hi[sp][jj][kk], hc);
-  const float d1 = __fsub_rn(S.hi[sm][jj][kk], hc);
-  const float d2 = __fsub_rn(S.hi[sc][jj + 1][kk], hc);
-  const float d3 = __fsub_rn(S.hi[sc][jj - 1][kk], hc);
-  const float d4 = __fsub_rn(S.hi[sc][jj][kk + 1], hc);
-  const float d5 = __fsub_rn(S.hi[sc][jj][kk - 1], hc);
-  float s, e, t;
-  df_two_sum(d0, d1, s, e);
-  df_two_sum(s, d2, s, t); e = __fadd_rn(e, t);
-  df_two_sum(s, d3, s, t); e = __fadd_rn(e, t);
-  df_two_sum(s, d4, s, t); e = __fadd_rn(e, t);
-  df_two_sum(s, d5, s, t); e = __fadd_rn(e, t);
-  const float lc = S.lo[sc][jj][kk];
-  const float ln = ((((S.lo[sp][jj][kk] + S.lo[sm][jj][kk]) + S.lo[sc][jj + 1][kk]) + S.lo[sc][jj - 1][kk]) +
-                    S.lo[sc][jj][kk + 1]) + S.lo[sc][jj][kk - 1];
-  const float ll = __fsub_rn(ln, __fmul_rn(6.0f, lc));
-  float r1, r1e;
-  df_two_sum(S.b[bs][jj][kk], -s, r1, r1e);
-  const float r = __fadd_rn(r1, __fsub_rn(r1e, __fadd_rn(e, ll)));
-  const float delta = __fmul_rn(r, -0.16666667f);
-  float s2, e2, h3, l3;
-  df_two_sum(hc, delta, s2, e2);
-  const float lnew = __fadd_rn(lc, e2);
-  df_fast_two_sum(s2, lnew, h3, l3);
-  S.hi[sc][jj][kk] = h3;
-  S.lo[sc][jj][kk] = l3;
-}
-
-// G must be a multiple of 4 (rows 16-byte aligned; a 16-byte group is wholly
-// inside or outside the grid).
-__global__ void __launch_bounds__(SW_THREADS)
-    k_sweep0(const float *__restrict__ hi_in, const float *__restrict__ lo_in, const float *__restrict__ b,
-             float *__restrict__ hi_out, float *__restrict__ lo_out, int G, int chunk) {
-  extern __shared__ __align__(16) unsigned char sw_raw[];
-  SweepSmem &S = *reinterpret_cast<SweepSmem *>(sw_raw);
-  const int tid = threadIdx.x;
-  const int j0 = 1 + blockIdx.y * SW_TJ;
-  const int k0 = 1 + blockIdx.x * SW_TK;
-  const int i0 = 1 + blockIdx.z * chunk;
-  const int i1 = min(i0 + chunk, G - 1);  // planes [i0, i1) are relaxed and stored
-  const size_t sj = (size_t)G, si = (size_t)G * G;
-  auto load_plane = [&](int p) {  // issue the copies of plane p into its slots (16-byte groups)
-    const int s = sw_slot(p), bs = sw_bslot(p);
-    for (int t = tid; t < SW_EJ * (SW_EK / 4); t += SW_THREADS) {
-      const int jj = t / (SW_EK / 4), q4 = t - jj * (SW_EK / 4);
-      const int j = j0 - SW_H + jj, k = k0 - SW_KO + 4 * q4;
-      const bool v = p >= 0 && p < G && j >= 0 && j < G && k >= 0 && k < G;
-      const size_t c = v ? (size_t)p * si + (size_t)j * sj + k : 0;
-      sw_cp16(&S.hi[s][jj][4 * q4], hi_in + c, v);
-      sw_cp16(&S.lo[s][jj][4 * q4], lo_in + c, v);
-      sw_cp16(&S.b[bs][jj][4 * q4], b + c, v);
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-  };
-  load_plane(i0 - 2);
-  load_plane(i0 - 1);
-  for (int p = i0 - 2; p <= i1 + 1; ++p) {
-    if (p + 2 <= i1 + 1) {
-      load_plane(p + 2);
-      asm volatile("cp.async.wait_group 2;" ::: "memory");  // plane p has landed
-    } else if (p + 1 <= i1 + 1) {
-      asm volatile("cp.async.wait_group 1;" ::: "memory");
+  float acc = 0.0f;
+  if (k <= G - 2 && j <= G - 2) {
+    const size_t sj = (size_t)G, si = (size_t)G * G;
+    const size_t c = (size_t)i * si + (size_t)j * sj + k;
+    float rv;
+    if (PLAIN) {
+      rv = f32_residual(hi, b[c], c, sj, si);
     } else {
-      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      float hc, lc;
+      rv = df_residual(hi, lo, b[c], c, sj, si, hc, lc);
     }
-    __syncthreads();
-    const int q = p - 1;  // red on plane q, tile + 1 halo
-    if (q >= i0 - 1 && q <= i1 && q >= 1 && q <= G - 2) {
-      const int sc = sw_slot(q), sm = sw_slot(q - 1), sp = sw_slot(q + 1), bs = sw_bslot(q);
-      for (int idx = tid; idx < (SW_EJ - 2) * 17; idx += SW_THREADS) {
-        const int row = idx / 17, m = idx - row * 17;
-        const int jj = 1 + row, j = j0 - SW_H + jj;
-        const int kk = SW_KO - 1 + 2 * m + ((q + j + k0 - 1) & 1), k = k0 - SW_KO + kk;
-        if (j < 1 || j > G - 2 || k < 1 || k > G - 2) continue;
-        sw_update(S, sm, sc, sp, bs, jj, kk);
-      }
+    if (SPLIT) {
+      const int col = (i + j + k) & 1;
+      const size_t s = ((size_t)i * G + j) * d.H + (k >> 1);
+      rout[(size_t)col * d.half + s] = rv;
+      if (e_first && col == 0) e_first[s] = (0.0f - rv) / 6.0f;
+    } else {
+      rout[c] = rv;
     }
-    __syncthreads();
-    const int r = p - 2;  // black on plane r, tile only; then store plane r
-    if (r >= i0 && r < i1) {
-      const int sc = sw_slot(r), sm = sw_slot(r - 1), sp = sw_slot(r + 1), bs = sw_bslot(r);
-      {
-        const int row = tid >> 4, m = tid & 15;
-        const int jj = SW_H + row, j = j0 + row;
-        const int kk = SW_KO + 2 * m + (((r + j + k0) & 1) ? 0 : 1), k = k0 - SW_KO + kk;
-        if (j <= G - 2 && k <= G - 2) sw_update(S, sm, sc, sp, bs, jj, kk);
-      }
-      __syncthreads();
-      for (int idx = tid; idx < SW_TJ * SW_TK; idx += SW_THREADS) {
-        const int row = idx >> 5, col = idx & 31;
-        const int j = j0 + row, k = k0 + col;
-        if (j > G - 2 || k > G - 2) continue;
-        const size_t c = (size_t)r * si + (size_t)j * sj + k;
-        hi_out[c] = S.hi[sc][SW_H + row][SW_KO + col];
-        lo_out[c] = S.lo[sc][SW_H + row][SW_KO + col];
-      }
-    }
-    __syncthreads();
+    acc = rv * rv;
+  }
+  const size_t bid = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+  block_sum_f32(acc, parts + bid);
+}
+
+// Residual of the correction equation, r - L e (e, r colour-split), written in
+// natural layout for the restriction: the arithmetic of k_resid on level 0.
+__global__ void __launch_bounds__(256)
+    k_resid0e(const float *__restrict__ e, const float *__restrict__ r, float *__restrict__ rc, Split0 d) {
+  const int G = d.G;
+  const int k = blockIdx.x * 32 + threadIdx.x + 1;
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  if (k > G - 2 || j > G - 2) return;
+  const int col = (i + j + k) & 1;
+  const size_t s = ((size_t)i * G + j) * d.H + (k >> 1);
+  const float *own = e + (size_t)col * d.half;
+  const float *oth = e + (size_t)(col ^ 1) * d.half;
+  const float sum = split_nbr_sum(oth, s, (size_t)G * d.H, d.H, k & 1);
+  const float diag = 6.0f;
+  rc[((size_t)i * G + j) * G + k] = r[(size_t)col * d.half + s] - (sum - diag * own[s]);
+}
+
+// Add the level-1 correction into the colour-split level-0 correction: black
+// nodes only when a red half-sweep follows (it overwrites the red half without
+// reading it), both colours otherwise.
+__global__ void __launch_bounds__(256)
+    k_prolong0s(const float *__restrict__ ec, LevelGeom cg, float *__restrict__ e, LevelGeom f, Split0 d,
+                int both) {
+  const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  if (kk >= d.H || j > d.G - 2) return;
+  const size_t s = ((size_t)i * d.G + j) * d.H + kk;
+  for (int col = both ? 0 : 1; col < 2; ++col) {
+    const int k = 2 * kk + ((col + i + j) & 1);
+    if (k < 1 || k > d.G - 2) continue;
+    e[(size_t)col * d.half + s] += prolong_value(ec, i, j, k, f, cg);
   }
 }
 
@@ -811,7 +927,7 @@ __global__ void __launch_bounds__(1024) k_tail(const float *__restrict__ b_in, f
 // Multipole Dirichlet faces (multigrid.py:261-295) evaluated in FP64 from the raw
 // moments (multigrid.py:378-389), written as double-float pairs.
 __global__ void __launch_bounds__(256)
-    k_faces(float *__restrict__ hi, float *__restrict__ lo, float *__restrict__ hi2, float *__restrict__ lo2, int G,
+    k_faces(float *__restrict__ hi, float *__restrict__ lo, int G,
             double dx, double grav, const double *__restrict__ mom) {
   // centre of mass and second moments about it, once per block (FP64 runs at a
   // small fraction of the f32 rate: each face node keeps only its own terms)
@@ -858,8 +974,6 @@ __global__ void __launch_bounds__(256)
   const float l = (float)(phi - (double)h);
   hi[c] = h;
   lo[c] = l;
-  hi2[c] = h;  // both buffers of the streaming sweep carry the faces
-  lo2[c] = l;
 }
 
 // Column moments of an f32 density: one warp per (i,j) column, Kahan-compensated
@@ -934,6 +1048,26 @@ __global__ void k_copy_hi_to(const float *__restrict__ hi, float *__restrict__ o
 }
 
 // ------------------------------------------------------------------------------
+// device-side stopping rule of the adaptive loop (graph-captured solves)
+// ------------------------------------------------------------------------------
+// The host loop of gc_mg_run, evaluated on the device after every residual: the
+// cycle count lives in dsmall[GC_S_CYCLES]; the loop continues while fewer than
+// max_cycles cycles ran and not (at least max(1, min_cycles) cycles ran and
+// ||r|| < tol ||b|| with ||b|| > 0). The verdict goes to the conditional node
+// that repeats the V-cycle body, the converged flag to dsmall[GC_S_CONVERGED].
+__global__ void k_mg_decide(cudaGraphConditionalHandle h, double *__restrict__ small, double tol, int min_c,
+                            int max_c, int first) {
+  if (threadIdx.x != 0) return;
+  const int c = first ? 0 : (int)small[GC_S_CYCLES] + 1;
+  small[GC_S_CYCLES] = (double)c;
+  const double b2 = small[GC_S_BNORM2], r2 = small[GC_S_RNORM2];
+  const int minc = min_c > 1 ? min_c : 1;
+  const bool conv = c >= minc && b2 > 0.0 && sqrt(r2) < tol * sqrt(b2);
+  small[GC_S_CONVERGED] = conv ? 1.0 : 0.0;
+  cudaGraphSetConditional(h, (!conv && c < max_c) ? 1u : 0u);
+}
+
+// ------------------------------------------------------------------------------
 // host orchestration
 // ------------------------------------------------------------------------------
 static dim3 rb_grid(const LevelGeom &g) {
@@ -941,70 +1075,6 @@ static dim3 rb_grid(const LevelGeom &g) {
   return dim3(gc_blocks(nkk, RB_TX), gc_blocks(g.J, RB_TY), (unsigned)g.J);
 }
 static dim3 node_grid(const LevelGeom &g) { return dim3(gc_blocks(g.J, 32), gc_blocks(g.J, 8), (unsigned)g.J); }
-// pairs (k, k+1), k = 0, 2, ..., J: J/2 + 1 pairs per row
-static dim3 pair_grid(const LevelGeom &g) {
-  return dim3(gc_blocks(g.J / 2 + 1, 32), gc_blocks(g.J, 8), (unsigned)g.J);
-}
-
-// Add the level-1 correction into the finest double-float potential: pairs of
-// nodes per thread when rows have an even length (so every pair starts on an
-// 8-byte boundary), one node per thread otherwise.
-static void launch_prolong0(gc_ctx *ctx, const LevelGeom &g) {
-  if (g.n % 2 == 0)
-    gc_launch(ctx, GK_PROLONG0, k_prolong0x2, dim3(pair_grid(g)), dim3(dim3(32, 8)), 0, ctx->e[1], ctx->lev[1],
-              ctx->hi, ctx->lo, g);
-  else
-    gc_launch(ctx, GK_PROLONG0, k_prolong0, dim3(node_grid(g)), dim3(dim3(32, 8)), 0, ctx->e[1], ctx->lev[1],
-              ctx->hi, ctx->lo, g);
-}
-
-// Finest-level smoothing: `sweeps` red-black sweeps, the first one preceded by
-// the prolongation of the level-1 correction when `with_corr` is set. Default:
-// in-place red and black half-sweep kernels. GC_MG_FUSED_SWEEP streams each
-// sweep from (hi, lo) into (hi2, lo2) and swaps the buffers (same arithmetic).
-static int launch_smooth0(gc_ctx *ctx, int sweeps, int with_corr, int flags) {
-  const LevelGeom &g = ctx->lev[0];
-  const int G = ctx->G;
-  if (!(flags & GC_MG_FUSED_SWEEP) || sweeps == 0 || G % 4 != 0) {
-    if (with_corr) {
-      launch_prolong0(ctx, g);
-    }
-    for (int s = 0; s < sweeps; ++s)
-      for (int color = 0; color < 2; ++color)
-        gc_launch(ctx, GK_SMOOTH0, k_smooth0, dim3(rb_grid(g)), dim3(dim3(RB_TX, RB_TY)), 0, ctx->hi, ctx->lo,
-                  ctx->b0, ctx->G, color);
-    GC_LAUNCH_CHECK(ctx, "smooth0");
-    return GC_OK;
-  }
-  if (with_corr)  // the coarse correction first (the streaming sweep starts from the corrected potential)
-    launch_prolong0(ctx, g);
-  if (!ctx->sw_smem_set) {  // 54 KB of dynamic shared memory: opt in once per context
-    GC_CUDA(ctx, cudaFuncSetAttribute(k_sweep0, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SweepSmem)));
-    ctx->sw_smem_set = 1;
-  }
-  const int tk = (G - 2 + SW_TK - 1) / SW_TK, tj = (G - 2 + SW_TJ - 1) / SW_TJ;
-  int nchunks = ((int)gc_sms() * 4 + tk * tj - 1) / (tk * tj);  // ~4 CTAs per SM
-  const int max_chunks = (G - 2 + 15) / 16;            // chunks of at least 16 planes
-  if (nchunks > max_chunks) nchunks = max_chunks;
-  if (nchunks < 1) nchunks = 1;
-  const int chunk = (G - 2 + nchunks - 1) / nchunks;
-  nchunks = (G - 2 + chunk - 1) / chunk;
-  // pairs of streaming sweeps (each swaps the buffers, so a pair leaves the
-  // potential where it started); an odd last sweep as two half-sweeps
-  for (int s = 0; s < (sweeps & ~1); ++s) {
-    gc_launch(ctx, GK_SWEEP0, k_sweep0, dim3(tk, tj, nchunks), dim3(SW_THREADS), sizeof(SweepSmem), ctx->hi,
-              ctx->lo, ctx->b0, ctx->hi2, ctx->lo2, G, chunk);
-    float *t = ctx->hi; ctx->hi = ctx->hi2; ctx->hi2 = t;
-    t = ctx->lo; ctx->lo = ctx->lo2; ctx->lo2 = t;
-  }
-  if (sweeps & 1)
-    for (int color = 0; color < 2; ++color)
-      gc_launch(ctx, GK_SMOOTH0, k_smooth0, dim3(rb_grid(g)), dim3(dim3(RB_TX, RB_TY)), 0, ctx->hi, ctx->lo,
-                ctx->b0, ctx->G, color);
-  GC_LAUNCH_CHECK(ctx, "sweep0");
-  return GC_OK;
-}
-
 static int launch_smooth(gc_ctx *ctx, int l, int sweeps) {
   const LevelGeom &g = ctx->lev[l];
   for (int s = 0; s < sweeps; ++s)
@@ -1036,34 +1106,210 @@ static int launch_tail(gc_ctx *ctx, const gc_mg_params *p) {
   return GC_OK;
 }
 
-static int vcycle(gc_ctx *ctx, const gc_mg_params *p) {
+static int finalize_to(gc_ctx *ctx, int nparts, int nv, int slot);
+
+static Split0 split0(const gc_ctx *ctx) {
+  Split0 d;
+  d.G = ctx->G;
+  d.H = ctx->H0;
+  d.half = ctx->half0;
+  return d;
+}
+// (kk, j, i) over the interior rows of the colour-split finest level
+static dim3 split_grid(const gc_ctx *ctx) {
+  return dim3(gc_blocks(ctx->H0, 64), gc_blocks(ctx->G - 2, 4), (unsigned)(ctx->G - 2));
+}
+#define SPLIT_BLOCK dim3(64, 4)
+
+// CTAs of the persistent coarse launches: as many as fit at once (a cooperative
+// launch needs them all resident), at most two per SM (fewer arrivals per grid
+// barrier), and no more than the largest phase has work for.
+static int coarse_grid(gc_ctx *ctx) {
+  if (ctx->coarse_blocks > 0) return GC_OK;
+  int occ_d = 0, occ_u = 0;
+  GC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_d, k_coarse_down, COARSE_THREADS, 0));
+  GC_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_u, k_coarse_up, COARSE_THREADS, 0));
+  int per_sm = occ_d < occ_u ? occ_d : occ_u;
+  if (per_sm > 2) per_sm = 2;
+  if (per_sm < 1) {
+    gc_set_error(ctx, "coarse levels: the persistent kernel does not fit on an SM");
+    return GC_ERR_CUDA;
+  }
+  const LevelGeom &g1 = ctx->lev[1];
+  const long long rows = (long long)g1.J * g1.J;  // one warp per row at the finest coarse level
+  long long nb = (long long)gc_sms() * per_sm;
+  const long long need = (rows + COARSE_THREADS / 32 - 1) / (COARSE_THREADS / 32);
+  if (nb > need) nb = need;
+  ctx->coarse_blocks = (int)(nb < 1 ? 1 : nb);
+  return GC_OK;
+}
+
+static int launch_coarse(gc_ctx *ctx, const gc_mg_params *p, bool up) {
+  CoarseDesc d;
+  memset(&d, 0, sizeof(d));
+  d.l0 = 1;
+  d.l1 = ctx->tail;
+  d.pre = p->pre_sweeps;
+  d.post = p->post_sweeps;
+  d.budget = 100000000LL;  // ~50 ms of SM clocks; a barrier normally takes microseconds
+  d.bar = reinterpret_cast<GridBar *>(ctx->dsmall + GC_S_GRIDBAR);
+  d.status = ctx->dstatus;
+  d.rc = ctx->rc;
+  for (int l = 1; l < ctx->nlev; ++l) {
+    d.g[l] = ctx->lev[l];
+    d.e[l] = ctx->e[l];
+    d.b[l] = ctx->b[l];
+  }
+  int st = coarse_grid(ctx);
+  if (st) return st;
+  void *args[] = {&d};
+  const void *fn = up ? (const void *)k_coarse_up : (const void *)k_coarse_down;
+  ctx->prof.launches[GK_COARSE]++;
+  const int slot = ctx->prof.enabled && !ctx->capturing ? gc_prof_slot(ctx, GK_COARSE) : -1;
+  if (slot >= 0) cudaEventRecord(ctx->prof.ev[2 * slot], ctx->stream);
+  GC_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(ctx->coarse_blocks), dim3(COARSE_THREADS), args, 0, ctx->stream));
+  if (slot >= 0) cudaEventRecord(ctx->prof.ev[2 * slot + 1], ctx->stream);
+  return GC_OK;
+}
+
+// Levels 1 .. nlev-1 of a V-cycle: b[1] in, e[1] out. Default: two persistent
+// launches around the single-CTA tail; the validation path (natural layout)
+// keeps one launch per phase.
+static int coarse_levels(gc_ctx *ctx, const gc_mg_params *p) {
   const int L = ctx->nlev;
-  if (L == 0) return GC_OK;
-  if (L == 1) return launch_smooth0(ctx, p->coarse_sweeps, 0, p->flags);
   int st;
-  if ((st = launch_smooth0(ctx, p->pre_sweeps, 0, p->flags))) return st;
-  const LevelGeom &g0 = ctx->lev[0];
-  gc_launch(ctx, GK_RESID0, k_resid0, dim3(node_grid(g0)), dim3(dim3(32, 8)), 0, ctx->hi, ctx->lo, ctx->b0, ctx->r0, nullptr, ctx->G);
-  gc_launch(ctx, GK_RESTRICT, k_restrict, dim3(node_grid(ctx->lev[1])), dim3(dim3(32, 8)), 0, ctx->r0, g0, ctx->b[1], ctx->lev[1]);
-  GC_LAUNCH_CHECK(ctx, "resid0/restrict");
+  if (!(p->flags & GC_MG_NATURAL_LAYOUT) && ctx->tail > 1) {
+    if ((st = launch_coarse(ctx, p, false))) return st;
+    if (ctx->tail < L && (st = launch_tail(ctx, p))) return st;
+    return launch_coarse(ctx, p, true);
+  }
   for (int l = 1; l < ctx->tail; ++l) {
     const LevelGeom &g = ctx->lev[l];
     const size_t n3 = (size_t)g.n * g.n * g.n;
     GC_CUDA(ctx, cudaMemsetAsync(ctx->e[l], 0, n3 * sizeof(float), ctx->stream));
     if ((st = launch_smooth(ctx, l, p->pre_sweeps))) return st;
     gc_launch(ctx, GK_RESID, k_resid, dim3(node_grid(g)), dim3(dim3(32, 8)), 0, ctx->e[l], ctx->b[l], ctx->rc, g);
-    gc_launch(ctx, GK_RESTRICT, k_restrict, dim3(node_grid(ctx->lev[l + 1])), dim3(dim3(32, 8)), 0, ctx->rc, g, ctx->b[l + 1], ctx->lev[l + 1]);
+    gc_launch(ctx, GK_RESTRICT, k_restrict, dim3(node_grid(ctx->lev[l + 1])), dim3(dim3(32, 8)), 0, ctx->rc, g,
+              ctx->b[l + 1], ctx->lev[l + 1]);
     GC_LAUNCH_CHECK(ctx, "resid/restrict");
   }
   if (ctx->tail < L) {
     if ((st = launch_tail(ctx, p))) return st;
   }
   for (int l = ctx->tail - 1; l >= 1; --l) {
-    gc_launch(ctx, GK_PROLONG, k_prolong, dim3(node_grid(ctx->lev[l])), dim3(dim3(32, 8)), 0, ctx->e[l + 1], ctx->lev[l + 1], ctx->e[l], ctx->lev[l]);
+    gc_launch(ctx, GK_PROLONG, k_prolong, dim3(node_grid(ctx->lev[l])), dim3(dim3(32, 8)), 0, ctx->e[l + 1],
+              ctx->lev[l + 1], ctx->e[l], ctx->lev[l]);
     GC_LAUNCH_CHECK(ctx, "prolong");
     if ((st = launch_smooth(ctx, l, p->post_sweeps))) return st;
   }
-  return launch_smooth0(ctx, p->post_sweeps, 1, p->flags);
+  return GC_OK;
+}
+
+// r = b0 - L phi on the finest interior (colour-split, or natural for the
+// validation path), with ||r||^2 into dsmall[GC_S_RNORM2] (async). The split
+// path also writes the first red half-sweep of the next pre-smoothing.
+static int residual0(gc_ctx *ctx, const gc_mg_params *p) {
+  const LevelGeom &g0 = ctx->lev[0];
+  const dim3 grid = node_grid(g0);
+  const size_t nb = (size_t)grid.x * grid.y * grid.z;
+  int st = gc_ensure_red(ctx, nb);
+  if (st) return st;
+  const bool plain = (p->flags & GC_MG_PLAIN_F32) != 0;
+  const Split0 d = split0(ctx);
+  if (p->flags & GC_MG_NATURAL_LAYOUT) {
+    if ((st = mg_alloc_natural(ctx))) return st;
+    if (plain)
+      gc_launch(ctx, GK_RESID0, k_resid0<true, false>, grid, dim3(32, 8), 0, ctx->hi, ctx->lo, ctx->b0, ctx->r0n,
+                nullptr, ctx->red, d);
+    else
+      gc_launch(ctx, GK_RESID0, k_resid0<false, false>, grid, dim3(32, 8), 0, ctx->hi, ctx->lo, ctx->b0, ctx->r0n,
+                nullptr, ctx->red, d);
+  } else {
+    const int pre = ctx->nlev == 1 ? p->coarse_sweeps : p->pre_sweeps;
+    float *ef = pre >= 1 ? ctx->e0s : nullptr;
+    if (plain)
+      gc_launch(ctx, GK_RESID0, k_resid0<true, true>, grid, dim3(32, 8), 0, ctx->hi, ctx->lo, ctx->b0, ctx->r0s, ef,
+                ctx->red, d);
+    else
+      gc_launch(ctx, GK_RESID0, k_resid0<false, true>, grid, dim3(32, 8), 0, ctx->hi, ctx->lo, ctx->b0, ctx->r0s, ef,
+                ctx->red, d);
+  }
+  GC_LAUNCH_CHECK(ctx, "resid0");
+  return finalize_to(ctx, (int)nb, 1, GC_S_RNORM2);
+}
+
+// One V-cycle of the defect correction: relax L e = r from e = 0 (FP32,
+// colour-split), restrict its residual, coarse correction, prolong, relax, then
+// phi += e and the new residual r = b0 - L phi with its norm. Expects r (and,
+// when pre-smoothing, the first red half-sweep) from the previous residual0.
+static int vcycle(gc_ctx *ctx, const gc_mg_params *p) {
+  const int L = ctx->nlev;
+  if (L == 0) return GC_OK;
+  const bool plain = (p->flags & GC_MG_PLAIN_F32) != 0;
+  const int pre = L == 1 ? p->coarse_sweeps : p->pre_sweeps;  // one level: relaxation alone
+  const int post = L == 1 ? 0 : p->post_sweeps;
+  const LevelGeom &g0 = ctx->lev[0];
+  const Split0 d = split0(ctx);
+  int st;
+  if (p->flags & GC_MG_NATURAL_LAYOUT) {
+    // the same cycle with the generic kernels on a natural-layout correction
+    const size_t g3 = (size_t)ctx->G * ctx->G * ctx->G;
+    GC_CUDA(ctx, cudaMemsetAsync(ctx->e0n, 0, g3 * sizeof(float), ctx->stream));
+    for (int h = 0; h < 2 * pre; ++h)
+      gc_launch(ctx, GK_SMOOTH0, k_smooth, rb_grid(g0), dim3(RB_TX, RB_TY), 0, ctx->e0n, ctx->r0n, g0, h & 1);
+    if (L > 1) {
+      gc_launch(ctx, GK_RESIDE, k_resid, node_grid(g0), dim3(32, 8), 0, ctx->e0n, ctx->r0n, ctx->r0, g0);
+      gc_launch(ctx, GK_RESTRICT, k_restrict, node_grid(ctx->lev[1]), dim3(32, 8), 0, ctx->r0, g0, ctx->b[1],
+                ctx->lev[1]);
+      GC_LAUNCH_CHECK(ctx, "natural resid/restrict");
+      if ((st = coarse_levels(ctx, p))) return st;
+      gc_launch(ctx, GK_PROLONG0, k_prolong, node_grid(g0), dim3(32, 8), 0, ctx->e[1], ctx->lev[1], ctx->e0n, g0);
+      for (int h = 0; h < 2 * post; ++h)
+        gc_launch(ctx, GK_SMOOTH0, k_smooth, rb_grid(g0), dim3(RB_TX, RB_TY), 0, ctx->e0n, ctx->r0n, g0, h & 1);
+    }
+    if (plain)
+      gc_launch(ctx, GK_UPDATE0, k_update0<true, false>, node_grid(g0), dim3(32, 8), 0, (const float *)ctx->e0n,
+                ctx->hi, ctx->lo, d);
+    else
+      gc_launch(ctx, GK_UPDATE0, k_update0<false, false>, node_grid(g0), dim3(32, 8), 0, (const float *)ctx->e0n,
+                ctx->hi, ctx->lo, d);
+    GC_LAUNCH_CHECK(ctx, "natural cycle");
+    return residual0(ctx, p);
+  }
+  const dim3 sg = split_grid(ctx);
+  if (pre == 0) GC_CUDA(ctx, cudaMemsetAsync(ctx->e0s, 0, 2 * ctx->half0 * sizeof(float), ctx->stream));
+  // half-sweep 0 (red, from zero) came with the residual
+  for (int h = 1; h < 2 * pre; ++h)
+    gc_launch(ctx, GK_SMOOTH0, k_rb0<false>, sg, SPLIT_BLOCK, 0, ctx->e0s, (const float *)ctx->r0s, d, h & 1);
+  if (L > 1) {
+    gc_launch(ctx, GK_RESIDE, k_resid0e, node_grid(g0), dim3(32, 8), 0, (const float *)ctx->e0s,
+              (const float *)ctx->r0s, ctx->r0, d);
+    gc_launch(ctx, GK_RESTRICT, k_restrict, node_grid(ctx->lev[1]), dim3(32, 8), 0, ctx->r0, g0, ctx->b[1],
+              ctx->lev[1]);
+    GC_LAUNCH_CHECK(ctx, "resid0e/restrict");
+    if ((st = coarse_levels(ctx, p))) return st;
+    gc_launch(ctx, GK_PROLONG0, k_prolong0s, sg, SPLIT_BLOCK, 0, (const float *)ctx->e[1], ctx->lev[1], ctx->e0s, g0,
+              d, post == 0 ? 1 : 0);
+    for (int h = 0; h < 2 * post - 1; ++h)
+      gc_launch(ctx, GK_SMOOTH0, k_rb0<false>, sg, SPLIT_BLOCK, 0, ctx->e0s, (const float *)ctx->r0s, d, h & 1);
+  }
+  if (post >= 1) {  // last half-sweep (black) and phi += e in one pass
+    if (plain)
+      gc_launch(ctx, GK_UPDATE0, k_rb0_last<true>, sg, SPLIT_BLOCK, 0, (const float *)ctx->e0s,
+                (const float *)ctx->r0s, ctx->hi, ctx->lo, d);
+    else
+      gc_launch(ctx, GK_UPDATE0, k_rb0_last<false>, sg, SPLIT_BLOCK, 0, (const float *)ctx->e0s,
+                (const float *)ctx->r0s, ctx->hi, ctx->lo, d);
+  } else {
+    if (plain)
+      gc_launch(ctx, GK_UPDATE0, k_update0<true, true>, node_grid(g0), dim3(32, 8), 0, (const float *)ctx->e0s,
+                ctx->hi, ctx->lo, d);
+    else
+      gc_launch(ctx, GK_UPDATE0, k_update0<false, true>, node_grid(g0), dim3(32, 8), 0, (const float *)ctx->e0s,
+                ctx->hi, ctx->lo, d);
+  }
+  GC_LAUNCH_CHECK(ctx, "finest cycle");
+  return residual0(ctx, p);
 }
 
 int gc_finalize(gc_ctx *ctx, const double *parts, int nparts, int nv, double *dst) {
@@ -1081,18 +1327,6 @@ int gc_finalize(gc_ctx *ctx, const double *parts, int nparts, int nv, double *ds
 
 static int finalize_to(gc_ctx *ctx, int nparts, int nv, int slot) {
   return gc_finalize(ctx, ctx->red, nparts, nv, ctx->dsmall + slot);
-}
-
-// ||r0||^2 into dsmall[GC_S_RNORM2] (async).
-static int resid_norm_async(gc_ctx *ctx) {
-  const LevelGeom &g0 = ctx->lev[0];
-  const dim3 grid = node_grid(g0);
-  const size_t nb = (size_t)grid.x * grid.y * grid.z;
-  int st = gc_ensure_red(ctx, nb);
-  if (st) return st;
-  gc_launch(ctx, GK_RESID0, k_resid0, dim3(grid), dim3(dim3(32, 8)), 0, ctx->hi, ctx->lo, ctx->b0, nullptr, ctx->red, ctx->G);
-  GC_LAUNCH_CHECK(ctx, "resid0 norm");
-  return finalize_to(ctx, (int)nb, 1, GC_S_RNORM2);
 }
 
 static int read_small(gc_ctx *ctx, int slot, int count) {
@@ -1115,24 +1349,89 @@ int gc_norm_b(gc_ctx *ctx) {
 
 int gc_faces_from_moments(gc_ctx *ctx) {
   const long long tot = 6LL * ctx->G * ctx->G;
-  gc_launch(ctx, GK_FACES, k_faces, dim3(gc_blocks(tot, 256)), dim3(256), 0, ctx->hi, ctx->lo, ctx->hi2, ctx->lo2, ctx->G, ctx->dx, ctx->grav, ctx->dmom);
+  gc_launch(ctx, GK_FACES, k_faces, dim3(gc_blocks(tot, 256)), dim3(256), 0, ctx->hi, ctx->lo, ctx->G, ctx->dx, ctx->grav, ctx->dmom);
   GC_LAUNCH_CHECK(ctx, "faces");
   return GC_OK;
 }
 
-// Adaptive V-cycling (multigrid.py:473-485). Expects b0, faces and the initial
-// interior guess in place and ||b0||^2 in dsmall.
+// The adaptive loop inside a stream capture: the residual of the initial guess
+// and the first decision, then a conditional while node whose body (captured on
+// the context's side stream) is one V-cycle, its residual and the next decision.
+// Same kernels in the same order as the host loop, so the same potential. The
+// cycle count, the converged flag and both norms are left in dsmall and copied
+// to the pinned host mirror at the end.
+static int mg_run_captured(gc_ctx *ctx, const gc_mg_params *p) {
+  int s;
+  if (ctx->nlev == 0) return GC_OK;
+  if ((s = residual0(ctx, p))) return s;
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t graph = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  GC_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, &graph, &deps, nullptr, &nd));
+  GC_REQUIRE(ctx, cs == cudaStreamCaptureStatusActive, "captured solve outside a stream capture");
+  cudaGraphConditionalHandle h;
+  GC_CUDA(ctx, cudaGraphConditionalHandleCreate(&h, graph, 0, 0));
+  gc_launch(ctx, GK_REDUCE, k_mg_decide, dim3(1), dim3(32), 0, h, ctx->dsmall, p->tol, p->min_cycles, p->max_cycles, 1);
+  GC_LAUNCH_CHECK(ctx, "decide");
+  GC_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, &graph, &deps, nullptr, &nd));
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t cond;
+  GC_CUDA(ctx, cudaGraphAddNode(&cond, graph, deps, nullptr, nd, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  cudaStream_t main = ctx->stream;
+  GC_CUDA(ctx, cudaStreamBeginCaptureToGraph(ctx->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  ctx->stream = ctx->side;
+  const long long before = gc_launch_total(ctx);
+  s = vcycle(ctx, p);
+  if (!s) {
+    gc_launch(ctx, GK_REDUCE, k_mg_decide, dim3(1), dim3(32), 0, h, ctx->dsmall, p->tol, p->min_cycles,
+              p->max_cycles, 0);
+    s = gc_check_launch(ctx, "decide");
+  }
+  ctx->cap_body_launches = gc_launch_total(ctx) - before;
+  cudaGraph_t got = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(ctx->side, &got);
+  ctx->stream = main;
+  if (s) return s;
+  GC_CUDA(ctx, e);
+  GC_CUDA(ctx, cudaStreamUpdateCaptureDependencies(main, &cond, nullptr, 1, cudaStreamSetCaptureDependencies));
+  GC_CUDA(ctx, cudaMemcpyAsync(ctx->hsmall, ctx->dsmall, GC_S_MIRROR * sizeof(double), cudaMemcpyDeviceToHost, main));
+  return GC_OK;
+}
+
+// Adaptive V-cycling (multigrid.py:473-485): at least one cycle, then stop once
+// ||r|| < tol ||b|| (never before min_cycles; no test when ||b|| = 0), at most
+// max_cycles. Expects b0, faces and the initial interior guess in place and
+// ||b0||^2 in dsmall. The residual of the initial guess is formed first; every
+// cycle ends with the residual of its result and its norm.
 int gc_mg_run(gc_ctx *ctx, const gc_mg_params *p, gc_mg_stats *stats) {
   gc_mg_stats st;
   memset(&st, 0, sizeof(st));
   int s;
+  // the persistent coarse launches' grid barrier starts every solve clean
+  GC_CUDA(ctx, cudaMemsetAsync(ctx->dsmall + GC_S_GRIDBAR, 0, 2 * sizeof(double), ctx->stream));
+  if (ctx->capturing && !(p->flags & GC_MG_FIXED_CYCLES)) {
+    if ((s = mg_run_captured(ctx, p))) return s;
+    st.cycles = -1;  // decided on the device: read them with gc_pm_graph_stats
+    st.converged = -1;
+    st.rhs_norm = st.res_norm = NAN;
+    ctx->last_stats = st;
+    ctx->solved_once = 1;
+    if (stats) *stats = st;
+    return GC_OK;
+  }
+  if (ctx->nlev > 0 && (s = residual0(ctx, p))) return s;
   if (p->flags & GC_MG_FIXED_CYCLES) {
     // exactly max_cycles V-cycles and no host read: the residual norm is left on
     // the device (gc_pm_last_residual reads it), so the solve can be captured in
     // a CUDA graph
     for (int c = 0; c < p->max_cycles && ctx->nlev > 0; ++c)
       if ((s = vcycle(ctx, p))) return s;
-    if (ctx->nlev > 0 && (s = resid_norm_async(ctx))) return s;
     // ||b0||^2 and ||r0||^2 (slots 0 and 1) to the pinned host mirror, stream
     // ordered: after a synchronisation the caller reads them without a copy
     GC_CUDA(ctx, cudaMemcpyAsync(ctx->hsmall, ctx->dsmall, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1144,37 +1443,30 @@ int gc_mg_run(gc_ctx *ctx, const gc_mg_params *p, gc_mg_stats *stats) {
     if (stats) *stats = st;
     return GC_OK;
   }
-  s = read_small(ctx, GC_S_BNORM2, 1);
-  if (s) return s;
+  if ((s = read_small(ctx, GC_S_BNORM2, 2))) return s;
   const double bnorm = sqrt(ctx->hsmall[GC_S_BNORM2]);
   const double h2 = ctx->dx * ctx->dx;
   st.rhs_norm = bnorm / h2;
-  st.cycles = p->max_cycles;
-  st.converged = 0;
-  double rnorm = NAN;
   if (ctx->nlev == 0) {
     st.cycles = 0;
     st.converged = 1;
     st.res_norm = 0.0;
   } else {
-    for (int c = 0; c < p->max_cycles; ++c) {
-      if ((s = vcycle(ctx, p))) return s;
-      if (c + 1 >= p->min_cycles && bnorm > 0.0) {
-        if ((s = resid_norm_async(ctx))) return s;
-        if ((s = read_small(ctx, GC_S_RNORM2, 1))) return s;
-        rnorm = sqrt(ctx->hsmall[GC_S_RNORM2]);
-        if (rnorm < p->tol * bnorm) {
-          st.cycles = c + 1;
-          st.converged = 1;
-          break;
-        }
+    double rnorm = sqrt(ctx->hsmall[GC_S_RNORM2]);
+    const int min_c = p->min_cycles > 1 ? p->min_cycles : 1;
+    int c = 0;
+    for (;;) {
+      if (c >= min_c && bnorm > 0.0 && rnorm < p->tol * bnorm) {
+        st.converged = 1;
+        break;
       }
-    }
-    if (!(rnorm == rnorm)) {
-      if ((s = resid_norm_async(ctx))) return s;
+      if (c >= p->max_cycles) break;
+      if ((s = vcycle(ctx, p))) return s;
+      ++c;
       if ((s = read_small(ctx, GC_S_RNORM2, 1))) return s;
       rnorm = sqrt(ctx->hsmall[GC_S_RNORM2]);
     }
+    st.cycles = c;
     st.res_norm = rnorm / h2;
   }
   ctx->last_stats = st;
@@ -1256,6 +1548,10 @@ extern "C" int gc_mg_solve(gc_ctx *ctx, const float *rho, float *phi, int warm_s
   if (flags & GC_FLAG_NONFINITE_RHO) {
     gc_set_error(ctx, "rho contains non-finite values");
     return GC_ERR_NONFINITE;
+  }
+  if (flags & GC_FLAG_TIMEOUT) {
+    gc_set_error(ctx, "a bounded device wait of the solve timed out (the potential is incomplete)");
+    return GC_ERR_TIMEOUT;
   }
   return GC_OK;
 }

@@ -26,8 +26,9 @@ GC_FLAG_NONFINITE_RHO = 0x2
 GC_FLAG_BAD_PID = 0x4
 GC_FLAG_IC_REJECT = 0x8
 GC_FLAG_TIMEOUT = 0x10
-GC_MG_FUSED_SWEEP = 0x1
 GC_MG_FIXED_CYCLES = 0x2
+GC_MG_PLAIN_F32 = 0x4
+GC_MG_NATURAL_LAYOUT = 0x8
 GC_STEP_GRAD_GRID = 0x1
 GC_STEP_SOLVE_ONLY = 0x2
 GC_STEP_PUSH_ONLY = 0x4
@@ -177,6 +178,11 @@ _PROTOS = {
     "gc_ws_status": (C.c_int, [_vp, C.POINTER(C.c_uint32), C.c_int]),
     "gc_ws_autotune": (C.c_int, [_vp, C.c_int, _vp]),
     "gc_ws_plan_info": (C.c_int, [_vp, C.c_int, C.c_int, _vp]),
+    "gc_pm_graph_create": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(StepParams), C.POINTER(_vp)]),
+    "gc_pm_graph_launch": (C.c_int, [_vp]),
+    "gc_pm_graph_destroy": (C.c_int, [_vp]),
+    "gc_pm_graph_info": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    "gc_pm_graph_stats": (C.c_int, [_ctxp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "gc_pm_set_warmstart": (C.c_int, [_ctxp, _vp, C.c_int, C.c_int]),
     "gc_pm_record_sample": (C.c_int, [_ctxp, _vp]),
 }
@@ -321,6 +327,35 @@ class Context:
         if getattr(self, "_h", None) is not None and self._h.value:
             self._lib.gc_ctx_destroy(self._h)
             self._h = _ctxp()
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown ordering
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class StepGraph:
+    """One captured ADVANCE step (``gc_pm_graph_create``): replay it with
+    :meth:`launch` on the stream it was captured on."""
+
+    def __init__(self, ctx: Context, particles: Particles, params: StepParams):
+        h = _vp()
+        ctx.call("gc_pm_graph_create", C.byref(particles), C.byref(params), C.byref(h), what="gc_pm_graph_create")
+        self._h = h
+        self._ctx = ctx
+        fixed, body = C.c_longlong(), C.c_longlong()
+        check(ctx._lib.gc_pm_graph_info(h, C.byref(fixed), C.byref(body)), ctx.handle, "gc_pm_graph_info")
+        self.fixed_launches = int(fixed.value)
+        self.body_launches = int(body.value)
+
+    def launch(self) -> None:
+        check(self._ctx._lib.gc_pm_graph_launch(self._h), self._ctx.handle, "gc_pm_graph_launch")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._ctx._lib.gc_pm_graph_destroy(self._h)
+            self._h = _vp()
 
     def __del__(self):  # pragma: no cover - interpreter shutdown ordering
         try:

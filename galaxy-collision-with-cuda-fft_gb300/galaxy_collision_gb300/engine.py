@@ -270,7 +270,7 @@ class PMEngine:
         self.steps_since_sort = 0
 
     # -- stepping ---------------------------------------------------------------
-    def _step(self, mode: int, dt: float, diagnostics: bool, phase_flags: int = 0) -> StepResult:
+    def _step_params(self, mode: int, dt: float, diagnostics: bool, phase_flags: int = 0) -> _native.StepParams:
         sp = _native.StepParams()
         sp.dt = float(dt)
         sp.mode = mode
@@ -281,6 +281,10 @@ class PMEngine:
         sp.flags = (_native.GC_STEP_GRAD_GRID if self.grad_grid else 0) | phase_flags
         if self.deposit_next:
             sp.flags |= _native.GC_STEP_DEPOSIT_NEXT
+        return sp
+
+    def _step(self, mode: int, dt: float, diagnostics: bool, phase_flags: int = 0) -> StepResult:
+        sp = self._step_params(mode, dt, diagnostics, phase_flags)
         st = _native.StepStats()
         p = self._struct(self.cur)
         self.ctx.call("gc_pm_step", C.byref(p), C.byref(sp), C.byref(st), what="gc_pm_step")
@@ -370,23 +374,47 @@ class PMEngine:
         return int(n.value)
 
     def advance_graph(self, dt: float) -> None:
-        """advance() through a CUDA graph of the whole step, captured on first use
-        for each particle-buffer parity (the sort, between graphs, swaps them). The
-        engine must be open with a complete warm-start history (3 steps)."""
+        """advance() through a CUDA graph of the whole step (gc_pm_graph_create),
+        captured on first use for each particle-buffer set and dt (the cell sort,
+        run between replays, swaps the buffers). The adaptive solve's stopping
+        rule is decided on the device, so a replay makes no host read; its
+        V-cycles and residual are read with graph_stats() after a
+        synchronisation. Needs an open engine that has taken at least three
+        steps (complete warm-start history). Ordered after the work already
+        queued on the current stream, and the current stream waits for it."""
         if self.state != "open":
             raise RuntimeError("advance_graph needs an open (primed) engine")
         if self.sort_every > 0 and self.steps_since_sort >= self.sort_every:
             self.sort()
         key = (self.cur["x"].data_ptr(), float(dt))
-        g = self._graphs.get(key)
-        if g is None:
-            g = torch.cuda.CUDAGraph()
-            torch.cuda.synchronize()
-            with torch.cuda.graph(g):
-                self.step_kernels(dt)
-            self._graphs[key] = g
-        g.replay()
+        main = torch.cuda.current_stream()
+        gs = self._graph_stream()
+        gs.wait_stream(main)
+        with torch.cuda.stream(gs):
+            g = self._graphs.get(key)
+            if g is None:
+                g = _native.StepGraph(self.ctx, self._struct(self.cur), self._step_params(_native.GC_STEP_ADVANCE, dt,
+                                                                                         False))
+                self._graphs[key] = g
+            self.ctx.bind_stream()
+            g.launch()
+        main.wait_stream(gs)
         self.steps_since_sort += 1
+        self.last_graph = g
+
+    def _graph_stream(self):
+        if getattr(self, "_gstream", None) is None:
+            self._gstream = torch.cuda.Stream()
+        return self._gstream
+
+    def graph_stats(self) -> StepResult:
+        """V-cycles, convergence and relative residual of the last graph-replayed
+        step (synchronises the device)."""
+        torch.cuda.synchronize()
+        c, conv, rel = C.c_int(), C.c_int(), C.c_double()
+        _native.check(self.ctx._lib.gc_pm_graph_stats(self.ctx.handle, C.byref(c), C.byref(conv), C.byref(rel)),
+                      self.ctx.handle, "graph_stats")
+        return StepResult(int(c.value), bool(conv.value), float(rel.value))
 
     def run(self, steps: int, dt: float) -> None:
         """Advance ``steps`` KDK steps from a synchronised state and end synchronised."""
@@ -408,6 +436,7 @@ class PMEngine:
         if mode not in modes:
             raise ValueError(f"unknown warm-start mode {mode!r} (expected one of {sorted(modes)})")
         self._ws_net = net  # keep the network alive while attached
+        self._graphs = {}   # captured steps embed the initial-guess kernels of the old mode
         h = net._h if net is not None else None
         self.ctx.call("gc_pm_set_warmstart", h, modes[mode], int(bool(track)), what="set_warmstart")
 

@@ -36,7 +36,8 @@ class MultigridPoissonSolver(PoissonSolver):
         tol: float = 1e-3,
         min_cycles: int = 1,
         *,
-        fused_sweep: bool = False,
+        plain_f32: bool = False,
+        natural_layout: bool = False,
     ):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
@@ -49,7 +50,13 @@ class MultigridPoissonSolver(PoissonSolver):
         self.min_cycles = max(1, int(min_cycles))
         self.last_cycles = 0
         self.last_stats = None
-        self.fused_sweep = bool(fused_sweep)  # finest level by the streaming sweep kernel (same results)
+        # plain_f32: the all-FP32 method (potential, residual and corrections in
+        # f32; stalls at the FP32 floor like the reference), the baseline the
+        # mixed-precision default is compared with
+        self.plain_f32 = bool(plain_f32)
+        # natural_layout: validation path, the finest correction in natural
+        # layout through the generic level kernels (identical potentials)
+        self.natural_layout = bool(natural_layout)
         self._ctx = _native.Context(self.grid_size, self.dx, self.G)
         self.sizes = [n for (n, _J, _p) in self._ctx.levels()]
 
@@ -61,7 +68,8 @@ class MultigridPoissonSolver(PoissonSolver):
         p.max_cycles = self.n_cycles
         p.min_cycles = self.min_cycles
         p.tol = self.tol
-        p.flags = _native.GC_MG_FUSED_SWEEP if self.fused_sweep else 0
+        p.flags = ((_native.GC_MG_PLAIN_F32 if self.plain_f32 else 0)
+                   | (_native.GC_MG_NATURAL_LAYOUT if self.natural_layout else 0))
         return p
 
     def solve(self, rho, phi, warm_start: bool = False) -> None:

@@ -31,6 +31,10 @@ from galaxy_collision_gb300.warmstart import WEIGHTS_PATH, WarmStartNet
 
 BOX, GRID, DT = 64.0, 256, 0.005
 
+# kernels of one solve: the multigrid, its faces, norms and b0 conversion, and the initial guess
+SOLVE_KERNELS = ("smooth0", "update0", "resid0", "resid0e", "restrict", "smooth", "resid", "prolong", "prolong0",
+                 "tail", "faces", "reduce", "convert_q", "warmstart")
+
 
 def random_collision(rng: np.random.Generator, n: int, dx: float = BOX / GRID) -> ic.ICResult:
     ratio = rng.uniform(1.0, 3.0)
@@ -139,9 +143,7 @@ def evaluate(net: WarmStartNet | None, n_particles: int = 10_000_000, steps: int
         torch.cuda.synchronize()
         stats = eng.ctx.kernel_stats()
         eng.ctx.profile(False)
-        solve = sum(v[2] for k, v in stats.items() if k in (
-            "smooth0", "sweep0", "resid0", "restrict", "smooth", "resid", "prolong", "prolong0", "tail", "faces",
-            "reduce", "warmstart"))
+        solve = sum(v[2] for k, v in stats.items() if k in SOLVE_KERNELS)
         res[mode] = {"mean_vcycles": float(np.mean(cycles)), "vcycles": cycles,
                      "ms_per_solve": solve / steps, "ms_per_step": ev0.elapsed_time(ev1) / steps,
                      "warmstart_ms_per_step": stats.get("warmstart", (0, 0, 0.0))[2] / steps}

@@ -49,16 +49,23 @@ enum gc_status_code {
 #define GC_FLAG_IC_REJECT 0x8u      /* a device IC rejection loop reached its attempt limit */
 #define GC_FLAG_TIMEOUT 0x10u       /* a bounded wait inside a kernel ran out; that kernel stopped early */
 
-/* gc_mg_params.flags: relax the finest level with the streaming sweep (one
- * red+black sweep per pass through shared memory, ping-pong buffers, the
- * prolongation folded into the first post-sweep) instead of the in-place
- * red and black half-sweep kernels. Identical results. */
-#define GC_MG_FUSED_SWEEP 0x1
 /* gc_mg_params.flags: run exactly max_cycles V-cycles without reading the
  * residual norm on the host (it is left on the device; gc_pm_last_residual
  * reads it). The engine's step then makes no host synchronisation, so it can be
  * captured in a CUDA graph. Stats report converged = -1 and NaN norms. */
 #define GC_MG_FIXED_CYCLES 0x2
+/* gc_mg_params.flags: the plain FP32 method. The potential is a single f32
+ * array (the lo part is ignored and left alone), the residual is formed in f32
+ * with the reference's left-to-right neighbour sum (multigrid.py:62-79) and the
+ * corrections are added in f32, so the residual stalls at the FP32 floor (about
+ * 1e-5 to 1e-4 of ||rhs||, as the reference's does) and the solve then runs to
+ * max_cycles. The comparison baseline for the mixed-precision default. */
+#define GC_MG_PLAIN_F32 0x4
+/* gc_mg_params.flags: validation path. The finest level's correction and
+ * residual are kept in natural (interleaved) layout and relaxed by the generic
+ * level kernels instead of the colour-split half-sweeps; the potential is
+ * identical bit for bit, it just moves more bytes. */
+#define GC_MG_NATURAL_LAYOUT 0x8
 
 typedef struct gc_ctx gc_ctx;
 
@@ -404,6 +411,30 @@ int gc_pm_residual_host(const gc_ctx *ctx, double *rel);
 /* Between a SOLVE_ONLY and a PUSH_ONLY step: more V-cycles on the current
  * potential until ||r|| < tol ||4 pi G rho|| (at least one); *cycles gets how many. */
 int gc_pm_refine(gc_ctx *ctx, const gc_mg_params *params, int *cycles);
+
+/* ---- the whole step as one CUDA graph (no reference counterpart: the reference
+ * synchronises with the host after every V-cycle, solver/multigrid.py:477-485) */
+
+/* Capture one ADVANCE step of the fused engine (same particles, parameters and
+ * flags as sp, without diagnostics) from the context's stream (set one with
+ * gc_set_stream) and instantiate it. The adaptive solve keeps the reference's
+ * stopping rule, decided on the device: a conditional while node repeats the
+ * V-cycle until ||r|| < tol ||b|| (at least max(1, min_cycles), at most
+ * max_cycles cycles). A replay (gc_pm_graph_launch) makes no host
+ * synchronisation and gives the state an eager gc_pm_step would, bit for bit.
+ * Needs an open engine that has taken at least three steps with these flags
+ * (the warm-start history must be complete); a graph stays valid while the
+ * particle arrays, the stream and the warm-start mode are unchanged (the cell
+ * sort swaps particle buffers: keep one graph per buffer set). */
+typedef struct gc_graph gc_graph;
+int gc_pm_graph_create(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp, gc_graph **out);
+int gc_pm_graph_launch(gc_graph *g);
+int gc_pm_graph_destroy(gc_graph *g);
+/* Kernels a replay launches: fixed_launches + cycles * body_launches. */
+int gc_pm_graph_info(const gc_graph *g, long long *fixed_launches, long long *body_launches);
+/* V-cycles, converged flag and relative residual of the last replayed solve,
+ * from the pinned mirror the graph writes: synchronise the stream first. */
+int gc_pm_graph_stats(const gc_ctx *ctx, int *cycles, int *converged, double *rel);
 
 /* ---- instrumentation (no kernel counterpart in the reference: it replaces the
  * sync-bracketed per-stage wall clock of bench.py:66-73, 176-186) ---------- */

@@ -89,13 +89,32 @@ def test_residual_norms_match_numpy(cuda, n, dx):
 
 
 @pytest.mark.parametrize("n,dx", [(16, 1.0), (37, 0.5), (100, 2.0), (130, 0.25)])
-def test_fused_sweep_bitwise_equals_half_sweeps(cuda, n, dx):
-    """The streaming sweep (and its fused prolongation) is the same arithmetic as
-    the in-place red and black half-sweeps: identical potentials."""
+@pytest.mark.parametrize("plain", [False, True])
+def test_split_layout_bitwise_equals_natural_layout(cuda, n, dx, plain):
+    """The colour-split finest level (half-sweeps reading only the other colour,
+    prolongation into the black half, last half-sweep fused with phi += e) is the
+    same arithmetic as the generic level kernels on a natural-layout correction:
+    identical potentials, odd and even grids, default and plain FP32."""
     rho = gaussian_rho(n, dx, 3.0 * dx, 1.5, center=(0.45 * n * dx, 0.5 * n * dx, 0.6 * n * dx))
-    _, _, a = _solve(rho, dx, 1.0, n_cycles=4, tol=0.0)
-    _, _, b = _solve(rho, dx, 1.0, n_cycles=4, tol=0.0, fused_sweep=True)
+    sa, _, a = _solve(rho, dx, 1.0, n_cycles=4, tol=0.0, plain_f32=plain)
+    sb, _, b = _solve(rho, dx, 1.0, n_cycles=4, tol=0.0, plain_f32=plain, natural_layout=True)
     np.testing.assert_array_equal(a.to_numpy(), b.to_numpy())
+    assert sa.last_stats["res_norm"] == sb.last_stats["res_norm"]
+
+
+def test_plain_f32_stalls_at_the_fp32_floor(cuda):
+    """The plain FP32 method (the reference's precision) cannot go below the
+    FP32 floor: asked for 1e-6 it runs to its cycle cap with the residual near
+    1e-5 of ||rhs||; the default reaches the tolerance in a few cycles, and both
+    potentials agree to the FP32 floor."""
+    n = 64
+    rho = gaussian_rho(n, 0.375, 1.2, 1.0, center=(11.0, 12.5, 12.0))
+    sp, _, pp = _solve(rho, 0.375, 1.0, n_cycles=20, tol=1e-6, plain_f32=True)
+    sd, _, pd = _solve(rho, 0.375, 1.0, n_cycles=20, tol=1e-6)
+    assert sd.last_stats["converged"] and sd.last_cycles <= 8
+    assert not sp.last_stats["converged"] and sp.last_cycles == 20
+    assert 1e-7 < sp.last_stats["rel_residual"] < 1e-4
+    assert rel_l2(pp.to_numpy(), pd.to_numpy()) < 1e-5
 
 
 def test_convergence_factor_per_vcycle(cuda):
