@@ -40,6 +40,9 @@ enum {
   GC_S_GRIDBAR = 10, // [10, 12): grid-barrier words of the persistent coarse launches
   GC_S_MASS = 12,    // total deposited density-mass used for the fixed-point quantum
   GC_S_QEXP = 13,    // quantum exponent E: quantum = 2^E (density units)
+  GC_S_SOLVES = 14,  // device-decided solves since the counters were reset ...
+  GC_S_CYC_TOTAL = 15, // ... their V-cycles ...
+  GC_S_MAXREL2 = 16, // ... and the largest (||r|| / ||b||)^2 they ended with
   GC_S_FIN_TMP = 128, // [128, 256): chunk partials of gc_finalize
   GC_S_NSLOTS = 256
 };

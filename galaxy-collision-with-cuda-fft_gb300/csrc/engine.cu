@@ -267,3 +267,22 @@ extern "C" int gc_pm_graph_stats(const gc_ctx *ctx, int *cycles, int *converged,
   if (rel) *rel = b2 > 0.0 ? sqrt(r2) / sqrt(b2) : 0.0;
   return GC_OK;
 }
+
+// Solves decided on the device (graph replays) since the last reset: count,
+// total V-cycles and the largest relative residual they ended with.
+// Synchronises; reset clears the counters afterwards.
+extern "C" int gc_pm_solve_counters(gc_ctx *ctx, double out[3], int reset) {
+  if (!ctx) return GC_ERR_ARG;
+  GC_REQUIRE(ctx, out, "gc_pm_solve_counters: NULL output");
+  double h[3];
+  GC_CUDA(ctx, cudaMemcpyAsync(h, ctx->dsmall + GC_S_SOLVES, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  out[0] = h[0];
+  out[1] = h[1];
+  out[2] = sqrt(h[2]);
+  if (reset) {
+    GC_CUDA(ctx, cudaMemsetAsync(ctx->dsmall + GC_S_SOLVES, 0, 3 * sizeof(double), ctx->stream));
+    GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  return GC_OK;
+}

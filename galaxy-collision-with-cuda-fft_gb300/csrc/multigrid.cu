@@ -182,31 +182,39 @@ __global__ void __launch_bounds__(256)
 // ------------------------------------------------------------------------------
 // finest level: double-float red-black Gauss-Seidel, residual, prolongation
 // ------------------------------------------------------------------------------
-// Accurate residual r = b - L_h2(hi + lo) at interior node c (h^2 units).
-__device__ __forceinline__ float df_residual(const float *__restrict__ hi, const float *__restrict__ lo,
-                                             float bc, size_t c, size_t sj, size_t si, float &hc_out,
-                                             float &lc_out) {
-  const float hc = hi[c];
-  const float d0 = __fsub_rn(hi[c + si], hc);
-  const float d1 = __fsub_rn(hi[c - si], hc);
-  const float d2 = __fsub_rn(hi[c + sj], hc);
-  const float d3 = __fsub_rn(hi[c - sj], hc);
-  const float d4 = __fsub_rn(hi[c + 1], hc);
-  const float d5 = __fsub_rn(hi[c - 1], hc);
+// Accurate residual r = b - L_h2(hi + lo) at an interior node (h^2 units) from
+// the pair at the node (hc, lc) and at its six neighbours in the order
+// i+1, i-1, j+1, j-1, k+1, k-1: exact neighbour differences summed with
+// error-free transforms, the lo parts' Laplacian added in f32.
+__device__ __forceinline__ float df_residual_v(float hc, float lc, const float (&h)[6], const float (&l)[6],
+                                               float bc) {
+  const float d0 = __fsub_rn(h[0], hc);
+  const float d1 = __fsub_rn(h[1], hc);
+  const float d2 = __fsub_rn(h[2], hc);
+  const float d3 = __fsub_rn(h[3], hc);
+  const float d4 = __fsub_rn(h[4], hc);
+  const float d5 = __fsub_rn(h[5], hc);
   float s, e, t;
   df_two_sum(d0, d1, s, e);
   df_two_sum(s, d2, s, t); e = __fadd_rn(e, t);
   df_two_sum(s, d3, s, t); e = __fadd_rn(e, t);
   df_two_sum(s, d4, s, t); e = __fadd_rn(e, t);
   df_two_sum(s, d5, s, t); e = __fadd_rn(e, t);
-  const float lc = lo[c];
-  const float ln = ((((lo[c + si] + lo[c - si]) + lo[c + sj]) + lo[c - sj]) + lo[c + 1]) + lo[c - 1];
+  const float ln = ((((l[0] + l[1]) + l[2]) + l[3]) + l[4]) + l[5];
   const float ll = __fsub_rn(ln, __fmul_rn(6.0f, lc));
   float r1, r1e;
   df_two_sum(bc, -s, r1, r1e);
-  hc_out = hc;
-  lc_out = lc;
   return __fadd_rn(r1, __fsub_rn(r1e, __fadd_rn(e, ll)));
+}
+
+__device__ __forceinline__ float df_residual(const float *__restrict__ hi, const float *__restrict__ lo,
+                                             float bc, size_t c, size_t sj, size_t si, float &hc_out,
+                                             float &lc_out) {
+  const float h[6] = {hi[c + si], hi[c - si], hi[c + sj], hi[c - sj], hi[c + 1], hi[c - 1]};
+  const float l[6] = {lo[c + si], lo[c - si], lo[c + sj], lo[c - sj], lo[c + 1], lo[c - 1]};
+  hc_out = hi[c];
+  lc_out = lo[c];
+  return df_residual_v(hc_out, lc_out, h, l, bc);
 }
 
 // FP64 verification residual: phi = (double)hi + (double)lo, or hi alone when lo is NULL.
@@ -262,6 +270,15 @@ __device__ __forceinline__ void sw_stencil(const float *__restrict__ e, size_t c
   diag = (ax.d + ay.d) + az.d;
 }
 
+// Gauss-Seidel value (sum - b) / diag. The common diagonal 6 (every node off a
+// Shortley-Weller face) multiplies by the correctly rounded 1/6 instead of
+// dividing; every smoother of every level and layout uses this one rule, with
+// explicitly rounded products so that no contraction can differ between them.
+#define GC_SIXTH 0.16666667f
+__device__ __forceinline__ float gs_value(float sum, float b, float diag) {
+  return diag == 6.0f ? __fmul_rn(sum - b, GC_SIXTH) : (sum - b) / diag;
+}
+
 __global__ void __launch_bounds__(RB_TX *RB_TY)
     k_smooth(float *__restrict__ e, const float *__restrict__ b, LevelGeom g, int color) {
   const int kk = blockIdx.x * RB_TX + threadIdx.x;
@@ -274,7 +291,7 @@ __global__ void __launch_bounds__(RB_TX *RB_TY)
   const size_t c = ((size_t)i * n + j) * n + k;
   float sum, diag;
   sw_stencil(e, c, i, j, k, g, sum, diag);
-  e[c] = (sum - b[c]) / diag;
+  e[c] = gs_value(sum, b[c], diag);
 }
 
 __global__ void __launch_bounds__(256)
@@ -465,25 +482,37 @@ __device__ __forceinline__ bool grid_barrier(GridBar *gb, unsigned *status, long
   return ok_s != 0;
 }
 
-// Work of a phase is split by rows: warp w of the grid takes rows (i, j)
-// w, w + W, ... (one integer division per row), its lanes the nodes of the row.
-__device__ __forceinline__ int p_warp() { return (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); }
-__device__ __forceinline__ int p_nwarps() { return (int)((gridDim.x * blockDim.x) >> 5); }
-__device__ __forceinline__ int p_lane() { return (int)(threadIdx.x & 31); }
+// A phase's nodes are numbered flat (k fastest); thread t of the grid takes
+// nodes t, t + T, t + 2T, ... (T threads) in batches of PB whose loads are all
+// issued before any result is stored, so that a thread has PB independent L2
+// round trips in flight instead of one. Within a phase no node reads a value
+// that the phase writes (a half-sweep reads only the other colour; the
+// residual, restriction and prolongation write other arrays or only the node
+// itself), so deferring the stores changes nothing.
+#define PB 4
+__device__ __forceinline__ unsigned p_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ unsigned p_nthreads() { return gridDim.x * blockDim.x; }
 
-// One red-black half-sweep of level g (k_smooth's arithmetic): row (i, j) has
-// the nodes k = 2 kk + ((color + i + j) & 1), kk = 0 .. J/2.
+// One red-black half-sweep of level g (k_smooth's slots and arithmetic): row
+// (i, j) holds the nodes k = 2 kk + ((color + i + j) & 1), kk = 0 .. J/2.
 __device__ void p_smooth(float *__restrict__ e, const float *__restrict__ b, const LevelGeom &g, int color,
                          bool first) {
-  const int J = g.J, n = g.n, nkk = J / 2 + 1, rows = J * J;
-  for (int row = p_warp(); row < rows; row += p_nwarps()) {
-    const int i = row / J + 1, j = row - (i - 1) * J + 1;
-    const int par = (color + i + j) & 1;
-    const size_t base = ((size_t)i * n + j) * n;
-    for (int kk = p_lane(); kk < nkk; kk += 32) {
-      const int k = 2 * kk + par;
+  const int J = g.J, n = g.n;
+  const unsigned nkk = (unsigned)(J / 2 + 1), tot = nkk * (unsigned)J * (unsigned)J, T = p_nthreads();
+  for (unsigned base = p_tid(); base < tot; base += PB * T) {
+    float val[PB];
+    size_t at[PB];
+    bool ok[PB];
+#pragma unroll
+    for (int u = 0; u < PB; ++u) {
+      const unsigned t = base + u * T;
+      ok[u] = false;
+      if (t >= tot) continue;
+      const unsigned kk = t % nkk, row = t / nkk;
+      const int j = (int)(row % (unsigned)J) + 1, i = (int)(row / (unsigned)J) + 1;
+      const int k = 2 * (int)kk + ((color + i + j) & 1);
       if (k < 1 || k > J) continue;
-      const size_t c = base + k;
+      const size_t c = ((size_t)i * n + j) * n + k;
       float sum, diag;
       if (first) {  // zero neighbours: the diagonal alone
         sum = 0.0f;
@@ -491,48 +520,82 @@ __device__ void p_smooth(float *__restrict__ e, const float *__restrict__ b, con
       } else {
         sw_stencil(e, c, i, j, k, g, sum, diag);
       }
-      e[c] = (sum - b[c]) / diag;
+      val[u] = gs_value(sum, b[c], diag);
+      at[u] = c;
+      ok[u] = true;
     }
+#pragma unroll
+    for (int u = 0; u < PB; ++u)
+      if (ok[u]) e[at[u]] = val[u];
   }
 }
 
 __device__ void p_zero(float *__restrict__ e, const LevelGeom &g) {
-  const long long tot = (long long)g.n * g.n * g.n;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x)
-    e[t] = 0.0f;
+  const size_t tot = (size_t)g.n * g.n * g.n;
+  for (size_t t = p_tid(); t < tot; t += p_nthreads()) e[t] = 0.0f;
 }
 
 __device__ void p_resid(const float *__restrict__ e, const float *__restrict__ b, float *__restrict__ r,
                         const LevelGeom &g) {
-  const int J = g.J, n = g.n, rows = J * J;
-  for (int row = p_warp(); row < rows; row += p_nwarps()) {
-    const int i = row / J + 1, j = row - (i - 1) * J + 1;
-    const size_t base = ((size_t)i * n + j) * n;
-    for (int k = p_lane() + 1; k <= J; k += 32) {
-      const size_t c = base + k;
+  const int J = g.J, n = g.n;
+  const unsigned tot = (unsigned)J * (unsigned)J * (unsigned)J, T = p_nthreads();
+  for (unsigned base = p_tid(); base < tot; base += PB * T) {
+    float val[PB];
+    size_t at[PB];
+#pragma unroll
+    for (int u = 0; u < PB; ++u) {
+      const unsigned t = base + u * T;
+      at[u] = (size_t)-1;
+      if (t >= tot) continue;
+      const int k = (int)(t % (unsigned)J) + 1;
+      const unsigned q = t / (unsigned)J;
+      const int j = (int)(q % (unsigned)J) + 1, i = (int)(q / (unsigned)J) + 1;
+      const size_t c = ((size_t)i * n + j) * n + k;
       float sum, diag;
       sw_stencil(e, c, i, j, k, g, sum, diag);
-      r[c] = b[c] - (sum - diag * e[c]);
+      val[u] = b[c] - (sum - diag * e[c]);
+      at[u] = c;
     }
+#pragma unroll
+    for (int u = 0; u < PB; ++u)
+      if (at[u] != (size_t)-1) r[at[u]] = val[u];
   }
 }
 
 __device__ void p_restrict(const float *__restrict__ rf, const LevelGeom &f, float *__restrict__ bc,
                            const LevelGeom &cg) {
-  const int J = cg.J, rows = J * J;
-  for (int row = p_warp(); row < rows; row += p_nwarps()) {
-    const int I = row / J + 1, Jj = row - (I - 1) * J + 1;
-    for (int K = p_lane() + 1; K <= J; K += 32) restrict_node(rf, f, bc, cg, I, Jj, K);
+  const int J = cg.J;
+  const unsigned tot = (unsigned)J * (unsigned)J * (unsigned)J;
+  for (unsigned t = p_tid(); t < tot; t += p_nthreads()) {
+    const int K = (int)(t % (unsigned)J) + 1;
+    const unsigned q = t / (unsigned)J;
+    const int Jj = (int)(q % (unsigned)J) + 1, I = (int)(q / (unsigned)J) + 1;
+    restrict_node(rf, f, bc, cg, I, Jj, K);
   }
 }
 
 __device__ void p_prolong(const float *__restrict__ ec, const LevelGeom &cg, float *__restrict__ ef,
                           const LevelGeom &f) {
-  const int J = f.J, n = f.n, rows = J * J;
-  for (int row = p_warp(); row < rows; row += p_nwarps()) {
-    const int i = row / J + 1, j = row - (i - 1) * J + 1;
-    const size_t base = ((size_t)i * n + j) * n;
-    for (int k = p_lane() + 1; k <= J; k += 32) ef[base + k] += prolong_value(ec, i, j, k, f, cg);
+  const int J = f.J, n = f.n;
+  const unsigned tot = (unsigned)J * (unsigned)J * (unsigned)J, T = p_nthreads();
+  for (unsigned base = p_tid(); base < tot; base += PB * T) {
+    float val[PB];
+    size_t at[PB];
+#pragma unroll
+    for (int u = 0; u < PB; ++u) {
+      const unsigned t = base + u * T;
+      at[u] = (size_t)-1;
+      if (t >= tot) continue;
+      const int k = (int)(t % (unsigned)J) + 1;
+      const unsigned q = t / (unsigned)J;
+      const int j = (int)(q % (unsigned)J) + 1, i = (int)(q / (unsigned)J) + 1;
+      const size_t c = ((size_t)i * n + j) * n + k;
+      val[u] = ef[c] + prolong_value(ec, i, j, k, f, cg);
+      at[u] = c;
+    }
+#pragma unroll
+    for (int u = 0; u < PB; ++u)
+      if (at[u] != (size_t)-1) ef[at[u]] = val[u];
   }
 }
 
@@ -616,14 +679,14 @@ __global__ void __launch_bounds__(256)
   const float *oth = e + (size_t)(color ^ 1) * d.half;
   const float rv = r[(size_t)color * d.half + s];
   const float sum = FIRST ? 0.0f : split_nbr_sum(oth, s, (size_t)d.G * d.H, d.H, p);
-  own[s] = (sum - rv) / 6.0f;
+  own[s] = __fmul_rn(sum - rv, GC_SIXTH);
 }
 
 // phi += e at natural node c: double-float add (or a plain f32 add).
 template <bool PLAIN>
 __device__ __forceinline__ void phi_add(float *__restrict__ hi, float *__restrict__ lo, size_t c, float ev) {
   if (PLAIN) {
-    hi[c] = hi[c] + ev;
+    hi[c] = __fadd_rn(hi[c], ev);
   } else {
     float s1, e1, h, l;
     df_two_sum(hi[c], ev, s1, e1);
@@ -652,7 +715,7 @@ __global__ void __launch_bounds__(256)
   const size_t row = ((size_t)i * d.G + j) * d.G;
   if (kb >= 1 && kb <= d.G - 2) {
     const float sum = split_nbr_sum(e, s, (size_t)d.G * d.H, d.H, pb);
-    const float eb = (sum - r[d.half + s]) / 6.0f;
+    const float eb = __fmul_rn(sum - r[d.half + s], GC_SIXTH);
     phi_add<PLAIN>(hi, lo, row + kb, eb);
   }
   if (kr >= 1 && kr <= d.G - 2) phi_add<PLAIN>(hi, lo, row + kr, e[s]);
@@ -705,7 +768,7 @@ __global__ void __launch_bounds__(256)
       const int col = (i + j + k) & 1;
       const size_t s = ((size_t)i * G + j) * d.H + (k >> 1);
       rout[(size_t)col * d.half + s] = rv;
-      if (e_first && col == 0) e_first[s] = (0.0f - rv) / 6.0f;
+      if (e_first && col == 0) e_first[s] = __fmul_rn(0.0f - rv, GC_SIXTH);
     } else {
       rout[c] = rv;
     }
@@ -749,6 +812,233 @@ __global__ void __launch_bounds__(256)
     if (k < 1 || k > d.G - 2) continue;
     e[(size_t)col * d.half + s] += prolong_value(ec, i, j, k, f, cg);
   }
+}
+
+// ---- the same finest-level kernels, vectorised (G % 4 == 0) --------------------
+// With G a multiple of 4 the split row length H = G/2 is even, so slot pairs
+// (2t, 2t+1) start on 8-byte boundaries, and natural rows of G nodes split into
+// 16-byte quads. Each thread then handles two slots of one colour (half-sweeps,
+// prolongation) or four consecutive nodes (residuals, update) with vector
+// loads; the arithmetic of every node is that of the scalar kernels above.
+__device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void st2(float *p, float a, float b) { *reinterpret_cast<float2 *>(p) = make_float2(a, b); }
+__device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+__device__ __forceinline__ float f4get(const float4 &v, int q) { return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w; }
+__device__ __forceinline__ void f4set(float4 &v, int q, float x) {
+  if (q == 0) v.x = x; else if (q == 1) v.y = x; else if (q == 2) v.z = x; else v.w = x;
+}
+
+// Half-sweep of colour `color`, slots 2t and 2t+1 of a row. Face slots (k = 0 or
+// G-1) are written back as zero, their value in the homogeneous correction.
+template <bool FIRST>
+__global__ void __launch_bounds__(256)
+    k_rb0x2(float *__restrict__ e, const float *__restrict__ r, Split0 d, int color) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  const int kk0 = 2 * t;
+  if (kk0 >= d.H || j > d.G - 2) return;
+  const int p = (color + i + j) & 1;
+  const int k0 = 2 * kk0 + p;  // the pair's nodes are k0 and k0 + 2
+  const size_t s = ((size_t)i * d.G + j) * d.H + kk0;
+  const float2 rv = ld2(r + (size_t)color * d.half + s);
+  float v0, v1;
+  if (FIRST) {
+    v0 = __fmul_rn(0.0f - rv.x, GC_SIXTH);
+    v1 = __fmul_rn(0.0f - rv.y, GC_SIXTH);
+  } else {
+    const float *o = e + (size_t)(color ^ 1) * d.half;
+    const size_t GH = (size_t)d.G * d.H;
+    const float2 xp = ld2(o + s + GH), xm = ld2(o + s - GH), yp = ld2(o + s + d.H), ym = ld2(o + s - d.H);
+    const float2 zc = ld2(o + s);
+    const float zo = p ? o[s + 2] : o[s - 1];
+    const float az0 = p ? zc.y + zc.x : zc.x + zo;  // (k+1) + (k-1) of node k0
+    const float az1 = p ? zo + zc.y : zc.y + zc.x;  // ... of node k0 + 2
+    const float sum0 = ((xp.x + xm.x) + (yp.x + ym.x)) + az0;
+    const float sum1 = ((xp.y + xm.y) + (yp.y + ym.y)) + az1;
+    v0 = __fmul_rn(sum0 - rv.x, GC_SIXTH);
+    v1 = __fmul_rn(sum1 - rv.y, GC_SIXTH);
+  }
+  if (k0 < 1) v0 = 0.0f;
+  if (k0 + 2 > d.G - 2) v1 = 0.0f;
+  st2(e + (size_t)color * d.half + s, v0, v1);
+}
+
+// Last (black) half-sweep fused with phi += e on four consecutive nodes
+// 4t .. 4t+3 of a row: the black slots 2t, 2t+1 and the red ones beside them.
+template <bool PLAIN>
+__global__ void __launch_bounds__(256)
+    k_rb0_lastx4(const float *__restrict__ e, const float *__restrict__ r, float *__restrict__ hi,
+                 float *__restrict__ lo, Split0 d) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  const int kk0 = 2 * t;
+  if (kk0 >= d.H || j > d.G - 2) return;
+  const int pb = (1 + i + j) & 1;  // k parity of the black nodes of the row
+  const size_t s = ((size_t)i * d.G + j) * d.H + kk0;
+  const size_t GH = (size_t)d.G * d.H;
+  const float *o = e;  // red half: the neighbours of the black nodes, and the red corrections
+  const float2 xp = ld2(o + s + GH), xm = ld2(o + s - GH), yp = ld2(o + s + d.H), ym = ld2(o + s - d.H);
+  const float2 zc = ld2(o + s);
+  const float zo = pb ? o[s + 2] : o[s - 1];
+  const float az0 = pb ? zc.y + zc.x : zc.x + zo;
+  const float az1 = pb ? zo + zc.y : zc.y + zc.x;
+  const float2 rb = ld2(r + d.half + s);
+  const float eb0 = __fmul_rn((((xp.x + xm.x) + (yp.x + ym.x)) + az0) - rb.x, GC_SIXTH);
+  const float eb1 = __fmul_rn((((xp.y + xm.y) + (yp.y + ym.y)) + az1) - rb.y, GC_SIXTH);
+  const size_t c0 = ((size_t)i * d.G + j) * d.G + 2 * kk0;
+  float4 h = ld4(hi + c0);
+  float4 l = PLAIN ? make_float4(0.f, 0.f, 0.f, 0.f) : ld4(lo + c0);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int k = 2 * kk0 + q;
+    if (k < 1 || k > d.G - 2) continue;
+    const bool black = (q & 1) == pb;
+    const float ev = black ? (q < 2 ? eb0 : eb1) : (q < 2 ? zc.x : zc.y);
+    if (PLAIN) {
+      f4set(h, q, __fadd_rn(f4get(h, q), ev));
+    } else {
+      float s1, e1, hh, llo;
+      df_two_sum(f4get(h, q), ev, s1, e1);
+      const float ln = __fadd_rn(f4get(l, q), e1);
+      df_fast_two_sum(s1, ln, hh, llo);
+      f4set(h, q, hh);
+      f4set(l, q, llo);
+    }
+  }
+  st4(hi + c0, h);
+  if (!PLAIN) st4(lo + c0, l);
+}
+
+// Residual of the potential on four consecutive nodes 4t .. 4t+3 (see k_resid0).
+template <bool PLAIN>
+__global__ void __launch_bounds__(256)
+    k_resid0x4(const float *__restrict__ hi, const float *__restrict__ lo, const float *__restrict__ b,
+               float *__restrict__ rout, float *__restrict__ e_first, double *__restrict__ parts, Split0 d) {
+  const int G = d.G;
+  const int t = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  float acc = 0.0f;
+  if (4 * t < G && j <= G - 2) {
+    const size_t sj = (size_t)G, si = (size_t)G * G;
+    const size_t c0 = (size_t)i * si + (size_t)j * sj + 4 * t;
+    const float4 hc = ld4(hi + c0), hxp = ld4(hi + c0 + si), hxm = ld4(hi + c0 - si), hyp = ld4(hi + c0 + sj),
+                 hym = ld4(hi + c0 - sj);
+    const float hzm = hi[c0 - 1], hzp = hi[c0 + 4];
+    float4 lc = make_float4(0.f, 0.f, 0.f, 0.f), lxp = lc, lxm = lc, lyp = lc, lym = lc;
+    float lzm = 0.f, lzp = 0.f;
+    if (!PLAIN) {
+      lc = ld4(lo + c0); lxp = ld4(lo + c0 + si); lxm = ld4(lo + c0 - si); lyp = ld4(lo + c0 + sj);
+      lym = ld4(lo + c0 - sj);
+      lzm = lo[c0 - 1]; lzp = lo[c0 + 4];
+    }
+    const float4 bv = ld4(b + c0);
+    float rv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float hk = f4get(hc, q);
+      const float hkp = q < 3 ? f4get(hc, q + 1) : hzp, hkm = q > 0 ? f4get(hc, q - 1) : hzm;
+      if (PLAIN) {
+        const float s6 = ((((f4get(hxp, q) + f4get(hxm, q)) + f4get(hyp, q)) + f4get(hym, q)) + hkp) + hkm;
+        rv[q] = f4get(bv, q) - (s6 - 6.0f * hk);
+      } else {
+        const float lkp = q < 3 ? f4get(lc, q + 1) : lzp, lkm = q > 0 ? f4get(lc, q - 1) : lzm;
+        const float h6[6] = {f4get(hxp, q), f4get(hxm, q), f4get(hyp, q), f4get(hym, q), hkp, hkm};
+        const float l6[6] = {f4get(lxp, q), f4get(lxm, q), f4get(lyp, q), f4get(lym, q), lkp, lkm};
+        rv[q] = df_residual_v(hk, f4get(lc, q), h6, l6, f4get(bv, q));
+      }
+      const int k = 4 * t + q;
+      if (k < 1 || k > G - 2) rv[q] = 0.0f;  // faces: no residual, zero correction
+    }
+    // nodes 4t, 4t+2 share a colour (slots 2t, 2t+1), as do 4t+1, 4t+3
+    const int c0col = (i + j) & 1;  // colour of node 4t
+    const size_t sl = ((size_t)i * G + j) * d.H + 2 * t;
+    st2(rout + (size_t)c0col * d.half + sl, rv[0], rv[2]);
+    st2(rout + (size_t)(c0col ^ 1) * d.half + sl, rv[1], rv[3]);
+    if (e_first) {  // red = colour 0
+      if (c0col == 0) st2(e_first + sl, __fmul_rn(0.0f - rv[0], GC_SIXTH), __fmul_rn(0.0f - rv[2], GC_SIXTH));
+      else st2(e_first + sl, __fmul_rn(0.0f - rv[1], GC_SIXTH), __fmul_rn(0.0f - rv[3], GC_SIXTH));
+    }
+    acc = ((rv[0] * rv[0] + rv[1] * rv[1]) + rv[2] * rv[2]) + rv[3] * rv[3];
+  }
+  const size_t bid = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+  block_sum_f32(acc, parts + bid);
+}
+
+// Residual of the correction equation on four consecutive nodes, natural output.
+__global__ void __launch_bounds__(256)
+    k_resid0ex4(const float *__restrict__ e, const float *__restrict__ r, float *__restrict__ rc, Split0 d) {
+  const int G = d.G;
+  const int t = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  if (4 * t >= G || j > G - 2) return;
+  const int ca = (i + j) & 1;  // colour of nodes 4t, 4t+2 (half A); 4t+1, 4t+3 are half B
+  const size_t s0 = ((size_t)i * G + j) * d.H + 2 * t;
+  const size_t GH = (size_t)G * d.H;
+  const float *A = e + (size_t)ca * d.half, *B = e + (size_t)(ca ^ 1) * d.half;
+  const float2 a0 = ld2(A + s0), axp = ld2(A + s0 + GH), axm = ld2(A + s0 - GH), ayp = ld2(A + s0 + d.H),
+               aym = ld2(A + s0 - d.H);
+  const float a2 = A[s0 + 2];
+  const float2 b0 = ld2(B + s0), bxp = ld2(B + s0 + GH), bxm = ld2(B + s0 - GH), byp = ld2(B + s0 + d.H),
+               bym = ld2(B + s0 - d.H);
+  const float bm = B[s0 - 1];
+  const float2 ra = ld2(r + (size_t)ca * d.half + s0), rb = ld2(r + (size_t)(ca ^ 1) * d.half + s0);
+  // node q: own value, other-colour sums (i, j, k) in split_nbr_sum's order
+  const float sum0 = ((bxp.x + bxm.x) + (byp.x + bym.x)) + (b0.x + bm);
+  const float sum1 = ((axp.x + axm.x) + (ayp.x + aym.x)) + (a0.y + a0.x);
+  const float sum2 = ((bxp.y + bxm.y) + (byp.y + bym.y)) + (b0.y + b0.x);
+  const float sum3 = ((axp.y + axm.y) + (ayp.y + aym.y)) + (a2 + a0.y);
+  const float diag = 6.0f;
+  float4 out;
+  out.x = ra.x - (sum0 - diag * a0.x);
+  out.y = rb.x - (sum1 - diag * b0.x);
+  out.z = ra.y - (sum2 - diag * a0.y);
+  out.w = rb.y - (sum3 - diag * b0.y);
+  if (4 * t == 0) out.x = 0.0f;           // face k = 0
+  if (4 * t + 3 == G - 1) out.w = 0.0f;  // face k = G-1
+  st4(rc + ((size_t)i * G + j) * G + 4 * t, out);
+}
+
+// Level-1 correction into the black half, slots 2t and 2t+1 of a row (the two
+// nodes share their i and j weights).
+__global__ void __launch_bounds__(256)
+    k_prolong0bx2(const float *__restrict__ ec, LevelGeom cg, float *__restrict__ e, LevelGeom f, Split0 d) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int i = blockIdx.z + 1;
+  const int kk0 = 2 * t;
+  if (kk0 >= d.H || j > d.G - 2) return;
+  const int pb = (1 + i + j) & 1;
+  const int k0 = 2 * kk0 + pb, k1 = k0 + 2;
+  int ci, cj, ck0, ck1;
+  float wi0, wi1, wj0, wj1, a0, a1, b0, b1;
+  const int ni = prolong_w(i, f, cg, ci, wi0, wi1);
+  const int nj = prolong_w(j, f, cg, cj, wj0, wj1);
+  const int nk0 = prolong_w(k0, f, cg, ck0, a0, a1);
+  const int nk1 = prolong_w(k1, f, cg, ck1, b0, b1);
+  const size_t m = cg.n;
+  float v0 = 0.0f, v1 = 0.0f;
+  for (int a = 0; a < ni; ++a) {
+    const float wa = a ? wi1 : wi0;
+    for (int bb = 0; bb < nj; ++bb) {
+      const float wb = bb ? wj1 : wj0;
+      const size_t row = ((size_t)(ci + a) * m + (cj + bb)) * m;
+      const float wab = wa * wb;
+      v0 += wab * a0 * ec[row + ck0];
+      if (nk0 == 2) v0 += wab * a1 * ec[row + ck0 + 1];
+      v1 += wab * b0 * ec[row + ck1];
+      if (nk1 == 2) v1 += wab * b1 * ec[row + ck1 + 1];
+    }
+  }
+  if (k0 < 1) v0 = 0.0f;
+  if (k1 > d.G - 2) v1 = 0.0f;
+  float *blk = e + d.half + ((size_t)i * d.G + j) * d.H + kk0;
+  const float2 old = ld2(blk);
+  st2(blk, old.x + v0, old.y + v1);
 }
 
 // ------------------------------------------------------------------------------
@@ -1064,7 +1354,14 @@ __global__ void k_mg_decide(cudaGraphConditionalHandle h, double *__restrict__ s
   const int minc = min_c > 1 ? min_c : 1;
   const bool conv = c >= minc && b2 > 0.0 && sqrt(r2) < tol * sqrt(b2);
   small[GC_S_CONVERGED] = conv ? 1.0 : 0.0;
-  cudaGraphSetConditional(h, (!conv && c < max_c) ? 1u : 0u);
+  const bool more = !conv && c < max_c;
+  if (!more) {  // the solve ends here: count it
+    small[GC_S_SOLVES] += 1.0;
+    small[GC_S_CYC_TOTAL] += (double)c;
+    const double rel2 = b2 > 0.0 ? r2 / b2 : 0.0;
+    if (rel2 > small[GC_S_MAXREL2]) small[GC_S_MAXREL2] = rel2;
+  }
+  cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
 // ------------------------------------------------------------------------------
@@ -1120,6 +1417,15 @@ static dim3 split_grid(const gc_ctx *ctx) {
   return dim3(gc_blocks(ctx->H0, 64), gc_blocks(ctx->G - 2, 4), (unsigned)(ctx->G - 2));
 }
 #define SPLIT_BLOCK dim3(64, 4)
+// slot pairs (vectorised kernels, G % 4 == 0)
+static dim3 split_grid2(const gc_ctx *ctx) {
+  return dim3(gc_blocks(ctx->H0 / 2, 64), gc_blocks(ctx->G - 2, 4), (unsigned)(ctx->G - 2));
+}
+// node quads of the interior rows (vectorised kernels, G % 4 == 0)
+static dim3 quad_grid(const gc_ctx *ctx) {
+  return dim3(gc_blocks(ctx->G / 4, 32), gc_blocks(ctx->G - 2, 8), (unsigned)(ctx->G - 2));
+}
+static bool vec4(const gc_ctx *ctx) { return ctx->G % 4 == 0; }
 
 // CTAs of the persistent coarse launches: as many as fit at once (a cooperative
 // launch needs them all resident), at most two per SM (fewer arrivals per grid
@@ -1136,9 +1442,9 @@ static int coarse_grid(gc_ctx *ctx) {
     return GC_ERR_CUDA;
   }
   const LevelGeom &g1 = ctx->lev[1];
-  const long long rows = (long long)g1.J * g1.J;  // one warp per row at the finest coarse level
+  const long long nodes = (long long)g1.J * g1.J * g1.J;  // the largest phase: level 1's residual
   long long nb = (long long)gc_sms() * per_sm;
-  const long long need = (rows + COARSE_THREADS / 32 - 1) / (COARSE_THREADS / 32);
+  const long long need = (nodes + (long long)PB * COARSE_THREADS - 1) / ((long long)PB * COARSE_THREADS);
   if (nb > need) nb = need;
   ctx->coarse_blocks = (int)(nb < 1 ? 1 : nb);
   return GC_OK;
@@ -1224,6 +1530,20 @@ static int residual0(gc_ctx *ctx, const gc_mg_params *p) {
     else
       gc_launch(ctx, GK_RESID0, k_resid0<false, false>, grid, dim3(32, 8), 0, ctx->hi, ctx->lo, ctx->b0, ctx->r0n,
                 nullptr, ctx->red, d);
+  } else if (vec4(ctx)) {
+    const int pre = ctx->nlev == 1 ? p->coarse_sweeps : p->pre_sweeps;
+    float *ef = pre >= 1 ? ctx->e0s : nullptr;
+    const dim3 qg = quad_grid(ctx);
+    const size_t nq = (size_t)qg.x * qg.y * qg.z;
+    if ((st = gc_ensure_red(ctx, nq))) return st;
+    if (plain)
+      gc_launch(ctx, GK_RESID0, k_resid0x4<true>, qg, dim3(32, 8), 0, ctx->hi, ctx->lo, ctx->b0, ctx->r0s, ef,
+                ctx->red, d);
+    else
+      gc_launch(ctx, GK_RESID0, k_resid0x4<false>, qg, dim3(32, 8), 0, ctx->hi, ctx->lo, ctx->b0, ctx->r0s, ef,
+                ctx->red, d);
+    GC_LAUNCH_CHECK(ctx, "resid0");
+    return finalize_to(ctx, (int)nq, 1, GC_S_RNORM2);
   } else {
     const int pre = ctx->nlev == 1 ? p->coarse_sweeps : p->pre_sweeps;
     float *ef = pre >= 1 ? ctx->e0s : nullptr;
@@ -1276,24 +1596,44 @@ static int vcycle(gc_ctx *ctx, const gc_mg_params *p) {
     GC_LAUNCH_CHECK(ctx, "natural cycle");
     return residual0(ctx, p);
   }
-  const dim3 sg = split_grid(ctx);
+  const dim3 sg = split_grid(ctx), sg2 = split_grid2(ctx), qg = quad_grid(ctx);
+  const bool v4 = vec4(ctx);
+  auto half_sweep = [&](int color) {
+    if (v4)
+      gc_launch(ctx, GK_SMOOTH0, k_rb0x2<false>, sg2, SPLIT_BLOCK, 0, ctx->e0s, (const float *)ctx->r0s, d, color);
+    else
+      gc_launch(ctx, GK_SMOOTH0, k_rb0<false>, sg, SPLIT_BLOCK, 0, ctx->e0s, (const float *)ctx->r0s, d, color);
+  };
   if (pre == 0) GC_CUDA(ctx, cudaMemsetAsync(ctx->e0s, 0, 2 * ctx->half0 * sizeof(float), ctx->stream));
   // half-sweep 0 (red, from zero) came with the residual
-  for (int h = 1; h < 2 * pre; ++h)
-    gc_launch(ctx, GK_SMOOTH0, k_rb0<false>, sg, SPLIT_BLOCK, 0, ctx->e0s, (const float *)ctx->r0s, d, h & 1);
+  for (int h = 1; h < 2 * pre; ++h) half_sweep(h & 1);
   if (L > 1) {
-    gc_launch(ctx, GK_RESIDE, k_resid0e, node_grid(g0), dim3(32, 8), 0, (const float *)ctx->e0s,
-              (const float *)ctx->r0s, ctx->r0, d);
+    if (v4)
+      gc_launch(ctx, GK_RESIDE, k_resid0ex4, qg, dim3(32, 8), 0, (const float *)ctx->e0s, (const float *)ctx->r0s,
+                ctx->r0, d);
+    else
+      gc_launch(ctx, GK_RESIDE, k_resid0e, node_grid(g0), dim3(32, 8), 0, (const float *)ctx->e0s,
+                (const float *)ctx->r0s, ctx->r0, d);
     gc_launch(ctx, GK_RESTRICT, k_restrict, node_grid(ctx->lev[1]), dim3(32, 8), 0, ctx->r0, g0, ctx->b[1],
               ctx->lev[1]);
     GC_LAUNCH_CHECK(ctx, "resid0e/restrict");
     if ((st = coarse_levels(ctx, p))) return st;
-    gc_launch(ctx, GK_PROLONG0, k_prolong0s, sg, SPLIT_BLOCK, 0, (const float *)ctx->e[1], ctx->lev[1], ctx->e0s, g0,
-              d, post == 0 ? 1 : 0);
-    for (int h = 0; h < 2 * post - 1; ++h)
-      gc_launch(ctx, GK_SMOOTH0, k_rb0<false>, sg, SPLIT_BLOCK, 0, ctx->e0s, (const float *)ctx->r0s, d, h & 1);
+    if (v4 && post >= 1)
+      gc_launch(ctx, GK_PROLONG0, k_prolong0bx2, sg2, SPLIT_BLOCK, 0, (const float *)ctx->e[1], ctx->lev[1], ctx->e0s,
+                g0, d);
+    else
+      gc_launch(ctx, GK_PROLONG0, k_prolong0s, sg, SPLIT_BLOCK, 0, (const float *)ctx->e[1], ctx->lev[1], ctx->e0s,
+                g0, d, post == 0 ? 1 : 0);
+    for (int h = 0; h < 2 * post - 1; ++h) half_sweep(h & 1);
   }
-  if (post >= 1) {  // last half-sweep (black) and phi += e in one pass
+  if (post >= 1 && v4) {  // last half-sweep (black) and phi += e in one pass
+    if (plain)
+      gc_launch(ctx, GK_UPDATE0, k_rb0_lastx4<true>, sg2, SPLIT_BLOCK, 0, (const float *)ctx->e0s,
+                (const float *)ctx->r0s, ctx->hi, ctx->lo, d);
+    else
+      gc_launch(ctx, GK_UPDATE0, k_rb0_lastx4<false>, sg2, SPLIT_BLOCK, 0, (const float *)ctx->e0s,
+                (const float *)ctx->r0s, ctx->hi, ctx->lo, d);
+  } else if (post >= 1) {  // last half-sweep (black) and phi += e in one pass
     if (plain)
       gc_launch(ctx, GK_UPDATE0, k_rb0_last<true>, sg, SPLIT_BLOCK, 0, (const float *)ctx->e0s,
                 (const float *)ctx->r0s, ctx->hi, ctx->lo, d);

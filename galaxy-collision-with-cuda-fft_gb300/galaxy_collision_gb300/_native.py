@@ -183,6 +183,7 @@ _PROTOS = {
     "gc_pm_graph_destroy": (C.c_int, [_vp]),
     "gc_pm_graph_info": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "gc_pm_graph_stats": (C.c_int, [_ctxp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "gc_pm_solve_counters": (C.c_int, [_ctxp, C.POINTER(C.c_double), C.c_int]),
     "gc_pm_set_warmstart": (C.c_int, [_ctxp, _vp, C.c_int, C.c_int]),
     "gc_pm_record_sample": (C.c_int, [_ctxp, _vp]),
 }

@@ -402,10 +402,34 @@ class PMEngine:
         self.steps_since_sort += 1
         self.last_graph = g
 
+    def prepare_graphs(self, dt: float) -> None:
+        """Capture the step graphs of both particle-buffer sets now (a capture
+        runs no kernels), so that later advance_graph calls only replay. The
+        engine must be open and have stepped (see advance_graph)."""
+        if self.state != "open":
+            raise RuntimeError("prepare_graphs needs an open (primed) engine")
+        main = torch.cuda.current_stream()
+        gs = self._graph_stream()
+        gs.wait_stream(main)
+        with torch.cuda.stream(gs):
+            for f in (self.cur, self.alt):
+                key = (f["x"].data_ptr(), float(dt))
+                if key not in self._graphs:
+                    self._graphs[key] = _native.StepGraph(self.ctx, self._struct(f),
+                                                          self._step_params(_native.GC_STEP_ADVANCE, dt, False))
+        main.wait_stream(gs)
+
     def _graph_stream(self):
         if getattr(self, "_gstream", None) is None:
             self._gstream = torch.cuda.Stream()
         return self._gstream
+
+    def solve_counters(self, reset: bool = True) -> dict:
+        """Totals of the device-decided (graph-replayed) solves since the last
+        reset: solves, V-cycles and the largest relative residual (synchronises)."""
+        out = (C.c_double * 3)()
+        self.ctx.call("gc_pm_solve_counters", out, int(bool(reset)), what="solve_counters")
+        return {"solves": int(out[0]), "cycles": int(out[1]), "max_rel_residual": float(out[2])}
 
     def graph_stats(self) -> StepResult:
         """V-cycles, convergence and relative residual of the last graph-replayed

@@ -435,6 +435,10 @@ int gc_pm_graph_info(const gc_graph *g, long long *fixed_launches, long long *bo
 /* V-cycles, converged flag and relative residual of the last replayed solve,
  * from the pinned mirror the graph writes: synchronise the stream first. */
 int gc_pm_graph_stats(const gc_ctx *ctx, int *cycles, int *converged, double *rel);
+/* Totals of the solves decided on the device since the last reset: out[0]
+ * solves, out[1] V-cycles, out[2] the largest relative residual they ended with.
+ * Synchronises; reset != 0 clears the totals afterwards. */
+int gc_pm_solve_counters(gc_ctx *ctx, double out[3], int reset);
 
 /* ---- instrumentation (no kernel counterpart in the reference: it replaces the
  * sync-bracketed per-stage wall clock of bench.py:66-73, 176-186) ---------- */
