@@ -421,10 +421,10 @@ __global__ void __launch_bounds__(256)
 // bit. The first half-sweep of a level starts from a zero correction and reads
 // no neighbour, so the level needs no clearing.
 struct GridBar {
-  unsigned count;  // arrivals at the current barrier
-  unsigned gen;    // barriers completed
+  unsigned count;  // arrivals since the start of the solve (grows by the grid size per barrier)
+  unsigned pad0;
   unsigned abort;  // set by a CTA that gave up waiting
-  unsigned pad;
+  unsigned pad1;
 };
 
 struct CoarseDesc {
@@ -445,37 +445,37 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
   return v;
 }
 
-// Grid-wide barrier of a cooperative launch. Thread 0 of each CTA reads the
-// generation, arrives, and the last arrival resets the count and advances the
-// generation; the others wait for it for at most `budget` clocks. A CTA that
-// gives up raises GC_FLAG_TIMEOUT and the abort word (so the others stop
-// waiting too) and the kernel returns; the barrier word is reset before every
-// solve.
-__device__ __forceinline__ bool grid_barrier(GridBar *gb, unsigned *status, long long budget) {
+// Grid-wide barrier of a cooperative launch on a monotonic arrival count: thread
+// 0 of each CTA adds one arrival (a release reduction, no return value) and
+// waits with acquire loads until the count reaches its target, a multiple of
+// the grid size. The count is cleared before every solve and only grows within
+// it; a launch starts from the count rounded down to a multiple of the grid
+// size (every barrier of earlier launches has completed, and a CTA that reads
+// it late can see at most the other CTAs' first arrivals). The wait is bounded
+// by `budget` clocks: a CTA that gives up raises GC_FLAG_TIMEOUT and the abort
+// word (so the others stop waiting too) and the kernel returns.
+__device__ __forceinline__ unsigned grid_barrier_base(GridBar *gb) {
+  return (ld_acquire_u32(&gb->count) / gridDim.x) * gridDim.x;
+}
+
+__device__ __forceinline__ bool grid_barrier(GridBar *gb, unsigned &target, unsigned *status, long long budget) {
   __shared__ int ok_s;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned gen = ld_acquire_u32(&gb->gen);
+    target += gridDim.x;
     __threadfence();
-    const unsigned arrived = atomicAdd(&gb->count, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(&gb->count, 0u);
-      __threadfence();
-      atomicAdd(&gb->gen, 1u);
-    } else {
-      const long long t0 = clock64();
-      while (ld_acquire_u32(&gb->gen) == gen) {
-        if (ld_acquire_u32(&gb->abort) || clock64() - t0 > budget) {
-          ok = 0;
-          atomicOr(status, GC_FLAG_TIMEOUT);
-          atomicExch(&gb->abort, 1u);
-          break;
-        }
-        __nanosleep(20);
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(&gb->count), "r"(1u) : "memory");
+    const long long t0 = clock64();
+    unsigned spins = 0;
+    while ((int)(ld_acquire_u32(&gb->count) - target) < 0) {
+      if ((++spins & 63u) == 0 && (ld_acquire_u32(&gb->abort) || clock64() - t0 > budget)) {
+        ok = 0;
+        atomicOr(status, GC_FLAG_TIMEOUT);
+        atomicExch(&gb->abort, 1u);
+        break;
       }
     }
-    __threadfence();
     ok_s = ok;
   }
   __syncthreads();
@@ -603,33 +603,35 @@ __device__ void p_prolong(const float *__restrict__ ec, const LevelGeom &cg, flo
 
 // Down: for each level, pre-smoothing, residual, restriction into b[l+1].
 __global__ void __launch_bounds__(COARSE_THREADS) k_coarse_down(CoarseDesc d) {
+  unsigned tgt = threadIdx.x == 0 ? grid_barrier_base(d.bar) : 0u;
   for (int l = d.l0; l < d.l1; ++l) {
     const LevelGeom &g = d.g[l];
     if (d.pre == 0) {
       p_zero(d.e[l], g);
-      if (!grid_barrier(d.bar, d.status, d.budget)) return;
+      if (!grid_barrier(d.bar, tgt, d.status, d.budget)) return;
     }
     for (int h = 0; h < 2 * d.pre; ++h) {
       p_smooth(d.e[l], d.b[l], g, h & 1, h == 0);
-      if (!grid_barrier(d.bar, d.status, d.budget)) return;
+      if (!grid_barrier(d.bar, tgt, d.status, d.budget)) return;
     }
     p_resid(d.e[l], d.b[l], d.rc, g);
-    if (!grid_barrier(d.bar, d.status, d.budget)) return;
+    if (!grid_barrier(d.bar, tgt, d.status, d.budget)) return;
     p_restrict(d.rc, g, d.b[l + 1], d.g[l + 1]);
-    if (l + 1 < d.l1 && !grid_barrier(d.bar, d.status, d.budget)) return;
+    if (l + 1 < d.l1 && !grid_barrier(d.bar, tgt, d.status, d.budget)) return;
   }
 }
 
 // Up: for each level from l1-1 down to l0, prolongation of e[l+1], post-smoothing.
 __global__ void __launch_bounds__(COARSE_THREADS) k_coarse_up(CoarseDesc d) {
+  unsigned tgt = threadIdx.x == 0 ? grid_barrier_base(d.bar) : 0u;
   for (int l = d.l1 - 1; l >= d.l0; --l) {
     const LevelGeom &g = d.g[l];
     p_prolong(d.e[l + 1], d.g[l + 1], d.e[l], g);
     for (int h = 0; h < 2 * d.post; ++h) {
-      if (!grid_barrier(d.bar, d.status, d.budget)) return;
+      if (!grid_barrier(d.bar, tgt, d.status, d.budget)) return;
       p_smooth(d.e[l], d.b[l], g, h & 1, false);
     }
-    if (l > d.l0 && !grid_barrier(d.bar, d.status, d.budget)) return;
+    if (l > d.l0 && !grid_barrier(d.bar, tgt, d.status, d.budget)) return;
   }
 }
 
@@ -1056,21 +1058,29 @@ __device__ void t_zero(T *a, int n3) {
   for (int i = threadIdx.x; i < n3; i += blockDim.x) a[i] = (T)0;
 }
 
+// Tail levels have J <= 15 (n <= GC_TAIL_MAX_N = 17), and the tail runs with
+// 1024 threads, so node indices come from the thread index by shifts: for a
+// half-sweep thread (kk, j, i0) = (t & 7, (t >> 3) & 15, t >> 7) takes the
+// colour slots k = 2 kk + parity of row (i, j) for i = i0 + 1, i0 + 9; for the
+// other phases (k, j, i0) = (t & 15, (t >> 4) & 15, t >> 8) takes i = i0 + 1,
+// i0 + 5, ...
 template <typename T>
 __device__ void t_smooth(T *e, const T *b, const LevelGeom &g, int sweeps) {
   const int n = g.n, J = g.J;
-  const int m = J * J * J;
+  const int kk = threadIdx.x & 7, j = ((threadIdx.x >> 3) & 15) + 1, i0 = (threadIdx.x >> 7) + 1;
   for (int s = 0; s < sweeps; ++s) {
     for (int color = 0; color < 2; ++color) {
-      for (int t = threadIdx.x; t < m; t += blockDim.x) {
-        const int k = t % J + 1, j = (t / J) % J + 1, i = t / (J * J) + 1;
-        if (((i + j + k) & 1) != color) continue;
-        const int c = (i * n + j) * n + k;
-        T sx, sy, sz, dx_, dy_, dz_;
-        if (i == J) { sx = (T)g.a * e[c - n * n]; dx_ = (T)g.dB; } else { sx = e[c + n * n] + e[c - n * n]; dx_ = 2; }
-        if (j == J) { sy = (T)g.a * e[c - n]; dy_ = (T)g.dB; } else { sy = e[c + n] + e[c - n]; dy_ = 2; }
-        if (k == J) { sz = (T)g.a * e[c - 1]; dz_ = (T)g.dB; } else { sz = e[c + 1] + e[c - 1]; dz_ = 2; }
-        e[c] = ((sx + sy + sz) - b[c]) / (dx_ + dy_ + dz_);
+      if (j <= J) {
+        for (int i = i0; i <= J; i += 8) {
+          const int k = 2 * kk + ((color + i + j) & 1);
+          if (k < 1 || k > J) continue;
+          const int c = (i * n + j) * n + k;
+          T sx, sy, sz, dx_, dy_, dz_;
+          if (i == J) { sx = (T)g.a * e[c - n * n]; dx_ = (T)g.dB; } else { sx = e[c + n * n] + e[c - n * n]; dx_ = 2; }
+          if (j == J) { sy = (T)g.a * e[c - n]; dy_ = (T)g.dB; } else { sy = e[c + n] + e[c - n]; dy_ = 2; }
+          if (k == J) { sz = (T)g.a * e[c - 1]; dz_ = (T)g.dB; } else { sz = e[c + 1] + e[c - 1]; dz_ = 2; }
+          e[c] = ((sx + sy + sz) - b[c]) / (dx_ + dy_ + dz_);
+        }
       }
       __syncthreads();
     }
@@ -1079,13 +1089,14 @@ __device__ void t_smooth(T *e, const T *b, const LevelGeom &g, int sweeps) {
 
 __device__ void t_resid(const float *e, const float *b, float *r, const LevelGeom &g) {
   const int n = g.n, J = g.J;
-  const int m = J * J * J;
-  for (int t = threadIdx.x; t < m; t += blockDim.x) {
-    const int k = t % J + 1, j = (t / J) % J + 1, i = t / (J * J) + 1;
-    const int c = (i * n + j) * n + k;
-    float sum, diag;
-    sw_stencil(e, (size_t)c, i, j, k, g, sum, diag);
-    r[c] = b[c] - (sum - diag * e[c]);
+  const int k = (threadIdx.x & 15) + 1, j = ((threadIdx.x >> 4) & 15) + 1;
+  if (k <= J && j <= J) {
+    for (int i = (threadIdx.x >> 8) + 1; i <= J; i += 4) {
+      const int c = (i * n + j) * n + k;
+      float sum, diag;
+      sw_stencil(e, (size_t)c, i, j, k, g, sum, diag);
+      r[c] = b[c] - (sum - diag * e[c]);
+    }
   }
   __syncthreads();
 }
@@ -1093,24 +1104,25 @@ __device__ void t_resid(const float *e, const float *b, float *r, const LevelGeo
 template <typename T>
 __device__ void t_restrict(const float *rf, const LevelGeom &f, T *bc, const LevelGeom &cg) {
   const int J = cg.J, m = cg.n, n = f.n;
-  const int tot = J * J * J;
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int K = t % J + 1, Jj = (t / J) % J + 1, I = t / (J * J) + 1;
-    float acc = 0.0f;
-    for (int a = -1; a <= 1; ++a) {
-      const float wa = restrict_w(I, a, f, cg);
-      if (wa == 0.0f) continue;
-      for (int bb = -1; bb <= 1; ++bb) {
-        const float wb = restrict_w(Jj, bb, f, cg);
-        if (wb == 0.0f) continue;
-        for (int c = -1; c <= 1; ++c) {
-          const float wc = restrict_w(K, c, f, cg);
-          if (wc == 0.0f) continue;
-          acc += wa * wb * wc * rf[((2 * I + a) * n + (2 * Jj + bb)) * n + (2 * K + c)];
+  const int K = (threadIdx.x & 15) + 1, Jj = ((threadIdx.x >> 4) & 15) + 1;
+  if (K <= J && Jj <= J) {
+    for (int I = (threadIdx.x >> 8) + 1; I <= J; I += 4) {
+      float acc = 0.0f;
+      for (int a = -1; a <= 1; ++a) {
+        const float wa = restrict_w(I, a, f, cg);
+        if (wa == 0.0f) continue;
+        for (int bb = -1; bb <= 1; ++bb) {
+          const float wb = restrict_w(Jj, bb, f, cg);
+          if (wb == 0.0f) continue;
+          for (int c = -1; c <= 1; ++c) {
+            const float wc = restrict_w(K, c, f, cg);
+            if (wc == 0.0f) continue;
+            acc += wa * wb * wc * rf[((2 * I + a) * n + (2 * Jj + bb)) * n + (2 * K + c)];
+          }
         }
       }
+      bc[(I * m + Jj) * m + K] = (T)(4.0f * acc);
     }
-    bc[(I * m + Jj) * m + K] = (T)(4.0f * acc);
   }
   __syncthreads();
 }
@@ -1118,22 +1130,23 @@ __device__ void t_restrict(const float *rf, const LevelGeom &f, T *bc, const Lev
 template <typename T>
 __device__ void t_prolong(const T *ec, const LevelGeom &cg, float *ef, const LevelGeom &f) {
   const int J = f.J, n = f.n, m = cg.n;
-  const int tot = J * J * J;
-  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-    const int k = t % J + 1, j = (t / J) % J + 1, i = t / (J * J) + 1;
-    int ci, cj, ck;
-    float wi0, wi1, wj0, wj1, wk0, wk1;
-    const int ni = prolong_w(i, f, cg, ci, wi0, wi1);
-    const int nj = prolong_w(j, f, cg, cj, wj0, wj1);
-    const int nk = prolong_w(k, f, cg, ck, wk0, wk1);
-    float val = 0.0f;
-    for (int a = 0; a < ni; ++a)
-      for (int bb = 0; bb < nj; ++bb)
-        for (int c = 0; c < nk; ++c) {
-          const float w = (a ? wi1 : wi0) * (bb ? wj1 : wj0) * (c ? wk1 : wk0);
-          val += w * (float)ec[((ci + a) * m + (cj + bb)) * m + (ck + c)];
-        }
-    ef[(i * n + j) * n + k] += val;
+  const int k = (threadIdx.x & 15) + 1, j = ((threadIdx.x >> 4) & 15) + 1;
+  if (k <= J && j <= J) {
+    for (int i = (threadIdx.x >> 8) + 1; i <= J; i += 4) {
+      int ci, cj, ck;
+      float wi0, wi1, wj0, wj1, wk0, wk1;
+      const int ni = prolong_w(i, f, cg, ci, wi0, wi1);
+      const int nj = prolong_w(j, f, cg, cj, wj0, wj1);
+      const int nk = prolong_w(k, f, cg, ck, wk0, wk1);
+      float val = 0.0f;
+      for (int a = 0; a < ni; ++a)
+        for (int bb = 0; bb < nj; ++bb)
+          for (int c = 0; c < nk; ++c) {
+            const float w = (a ? wi1 : wi0) * (bb ? wj1 : wj0) * (c ? wk1 : wk0);
+            val += w * (float)ec[((ci + a) * m + (cj + bb)) * m + (ck + c)];
+          }
+      ef[(i * n + j) * n + k] += val;
+    }
   }
   __syncthreads();
 }
@@ -1391,7 +1404,7 @@ static int launch_tail(gc_ctx *ctx, const gc_mg_params *p) {
   // The coarsest level has at most 3^3 unknowns: a few FP64 Gauss-Seidel sweeps
   // solve it far below the V-cycle's contraction (J = 1 is exact in one sweep).
   const int Jc = d.g[d.nl - 1].J;
-  d.coarse = p->coarse_sweeps < 8 * Jc ? p->coarse_sweeps : 8 * Jc;
+  d.coarse = Jc == 1 ? 1 : (p->coarse_sweeps < 8 * Jc ? p->coarse_sweeps : 8 * Jc);
   const size_t smem = tail_smem_bytes(ctx);
   static int attr_set_for = -1;
   if (smem > 48 * 1024 && attr_set_for != (int)smem) {
