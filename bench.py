@@ -94,6 +94,10 @@ def _parse(argv=None):
                     help="steps of the stepwise (unfused) chain timed for comparison; 0 skips it")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the potential/force error against the FP64 FFT and the converged multigrid")
+    ap.add_argument("--accuracy-steps", type=int, default=200,
+                    help="length of the accuracy run (the precision configuration: 200 steps)")
+    ap.add_argument("--accuracy-every", type=int, default=50,
+                    help="steps between its FP64 checks (the precision configuration: every 50th step)")
     ap.add_argument("--graph", type=int, default=1,
                     help="1: time whole-step CUDA graph replays (stopping rule decided on the device); "
                          "0: eager steps that read the residual on the host after every V-cycle")
@@ -166,10 +170,12 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------- CPU arm
-def _reference_chain(pos_grid, vel, mass, G, dx, dt, steps, budget_s, threads=None):
+def _reference_chain(pos_grid, vel, mass, G, dx, dt, steps, budget_s, threads=None, fp64_tol=None):
     """The reference's KDK step (bench.py:145-152 / sim.py:320-327) on the C restatement
     of its kernels: kick, drift, deposit (parallel f32 atomics), multigrid with its
-    schedule (tol 1e-3, 20 cycles, warm start), grad, gather, kick.
+    schedule (tol 1e-3, 20 cycles, warm start), grad, gather, kick. With
+    ``fp64_tol`` the multigrid is the same algorithm in FP64 iterated (warm
+    started, at most 100 cycles) to that relative residual instead.
     Returns (seconds per step list, last solver cycles, residual ratio reached)."""
     from oracle import pm
 
@@ -178,8 +184,12 @@ def _reference_chain(pos_grid, vel, mass, G, dx, dt, steps, budget_s, threads=No
     x = [np.ascontiguousarray(pos_grid[:, i], dtype=np.float32) for i in range(3)]
     v = [np.ascontiguousarray(vel[:, i], dtype=np.float32) for i in range(3)]
     m = np.ascontiguousarray(mass, dtype=np.float32)
-    phi = np.zeros((G, G, G), np.float32)
-    mg = pm.ReferenceMultigrid(G, dx=dx, grav_constant=1.0)
+    if fp64_tol is None:
+        phi = np.zeros((G, G, G), np.float32)
+        mg = pm.ReferenceMultigrid(G, dx=dx, grav_constant=1.0)
+    else:
+        phi = np.zeros((G, G, G), np.float64)
+        mg = pm.ReferenceMultigrid64(G, dx=dx, grav_constant=1.0, tol=fp64_tol, n_cycles=100)
     warm = {"on": False}
     acc = [None]
 
@@ -188,7 +198,7 @@ def _reference_chain(pos_grid, vel, mass, G, dx, dt, steps, budget_s, threads=No
         pm.lib().or_deposit_f32(x[0], x[1], x[2], m, m.shape[0], float(dx), int(G), rho, 1)
         mg.solve(rho, phi, warm_start=warm["on"])
         warm["on"] = True
-        acc[0] = pm.gather(np.stack(x, 1), *pm.grad(phi, dx), dx)
+        acc[0] = pm.gather(np.stack(x, 1), *pm.grad(phi.astype(np.float32), dx), dx)
 
     accel()
     times = []
@@ -203,6 +213,39 @@ def _reference_chain(pos_grid, vel, mass, G, dx, dt, steps, budget_s, threads=No
             break
     ratio = mg.norms[1] / mg.norms[0] if mg.norms[0] > 0 else 0.0
     return times, mg.last_cycles, float(ratio)
+
+
+def _cpu_baseline(args, icr, cfg, n, G, dx, dt):
+    """The reference chain restated in C on this host's cores: the reference's
+    schedule on the full workload (the headline CPU number), the same chain with
+    the FP64 multigrid driven to the GPU's tolerance, and the Plummer
+    configuration's full 200-step run."""
+    from galaxy_collision_gb300 import ic
+
+    pos_grid = (icr.pos.astype(np.float64) - np.asarray(cfg["origin"])).astype(np.float32)
+    times, cyc, ratio = _reference_chain(pos_grid, icr.vel, icr.mass, G, dx, dt, 3, args.cpu_budget_s)
+    out = {
+        "value": n * len(times) / sum(times), "unit": UNIT, "cores": _cpu_cores(), "kind": "port",
+        "sample": f"{len(times)} KDK step(s) of the full workload ({n:,} particles, {G}^3) after one priming "
+                  f"force evaluation; reference schedule tol=1e-3, n_cycles=20, warm start (last solve "
+                  f"{cyc} cycles, residual ratio {ratio:.2e})",
+    }
+    t64, c64, r64 = _reference_chain(pos_grid, icr.vel, icr.mass, G, dx, dt, 2, args.cpu_budget_s,
+                                     fp64_tol=args.tol)
+    out["fp64_to_tol"] = {
+        "value": n * len(t64) / sum(t64), "unit": UNIT,
+        "sample": f"{len(t64)} KDK step(s) of the full workload, the same chain with the reference multigrid in "
+                  f"FP64 iterated to {args.tol:g} (last solve {c64} cycles, residual ratio {r64:.2e})"}
+    p_icr, p_cfg = ic.build("plummer_131k")
+    p_pos = (p_icr.pos.astype(np.float64) - np.asarray(p_cfg["origin"])).astype(np.float32)
+    tp, cp, rp = _reference_chain(p_pos, p_icr.vel, p_icr.mass, p_cfg["grid"], p_cfg["dx"], p_cfg["dt"],
+                                  p_cfg["steps"], 10.0 * args.cpu_budget_s)
+    out["plummer_131k_full_run"] = {
+        "value": p_icr.n * len(tp) / sum(tp), "unit": UNIT, "steps": len(tp),
+        "sample": f"the Plummer configuration ({p_icr.n:,} particles, {p_cfg['grid']}^3, dt {p_cfg['dt']}): "
+                  f"{len(tp)} of {p_cfg['steps']} steps, reference schedule (last solve {cp} cycles, residual "
+                  f"ratio {rp:.2e})"}
+    return out
 
 
 def _cpu_cores():
@@ -298,10 +341,10 @@ def run_ours(args):
 
     net = _load_net() if args.warmstart == "learned" else None
 
-    def make_engine(mode=None):
-        e = PMEngine(G, dx, grav=1.0, origin=cfg["origin"], tol=args.tol, max_cycles=60, fixed_point_bits=bits,
-                     sort_every=args.sort_every, grad_grid=bool(args.grad_grid), pre_sweeps=args.pre_sweeps,
-                     post_sweeps=args.post_sweeps)
+    def make_engine(mode=None, plain_f32=False):
+        e = PMEngine(G, dx, grav=1.0, origin=cfg["origin"], tol=args.tol, max_cycles=20 if plain_f32 else 60,
+                     fixed_point_bits=bits, sort_every=args.sort_every, grad_grid=bool(args.grad_grid),
+                     pre_sweeps=args.pre_sweeps, post_sweeps=args.post_sweeps, plain_f32=plain_f32)
         m = mode or args.warmstart
         e.set_warmstart(m, net=(net if net is not None else _load_net()) if m == "learned" else None)
         return e
@@ -396,15 +439,18 @@ def run_ours(args):
         line["poisson"]["ms_per_solve"] = round(poisson_ms, 4)
         line["poisson"]["warm_start"] = args.warmstart
 
-        if not args.no_accuracy:
-            eng.synchronize(dt)
-            acc = force_chain_errors(eng)
-            line["accuracy"] = {k: (float(f"{v:.4e}") if isinstance(v, float) else v) for k, v in acc.items()}
-            line["accuracy"]["note"] = ("relative L2 over the grid (phi) and over all particles and components "
-                                        "(CIC-gathered -grad phi) of the engine's synchronised state after the "
-                                        "timed and profiled steps, against the FP64 zero-padded FFT of the same "
-                                        "density and against the multigrid converged to 1e-10")
         del eng  # its blocks stay in torch's cache for the e2e engine (no cudaMalloc in that timed region)
+        if not args.no_accuracy:
+            line["accuracy_schedule"] = _accuracy_schedule(args, icr, make_engine, dt)
+            line["accuracy"] = dict(line["accuracy_schedule"][-1])
+            line["accuracy"]["note"] = (
+                "relative L2 over the grid (phi) and over all particles and components (CIC-gathered -grad phi) "
+                "of the engine's synchronised state against three FP64 references of the same density: the "
+                "zero-padded FFT with the reference's continuum kernel (fft: discretisation + boundary + "
+                "solver), the same FFT with the lattice Green's function of the 7-point Laplacian (lattice: "
+                "boundary + solver) and the multigrid converged to 1e-10 (converged: solver); last sample of "
+                "accuracy_schedule")
+            torch.cuda.empty_cache()
         if not args.no_e2e:
             line["e2e"] = _e2e(args, icr, make_engine, dt)
         torch.cuda.empty_cache()
@@ -415,18 +461,44 @@ def run_ours(args):
             line["plain_chain"]["fused_speedup"] = round(line["plain_chain"]["ms_per_step"] /
                                                          line["ms_per_step"], 3)
         if not args.no_cpu_baseline and world == 1:
-            pos_grid = (icr.pos.astype(np.float64) - np.asarray(cfg["origin"])).astype(np.float32)
-            times, cyc, ratio = _reference_chain(pos_grid, icr.vel, icr.mass, G, dx, dt, 3, args.cpu_budget_s)
-            line["cpu_baseline"] = {
-                "value": n * len(times) / sum(times), "unit": UNIT, "cores": _cpu_cores(), "kind": "port",
-                "sample": f"{len(times)} KDK step(s) of the full workload ({n:,} particles, {G}^3) after one priming "
-                          f"force evaluation; reference schedule tol=1e-3, n_cycles=20, warm start (last solve "
-                          f"{cyc} cycles, residual ratio {ratio:.2e})",
-            }
+            line["cpu_baseline"] = _cpu_baseline(args, icr, cfg, n, G, dx, dt)
     if world > 1:
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def _accuracy_schedule(args, icr, make_engine, dt):
+    """The precision configuration's check: a fresh run of ``accuracy_steps``
+    steps from the same initial conditions, the potential and force errors of
+    its synchronised state against the FP64 references (see force_chain_errors)
+    at step 0 and every ``accuracy_every`` steps."""
+    import torch
+    from galaxy_collision_gb300.accuracy import force_chain_errors
+
+    eng = make_engine()
+    eng.load(icr.pos, icr.vel, icr.mass, icr.gid, sort=True)
+    solvers = {}  # the two 512^3 FP64 kernels are transformed once
+
+    def sample(step):
+        acc = force_chain_errors(eng, solvers=solvers)
+        row = {"step": step}
+        row.update({k: (float(f"{v:.4e}") if isinstance(v, float) else v) for k, v in acc.items()})
+        return row
+
+    rows = [sample(0)]
+    done = 0
+    while done < args.accuracy_steps:
+        k = min(args.accuracy_every, args.accuracy_steps - done)
+        eng.prime(dt)
+        for _ in range(k - 1):
+            eng.advance(dt)
+        eng.synchronize(dt)
+        done += k
+        rows.append(sample(done))
+    del eng, solvers
+    torch.cuda.empty_cache()
+    return rows
 
 
 def _load_net():
@@ -444,9 +516,11 @@ def _compare_warm_starts(icr, make_engine, dt, steps, warm=4):
     import torch
 
     out = {}
-    modes = ["plain", "extrapolate"] + (["learned"] if _load_net() is not None else [])
+    modes = ["plain_f32", "plain", "extrapolate"] + (["learned"] if _load_net() is not None else [])
     for mode in modes:
-        eng = make_engine(mode)
+        # plain_f32: the plain FP32 chain (previous-step warm start, all-FP32 multigrid, the reference's cap
+        # of 20 V-cycles since it cannot reach the tolerance)
+        eng = make_engine("plain", plain_f32=True) if mode == "plain_f32" else make_engine(mode)
         eng.load(icr.pos, icr.vel, icr.mass, icr.gid, sort=True)
         eng.prime(dt)
         for _ in range(warm):
@@ -470,7 +544,9 @@ def _compare_warm_starts(icr, make_engine, dt, steps, warm=4):
         del eng
         torch.cuda.empty_cache()
     out["note"] = ("same initial conditions, steps after a short warm-up; solve = multigrid kernels + faces + "
-                   "initial-guess kernels (network included); all reach the same relative residual")
+                   "initial-guess kernels, the network's convolutions included; plain, extrapolate and learned "
+                   "reach the same relative residual; plain_f32 is the plain FP32 chain (previous-step warm start, "
+                   "all-FP32 multigrid) stopped at the reference's 20 V-cycles with the residual it reached")
     return out
 
 

@@ -1560,10 +1560,15 @@ int gc_ws_pre_solve(gc_ctx *ctx, int warm, int mode) {
       return GC_ERR_STATE;
     }
     ws->stream = ctx->stream;
+    // the network's convolutions are timed as one warm-start interval (they
+    // launch on the network object, not through the context's launcher)
+    const int slot = ctx->prof.enabled && !ctx->capturing ? gc_prof_slot(ctx, GK_WARMSTART) : -1;
+    if (slot >= 0) cudaEventRecord(ctx->prof.ev[2 * slot], ctx->stream);
     if ((s = gc_ws_forward(ws, w.feat, w.y))) {
       gc_set_error(ctx, "warm-start network: %s", ws->err);
       return s;
     }
+    if (slot >= 0) cudaEventRecord(ctx->prof.ev[2 * slot + 1], ctx->stream);
     ctx->prof.launches[GK_WARMSTART] += 18;
     yc = w.y;
   }

@@ -7,6 +7,11 @@ positions) this measures, on the device:
   zero-padded isolated FFT convolution (``FFTPoissonSolver``, pad factor 2, the
   reference's validation solver, solver/fft_oracle.py:54-109). This is the
   model error of the open-boundary 7-point discretisation plus the solver's.
+* ``phi_vs_lattice`` / ``force_vs_lattice`` -- the same against the FP64 FFT
+  convolution with the lattice Green's function of the 7-point Laplacian
+  (``FFTPoissonSolver(green="lattice")``): the exact free-space solution of the
+  discrete problem, so this is the multipole boundary's error plus the
+  solver's, without the discretisation.
 * ``phi_vs_converged`` / ``force_vs_converged`` -- the same against the
   multigrid driven to a 1e-10 relative residual on the same density: the error
   that stopping at the working tolerance leaves.
@@ -42,7 +47,8 @@ def _forces(parts, phi: torch.Tensor, dx: float):
     return torch.stack(acc, 0)
 
 
-def force_chain_errors(eng, *, pad_factor: int = 2, converged_tol: float = 1e-10, with_fft: bool = True) -> dict:
+def force_chain_errors(eng, *, pad_factor: int = 2, converged_tol: float = 1e-10, with_fft: bool = True,
+                       with_lattice: bool = True, solvers: dict | None = None) -> dict:
     """Relative-L2 errors of the engine's current potential and particle forces."""
     from galaxy_collision_gb300.solver import make_solver
 
@@ -65,15 +71,26 @@ def force_chain_errors(eng, *, pad_factor: int = 2, converged_tol: float = 1e-10
     out["force_vs_converged"] = _rel_l2(a, a_c)
     del a_c, phi_c
 
-    if with_fft:
-        fft = make_solver("fft", G, dx=dx, grav_constant=eng.grav, pad_factor=pad_factor)
+    # the FP64 FFT references (their kernels' transforms are kept in `solvers`,
+    # when given, for the next call)
+    cache = solvers if solvers is not None else {}
+    for key, green, on in (("fft", "continuum", with_fft), ("lattice", "lattice", with_lattice)):
+        if not on:
+            continue
+        fft = cache.get(green)
+        if fft is None:
+            fft = make_solver("fft", G, dx=dx, grav_constant=eng.grav, pad_factor=pad_factor, green=green)
+            if solvers is not None:
+                cache[green] = fft
         phi64 = fft.potential64(rho)
-        out["phi_vs_fft"] = _rel_l2(phi, phi64)
+        out[f"phi_vs_{key}"] = _rel_l2(phi, phi64)
         phi_f = phi64.to(torch.float32)
         del phi64, fft
-        torch.cuda.empty_cache()
+        if solvers is None:
+            torch.cuda.empty_cache()
         a_f = _forces(parts, phi_f, dx)
-        out["force_vs_fft"] = _rel_l2(a, a_f)
+        out[f"force_vs_{key}"] = _rel_l2(a, a_f)
+        del phi_f, a_f
         out["fft_grid"] = pad_factor * G
     return out
 

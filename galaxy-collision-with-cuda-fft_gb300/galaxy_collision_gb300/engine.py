@@ -41,7 +41,7 @@ class PMEngine:
     def __init__(self, grid_size: int, dx: float, grav: float = 1.0, *, origin=(0.0, 0.0, 0.0), tol: float = 1e-6,
                  max_cycles: int = 50, pre_sweeps: int = 2, post_sweeps: int = 2, coarse_sweeps: int = 40,
                  fixed_point_bits: int = 52, sort_every: int = 20, grad_grid: bool = True, fixed_cycles: int = 0,
-                 max_particles: int = 0, deposit_next: bool = False):
+                 max_particles: int = 0, deposit_next: bool = False, plain_f32: bool = False):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
         self.grav = float(grav)
@@ -54,6 +54,8 @@ class PMEngine:
         self.mg.max_cycles = int(max_cycles)
         self.mg.min_cycles = 1
         self.mg.tol = float(tol)
+        if plain_f32:  # the all-FP32 method: stalls at the FP32 floor, runs to max_cycles
+            self.mg.flags |= _native.GC_MG_PLAIN_F32
         # fixed_cycles > 0: exactly that many V-cycles per solve and no host read in
         # the step (the residual stays on the device, see last_residual), which is
         # what lets a step be captured as a CUDA graph

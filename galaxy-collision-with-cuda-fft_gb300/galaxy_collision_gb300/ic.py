@@ -282,7 +282,7 @@ def equilibrate_disk_velocities(ic, *, dx: float, grid: int, origin, grav: float
 CONFIGS = {
     "plummer_131k": dict(kind="plummer", n=131072, seed=0, box=24.0, grid=64, dt=0.01, steps=200),
     "two_disk_10M": dict(kind="two_disk", n1=4_000_000, n2=6_000_000, seed=1, box=64.0, grid=256, dt=0.005,
-                         steps=500),
+                         steps=500, fixed_point_bits=44),
     "two_disk_100M": dict(kind="two_disk", n1=40_000_000, n2=60_000_000, seed=2, box=64.0, grid=256, dt=0.005,
                           steps=200, fixed_point_bits=40),
 }

@@ -6,6 +6,12 @@ done by FFT on a (pad_factor*G)^3 zero-padded grid so there are no periodic
 images. The transforms are cuFFT calls through ``torch.fft`` in float64; this
 solver validates the multigrid and measures its force error, it is not the
 production solve.
+
+``green="lattice"`` (an addition; the reference has only the continuum kernel)
+convolves with the lattice Green's function of the 7-point Laplacian instead
+(``solver/lattice_green.py``): the exact free-space solution of the discrete
+problem the multigrid solves, which separates the multigrid's boundary and
+solver error from the discretisation error of the 7-point stencil.
 """
 
 from __future__ import annotations
@@ -19,7 +25,7 @@ from galaxy_collision_gb300.solver.base import PoissonSolver
 
 class FFTPoissonSolver(PoissonSolver):
     def __init__(self, grid_size: int, dx: float = 1.0, pad_factor: int = 2, grav_constant: float | None = None,
-                 use_gpu: bool | None = None):
+                 use_gpu: bool | None = None, *, green: str = "continuum"):
         if pad_factor < 2:
             raise ValueError(f"pad_factor must be >= 2 to avoid circular wrap, got {pad_factor}")
         self.grid_size = int(grid_size)
@@ -28,9 +34,20 @@ class FFTPoissonSolver(PoissonSolver):
         self.G = units.G if grav_constant is None else float(grav_constant)
         if use_gpu is False:
             raise ValueError("this FFTPoissonSolver runs on the GPU only")
+        if green not in ("continuum", "lattice"):
+            raise ValueError(f"unknown Green's function {green!r} (expected 'continuum' or 'lattice')")
+        self.green = green
         self._greens_ft = None
 
     def _green(self, device):
+        if self._greens_ft is None and self.green == "lattice":
+            from galaxy_collision_gb300.solver.lattice_green import lattice_green_kernel
+
+            # phi = -(4 pi G / dx) (g * m), m = rho dx^3: L phi / dx^2 = 4 pi G rho
+            ker = lattice_green_kernel(self.pad, device)
+            ker *= -4.0 * 3.141592653589793 * self.G * self.dx**2
+            self._greens_ft = torch.fft.rfftn(ker)
+            del ker
         if self._greens_ft is None:
             m = self.pad
             a = torch.arange(m, device=device, dtype=torch.float64)

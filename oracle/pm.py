@@ -43,6 +43,12 @@ def lib():
         L.or_moments.argtypes = [_f, C.c_int, C.c_float, _d]
         L.or_residual64.argtypes = [_f, _d, C.c_int, C.c_float, C.c_double, C.POINTER(C.c_double)]
         L.or_residual64.restype = C.c_double
+        L.or_mg64_create.restype = C.c_void_p
+        L.or_mg64_create.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                     C.c_int]
+        L.or_mg64_destroy.argtypes = [C.c_void_p]
+        L.or_mg64_solve.argtypes = [C.c_void_p, _f, _d, C.c_int, _d]
+        L.or_mg64_solve.restype = C.c_int
         _lib = L
     return _lib
 
@@ -167,5 +173,29 @@ class ReferenceMultigrid:
     def __del__(self):
         try:
             lib().or_mg_destroy(self._h)
+        except Exception:
+            pass
+
+
+class ReferenceMultigrid64:
+    """The reference multigrid (solver/multigrid.py:298-494) in FP64 throughout:
+    the same algorithm driven below the FP32 floor (the CPU baseline at 1e-6)."""
+
+    def __init__(self, grid_size, dx=1.0, grav_constant=1.0, n_cycles=100, pre_sweeps=2, post_sweeps=2,
+                 coarse_sweeps=40, tol=1e-6, min_cycles=1):
+        self.grid_size = int(grid_size)
+        self._h = lib().or_mg64_create(self.grid_size, float(dx), float(grav_constant), int(n_cycles),
+                                       int(pre_sweeps), int(post_sweeps), int(coarse_sweeps), float(tol),
+                                       int(min_cycles))
+        self.last_cycles = 0
+        self.norms = np.zeros(2)
+
+    def solve(self, rho, phi64, warm_start=False):
+        """rho: (G,G,G); phi64: float64 C-contiguous array updated in place."""
+        self.last_cycles = lib().or_mg64_solve(self._h, _f32(rho), phi64, int(bool(warm_start)), self.norms)
+
+    def __del__(self):
+        try:
+            lib().or_mg64_destroy(self._h)
         except Exception:
             pass

@@ -547,3 +547,199 @@ double or_residual64(const float *rho, const double *phi, int G, float dx, doubl
   if (rhs_norm) *rhs_norm = sqrt(bb);
   return sqrt(rr);
 }
+
+/* ---- the same multigrid in FP64 (multigrid.py:46-130, 261-295, 429-487) ----
+ * The reference algorithm (vertex-centred coarsening, red-black Gauss-Seidel,
+ * full weighting, trilinear prolongation, multipole faces) with every array
+ * and every operation in double precision, so that the adaptive loop can be
+ * driven below the FP32 floor (to 1e-6 and beyond): the CPU baseline of the
+ * mixed-precision GPU solve at the same tolerance. */
+typedef struct {
+  int G, nlev;
+  double dx, grav, tol;
+  int n_cycles, nu1, nu2, coarse_sweeps, min_cycles;
+  int sizes[32];
+  double dxs[32];
+  double *phi[32], *rhs[32], *res[32];
+  int last_cycles;
+} or_mg64;
+
+or_mg64 *or_mg64_create(int G, double dx, double grav, int n_cycles, int nu1, int nu2, int coarse_sweeps, double tol,
+                        int min_cycles) {
+  or_mg64 *h = (or_mg64 *)calloc(1, sizeof(or_mg64));
+  h->G = G;
+  h->dx = dx;
+  h->grav = grav;
+  h->n_cycles = n_cycles;
+  h->nu1 = nu1;
+  h->nu2 = nu2;
+  h->coarse_sweeps = coarse_sweeps;
+  h->tol = tol;
+  h->min_cycles = min_cycles < 1 ? 1 : min_cycles;
+  int nl = 0;
+  h->sizes[nl++] = G;
+  while (h->sizes[nl - 1] % 2 == 0 && h->sizes[nl - 1] / 2 >= 3 && nl < 32) {
+    h->sizes[nl] = h->sizes[nl - 1] / 2;
+    ++nl;
+  }
+  h->nlev = nl;
+  for (int l = 0; l < nl; ++l) {
+    h->dxs[l] = dx * (double)(1 << l);
+    const size_t n3 = (size_t)h->sizes[l] * h->sizes[l] * h->sizes[l];
+    h->phi[l] = (double *)calloc(n3, sizeof(double));
+    h->rhs[l] = (double *)calloc(n3, sizeof(double));
+    h->res[l] = (double *)calloc(n3, sizeof(double));
+  }
+  return h;
+}
+
+void or_mg64_destroy(or_mg64 *h) {
+  if (!h) return;
+  for (int l = 0; l < h->nlev; ++l) {
+    free(h->phi[l]);
+    free(h->rhs[l]);
+    free(h->res[l]);
+  }
+  free(h);
+}
+
+static void gs_rb64(double *phi, const double *rhs, int n, double h2, int color) {
+#pragma omp parallel for schedule(static)
+  for (int i = 1; i < n - 1; ++i)
+    for (int j = 1; j < n - 1; ++j)
+      for (int k = 1 + ((i + j + 1 + color) & 1); k < n - 1; k += 2) {
+        const size_t c = IDX(i, j, k, n);
+        const size_t si = (size_t)n * n, sj = (size_t)n;
+        phi[c] = (phi[c + si] + phi[c - si] + phi[c + sj] + phi[c - sj] + phi[c + 1] + phi[c - 1] - h2 * rhs[c]) / 6.0;
+      }
+}
+
+static void residual64(const double *phi, const double *rhs, double *res, int n, double inv_h2) {
+  memset(res, 0, (size_t)n * n * n * sizeof(double));
+#pragma omp parallel for schedule(static)
+  for (int i = 1; i < n - 1; ++i)
+    for (int j = 1; j < n - 1; ++j)
+      for (int k = 1; k < n - 1; ++k) {
+        const size_t c = IDX(i, j, k, n);
+        const size_t si = (size_t)n * n, sj = (size_t)n;
+        const double lap =
+            (phi[c + si] + phi[c - si] + phi[c + sj] + phi[c - sj] + phi[c + 1] + phi[c - 1] - 6.0 * phi[c]) * inv_h2;
+        res[c] = rhs[c] - lap;
+      }
+}
+
+static void restrict_fw64(const double *rf, int nf, double *rc, int nc) {
+  memset(rc, 0, (size_t)nc * nc * nc * sizeof(double));
+#pragma omp parallel for schedule(static)
+  for (int J = 1; J < nc - 1; ++J)
+    for (int K = 1; K < nc - 1; ++K)
+      for (int L = 1; L < nc - 1; ++L) {
+        double acc = 0.0;
+        for (int a = -1; a <= 1; ++a)
+          for (int b = -1; b <= 1; ++b)
+            for (int c = -1; c <= 1; ++c)
+              acc += (a ? 1.0 : 2.0) * (b ? 1.0 : 2.0) * (c ? 1.0 : 2.0) * rf[IDX(2 * J + a, 2 * K + b, 2 * L + c, nf)];
+        rc[IDX(J, K, L, nc)] = acc / 64.0;
+      }
+}
+
+static void prolong_add64(const double *pc, int nc, double *pf, int nf) {
+#pragma omp parallel for schedule(static)
+  for (int i = 1; i < nf - 1; ++i)
+    for (int j = 1; j < nf - 1; ++j)
+      for (int k = 1; k < nf - 1; ++k) {
+        const int ci = i / 2, cj = j / 2, ck = k / 2, oi = i & 1, oj = j & 1, ok = k & 1;
+        double val = 0.0;
+        for (int di = 0; di <= oi; ++di)
+          for (int dj = 0; dj <= oj; ++dj)
+            for (int dk = 0; dk <= ok; ++dk)
+              val += (oi ? 0.5 : 1.0) * (oj ? 0.5 : 1.0) * (ok ? 0.5 : 1.0) * pc[IDX(ci + di, cj + dj, ck + dk, nc)];
+        pf[IDX(i, j, k, nf)] += val;
+      }
+}
+
+static void vcycle64(or_mg64 *h, int l) {
+  const int n = h->sizes[l];
+  const double h2 = h->dxs[l] * h->dxs[l];
+  const int pre = l == h->nlev - 1 ? h->coarse_sweeps : h->nu1;
+  for (int s = 0; s < pre; ++s) {
+    gs_rb64(h->phi[l], h->rhs[l], n, h2, 0);
+    gs_rb64(h->phi[l], h->rhs[l], n, h2, 1);
+  }
+  if (l == h->nlev - 1) return;
+  residual64(h->phi[l], h->rhs[l], h->res[l], n, 1.0 / h2);
+  restrict_fw64(h->res[l], n, h->rhs[l + 1], h->sizes[l + 1]);
+  memset(h->phi[l + 1], 0, (size_t)h->sizes[l + 1] * h->sizes[l + 1] * h->sizes[l + 1] * sizeof(double));
+  vcycle64(h, l + 1);
+  prolong_add64(h->phi[l + 1], h->sizes[l + 1], h->phi[l], n);
+  for (int s = 0; s < h->nu2; ++s) {
+    gs_rb64(h->phi[l], h->rhs[l], n, h2, 0);
+    gs_rb64(h->phi[l], h->rhs[l], n, h2, 1);
+  }
+}
+
+static double sumsq64(const double *a, size_t n) {
+  double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+  for (size_t i = 0; i < n; ++i) s += a[i] * a[i];
+  return s;
+}
+
+/* rho f32 (the deposited density), phi f64 in/out. Returns the V-cycles run;
+ * out_norms = [||rhs||, ||res||]. */
+int or_mg64_solve(or_mg64 *h, const float *rho, double *phi, int warm_start, double *out_norms) {
+  const int G = h->G;
+  const size_t g3 = (size_t)G * G * G;
+  double s[10];
+  or_moments(rho, G, (float)h->dx, s);
+  double M = s[0], cx = 0, cy = 0, cz = 0, S[6] = {0, 0, 0, 0, 0, 0};
+  if (M > 0.0) {
+    cx = s[1] / M; cy = s[2] / M; cz = s[3] / M;
+    S[0] = s[4] - M * cx * cx; S[1] = s[5] - M * cy * cy; S[2] = s[6] - M * cz * cz;
+    S[3] = s[7] - M * cx * cy; S[4] = s[8] - M * cx * cz; S[5] = s[9] - M * cy * cz;
+  }
+  const double fpg = 4.0 * M_PI * h->grav;
+  for (size_t i = 0; i < g3; ++i) h->rhs[0][i] = fpg * (double)rho[i];
+  if (warm_start)
+    memcpy(h->phi[0], phi, g3 * sizeof(double));
+  else
+    memset(h->phi[0], 0, g3 * sizeof(double));
+  const double trS = S[0] + S[1] + S[2];
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < G; ++i)
+    for (int j = 0; j < G; ++j)
+      for (int k = 0; k < G; ++k) {
+        if (!(i == 0 || i == G - 1 || j == 0 || j == G - 1 || k == 0 || k == G - 1)) continue;
+        double v = 0.0;
+        if (M > 0.0) {
+          const double rx = i * h->dx - cx, ry = j * h->dx - cy, rz = k * h->dx - cz;
+          const double d2 = rx * rx + ry * ry + rz * rz + 1e-12, d = sqrt(d2);
+          const double nx = rx / d, ny = ry / d, nz = rz / d;
+          const double nsn = nx * nx * S[0] + ny * ny * S[1] + nz * nz * S[2] +
+                             2.0 * (nx * ny * S[3] + nx * nz * S[4] + ny * nz * S[5]);
+          v = -h->grav * (M / d + (3.0 * nsn - trS) / (2.0 * d2 * d));
+        }
+        h->phi[0][IDX(i, j, k, G)] = v;
+      }
+  const double inv_h2 = 1.0 / (h->dx * h->dx);
+  const double rhs_norm = sqrt(sumsq64(h->rhs[0], g3));
+  double rn = NAN;
+  h->last_cycles = h->n_cycles;
+  for (int c = 0; c < h->n_cycles; ++c) {
+    vcycle64(h, 0);
+    if (c + 1 >= h->min_cycles && rhs_norm > 0.0) {
+      residual64(h->phi[0], h->rhs[0], h->res[0], G, inv_h2);
+      rn = sqrt(sumsq64(h->res[0], g3));
+      if (rn < h->tol * rhs_norm) {
+        h->last_cycles = c + 1;
+        break;
+      }
+    }
+  }
+  memcpy(phi, h->phi[0], g3 * sizeof(double));
+  if (out_norms) {
+    out_norms[0] = rhs_norm;
+    out_norms[1] = rn;
+  }
+  return h->last_cycles;
+}
