@@ -404,6 +404,22 @@ class PMEngine:
         self.steps_since_sort += 1
         self.last_graph = g
 
+    def launch_graph(self, dt: float):
+        """Replay the step graph of the current buffer set on this engine's graph
+        stream and return that stream, without ordering it against any other
+        stream (the caller does: make it wait for the work the step depends on,
+        and wait for it before using the results). For many engines stepping
+        concurrently; prepare_graphs first, and sort (with the usual ordering)
+        before calling when a sort is due."""
+        g = self._graphs[(self.cur["x"].data_ptr(), float(dt))]
+        gs = self._graph_stream()
+        with torch.cuda.stream(gs):
+            self.ctx.bind_stream()
+            g.launch()
+        self.steps_since_sort += 1
+        self.last_graph = g
+        return gs
+
     def prepare_graphs(self, dt: float) -> None:
         """Capture the step graphs of both particle-buffer sets now (a capture
         runs no kernels), so that later advance_graph calls only replay. The
