@@ -207,26 +207,6 @@ static inline unsigned gc_blocks(long long n, int threads) {
   return (unsigned)b;
 }
 
-// ---- packed FP32 pairs (sm_100+ f32x2 instructions) ----------------------------
-// Two f32 operations in one instruction; each lane is rounded exactly as the
-// scalar __fmul_rn / __fadd_rn (no fusion), so results are bit-identical.
-__device__ __forceinline__ float2 f2_mul(float2 a, float2 b) {
-  float2 r;
-  asm("{\n\t.reg .b64 A, B, D;\n\tmov.b64 A, {%2, %3};\n\tmov.b64 B, {%4, %5};\n\t"
-      "mul.rn.f32x2 D, A, B;\n\tmov.b64 {%0, %1}, D;\n\t}"
-      : "=f"(r.x), "=f"(r.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-  return r;
-}
-__device__ __forceinline__ float2 f2_add(float2 a, float2 b) {
-  float2 r;
-  asm("{\n\t.reg .b64 A, B, D;\n\tmov.b64 A, {%2, %3};\n\tmov.b64 B, {%4, %5};\n\t"
-      "add.rn.f32x2 D, A, B;\n\tmov.b64 {%0, %1}, D;\n\t}"
-      : "=f"(r.x), "=f"(r.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-  return r;
-}
-
 // ---- double-float (FP32 pair) arithmetic ---------------------------------------
 // Error-free transforms with explicit round-to-nearest intrinsics so that no
 // contraction or reassociation can break them.

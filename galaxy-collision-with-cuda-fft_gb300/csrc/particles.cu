@@ -390,42 +390,32 @@ __device__ __forceinline__ void dep_warp_runs(const float (&px)[NJ], const float
   for (int j = 0; j < NJ; ++j) {
     float gx, gy, gz;
     if (POW2) {  // x / dx == x * (1/dx) exactly when dx is a power of two
-      const float2 gxy = f2_mul(make_float2(px[j], py[j]), make_float2(inv_dx, inv_dx));
-      gx = gxy.x; gy = gxy.y; gz = __fmul_rn(pz[j], inv_dx);
+      gx = __fmul_rn(px[j], inv_dx); gy = __fmul_rn(py[j], inv_dx); gz = __fmul_rn(pz[j], inv_dx);
     } else {
       gx = __fdiv_rn(px[j], d.dx); gy = __fdiv_rn(py[j], d.dx); gz = __fdiv_rn(pz[j], d.dx);
     }
     const bool inr = gx >= -1.0f && gx < hi && gy >= -1.0f && gy < hi && gz >= -1.0f && gz < hi;
     const int ix = __float2int_rd(gx), iy = __float2int_rd(gy), iz = __float2int_rd(gz);
-    // the reference's f32 products (deposit.py:69-82) two at a time: each lane
-    // is the scalar op with its own rounding, so the integers are unchanged
-    const float2 fxy = f2_add(make_float2(gx, gy), make_float2(-__int2float_rn(ix), -__int2float_rn(iy)));
-    const float fx = fxy.x, fy = fxy.y, fz = __fsub_rn(gz, __int2float_rn(iz));
+    const float fx = __fsub_rn(gx, __int2float_rn(ix)), fy = __fsub_rn(gy, __int2float_rn(iy)),
+                fz = __fsub_rn(gz, __int2float_rn(iz));
     const float mmq = __fmul_rn(__fmul_rn(pm[j], d.inv_vol), qscale);
     const bool small = fabsf(mmq) < 4194304.0f;
     if (!inr && 32 * j < nrem && !gc_finite3(px[j], py[j], pz[j])) atomicOr(status, GC_FLAG_NONFINITE_POS);
     if (inr && !small) large |= 1u << j;
     const bool ok = inr && small;
     const float s = ok ? mmq : 0.0f;
-    const float2 w0xy = f2_add(make_float2(1.0f, 1.0f), make_float2(-fx, -fy));
-    const float wz0 = __fsub_rn(1.0f, fz);
-    const float2 a = f2_mul(make_float2(s, s), make_float2(w0xy.x, fx));      // a0, a1
-    const float2 b0 = f2_mul(make_float2(a.x, a.x), make_float2(w0xy.y, fy));  // b00, b01
-    const float2 b1 = f2_mul(make_float2(a.y, a.y), make_float2(w0xy.y, fy));  // b10, b11
-    const float2 wz = make_float2(wz0, fz), bias = make_float2(12582912.0f, 12582912.0f);
-    const float2 r0 = f2_add(f2_mul(make_float2(b0.x, b0.x), wz), bias);
-    const float2 r1 = f2_add(f2_mul(make_float2(b0.y, b0.y), wz), bias);
-    const float2 r2 = f2_add(f2_mul(make_float2(b1.x, b1.x), wz), bias);
-    const float2 r3 = f2_add(f2_mul(make_float2(b1.y, b1.y), wz), bias);
+    const float wx0 = __fsub_rn(1.0f, fx), wy0 = __fsub_rn(1.0f, fy), wz0 = __fsub_rn(1.0f, fz);
+    const float a0 = __fmul_rn(s, wx0), a1 = __fmul_rn(s, fx);
+    const float b00 = __fmul_rn(a0, wy0), b01 = __fmul_rn(a0, fy), b10 = __fmul_rn(a1, wy0), b11 = __fmul_rn(a1, fy);
     int v[8];
-    v[0] = (int)(__float_as_uint(r0.x) - DEP_BIAS);
-    v[1] = (int)(__float_as_uint(r0.y) - DEP_BIAS);
-    v[2] = (int)(__float_as_uint(r1.x) - DEP_BIAS);
-    v[3] = (int)(__float_as_uint(r1.y) - DEP_BIAS);
-    v[4] = (int)(__float_as_uint(r2.x) - DEP_BIAS);
-    v[5] = (int)(__float_as_uint(r2.y) - DEP_BIAS);
-    v[6] = (int)(__float_as_uint(r3.x) - DEP_BIAS);
-    v[7] = (int)(__float_as_uint(r3.y) - DEP_BIAS);
+    v[0] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b00, wz0), 12582912.0f)) - DEP_BIAS);
+    v[1] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b00, fz), 12582912.0f)) - DEP_BIAS);
+    v[2] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b01, wz0), 12582912.0f)) - DEP_BIAS);
+    v[3] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b01, fz), 12582912.0f)) - DEP_BIAS);
+    v[4] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b10, wz0), 12582912.0f)) - DEP_BIAS);
+    v[5] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b10, fz), 12582912.0f)) - DEP_BIAS);
+    v[6] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b11, wz0), 12582912.0f)) - DEP_BIAS);
+    v[7] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b11, fz), 12582912.0f)) - DEP_BIAS);
     const unsigned key = ok ? (unsigned)(((ix + 1) * G1 + (iy + 1)) * G1 + (iz + 1)) : DEP_NONE;
     // the lane's node in the box (unsigned: a lane without a key may hold any cell)
     const int bo = (int)((((unsigned)ix - (unsigned)bx.x0) * (unsigned)bx.ny + ((unsigned)iy - (unsigned)bx.y0)) *
