@@ -486,6 +486,7 @@ def _accuracy_schedule(args, icr, make_engine, dt):
         row.update({k: (float(f"{v:.4e}") if isinstance(v, float) else v) for k, v in acc.items()})
         return row
 
+    eng.evaluate(diagnostics=False)  # the potential of the initial state
     rows = [sample(0)]
     done = 0
     while done < args.accuracy_steps:
