@@ -4,9 +4,11 @@
 // and integrator.py operation by operation in f32 with explicit
 // round-to-nearest intrinsics (no FMA contraction), so the CPU restatement can
 // reproduce them bit for bit. The deposit accumulates the reference's per-corner
-// f32 contributions m*wx*wy*wz into an int64 fixed-point grid: integer addition
-// is associative, so the density is bit-identical whatever the particle order or
-// atomic interleaving.
+// contributions m*wx*wy*wz into an int64 fixed-point grid: the partial product
+// (m/dx^3*wx)*wy is rounded to f32 as the reference rounds it, and its exact
+// product with wz is rounded once to the nearest quantum (one fused
+// multiply-add). Integer addition is associative, so the density is
+// bit-identical whatever the particle order or atomic interleaving.
 #include "common.cuh"
 #include "umma.cuh"
 
@@ -102,12 +104,43 @@ int gc_fixed_point_setup(gc_ctx *ctx, const float *m, int64_t n, int bits, int m
 // ------------------------------------------------------------------------------
 // deposit (deposit.py:47-82)
 // ------------------------------------------------------------------------------
+// RNE(a * b * 2^k) as an int64, for finite a, b and |a * b * 2^k| < 2^62: the
+// product of the two 24-bit significands is exact in 64 bits, so the rounding
+// is the single rounding of the exact product (integer ALUs only).
+__device__ __forceinline__ long long prod_to_i64_rn(float a, float b, int k) {
+  const unsigned ua = __float_as_uint(a), ub = __float_as_uint(b);
+  int ea = (int)((ua >> 23) & 0xffu), eb = (int)((ub >> 23) & 0xffu);
+  const unsigned long long ma = (ua & 0x7fffffu) | (ea ? 0x800000u : 0u);
+  const unsigned long long mb = (ub & 0x7fffffu) | (eb ? 0x800000u : 0u);
+  if (ea == 0) ea = 1;
+  if (eb == 0) eb = 1;
+  const unsigned long long prod = ma * mb;  // < 2^48
+  const int sh = ea + eb - 300 + k;          // |a * b * 2^k| = prod * 2^sh
+  long long r;
+  if (sh >= 0) {
+    r = (long long)(prod << sh);
+  } else if (sh <= -49) {
+    r = 0;  // below 1/2
+  } else {
+    const int rs = -sh;
+    unsigned long long q = prod >> rs;
+    const unsigned long long rem = prod & ((1ull << rs) - 1ull), half = 1ull << (rs - 1);
+    if (rem > half || (rem == half && (q & 1ull))) q += 1ull;
+    r = (long long)q;
+  }
+  return ((ua ^ ub) >> 31) ? -r : r;
+}
+
+// The exponent k of a power of two 2^k held in a normal f32.
+__device__ __forceinline__ int pow2_exponent(float p) { return (int)((__float_as_uint(p) >> 23) & 0xffu) - 127; }
+
 // Per-corner int64 contributions of one particle; corners outside the box are 0.
 // Returns false when the particle deposits nothing.
 __device__ __forceinline__ bool cic_contrib(float x, float y, float z, float mass, const DepCtx &d, float qscale,
                                             CellPos &c, long long (&q)[8]) {
   if (!gc_cell_of(x, y, z, d.dx, d.G, c)) return false;
   const float mm = __fmul_rn(mass, d.inv_vol);
+  const int qk = pow2_exponent(qscale);
   const float wx[2] = {__fsub_rn(1.0f, c.fx), c.fx};
   const float wy[2] = {__fsub_rn(1.0f, c.fy), c.fy};
   const float wz[2] = {__fsub_rn(1.0f, c.fz), c.fz};
@@ -119,8 +152,8 @@ __device__ __forceinline__ bool cic_contrib(float x, float y, float z, float mas
       for (int cz = 0; cz < 2; ++cz) {
         const int jx = c.ix + cx, jy = c.iy + cy, jz = c.iz + cz;
         const bool in = (unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G && (unsigned)jz < (unsigned)d.G;
-        const float w = __fmul_rn(__fmul_rn(__fmul_rn(mm, wx[cx]), wy[cy]), wz[cz]);
-        q[(cx * 2 + cy) * 2 + cz] = in ? f32_to_i64_rn(__fmul_rn(w, qscale)) : 0LL;
+        const float b = __fmul_rn(__fmul_rn(mm, wx[cx]), wy[cy]);
+        q[(cx * 2 + cy) * 2 + cz] = in ? prod_to_i64_rn(b, wz[cz], qk) : 0LL;
       }
   return true;
 }
@@ -186,12 +219,13 @@ __global__ void __launch_bounds__(256)
 // sort they share one or two cells, and the particles that drifted into a
 // neighbouring cell since the sort are scattered among them.
 //
-// Per particle the 8 corner contributions are the reference's f32 products
+// Per particle the 8 corner contributions are the reference's products
 // m/dx^3 * wx * wy * wz (deposit.py:69-82) scaled by the quantum (a power of
-// two: exact) and rounded to the nearest integer. The rounding adds 1.5 * 2^23
-// (the f32 spacing is 1 in [2^23, 2^24)) and keeps the bits; the bias is
-// subtracted in integer arithmetic, and the corner values are summed in int32,
-// which is exact because every partial sum fits.
+// two: exact) and rounded to the nearest integer (dep_corners: the last
+// multiplication fused with the rounding, two corners per packed f32x2
+// instruction). The bias of the rounding is subtracted in integer arithmetic,
+// and the corner values are summed in int32, which is exact because every
+// partial sum fits.
 //
 // Into the shared-memory box (below) the warp keeps a run cell (dep_warp_runs):
 // lanes in it add their corners in registers, and the run is reduced across the
@@ -220,16 +254,53 @@ __global__ void __launch_bounds__(256)
 #define DEP_WBOX (DEP_BOX / 8)  // nodes of one warp's box
 #define DEP_BIAS 0x4B400000u
 
+// Packed f32x2 arithmetic (two lanes of a 64-bit register, IEEE round to
+// nearest per lane).
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 A, B, D;\n\tmov.b64 A, {%2, %3};\n\tmov.b64 B, {%4, %5};\n\t"
+      "mul.rn.f32x2 D, A, B;\n\tmov.b64 {%0, %1}, D;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) {
+  float2 r;
+  asm("{\n\t.reg .b64 A, B, C, D;\n\tmov.b64 A, {%2, %3};\n\tmov.b64 B, {%4, %5};\n\tmov.b64 C, {%6, %7};\n\t"
+      "fma.rn.f32x2 D, A, B, C;\n\tmov.b64 {%0, %1}, D;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return r;
+}
+
+// The 8 corner values of a particle of s quanta (|s| < 2^22) with weights
+// (wx0, fx), (wy0, fy), (wz0, fz), as the bits of 1.5 * 2^23 + RNE(b * wz)
+// (corner order (cx, cy, cz)): the partial products a = s*wx and b = a*wy are
+// rounded to f32, and b * wz + 1.5 * 2^23 is one fused multiply-add, whose single
+// rounding (spacing 1 in [2^23, 2^24)) is the rounding of the exact product to
+// the nearest integer. Two corners per packed instruction.
+__device__ __forceinline__ void dep_corners(float s, float wx0, float fx, float wy0, float fy, float wz0, float fz,
+                                            unsigned (&r)[8]) {
+  const float2 a = f2_mul(make_float2(s, s), make_float2(wx0, fx));
+  const float2 wy = make_float2(wy0, fy), wz = make_float2(wz0, fz), M = make_float2(12582912.0f, 12582912.0f);
+  const float2 b0 = f2_mul(make_float2(a.x, a.x), wy), b1 = f2_mul(make_float2(a.y, a.y), wy);
+  const float2 r01 = f2_fma(make_float2(b0.x, b0.x), wz, M), r23 = f2_fma(make_float2(b0.y, b0.y), wz, M);
+  const float2 r45 = f2_fma(make_float2(b1.x, b1.x), wz, M), r67 = f2_fma(make_float2(b1.y, b1.y), wz, M);
+  r[0] = __float_as_uint(r01.x); r[1] = __float_as_uint(r01.y);
+  r[2] = __float_as_uint(r23.x); r[3] = __float_as_uint(r23.y);
+  r[4] = __float_as_uint(r45.x); r[5] = __float_as_uint(r45.y);
+  r[6] = __float_as_uint(r67.x); r[7] = __float_as_uint(r67.y);
+}
+
 // Corner contributions of a particle whose mass exceeds 2^22 quanta.
 __device__ __forceinline__ void cic_q_large(float mm, float fx, float fy, float fz, float qscale, long long (&q)[8]) {
   const float wx[2] = {__fsub_rn(1.0f, fx), fx};
   const float wy[2] = {__fsub_rn(1.0f, fy), fy};
   const float wz[2] = {__fsub_rn(1.0f, fz), fz};
+  const int qk = pow2_exponent(qscale);
 #pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const float w = __fmul_rn(__fmul_rn(__fmul_rn(mm, wx[c >> 2]), wy[(c >> 1) & 1]), wz[c & 1]);
-    q[c] = f32_to_i64_rn(__fmul_rn(w, qscale));
-  }
+  for (int c = 0; c < 8; ++c)
+    q[c] = prod_to_i64_rn(__fmul_rn(__fmul_rn(mm, wx[c >> 2]), wy[(c >> 1) & 1]), wz[c & 1], qk);
 }
 
 // Add 8 corner values to the int64 grid, dropping corners outside it.
@@ -327,17 +398,8 @@ __device__ __forceinline__ void dep_warp_pass(const float (&px)[NJ], const float
     const bool ok = inr && small;
     const float s = ok ? mmq : 0.0f;
     const float wx0 = __fsub_rn(1.0f, fx), wy0 = __fsub_rn(1.0f, fy), wz0 = __fsub_rn(1.0f, fz);
-    const float a0 = __fmul_rn(s, wx0), a1 = __fmul_rn(s, fx);
-    const float b00 = __fmul_rn(a0, wy0), b01 = __fmul_rn(a0, fy), b10 = __fmul_rn(a1, wy0), b11 = __fmul_rn(a1, fy);
     unsigned r[8];
-    r[0] = __float_as_uint(__fadd_rn(__fmul_rn(b00, wz0), 12582912.0f));
-    r[1] = __float_as_uint(__fadd_rn(__fmul_rn(b00, fz), 12582912.0f));
-    r[2] = __float_as_uint(__fadd_rn(__fmul_rn(b01, wz0), 12582912.0f));
-    r[3] = __float_as_uint(__fadd_rn(__fmul_rn(b01, fz), 12582912.0f));
-    r[4] = __float_as_uint(__fadd_rn(__fmul_rn(b10, wz0), 12582912.0f));
-    r[5] = __float_as_uint(__fadd_rn(__fmul_rn(b10, fz), 12582912.0f));
-    r[6] = __float_as_uint(__fadd_rn(__fmul_rn(b11, wz0), 12582912.0f));
-    r[7] = __float_as_uint(__fadd_rn(__fmul_rn(b11, fz), 12582912.0f));
+    dep_corners(s, wx0, fx, wy0, fy, wz0, fz, r);
     const unsigned key = ok ? (unsigned)(((ix + 1) * G1 + (iy + 1)) * G1 + (iz + 1)) : DEP_NONE;
     const unsigned kA = __shfl_sync(0xffffffffu, key, 0), kB = __shfl_sync(0xffffffffu, key, 31);
     const bool inA = key == kA, inB = key == kB;
@@ -405,17 +467,11 @@ __device__ __forceinline__ void dep_warp_runs(const float (&px)[NJ], const float
     const bool ok = inr && small;
     const float s = ok ? mmq : 0.0f;
     const float wx0 = __fsub_rn(1.0f, fx), wy0 = __fsub_rn(1.0f, fy), wz0 = __fsub_rn(1.0f, fz);
-    const float a0 = __fmul_rn(s, wx0), a1 = __fmul_rn(s, fx);
-    const float b00 = __fmul_rn(a0, wy0), b01 = __fmul_rn(a0, fy), b10 = __fmul_rn(a1, wy0), b11 = __fmul_rn(a1, fy);
+    unsigned r[8];
+    dep_corners(s, wx0, fx, wy0, fy, wz0, fz, r);
     int v[8];
-    v[0] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b00, wz0), 12582912.0f)) - DEP_BIAS);
-    v[1] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b00, fz), 12582912.0f)) - DEP_BIAS);
-    v[2] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b01, wz0), 12582912.0f)) - DEP_BIAS);
-    v[3] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b01, fz), 12582912.0f)) - DEP_BIAS);
-    v[4] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b10, wz0), 12582912.0f)) - DEP_BIAS);
-    v[5] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b10, fz), 12582912.0f)) - DEP_BIAS);
-    v[6] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b11, wz0), 12582912.0f)) - DEP_BIAS);
-    v[7] = (int)(__float_as_uint(__fadd_rn(__fmul_rn(b11, fz), 12582912.0f)) - DEP_BIAS);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v[c] = (int)(r[c] - DEP_BIAS);
     const unsigned key = ok ? (unsigned)(((ix + 1) * G1 + (iy + 1)) * G1 + (iz + 1)) : DEP_NONE;
     // the lane's node in the box (unsigned: a lane without a key may hold any cell)
     const int bo = (int)((((unsigned)ix - (unsigned)bx.x0) * (unsigned)bx.ny + ((unsigned)iy - (unsigned)bx.y0)) *
@@ -457,6 +513,31 @@ __device__ __forceinline__ void dep_warp_runs(const float (&px)[NJ], const float
     for (int c = 0; c < 8; ++c) t[c] = __reduce_add_sync(0xffffffffu, acc[c]);
     if (lane == 0) dep_put<true>(Kbo, bx, nullptr, d.G, 0, 0, 0, t);
   }
+}
+
+// The warp's particles straight into the grid (a tile whose cells do not fit the
+// box): out of line, reloading the particles, so that the registers of the box
+// path are not shaped by this rare one. Returns the `large` bits.
+template <bool POW2>
+__device__ __noinline__ unsigned dep_warp_direct(const float *__restrict__ x, const float *__restrict__ y,
+                                                 const float *__restrict__ z, const float *__restrict__ m, long long wb,
+                                                 long long nrem, const DepCtx d, float inv_dx, float qscale,
+                                                 long long *__restrict__ qg, unsigned *__restrict__ status, int lane) {
+  float px[DEP_PER], py[DEP_PER], pz[DEP_PER], pm[DEP_PER];
+#pragma unroll
+  for (int j = 0; j < DEP_PER; ++j) {
+    if (32 * j < nrem) {
+      px[j] = __ldg(x + wb + 32 * j); py[j] = __ldg(y + wb + 32 * j); pz[j] = __ldg(z + wb + 32 * j);
+      pm[j] = __ldg(m + wb + 32 * j);
+    } else {
+      px[j] = py[j] = pz[j] = __int_as_float(0x7fc00000);
+      pm[j] = 0.0f;
+    }
+  }
+  DepBox bx = {};
+  unsigned large = 0;
+  dep_warp_pass<POW2, false>(px, py, pz, pm, nrem, d, inv_dx, qscale, bx, qg, status, lane, large);
+  return large;
 }
 
 template <bool POW2>
@@ -529,7 +610,7 @@ __global__ void __launch_bounds__(256, 4)
     if (use_box)
       dep_warp_runs<POW2>(px, py, pz, pm, nrem, d, inv_dx, qscale, bx, status, lane, large);
     else
-      dep_warp_pass<POW2, false>(px, py, pz, pm, nrem, d, inv_dx, qscale, bx, qg, status, lane, large);
+      large = dep_warp_direct<POW2>(x, y, z, m, wb, nrem, d, inv_dx, qscale, qg, status, lane);
     while (large) {  // rare: point masses
       const int j = __ffs(large) - 1;
       large &= large - 1;

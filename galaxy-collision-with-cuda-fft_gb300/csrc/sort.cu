@@ -8,6 +8,8 @@
 // order and the permutation is unique.
 #include "common.cuh"
 
+#include <cmath>
+
 #define RS_BITS 8
 #define RS_RADIX 256
 #define RS_THREADS 256
@@ -344,9 +346,39 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Cell keys of the positions predicted tau ahead, x + v tau (f32, rounded per
+// operation), or of the current position when the predicted one deposits
+// nothing (or v is not finite). Sorting by these keys puts the particles in the
+// order of their cells at the middle of the next sort period, so that the
+// deposit and gather passes see them drift by half as much.
+__global__ void __launch_bounds__(256)
+    k_cell_keys_ahead(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
+                      const float *__restrict__ vx, const float *__restrict__ vy, const float *__restrict__ vz,
+                      float tau, long long n, float dx, int G, uint32_t *__restrict__ keys,
+                      uint32_t *__restrict__ iota) {
+  const uint32_t g1 = (uint32_t)(G + 1), sentinel = g1 * g1 * g1;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const float px = x[p], py = y[p], pz = z[p];
+    CellPos c;
+    uint32_t key = sentinel;
+    if (gc_cell_of(__fadd_rn(px, __fmul_rn(vx[p], tau)), __fadd_rn(py, __fmul_rn(vy[p], tau)),
+                   __fadd_rn(pz, __fmul_rn(vz[p], tau)), dx, G, c) ||
+        gc_cell_of(px, py, pz, dx, G, c))
+      key = ((uint32_t)(c.ix + 1) * g1 + (uint32_t)(c.iy + 1)) * g1 + (uint32_t)(c.iz + 1);
+    keys[p] = key;
+    iota[p] = (uint32_t)p;
+  }
+}
+
 extern "C" int gc_pm_sort(gc_ctx *ctx, const gc_particles *in, const gc_particles *out) {
+  return gc_pm_sort_ahead(ctx, in, out, 0.0f);
+}
+
+extern "C" int gc_pm_sort_ahead(gc_ctx *ctx, const gc_particles *in, const gc_particles *out, float tau) {
   if (!ctx) return GC_ERR_ARG;
   GC_REQUIRE(ctx, in && out, "gc_pm_sort: NULL particle set");
+  GC_REQUIRE(ctx, std::isfinite(tau), "gc_pm_sort_ahead: tau must be finite, got %g", (double)tau);
+  GC_REQUIRE(ctx, tau == 0.0f || (in->vx && in->vy && in->vz), "gc_pm_sort_ahead: velocities required for tau != 0");
   const int64_t n = in->n;
   GC_REQUIRE(ctx, n >= 0 && n < (1LL << 31), "particle count out of range");
   GC_REQUIRE(ctx, out->n == n, "gc_pm_sort: in and out sizes differ");
@@ -356,8 +388,12 @@ extern "C" int gc_pm_sort(gc_ctx *ctx, const gc_particles *in, const gc_particle
   if (s) return s;
   unsigned nb = gc_blocks(n, 256);
   if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
-  gc_launch(ctx, GK_KEYS, k_cell_keys, dim3(nb), dim3(256), 0, in->x, in->y, in->z, (long long)n, (float)ctx->dx, ctx->G, ctx->keys2,
-                                           ctx->vals2);
+  if (tau == 0.0f)
+    gc_launch(ctx, GK_KEYS, k_cell_keys, dim3(nb), dim3(256), 0, in->x, in->y, in->z, (long long)n, (float)ctx->dx,
+              ctx->G, ctx->keys2, ctx->vals2);
+  else
+    gc_launch(ctx, GK_KEYS, k_cell_keys_ahead, dim3(nb), dim3(256), 0, in->x, in->y, in->z, in->vx, in->vy, in->vz,
+              tau, (long long)n, (float)ctx->dx, ctx->G, ctx->keys2, ctx->vals2);
   GC_LAUNCH_CHECK(ctx, "cell keys");
   uint32_t *ko, *vo;
   if ((s = gc_radix_sort_pairs(ctx, ctx->keys2, ctx->vals2, n, key_bits(ctx->G), &ko, &vo))) return s;

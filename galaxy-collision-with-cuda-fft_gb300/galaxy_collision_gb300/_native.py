@@ -140,6 +140,7 @@ _PROTOS = {
     "gc_splat_points": (C.c_int, [_ctxp, _vp, _vp, _i64, C.POINTER(C.c_float), C.c_int, C.c_int, C.c_float,
                                   C.POINTER(C.c_float), _vp, _vp]),
     "gc_pm_sort": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(Particles)]),
+    "gc_pm_sort_ahead": (C.c_int, [_ctxp, C.POINTER(Particles), C.POINTER(Particles), C.c_float]),
     "gc_pm_reserve": (C.c_int, [_ctxp, _i64]),
     "gc_pm_import": (C.c_int, [_ctxp, _vp, _vp, _vp, _vp, C.POINTER(C.c_double), C.POINTER(Particles)]),
     "gc_pm_import_sorted": (C.c_int, [_ctxp, _vp, _vp, _vp, _vp, C.POINTER(C.c_double), C.POINTER(Particles)]),

@@ -41,7 +41,8 @@ class PMEngine:
     def __init__(self, grid_size: int, dx: float, grav: float = 1.0, *, origin=(0.0, 0.0, 0.0), tol: float = 1e-6,
                  max_cycles: int = 50, pre_sweeps: int = 2, post_sweeps: int = 2, coarse_sweeps: int = 40,
                  fixed_point_bits: int = 52, sort_every: int = 20, grad_grid: bool = True, fixed_cycles: int = 0,
-                 max_particles: int = 0, deposit_next: bool = False, plain_f32: bool = False):
+                 max_particles: int = 0, deposit_next: bool = False, plain_f32: bool = False,
+                 sort_ahead: float | None = None):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
         self.grav = float(grav)
@@ -66,6 +67,11 @@ class PMEngine:
             self.mg.min_cycles = self.fixed_cycles
         self.fixed_point_bits = int(fixed_point_bits)
         self.sort_every = int(sort_every)
+        # the periodic sort orders the particles by their cells predicted
+        # sort_ahead steps later (x + v * sort_ahead * dt; default half the sort
+        # period, so that they drift from their sorted cells by half as much);
+        # 0: by the current cells
+        self.sort_ahead = self.sort_every / 2.0 if sort_ahead is None else float(sort_ahead)
         self.grad_grid = bool(grad_grid)  # gather from a float4 -grad(phi) grid (same results)
         # the particle pass deposits the drifted positions for the next step (same
         # density, one pass fewer); off by default: at 100M particles on GB300 the
@@ -264,10 +270,12 @@ class PMEngine:
         p.n = self.n
         return p
 
-    def sort(self) -> None:
-        """Stable cell-key sort of all particle arrays (ping-pong buffers)."""
+    def sort(self, dt: float | None = None) -> None:
+        """Stable cell-key sort of all particle arrays (ping-pong buffers), by
+        the cells predicted sort_ahead steps of dt later when both are set."""
         a, b = self._struct(self.cur), self._struct(self.alt)
-        self.ctx.call("gc_pm_sort", C.byref(a), C.byref(b), what="gc_pm_sort")
+        tau = self.sort_ahead * float(dt) if dt else 0.0
+        self.ctx.call("gc_pm_sort_ahead", C.byref(a), C.byref(b), C.c_float(tau), what="gc_pm_sort_ahead")
         self.cur, self.alt = self.alt, self.cur
         self.steps_since_sort = 0
 
@@ -319,7 +327,7 @@ class PMEngine:
         if self.state != "open":
             raise RuntimeError("advance needs an open (primed) engine")
         if self.sort_every > 0 and self.steps_since_sort >= self.sort_every:
-            self.sort()
+            self.sort(dt)
         r = self._step(_native.GC_STEP_ADVANCE, dt, diagnostics)
         self.steps_since_sort += 1
         return r
@@ -387,7 +395,7 @@ class PMEngine:
         if self.state != "open":
             raise RuntimeError("advance_graph needs an open (primed) engine")
         if self.sort_every > 0 and self.steps_since_sort >= self.sort_every:
-            self.sort()
+            self.sort(dt)
         key = (self.cur["x"].data_ptr(), float(dt))
         main = torch.cuda.current_stream()
         gs = self._graph_stream()

@@ -90,7 +90,7 @@ class Ensemble:
         main = torch.cuda.current_stream()
         if self.sort_every > 0 and self.steps_since_sort >= self.sort_every:
             for e in self.engines:
-                e.sort()
+                e.sort(self.dt)
             self.steps_since_sort = 0
         ready = torch.cuda.Event()
         ready.record(main)

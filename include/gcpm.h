@@ -333,6 +333,13 @@ int gc_splat_points(gc_ctx *ctx, const float *pos, const float *col, int64_t m, 
  * (every non-NULL array of in is permuted into the matching array of out). */
 int gc_pm_sort(gc_ctx *ctx, const gc_particles *in, const gc_particles *out);
 
+/* gc_pm_sort by the cells of the positions predicted tau ahead, x + v*tau (f32,
+ * rounded per operation; the current cell where the predicted position
+ * deposits nothing). With tau = half the time to the next sort the deposit and
+ * gather passes see the particles drift from their sorted cells by half as
+ * much. tau = 0 is gc_pm_sort; tau != 0 needs the velocities. */
+int gc_pm_sort_ahead(gc_ctx *ctx, const gc_particles *in, const gc_particles *out, float tau);
+
 /* Allocate the sort scratch of the context for n particles now (keys, values,
  * digit histograms), so that the first gc_pm_sort allocates nothing. Optional. */
 int gc_pm_reserve(gc_ctx *ctx, int64_t n);

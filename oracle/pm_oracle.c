@@ -142,9 +142,23 @@ void or_deposit_f64(const float *x, const float *y, const float *z, const float 
   }
 }
 
+/* The partial products b = (mm*wx)*wy (f32, the reference's order) of the
+ * four (cx,cy) corner columns, and the z weights. */
+static inline void contrib_cols(const cellpos *c, float mm, float b[4], float wz[2]) {
+  const float wx[2] = {1.0f - c->fx, c->fx};
+  const float wy[2] = {1.0f - c->fy, c->fy};
+  wz[0] = 1.0f - c->fz;
+  wz[1] = c->fz;
+  for (int a = 0; a < 2; ++a)
+    for (int e = 0; e < 2; ++e) b[a * 2 + e] = (mm * wx[a]) * wy[e];
+}
+
 /* Fixed-point deposit with the GPU library's quantum: E = exponent(S) - bits,
- * S = sum of m/dx^3 (frexp exponent), each contribution rounded to nearest
- * multiple of 2^E, summed in int64, rho = f32(q) * 2^E. Returns E. */
+ * S = sum of m/dx^3 (frexp exponent). Each corner contribution is the exact
+ * product b*wz of the f32 partial product b = (m/dx^3*wx)*wy and the z weight,
+ * rounded once to the nearest multiple of 2^E (ties to even; the product of two
+ * f32 values is exact in f64, so llrint of it rounds exactly), summed in int64,
+ * rho = f32(q) * 2^E. Returns E. */
 int or_deposit_fixed(const float *x, const float *y, const float *z, const float *m, int64_t n, float dx, int G,
                      int bits, float *rho, int64_t *q) {
   const size_t g3 = (size_t)G * G * G;
@@ -184,12 +198,12 @@ int or_deposit_fixed(const float *x, const float *y, const float *z, const float
   for (int64_t p = 0; p < n; ++p) {
     cellpos c;
     if (!cell_of(x[p], y[p], z[p], dx, G, &c)) continue;
-    float w[8];
-    contribs(&c, m[p] * inv_vol, w);
+    float b[4], wz[2];
+    contrib_cols(&c, m[p] * inv_vol, b, wz);
     for (int t = 0; t < 8; ++t) {
       const int jx = c.ix + (t >> 2), jy = c.iy + ((t >> 1) & 1), jz = c.iz + (t & 1);
       if (jx >= 0 && jx < G && jy >= 0 && jy < G && jz >= 0 && jz < G)
-        q[IDX(jx, jy, jz, G)] += (int64_t)llrintf(w[t] * qscale);
+        q[IDX(jx, jy, jz, G)] += (int64_t)llrint((double)b[t >> 1] * (double)wz[t & 1] * (double)qscale);
     }
   }
   const float qinv = ldexpf(1.0f, E);

@@ -103,6 +103,38 @@ def test_pm_sort_permutes_all_arrays(cuda):
     np.testing.assert_array_equal(cur["gid"], gid[perm])
 
 
+def test_pm_sort_ahead_orders_by_predicted_cells(cuda):
+    """gc_pm_sort_ahead: keys of x + v*tau (f32, rounded per operation), the
+    current cell where the predicted position deposits nothing; stable."""
+    from galaxy_collision_gb300.engine import PMEngine
+
+    G, dx, n, dt = 32, 1.0, 30001, 0.1
+    rng = np.random.default_rng(8)
+    pos = rng.uniform(-1, G, size=(n, 3)).astype(np.float32)
+    vel = rng.normal(scale=4.0, size=(n, 3)).astype(np.float32)
+    vel[:5] = [[np.nan, 0, 0], [np.inf, 0, 0], [0, -np.inf, 0], [1e30, 0, 0], [0, 0, -40.0]]
+    mass = rng.uniform(0.5, 1.5, size=n).astype(np.float32)
+    eng = PMEngine(G, dx, sort_every=0, sort_ahead=5.0)
+    eng.load(pos, vel, mass, None, sort=False)
+    eng.sort(dt)
+    tau = np.float32(5.0 * dt)
+    with np.errstate(invalid="ignore", over="ignore"):
+        ahead = pos + vel * tau
+    k_ahead, k_now = pm.cell_keys(ahead, dx, G), pm.cell_keys(pos, dx, G)
+    keys = np.where(k_ahead != (G + 1) ** 3, k_ahead, k_now)
+    assert (keys != k_now).mean() > 0.5
+    perm = pm.stable_sort_perm(keys)
+    cur = {k: v.cpu().numpy() for k, v in eng.cur.items() if not k.startswith("_")}
+    np.testing.assert_array_equal(cur["pid"], perm.astype(np.int32))
+    np.testing.assert_array_equal(cur["y"], pos[perm, 1])
+    np.testing.assert_array_equal(cur["vx"], vel[perm, 0])
+    # tau = 0 is the plain cell sort
+    eng0 = PMEngine(G, dx, sort_every=0)
+    eng0.load(pos, vel, mass, None, sort=False)
+    eng0.sort(dt)
+    np.testing.assert_array_equal(eng0.cur["pid"].cpu().numpy(), pm.stable_sort_perm(k_now).astype(np.int32))
+
+
 @pytest.mark.parametrize("G,dx,bits", [(16, 1.0, 52), (48, 0.375, 52), (64, 2.5, 40), (33, 1.0, 56)])
 def test_deposit_bit_exact_vs_fixed_point_oracle(cuda, G, dx, bits):
     from galaxy_collision_gb300.data import Field
