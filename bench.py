@@ -63,7 +63,7 @@ ALGO_BYTES = {
 }
 # Kernels of the Poisson solve (the multigrid, its faces and norms, and the b0 conversion).
 MG_KERNELS = ("smooth0", "update0", "resid0", "resid0e", "restrict", "smooth", "resid", "prolong", "prolong0",
-              "tail", "faces", "reduce", "convert_q")
+              "coarse", "tail", "faces", "moments", "rhs", "reduce", "convert_q")
 
 
 def _parse(argv=None):

@@ -33,7 +33,7 @@ BOX, GRID, DT = 64.0, 256, 0.005
 
 # kernels of one solve: the multigrid, its faces, norms and b0 conversion, and the initial guess
 SOLVE_KERNELS = ("smooth0", "update0", "resid0", "resid0e", "restrict", "smooth", "resid", "prolong", "prolong0",
-                 "tail", "faces", "reduce", "convert_q", "warmstart")
+                 "coarse", "tail", "faces", "moments", "rhs", "reduce", "convert_q", "warmstart")
 
 
 def random_collision(rng: np.random.Generator, n: int, dx: float = BOX / GRID) -> ic.ICResult:
