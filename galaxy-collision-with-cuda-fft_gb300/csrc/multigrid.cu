@@ -1345,6 +1345,12 @@ __global__ void __launch_bounds__(256) k_sumsq(const float *__restrict__ a, size
   block_sum_f32(acc, parts + blockIdx.x);
 }
 
+// Zero the interior nodes 1 .. G-2 of a G^3 array (node_grid launch shape).
+__global__ void __launch_bounds__(256) k_zero_interior(float *__restrict__ a, int G) {
+  const int k = blockIdx.x * 32 + threadIdx.x + 1, j = blockIdx.y * 8 + threadIdx.y + 1, i = blockIdx.z + 1;
+  if (k <= G - 2 && j <= G - 2) a[((size_t)i * G + j) * G + k] = 0.0f;
+}
+
 __global__ void k_copy_hi_to(const float *__restrict__ hi, float *__restrict__ out, size_t n) {
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
     out[t] = hi[t];
@@ -1885,13 +1891,19 @@ extern "C" int gc_mg_solve(gc_ctx *ctx, const float *rho, float *phi, int warm_s
     if ((s = finalize_to(ctx, nb, 1, GC_S_BNORM2))) return s;
   }
   // initial guess (multigrid.py:464-467): previous phi or zero; the lo part starts at zero
-  if (warm_start) {
+  if (p.flags & GC_MG_FACES_GIVEN) {  // faces (and the guess) from phi
+    GC_CUDA(ctx, cudaMemcpyAsync(ctx->hi, phi, g3 * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+    if (!warm_start && ctx->nlev > 0) {
+      gc_launch(ctx, GK_COPY, k_zero_interior, dim3(node_grid(ctx->lev[0])), dim3(32, 8), 0, ctx->hi, ctx->G);
+      GC_LAUNCH_CHECK(ctx, "zero interior");
+    }
+  } else if (warm_start) {
     GC_CUDA(ctx, cudaMemcpyAsync(ctx->hi, phi, g3 * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
   } else {
     GC_CUDA(ctx, cudaMemsetAsync(ctx->hi, 0, g3 * sizeof(float), ctx->stream));
   }
   GC_CUDA(ctx, cudaMemsetAsync(ctx->lo, 0, g3 * sizeof(float), ctx->stream));
-  if ((s = gc_faces_from_moments(ctx))) return s;
+  if (!(p.flags & GC_MG_FACES_GIVEN) && (s = gc_faces_from_moments(ctx))) return s;
   if ((s = gc_mg_run(ctx, &p, stats))) return s;
   // phi = f32(hi + lo) == hi (the pair is normalised)
   gc_launch(ctx, GK_COPY, k_copy_hi_to, dim3(1024), dim3(256), 0, ctx->hi, phi, g3);

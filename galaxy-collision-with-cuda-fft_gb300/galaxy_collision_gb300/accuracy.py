@@ -15,6 +15,11 @@ positions) this measures, on the device:
 * ``phi_vs_converged`` / ``force_vs_converged`` -- the same against the
   multigrid driven to a 1e-10 relative residual on the same density: the error
   that stopping at the working tolerance leaves.
+* ``phi_isolated_vs_lattice`` / ``force_isolated_vs_lattice`` -- the multigrid
+  with the isolated boundary (``boundary="isolated"``: James's method, faces
+  from the lattice Green's function) at the engine's working tolerance, against
+  the lattice-Green solution: the solver's error alone, without the multipole
+  boundary's.
 
 Forces are -grad(phi) (deposit.py:132-174) CIC-gathered at every particle
 (deposit.py:85-129); the error is ||a - a_ref||_2 / ||a_ref||_2 over all
@@ -48,7 +53,7 @@ def _forces(parts, phi: torch.Tensor, dx: float):
 
 
 def force_chain_errors(eng, *, pad_factor: int = 2, converged_tol: float = 1e-10, with_fft: bool = True,
-                       with_lattice: bool = True, solvers: dict | None = None) -> dict:
+                       with_lattice: bool = True, with_isolated: bool = True, solvers: dict | None = None) -> dict:
     """Relative-L2 errors of the engine's current potential and particle forces."""
     from galaxy_collision_gb300.solver import make_solver
 
@@ -90,6 +95,16 @@ def force_chain_errors(eng, *, pad_factor: int = 2, converged_tol: float = 1e-10
             torch.cuda.empty_cache()
         a_f = _forces(parts, phi_f, dx)
         out[f"force_vs_{key}"] = _rel_l2(a, a_f)
+        if key == "lattice" and with_isolated and pad_factor == 2:
+            iso = make_solver("multigrid", G, dx=dx, grav_constant=eng.grav, tol=float(eng.mg.tol), n_cycles=80,
+                              boundary="isolated")
+            iso._lattice = cache.get("lattice")  # the kernel transform, when kept
+            phi_i = torch.zeros_like(phi)
+            iso.solve(rho, phi_i)
+            out["isolated_cycles"] = [int(iso.last_stats["cycles_zero_faces"]), int(iso.last_cycles)]
+            out["phi_isolated_vs_lattice"] = _rel_l2(phi_i, phi_f)
+            out["force_isolated_vs_lattice"] = _rel_l2(_forces(parts, phi_i, dx), a_f)
+            del iso, phi_i
         del phi_f, a_f
         out["fft_grid"] = pad_factor * G
     return out

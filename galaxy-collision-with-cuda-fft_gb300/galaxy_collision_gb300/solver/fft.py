@@ -61,9 +61,13 @@ class FFTPoissonSolver(PoissonSolver):
         return self._greens_ft
 
     def potential64(self, rho) -> torch.Tensor:
-        """The FP64 potential (G^3) of rho, without rounding to f32."""
+        """The FP64 potential (G^3) of rho (f32, or an FP64 CUDA tensor), without
+        rounding to f32."""
         n, m = self.grid_size, self.pad
-        r = as_tensor(rho, shape=(n, n, n), name="rho")
+        if isinstance(rho, torch.Tensor) and rho.dtype == torch.float64:
+            r = as_tensor(rho, dtype=torch.float64, shape=(n, n, n), name="rho")
+        else:
+            r = as_tensor(rho, shape=(n, n, n), name="rho")
         padded = torch.zeros((m, m, m), dtype=torch.float64, device=r.device)
         padded[:n, :n, :n] = r.to(torch.float64)
         spec = torch.fft.rfftn(padded) * self._green(r.device)

@@ -10,6 +10,16 @@ is solved (see ``csrc/multigrid.cu``): Shortley-Weller coarse levels that
 converge at ~0.1 per V-cycle instead of the reference's ~0.6, a double-float
 finest level so the residual can go below the FP32 floor, device-side moments
 and norms, and an FP64 coarsest solve.
+
+``boundary="isolated"`` (an addition) replaces the multipole faces by the exact
+free-space boundary values of the discrete problem, by James's method: solve
+with zero faces (phi0), take the screening charge phi0 leaves on the boundary
+nodes (the 7-point Laplacian of phi0 continued by zero there: the sum of its
+interior neighbours), evaluate its potential and that of rho's own boundary
+nodes on the faces with the lattice Green's function of the 7-point stencil
+(the FP64 zero-padded FFT convolution of ``FFTPoissonSolver(green="lattice")``),
+and solve again with those faces. The result is the free-space solution of the
+7-point problem (the lattice-Green potential) up to the solver tolerance.
 """
 
 from __future__ import annotations
@@ -38,6 +48,7 @@ class MultigridPoissonSolver(PoissonSolver):
         *,
         plain_f32: bool = False,
         natural_layout: bool = False,
+        boundary: str = "multipole",
     ):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
@@ -57,6 +68,10 @@ class MultigridPoissonSolver(PoissonSolver):
         # natural_layout: validation path, the finest correction in natural
         # layout through the generic level kernels (identical potentials)
         self.natural_layout = bool(natural_layout)
+        if boundary not in ("multipole", "isolated"):
+            raise ValueError(f"unknown boundary {boundary!r} (expected 'multipole' or 'isolated')")
+        self.boundary = boundary
+        self._lattice = None
         self._ctx = _native.Context(self.grid_size, self.dx, self.G)
         self.sizes = [n for (n, _J, _p) in self._ctx.levels()]
 
@@ -76,7 +91,59 @@ class MultigridPoissonSolver(PoissonSolver):
         G = self.grid_size
         r = as_tensor(rho, shape=(G, G, G), name="rho")
         f = as_tensor(phi, shape=(G, G, G), name="phi")
+        if self.boundary == "isolated":
+            self._solve_isolated(r, f)
+            return
+        self._solve(r, f, warm_start, self._params())
+
+    def isolated_faces(self, rho, phi0):
+        """The free-space potential of rho on the boundary nodes (FP64, G^3 with
+        the interior zero), from phi0, the solution with zero faces."""
+        import torch
+
+        from galaxy_collision_gb300.solver.fft import FFTPoissonSolver
+
+        G = self.grid_size
+        if self._lattice is None:
+            self._lattice = FFTPoissonSolver(G, dx=self.dx, grav_constant=self.G, green="lattice")
+        p0 = phi0.to(torch.float64)
+        # screening charge: L phi0 on the boundary nodes, phi0 continued by zero
+        s = torch.zeros_like(p0)
+        s[0, 1:-1, 1:-1] = p0[1, 1:-1, 1:-1]
+        s[-1, 1:-1, 1:-1] = p0[-2, 1:-1, 1:-1]
+        s[1:-1, 0, 1:-1] = p0[1:-1, 1, 1:-1]
+        s[1:-1, -1, 1:-1] = p0[1:-1, -2, 1:-1]
+        s[1:-1, 1:-1, 0] = p0[1:-1, 1:-1, 1]
+        s[1:-1, 1:-1, -1] = p0[1:-1, 1:-1, -2]
+        # phi_free = phi0 + g * s on Z^3 (L g = -delta); FFTPoissonSolver(lattice)
+        # returns -4 pi G dx^2 (g * src), so s enters as -s / (4 pi G dx^2); the
+        # boundary nodes' own mass (which the interior equations never see) as is
+        src = -s / (4.0 * 3.141592653589793 * self.G * self.dx**2)
+        rb = rho.to(torch.float64)
+        src[0] += rb[0]
+        src[-1] += rb[-1]
+        src[1:-1, 0] += rb[1:-1, 0]
+        src[1:-1, -1] += rb[1:-1, -1]
+        src[1:-1, 1:-1, 0] += rb[1:-1, 1:-1, 0]
+        src[1:-1, 1:-1, -1] += rb[1:-1, 1:-1, -1]
+        faces = self._lattice.potential64(src)
+        faces[1:-1, 1:-1, 1:-1] = 0.0
+        return faces
+
+    def _solve_isolated(self, r, f) -> None:
         p = self._params()
+        p.flags |= _native.GC_MG_FACES_GIVEN
+        f.zero_()
+        self._solve(r, f, False, p)  # phi0: zero faces
+        cycles0 = self.last_cycles
+        faces = self.isolated_faces(r, f)
+        interior = f[1:-1, 1:-1, 1:-1].clone()
+        f.copy_(faces.to(f.dtype))
+        f[1:-1, 1:-1, 1:-1] = interior  # phi0 as the initial guess
+        self._solve(r, f, True, p)
+        self.last_stats["cycles_zero_faces"] = cycles0
+
+    def _solve(self, r, f, warm_start: bool, p) -> None:
         st = _native.MGStats()
         self._ctx.call("gc_mg_solve", r.data_ptr(), f.data_ptr(), int(bool(warm_start)), C.byref(p), C.byref(st),
                        what="MultigridPoissonSolver.solve")

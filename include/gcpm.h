@@ -66,6 +66,12 @@ enum gc_status_code {
  * level kernels instead of the colour-split half-sweeps; the potential is
  * identical bit for bit, it just moves more bytes. */
 #define GC_MG_NATURAL_LAYOUT 0x8
+/* gc_mg_params.flags (gc_mg_solve): the Dirichlet face values are the boundary
+ * nodes of phi as passed, instead of the multipole faces from the moments of
+ * rho (multigrid.py:261-295); phi's interior is the initial guess when
+ * warm_start, else zero. With faces from a free-space (lattice Green's function)
+ * evaluation this is the isolated-boundary solve of James's method. */
+#define GC_MG_FACES_GIVEN 0x10
 
 typedef struct gc_ctx gc_ctx;
 

@@ -35,13 +35,12 @@ def test_lattice_fft_solver_matches_oracle(cuda):
         make_solver("fft", n, dx=dx, green="spectral")
 
 
-def test_multigrid_force_error_splits_into_boundary_and_discretisation(cuda):
+def _two_disk_128():
     from galaxy_collision_gb300 import ic
     from galaxy_collision_gb300.deposit import deposit_density, gather_acceleration, potential_to_accel
-    from galaxy_collision_gb300.solver import make_solver
     from types import SimpleNamespace
 
-    G, dx, grav = 128, 0.5, 1.0  # the two-disk box [-32, 32]^3 at half the resolution
+    G, dx = 128, 0.5  # the two-disk box [-32, 32]^3 at half the resolution
     icr = ic.two_disk(200000, 300000, seed=1, dx=dx)
     pos = (icr.pos.astype(np.float64) + 32.0).astype(np.float32)
     cols = [torch.from_numpy(np.ascontiguousarray(pos[:, i])).cuda() for i in range(3)]
@@ -57,6 +56,14 @@ def test_multigrid_force_error_splits_into_boundary_and_discretisation(cuda):
         gather_acceleration(parts, *grids, *acc, dx)
         return torch.stack(acc).cpu().numpy().astype(np.float64)
 
+    return G, dx, pos, rho, forces
+
+
+def test_multigrid_force_error_splits_into_boundary_and_discretisation(cuda):
+    from galaxy_collision_gb300.solver import make_solver
+
+    grav = 1.0
+    G, dx, pos, rho, forces = _two_disk_128()
     mg = make_solver("multigrid", G, dx=dx, grav_constant=grav, tol=1e-10, n_cycles=80)
     phi_mg = torch.zeros_like(rho)
     mg.solve(rho, phi_mg)
@@ -72,3 +79,33 @@ def test_multigrid_force_error_splits_into_boundary_and_discretisation(cuda):
     # the oracle's gather of the lattice potential agrees with the GPU chain
     a_or = np.stack(pm.gather(pos, *pm.grad(lat.cpu().numpy().astype(np.float32), dx), dx)).astype(np.float64)
     assert rel_l2(a_lat, a_or) < 1e-6
+
+
+def test_isolated_boundary_multigrid_is_the_lattice_green_solution(cuda):
+    """James's method (zero-face solve, boundary screening charge, faces from the
+    lattice Green's function, second solve) removes the boundary error: the
+    multigrid's forces equal the lattice-Green FFT solution's to the f32
+    rounding of the potentials, well below the multipole faces' error."""
+    from galaxy_collision_gb300.solver import make_solver
+
+    grav = 1.0
+    G, dx, pos, rho, forces = _two_disk_128()
+    lat = make_solver("fft", G, dx=dx, grav_constant=grav, green="lattice").potential64(rho)
+    a_lat = forces(lat.to(torch.float32))
+    iso = make_solver("multigrid", G, dx=dx, grav_constant=grav, tol=1e-10, n_cycles=80, boundary="isolated")
+    phi_iso = torch.zeros_like(rho)
+    iso.solve(rho, phi_iso)
+    assert iso.last_stats["converged"] and iso.last_stats["cycles_zero_faces"] > 0
+    # the potential itself: faces and interior against the FP64 lattice solution
+    ref = lat.cpu().numpy()
+    got = phi_iso.cpu().numpy().astype(np.float64)
+    assert np.abs(got - ref).max() < 1e-6 * np.abs(ref).max()
+    mp = make_solver("multigrid", G, dx=dx, grav_constant=grav, tol=1e-10, n_cycles=80)
+    phi_mp = torch.zeros_like(rho)
+    mp.solve(rho, phi_mp)
+    err_iso = rel_l2(forces(phi_iso), a_lat)
+    err_mp = rel_l2(forces(phi_mp), a_lat)
+    assert err_iso < 1e-5, err_iso
+    assert err_iso < err_mp / 4, (err_iso, err_mp)
+    with pytest.raises(ValueError):
+        make_solver("multigrid", G, dx=dx, boundary="periodic")
