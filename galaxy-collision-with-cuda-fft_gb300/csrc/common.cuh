@@ -43,6 +43,7 @@ enum {
   GC_S_SOLVES = 14,  // device-decided solves since the counters were reset ...
   GC_S_CYC_TOTAL = 15, // ... their V-cycles ...
   GC_S_MAXREL2 = 16, // ... and the largest (||r|| / ||b||)^2 they ended with
+  GC_S_TICKET = 17,  // block ticket of the last-block grid reductions (an unsigned, 0 between them)
   GC_S_FIN_TMP = 128, // [128, 256): chunk partials of gc_finalize
   GC_S_NSLOTS = 256
 };
@@ -79,6 +80,8 @@ struct gc_ctx {
   int coarse_blocks;    // CTAs of the persistent coarse-level launches (0: not sized yet)
   int capturing;        // a gc_pm_graph_create capture is in progress (no host reads, no events)
   cudaStream_t side;    // stream the V-cycle body of a captured solve is recorded on
+  cudaStream_t fork;    // second stream of the engine step (the faces beside the warm-start passes)
+  cudaEvent_t ev_fork, ev_join;  // its fork and join (no timing)
   long long cap_body_launches;  // kernel launches in that body (one V-cycle)
   int nlev;             // multigrid levels (0 = finest)
   int tail;             // first level handled by the single-CTA tail kernel (== nlev if none)
@@ -351,6 +354,55 @@ __device__ __forceinline__ void block_sum_f32(float v, double *out) {
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if (lane == 0) *out = (double)x;
   }
+}
+
+// Last-block finish of a grid reduction of NV values per block, for grids of a
+// few hundred blocks (every block takes a ticket on one counter). Every block
+// has written its NV partials to parts[bid * NV + v] from its thread 0 (and
+// calls this with all its threads); the block that takes the last ticket sums
+// the nparts rows in a fixed order, writes the NV sums to dst[v] and resets
+// the ticket to 0, so the sums do not depend on which block finishes last and
+// no second launch is needed. Thread t adds value v = t mod NV of the rows
+// g, g + P, ... (g = t / NV, P = T / NV threads per value) into eight
+// accumulators; a warp per value then adds the P partials in order. Returns
+// true in the last block.
+template <int NV>
+__device__ bool grid_finish_sum(const double *parts, unsigned nparts, unsigned *ticket, double *dst) {
+  __shared__ bool last_s;
+  __shared__ double part_s[1024];
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthr = blockDim.x * blockDim.y * blockDim.z;
+  const int lane = tid & 31, wid = tid >> 5, nw = (nthr + 31) >> 5;
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();  // this block's partials (written by thread 0) before its ticket
+    last_s = atomicAdd(ticket, 1u) == nparts - 1u;
+  }
+  __syncthreads();
+  if (!last_s) return false;
+  __threadfence();  // every other block's partials after the last ticket
+  const int P = nthr / NV, v = tid % NV, g = tid / NV;
+  double xs[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (g < P) {
+    for (unsigned q0 = (unsigned)g; q0 < nparts; q0 += 8u * (unsigned)P) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const unsigned q = q0 + (unsigned)u * (unsigned)P;
+        if (q < nparts) xs[u] += __ldcg(parts + (size_t)q * NV + v);
+      }
+    }
+  }
+  part_s[tid] = ((xs[0] + xs[1]) + (xs[2] + xs[3])) + ((xs[4] + xs[5]) + (xs[6] + xs[7]));
+  __syncthreads();
+  for (int vv = wid; vv < NV; vv += nw) {
+    double x = 0.0;
+    for (int gg = lane; gg < P; gg += 32) x += part_s[gg * NV + vv];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) dst[vv] = x;
+  }
+  if (tid == 0) *ticket = 0u;
+  __syncthreads();  // dst complete for every thread of the block
+  return true;
 }
 
 // Internals shared between translation units

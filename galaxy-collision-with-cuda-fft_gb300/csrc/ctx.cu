@@ -220,6 +220,9 @@ extern "C" int gc_ctx_destroy(gc_ctx *ctx) {
   cudaFree(ctx->hist); cudaFree(ctx->hist_aux);
   for (int i = 0; i < 2 * ctx->prof.nev_created; ++i) cudaEventDestroy(ctx->prof.ev[i]);
   if (ctx->side) cudaStreamDestroy(ctx->side);
+  if (ctx->fork) cudaStreamDestroy(ctx->fork);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   free(ctx);
   return GC_OK;
 }

@@ -35,9 +35,26 @@ static int pm_solve(gc_ctx *ctx, const gc_particles *p, const gc_step_params *sp
     GC_CUDA(ctx, cudaMemsetAsync(ctx->hi, 0, g3 * sizeof(float), ctx->stream));
     GC_CUDA(ctx, cudaMemsetAsync(ctx->lo, 0, g3 * sizeof(float), ctx->stream));
   }
-  // learned / extrapolated correction of the previous potential, sample recording
+  // The faces (FP64-bound) on the fork stream, beside the learned / extrapolated
+  // correction of the previous potential and the sample recording (bound by
+  // memory, and they leave the face nodes alone); joined before the V-cycles.
+  if (!ctx->fork) {
+    GC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->fork, cudaStreamNonBlocking));
+    GC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+    GC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+  }
+  GC_CUDA(ctx, cudaEventRecord(ctx->ev_fork, ctx->stream));
+  GC_CUDA(ctx, cudaStreamWaitEvent(ctx->fork, ctx->ev_fork, 0));
+  {
+    cudaStream_t main = ctx->stream;
+    ctx->stream = ctx->fork;
+    s = gc_faces_from_moments(ctx);
+    ctx->stream = main;
+    if (s) return s;
+  }
+  GC_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->fork));
   if ((s = gc_ws_pre_solve(ctx, warm, sp->mode))) return s;
-  if ((s = gc_faces_from_moments(ctx))) return s;
+  GC_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
   return gc_mg_run(ctx, &sp->mg, mst);
 }
 

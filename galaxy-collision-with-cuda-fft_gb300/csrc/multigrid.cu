@@ -482,127 +482,136 @@ __device__ __forceinline__ bool grid_barrier(GridBar *gb, unsigned &target, unsi
   return ok_s != 0;
 }
 
-// A phase's nodes are numbered flat (k fastest); thread t of the grid takes
-// nodes t, t + T, t + 2T, ... (T threads) in batches of PB whose loads are all
-// issued before any result is stored, so that a thread has PB independent L2
-// round trips in flight instead of one. Within a phase no node reads a value
-// that the phase writes (a half-sweep reads only the other colour; the
-// residual, restriction and prolongation write other arrays or only the node
-// itself), so deferring the stores changes nothing.
-#define PB 4
-__device__ __forceinline__ unsigned p_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
-__device__ __forceinline__ unsigned p_nthreads() { return gridDim.x * blockDim.x; }
+// A phase deals the rows (i, j), 1 <= i, j <= J, of its level to the grid's
+// warps round robin, PR rows per warp per round, and the lanes of a warp take
+// the nodes k of a row (SK per lane per group of 32 * SK): one division per
+// row instead of per node, coalesced row accesses, and up to PR * SK nodes per
+// lane whose loads are all issued before any result is stored, so that a lane
+// has several independent L2 round trips in flight. Within a phase no node
+// reads a value that the phase writes (a half-sweep reads only the other
+// colour; the residual, restriction and prolongation write other arrays or
+// only the node itself), so deferring the stores changes nothing.
+#define PR 2
+#define SK 2
+__device__ __forceinline__ unsigned p_warp() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+__device__ __forceinline__ unsigned p_nwarps() { return (gridDim.x * blockDim.x) >> 5; }
 
 // One red-black half-sweep of level g (k_smooth's slots and arithmetic): row
 // (i, j) holds the nodes k = 2 kk + ((color + i + j) & 1), kk = 0 .. J/2.
 __device__ void p_smooth(float *__restrict__ e, const float *__restrict__ b, const LevelGeom &g, int color,
                          bool first) {
-  const int J = g.J, n = g.n;
-  const unsigned nkk = (unsigned)(J / 2 + 1), tot = nkk * (unsigned)J * (unsigned)J, T = p_nthreads();
-  for (unsigned base = p_tid(); base < tot; base += PB * T) {
-    float val[PB];
-    size_t at[PB];
-    bool ok[PB];
+  const int J = g.J, n = g.n, nkk = J / 2 + 1;
+  const unsigned rows = (unsigned)J * (unsigned)J, NW = p_nwarps(), lane = threadIdx.x & 31u;
+  for (unsigned r0 = p_warp(); r0 < rows; r0 += PR * NW) {
+    for (int kk0 = 0; kk0 < nkk; kk0 += 32 * SK) {
+      float val[PR][SK];
+      unsigned at[PR][SK];  // coarse levels have < 2^32 nodes
+      bool ok[PR][SK];
 #pragma unroll
-    for (int u = 0; u < PB; ++u) {
-      const unsigned t = base + u * T;
-      ok[u] = false;
-      if (t >= tot) continue;
-      const unsigned kk = t % nkk, row = t / nkk;
-      const int j = (int)(row % (unsigned)J) + 1, i = (int)(row / (unsigned)J) + 1;
-      const int k = 2 * (int)kk + ((color + i + j) & 1);
-      if (k < 1 || k > J) continue;
-      const size_t c = ((size_t)i * n + j) * n + k;
-      float sum, diag;
-      if (first) {  // zero neighbours: the diagonal alone
-        sum = 0.0f;
-        diag = ((i == J ? g.dB : 2.0f) + (j == J ? g.dB : 2.0f)) + (k == J ? g.dB : 2.0f);
-      } else {
-        sw_stencil(e, c, i, j, k, g, sum, diag);
+      for (int u = 0; u < PR; ++u) {
+        const unsigned r = r0 + u * NW;
+        const int i = (int)(r / (unsigned)J) + 1, j = (int)(r % (unsigned)J) + 1;
+        const int par = (color + i + j) & 1;
+#pragma unroll
+        for (int q = 0; q < SK; ++q) {
+          const int k = 2 * (kk0 + (int)lane + 32 * q) + par;
+          ok[u][q] = r < rows && k >= 1 && k <= J;
+          if (!ok[u][q]) continue;
+          const size_t c = ((size_t)i * n + j) * n + k;
+          float sum, diag;
+          if (first) {  // zero neighbours: the diagonal alone
+            sum = 0.0f;
+            diag = ((i == J ? g.dB : 2.0f) + (j == J ? g.dB : 2.0f)) + (k == J ? g.dB : 2.0f);
+          } else {
+            sw_stencil(e, c, i, j, k, g, sum, diag);
+          }
+          val[u][q] = gs_value(sum, b[c], diag);
+          at[u][q] = (unsigned)c;
+        }
       }
-      val[u] = gs_value(sum, b[c], diag);
-      at[u] = c;
-      ok[u] = true;
-    }
 #pragma unroll
-    for (int u = 0; u < PB; ++u)
-      if (ok[u]) e[at[u]] = val[u];
+      for (int u = 0; u < PR; ++u)
+#pragma unroll
+        for (int q = 0; q < SK; ++q)
+          if (ok[u][q]) e[at[u][q]] = val[u][q];
+    }
   }
 }
 
 __device__ void p_zero(float *__restrict__ e, const LevelGeom &g) {
-  const size_t tot = (size_t)g.n * g.n * g.n;
-  for (size_t t = p_tid(); t < tot; t += p_nthreads()) e[t] = 0.0f;
+  const size_t tot = (size_t)g.n * g.n * g.n, T = (size_t)gridDim.x * blockDim.x;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += T) e[t] = 0.0f;
 }
 
-__device__ void p_resid(const float *__restrict__ e, const float *__restrict__ b, float *__restrict__ r,
-                        const LevelGeom &g) {
-  const int J = g.J, n = g.n;
-  const unsigned tot = (unsigned)J * (unsigned)J * (unsigned)J, T = p_nthreads();
-  for (unsigned base = p_tid(); base < tot; base += PB * T) {
-    float val[PB];
-    size_t at[PB];
+// The nodes k = k0 + lane + 32 q (1 <= k <= J) of RR rows per round, for the
+// residual and the prolongation: node(i, j, k, v) returns the node's index in
+// `out` and sets its new value v; all of a lane's values are stored after all
+// of its nodes are computed.
+template <int RR, typename F>
+__device__ __forceinline__ void p_node_rows(int J, float *__restrict__ out, F node) {
+  const unsigned rows = (unsigned)J * (unsigned)J, NW = p_nwarps(), lane = threadIdx.x & 31u;
+  for (unsigned r0 = p_warp(); r0 < rows; r0 += RR * NW) {
+    for (int k0 = 1; k0 <= J; k0 += 32 * SK) {
+      float val[RR][SK];
+      unsigned at[RR][SK];  // coarse levels have < 2^32 nodes
+      bool ok[RR][SK];
 #pragma unroll
-    for (int u = 0; u < PB; ++u) {
-      const unsigned t = base + u * T;
-      at[u] = (size_t)-1;
-      if (t >= tot) continue;
-      const int k = (int)(t % (unsigned)J) + 1;
-      const unsigned q = t / (unsigned)J;
-      const int j = (int)(q % (unsigned)J) + 1, i = (int)(q / (unsigned)J) + 1;
-      const size_t c = ((size_t)i * n + j) * n + k;
-      float sum, diag;
-      sw_stencil(e, c, i, j, k, g, sum, diag);
-      val[u] = b[c] - (sum - diag * e[c]);
-      at[u] = c;
+      for (int u = 0; u < RR; ++u) {
+        const unsigned r = r0 + u * NW;
+        const int i = (int)(r / (unsigned)J) + 1, j = (int)(r % (unsigned)J) + 1;
+#pragma unroll
+        for (int q = 0; q < SK; ++q) {
+          const int k = k0 + (int)lane + 32 * q;
+          ok[u][q] = r < rows && k <= J;
+          if (ok[u][q]) at[u][q] = node(i, j, k, val[u][q]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < RR; ++u)
+#pragma unroll
+        for (int q = 0; q < SK; ++q)
+          if (ok[u][q]) out[at[u][q]] = val[u][q];
     }
-#pragma unroll
-    for (int u = 0; u < PB; ++u)
-      if (at[u] != (size_t)-1) r[at[u]] = val[u];
   }
+}
+
+__device__ void p_resid(const float *__restrict__ e, const float *__restrict__ b, float *__restrict__ r_out,
+                        const LevelGeom &g) {
+  const size_t n = (size_t)g.n;
+  p_node_rows<1>(g.J, r_out, [&](int i, int j, int k, float &v) {
+    const size_t c = ((size_t)i * n + j) * n + k;
+    float sum, diag;
+    sw_stencil(e, c, i, j, k, g, sum, diag);
+    v = b[c] - (sum - diag * e[c]);
+    return (unsigned)c;
+  });
 }
 
 __device__ void p_restrict(const float *__restrict__ rf, const LevelGeom &f, float *__restrict__ bc,
                            const LevelGeom &cg) {
   const int J = cg.J;
-  const unsigned tot = (unsigned)J * (unsigned)J * (unsigned)J;
-  for (unsigned t = p_tid(); t < tot; t += p_nthreads()) {
-    const int K = (int)(t % (unsigned)J) + 1;
-    const unsigned q = t / (unsigned)J;
-    const int Jj = (int)(q % (unsigned)J) + 1, I = (int)(q / (unsigned)J) + 1;
-    restrict_node(rf, f, bc, cg, I, Jj, K);
+  const unsigned rows = (unsigned)J * (unsigned)J, NW = p_nwarps(), lane = threadIdx.x & 31u;
+  for (unsigned r = p_warp(); r < rows; r += NW) {
+    const int I = (int)(r / (unsigned)J) + 1, Jj = (int)(r % (unsigned)J) + 1;
+    for (int K = 1 + (int)lane; K <= J; K += 32) restrict_node(rf, f, bc, cg, I, Jj, K);
   }
 }
 
 __device__ void p_prolong(const float *__restrict__ ec, const LevelGeom &cg, float *__restrict__ ef,
                           const LevelGeom &f) {
-  const int J = f.J, n = f.n;
-  const unsigned tot = (unsigned)J * (unsigned)J * (unsigned)J, T = p_nthreads();
-  for (unsigned base = p_tid(); base < tot; base += PB * T) {
-    float val[PB];
-    size_t at[PB];
-#pragma unroll
-    for (int u = 0; u < PB; ++u) {
-      const unsigned t = base + u * T;
-      at[u] = (size_t)-1;
-      if (t >= tot) continue;
-      const int k = (int)(t % (unsigned)J) + 1;
-      const unsigned q = t / (unsigned)J;
-      const int j = (int)(q % (unsigned)J) + 1, i = (int)(q / (unsigned)J) + 1;
-      const size_t c = ((size_t)i * n + j) * n + k;
-      val[u] = ef[c] + prolong_value(ec, i, j, k, f, cg);
-      at[u] = c;
-    }
-#pragma unroll
-    for (int u = 0; u < PB; ++u)
-      if (at[u] != (size_t)-1) ef[at[u]] = val[u];
-  }
+  const size_t n = (size_t)f.n;
+  // one row per round: the prolongation's weights take the registers
+  p_node_rows<1>(f.J, ef, [&](int i, int j, int k, float &v) {
+    const size_t c = ((size_t)i * n + j) * n + k;
+    v = ef[c] + prolong_value(ec, i, j, k, f, cg);
+    return (unsigned)c;
+  });
 }
 
 #define COARSE_THREADS 512
 
 // Down: for each level, pre-smoothing, residual, restriction into b[l+1].
-__global__ void __launch_bounds__(COARSE_THREADS) k_coarse_down(CoarseDesc d) {
+__global__ void __launch_bounds__(COARSE_THREADS, 2) k_coarse_down(CoarseDesc d) {
   unsigned tgt = threadIdx.x == 0 ? grid_barrier_base(d.bar) : 0u;
   for (int l = d.l0; l < d.l1; ++l) {
     const LevelGeom &g = d.g[l];
@@ -622,7 +631,7 @@ __global__ void __launch_bounds__(COARSE_THREADS) k_coarse_down(CoarseDesc d) {
 }
 
 // Up: for each level from l1-1 down to l0, prolongation of e[l+1], post-smoothing.
-__global__ void __launch_bounds__(COARSE_THREADS) k_coarse_up(CoarseDesc d) {
+__global__ void __launch_bounds__(COARSE_THREADS, 2) k_coarse_up(CoarseDesc d) {
   unsigned tgt = threadIdx.x == 0 ? grid_barrier_base(d.bar) : 0u;
   for (int l = d.l1 - 1; l >= d.l0; --l) {
     const LevelGeom &g = d.g[l];
@@ -1079,7 +1088,10 @@ __device__ void t_smooth(T *e, const T *b, const LevelGeom &g, int sweeps) {
           if (i == J) { sx = (T)g.a * e[c - n * n]; dx_ = (T)g.dB; } else { sx = e[c + n * n] + e[c - n * n]; dx_ = 2; }
           if (j == J) { sy = (T)g.a * e[c - n]; dy_ = (T)g.dB; } else { sy = e[c + n] + e[c - n]; dy_ = 2; }
           if (k == J) { sz = (T)g.a * e[c - 1]; dz_ = (T)g.dB; } else { sz = e[c + 1] + e[c - 1]; dz_ = 2; }
-          e[c] = ((sx + sy + sz) - b[c]) / (dx_ + dy_ + dz_);
+          if constexpr (sizeof(T) == sizeof(float))
+            e[c] = gs_value((sx + sy) + sz, b[c], (dx_ + dy_) + dz_);  // the shared rule: 1/6 off the far faces
+          else
+            e[c] = ((sx + sy + sz) - b[c]) / (dx_ + dy_ + dz_);
         }
       }
       __syncthreads();
@@ -1264,13 +1276,19 @@ __global__ void __launch_bounds__(256)
   if (M > 0.0) {
     const double rx = i * dx - sm[1], ry = j * dx - sm[2], rz = k * dx - sm[3];
     const double d2 = rx * rx + ry * ry + rz * rz + 1e-12;
-    const double inv = 1.0 / sqrt(d2);
-    const double nx = rx * inv, ny = ry * inv, nz = rz * inv;
-    const double nsn = nx * nx * sm[4] + ny * ny * sm[5] + nz * nz * sm[6] +
-                       2.0 * (nx * ny * sm[7] + nx * nz * sm[8] + ny * nz * sm[9]);
-    const double quad = 3.0 * nsn - sm[10];
+    // 1/sqrt(d2): the f32 estimate refined by two Newton steps y <- y (3 - d2 y^2) / 2
+    // in FP64 (relative error 2^-23 -> 2^-46 -> below the FP64 rounding), a
+    // handful of FP64 operations instead of a square root and a division
+    double inv = (double)rsqrtf((float)d2);
+    inv = inv * (1.5 - 0.5 * d2 * inv * inv);
+    inv = inv * (1.5 - 0.5 * d2 * inv * inv);
+    // n.S.n d^2 as the quadratic form of r (no normalised n)
+    const double rsr = rx * (rx * sm[4] + 2.0 * (ry * sm[7] + rz * sm[8])) + ry * (ry * sm[5] + 2.0 * rz * sm[9]) +
+                       rz * rz * sm[6];
+    const double inv2 = inv * inv;
+    const double quad = 3.0 * rsr * inv2 - sm[10];
     // Phi = -G (M/d + (3 n.S.n - tr S) / (2 d^3)), multigrid.py:261-295
-    phi = -grav * (M * inv + quad * (0.5 * inv * inv * inv));
+    phi = -grav * (M * inv + quad * (0.5 * inv2 * inv));
   }
   const size_t c = ((size_t)i * G + j) * G + k;
   const float h = (float)phi;
@@ -1461,9 +1479,10 @@ static int coarse_grid(gc_ctx *ctx) {
     return GC_ERR_CUDA;
   }
   const LevelGeom &g1 = ctx->lev[1];
-  const long long nodes = (long long)g1.J * g1.J * g1.J;  // the largest phase: level 1's residual
+  const long long rows = (long long)g1.J * g1.J;  // the largest phase: level 1's rows
   long long nb = (long long)gc_sms() * per_sm;
-  const long long need = (nodes + (long long)PB * COARSE_THREADS - 1) / ((long long)PB * COARSE_THREADS);
+  const long long per_block = (long long)PR * (COARSE_THREADS / 32);
+  const long long need = (rows + per_block - 1) / per_block;
   if (nb > need) nb = need;
   ctx->coarse_blocks = (int)(nb < 1 ? 1 : nb);
   return GC_OK;
@@ -1562,6 +1581,8 @@ static int residual0(gc_ctx *ctx, const gc_mg_params *p) {
       gc_launch(ctx, GK_RESID0, k_resid0x4<false>, qg, dim3(32, 8), 0, ctx->hi, ctx->lo, ctx->b0, ctx->r0s, ef,
                 ctx->red, d);
     GC_LAUNCH_CHECK(ctx, "resid0");
+    // (a last-block sum of the 16k block partials in this kernel was slower: the
+    // blocks' tickets serialise on one counter)
     return finalize_to(ctx, (int)nq, 1, GC_S_RNORM2);
   } else {
     const int pre = ctx->nlev == 1 ? p->coarse_sweeps : p->pre_sweeps;

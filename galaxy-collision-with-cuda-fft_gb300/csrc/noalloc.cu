@@ -47,7 +47,8 @@ __global__ void __launch_bounds__(256)
               long long *__restrict__ qg, unsigned *__restrict__ status);
 __global__ void __launch_bounds__(256)
     k_convert_q(long long *__restrict__ qg, int G, double dx, const double *__restrict__ qexp, float *__restrict__ rho,
-                float *__restrict__ b, double bfac, double *__restrict__ parts);
+                float *__restrict__ b, double bfac, double *__restrict__ parts, unsigned *__restrict__ ticket,
+                double *__restrict__ mom, double *__restrict__ bnorm2);
 
 // Layout of the scratch array (byte offsets, each 256-byte aligned).
 #define NA_Q_BYTES ((size_t)GC_NOALLOC_MAX_GRID * GC_NOALLOC_MAX_GRID * GC_NOALLOC_MAX_GRID * 8)
@@ -157,7 +158,7 @@ extern "C" int gc_deposit_cic_noalloc(const float *x, const float *y, const floa
   }
   // rho from q (q is cleared again by the conversion); the moments land in parts
   const unsigned nbc = gc_blocks((long long)G * G, 8);
-  k_convert_q<<<nbc, 256, 0, st>>>(q, G, dx, small + 1, rho, nullptr, 1.0, parts);
+  k_convert_q<<<nbc, 256, 0, st>>>(q, G, dx, small + 1, rho, nullptr, 1.0, parts, nullptr, nullptr, nullptr);
   e = cudaGetLastError();
   if (e != cudaSuccess) {
     gc_set_error(nullptr, "gc_deposit_cic_noalloc: launch failed: %s", cudaGetErrorString(e));

@@ -671,7 +671,8 @@ int gc_deposit_q(gc_ctx *ctx, const float *x, const float *y, const float *z, co
 // moments + ||b||^2.
 __global__ void __launch_bounds__(256)
     k_convert_q(long long *__restrict__ qg, int G, double dx, const double *__restrict__ qexp, float *__restrict__ rho,
-                float *__restrict__ b, double bfac, double *__restrict__ parts) {
+                float *__restrict__ b, double bfac, double *__restrict__ parts, unsigned *__restrict__ ticket,
+                double *__restrict__ mom, double *__restrict__ bnorm2) {
   __shared__ double wsum[8][11];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int E = (int)(*qexp);
@@ -750,11 +751,16 @@ __global__ void __launch_bounds__(256)
     for (int t = 0; t < 11; ++t) wsum[wid][t] = v[t];
   }
   __syncthreads();
-  if (threadIdx.x < 11) {
-    double a = 0.0;
-    for (int w = 0; w < 8; ++w) a += wsum[w][threadIdx.x];
-    parts[(size_t)blockIdx.x * 11 + threadIdx.x] = a;
+  if (threadIdx.x == 0) {  // one writer: the last-block reduction below fences its stores
+#pragma unroll 1
+    for (int t = 0; t < 11; ++t) {
+      double a = 0.0;
+      for (int w = 0; w < 8; ++w) a += wsum[w][t];
+      parts[(size_t)blockIdx.x * 11 + t] = a;
+    }
   }
+  // the moments and ||b||^2 from the block partials by the last block
+  if (ticket && grid_finish_sum<11>(parts, gridDim.x, ticket, mom) && threadIdx.x == 0) *bnorm2 = mom[10];
 }
 
 int gc_max_fixed_point_bits(const gc_ctx *ctx) {
@@ -771,11 +777,10 @@ int gc_convert_q(gc_ctx *ctx, const double *qexp, float *rho_out, float *b_out) 
   int s = gc_ensure_red(ctx, (size_t)nb * 11);
   if (s) return s;
   const double bfac = 4.0 * M_PI * ctx->grav * ctx->dx * ctx->dx;
-  gc_launch(ctx, GK_CONVERT_Q, k_convert_q, dim3(nb), dim3(256), 0, ctx->q, ctx->G, ctx->dx, qexp, rho_out, b_out, bfac, ctx->red);
+  gc_launch(ctx, GK_CONVERT_Q, k_convert_q, dim3(nb), dim3(256), 0, ctx->q, ctx->G, ctx->dx, qexp, rho_out, b_out,
+            bfac, ctx->red, reinterpret_cast<unsigned *>(ctx->dsmall + GC_S_TICKET), ctx->dmom,
+            ctx->dsmall + GC_S_BNORM2);
   GC_LAUNCH_CHECK(ctx, "convert q");
-  if ((s = gc_finalize(ctx, ctx->red, (int)nb, 11, ctx->dmom))) return s;
-  GC_CUDA(ctx, cudaMemcpyAsync(ctx->dsmall + GC_S_BNORM2, ctx->dmom + 10, sizeof(double), cudaMemcpyDeviceToDevice,
-                               ctx->stream));
   return GC_OK;
 }
 

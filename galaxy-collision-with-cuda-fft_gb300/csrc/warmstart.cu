@@ -1425,6 +1425,8 @@ __global__ void __launch_bounds__(128) k_ws_apply(const float *__restrict__ yc, 
                                                   float *__restrict__ prev) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
   if (k >= G) return;
+  // the face nodes are the multipole faces' (computed beside this pass)
+  if (i == 0 || j == 0 || k == 0 || i == G - 1 || j == G - 1 || k == G - 1) return;
   const int R = G >> 1;
   const size_t v = ((size_t)i * G + j) * G + k;
   const float h = hi[v], l = lo[v];
