@@ -317,7 +317,10 @@ __device__ __forceinline__ float restrict_w(int Jc, int o, const LevelGeom &f, c
   return 0.5f * (f.p - (float)i) / (f.p - (float)(2 * Jc));
 }
 
-// b_c = 4 * R(r_f) at coarse node (I, Jj, K): full weighting (transpose of trilinear prolongation).
+// b_c = 4 * R(r_f) at coarse node (I, Jj, K): full weighting (transpose of
+// trilinear prolongation), summed separably: the three k terms of each of the
+// nine (i, j) fine rows, then the rows' j weights, then the i weights. Terms of
+// weight zero (fine nodes on a face) are not read.
 __device__ __forceinline__ void restrict_node(const float *__restrict__ rf, const LevelGeom &f,
                                               float *__restrict__ bc, const LevelGeom &cg, int I, int Jj, int K) {
   float wi[3], wj[3], wk[3];
@@ -328,23 +331,22 @@ __device__ __forceinline__ void restrict_node(const float *__restrict__ rf, cons
     wk[o + 1] = restrict_w(K, o, f, cg);
   }
   const size_t n = f.n;
+  const float *base = rf + ((size_t)(2 * I - 1) * n + (size_t)(2 * Jj - 1)) * n + (size_t)(2 * K - 1);
   float acc = 0.0f;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     if (wi[a] == 0.0f) continue;
-    const size_t fi = (size_t)(2 * I + a - 1);
+    float ta = 0.0f;
 #pragma unroll
     for (int bb = 0; bb < 3; ++bb) {
       if (wj[bb] == 0.0f) continue;
-      const size_t fj = (size_t)(2 * Jj + bb - 1);
-      const float wij = wi[a] * wj[bb];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        if (wk[c] == 0.0f) continue;
-        const size_t fk = (size_t)(2 * K + c - 1);
-        acc += wij * wk[c] * rf[(fi * n + fj) * n + fk];
-      }
+      const float *row = base + ((size_t)a * n + (size_t)bb) * n;
+      float sab = wk[1] * row[1];
+      if (wk[0] != 0.0f) sab += wk[0] * row[0];
+      if (wk[2] != 0.0f) sab += wk[2] * row[2];
+      ta += wj[bb] * sab;
     }
+    acc += wi[a] * ta;
   }
   const size_t m = cg.n;
   bc[((size_t)I * m + Jj) * m + K] = 4.0f * acc;

@@ -5,18 +5,18 @@
 // Each radix pass is reduce-then-scan: per-tile digit histograms, one exclusive
 // scan of the digit-major histogram, then a stable scatter in which every warp
 // ranks its items round by round with match.any, so equal keys keep their input
-// order and the permutation is unique.
+// order and the permutation is unique. Digits are up to 9 bits wide (the 25-bit
+// cell keys of a 256^3 grid take three passes), tiles 4096 items.
 #include "common.cuh"
 
 #include <cmath>
 
-#define RS_BITS 8
-#define RS_RADIX 256
+#define RS_MAX_BITS 9                      // widest digit of a pass
+#define RS_MAX_RADIX (1 << RS_MAX_BITS)
 #define RS_THREADS 256
 #define RS_WARPS (RS_THREADS / 32)
-#define RS_IPT 4                           // items per thread (small tiles: more CTAs in flight)
-#define RS_TILE (RS_THREADS * RS_IPT)      // 1024 items per tile
-static_assert(RS_THREADS == RS_RADIX, "the scatter's per-digit phase has one thread per digit");
+#define RS_IPT 16                          // items per thread
+#define RS_TILE (RS_THREADS * RS_IPT)      // 4096 items per tile
 
 __global__ void __launch_bounds__(256)
     k_cell_keys(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z, long long n,
@@ -32,19 +32,29 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Digit histogram of each tile: hist[d * ntiles + tile].
+// Digit histogram of each tile: hist[d * ntiles + tile], digits of BITS bits
+// at `shift`. The lanes of a warp that hold the same digit add their count
+// once (match.any), so that nearly sorted keys do not serialise on one counter.
+template <int BITS>
 __global__ void __launch_bounds__(RS_THREADS)
     k_rs_hist(const uint32_t *__restrict__ keys, long long n, int shift, unsigned *__restrict__ hist, int ntiles) {
-  __shared__ unsigned cnt[RS_RADIX];
-  for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) cnt[d] = 0;
+  constexpr int RADIX = 1 << BITS;
+  __shared__ unsigned cnt[RADIX];
+  for (int d = threadIdx.x; d < RADIX; d += RS_THREADS) cnt[d] = 0;
   __syncthreads();
+  const int lane = threadIdx.x & 31;
   const long long base = (long long)blockIdx.x * RS_TILE;
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll 4
   for (int t = threadIdx.x; t < RS_TILE; t += RS_THREADS) {
     const long long p = base + t;
-    if (p < n) atomicAdd(&cnt[(keys[p] >> shift) & (RS_RADIX - 1)], 1u);
+    const bool ok = p < n;
+    const unsigned d = ok ? ((keys[p] >> shift) & (RADIX - 1)) : (unsigned)RADIX + lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    if (ok && (peers & lt) == 0) atomicAdd(&cnt[d], (unsigned)__popc(peers));
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) hist[(size_t)d * ntiles + blockIdx.x] = cnt[d];
+  for (int d = threadIdx.x; d < RADIX; d += RS_THREADS) hist[(size_t)d * ntiles + blockIdx.x] = cnt[d];
 }
 
 // Exclusive scan of an unsigned array in three phases (tile sums, scan of sums, apply).
@@ -127,17 +137,28 @@ __global__ void __launch_bounds__(SC_THREADS) k_scan_apply(unsigned *__restrict_
 // input order. Ranks within the tile (per-warp digit counts, then across warps
 // and digits) place every item at its slot of the tile's digit-sorted order in
 // shared memory; the items are then written out from there, so consecutive
-// threads write consecutive addresses of one digit's output segment.
+// threads write consecutive addresses of one digit's output segment. Dynamic
+// shared memory: scatter_smem_bytes(BITS).
+template <int BITS>
+constexpr size_t scatter_smem_bytes() {
+  return sizeof(unsigned) * ((size_t)RS_WARPS * (1 << BITS) + 2 * (1 << BITS) + RS_WARPS + 2 * RS_TILE);
+}
+
+template <int BITS>
 __global__ void __launch_bounds__(RS_THREADS)
     k_rs_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, long long n, int shift,
                  const unsigned *__restrict__ hist, int ntiles, uint32_t *__restrict__ kout,
                  uint32_t *__restrict__ vout) {
-  __shared__ unsigned whist[RS_WARPS][RS_RADIX];
-  __shared__ unsigned dstart[RS_RADIX];  // first slot of each digit in the tile's sorted order
-  __shared__ unsigned gofs[RS_RADIX];    // output index of the tile's first item of each digit
-  __shared__ uint32_t sk[RS_TILE], sv[RS_TILE];
+  constexpr int RADIX = 1 << BITS;
+  constexpr int DPT = (RADIX + RS_THREADS - 1) / RS_THREADS;  // digits per thread in the per-digit phase
+  extern __shared__ __align__(16) unsigned rs_smem[];
+  unsigned (*whist)[RADIX] = reinterpret_cast<unsigned (*)[RADIX]>(rs_smem);
+  unsigned *dstart = rs_smem + RS_WARPS * RADIX;  // first slot of each digit in the tile's sorted order
+  unsigned *gofs = dstart + RADIX;                // output index of the tile's first item of each digit
+  unsigned *wsum = gofs + RADIX;
+  uint32_t *sk = wsum + RS_WARPS, *sv = sk + RS_TILE;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int t = threadIdx.x; t < RS_WARPS * RS_RADIX; t += RS_THREADS) (&whist[0][0])[t] = 0;
+  for (int t = threadIdx.x; t < RS_WARPS * RADIX; t += RS_THREADS) rs_smem[t] = 0;
   __syncthreads();
   const long long tile0 = (long long)blockIdx.x * RS_TILE;
   const int cnt = (int)(n - tile0 < RS_TILE ? n - tile0 : RS_TILE);
@@ -151,7 +172,11 @@ __global__ void __launch_bounds__(RS_THREADS)
     const bool ok = p < n;
     k[r] = ok ? kin[p] : 0u;
     v[r] = ok ? vin[p] : 0u;
-    const unsigned d = ok ? ((k[r] >> shift) & (RS_RADIX - 1)) : (unsigned)RS_RADIX + lane;
+  }
+#pragma unroll
+  for (int r = 0; r < RS_IPT; ++r) {
+    const bool ok = seg + r * 32 + lane < n;
+    const unsigned d = ok ? ((k[r] >> shift) & (RADIX - 1)) : (unsigned)RADIX + lane;
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     unsigned old = 0;
     if (ok) old = whist[w][d];
@@ -161,39 +186,49 @@ __global__ void __launch_bounds__(RS_THREADS)
     rank[r] = old + __popc(peers & lt);
   }
   __syncthreads();
-  // per digit: exclusive prefix over the warps, the digit's tile total, and the
-  // tile's global offset for it
-  unsigned tot = 0;
-  {
-    const int d = threadIdx.x;  // RS_THREADS == RS_RADIX
-    for (int ww = 0; ww < RS_WARPS; ++ww) {
-      const unsigned c = whist[ww][d];
-      whist[ww][d] = tot;
-      tot += c;
+  // per digit (thread t takes digits t*DPT .. t*DPT+DPT-1): exclusive prefix
+  // over the warps, the digit's tile total, and the tile's global offset for it
+  unsigned tot[DPT], mine = 0;
+#pragma unroll
+  for (int q = 0; q < DPT; ++q) {
+    const int d = threadIdx.x * DPT + q;
+    tot[q] = 0;
+    if (d < RADIX) {
+      for (int ww = 0; ww < RS_WARPS; ++ww) {
+        const unsigned c = whist[ww][d];
+        whist[ww][d] = tot[q];
+        tot[q] += c;
+      }
+      gofs[d] = hist[(size_t)d * ntiles + blockIdx.x];
     }
-    gofs[d] = hist[(size_t)d * ntiles + blockIdx.x];
+    mine += tot[q];
   }
-  // exclusive scan of the digit totals over the block
+  // exclusive scan of the digit totals over the block (threads in digit order)
   {
-    unsigned x = tot;
+    unsigned x = mine;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
       if (lane >= o) x += y;
     }
-    __shared__ unsigned wsum[RS_WARPS];
     if (lane == 31) wsum[w] = x;
     __syncthreads();
     unsigned before = 0;
     for (int ww = 0; ww < w; ++ww) before += wsum[ww];
-    dstart[threadIdx.x] = before + x - tot;
+    unsigned at = before + x - mine;
+#pragma unroll
+    for (int q = 0; q < DPT; ++q) {
+      const int d = threadIdx.x * DPT + q;
+      if (d < RADIX) dstart[d] = at;
+      at += tot[q];
+    }
   }
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < RS_IPT; ++r) {
     const long long p = seg + r * 32 + lane;
     if (p < n) {
-      const unsigned d = (k[r] >> shift) & (RS_RADIX - 1);
+      const unsigned d = (k[r] >> shift) & (RADIX - 1);
       const unsigned slot = dstart[d] + whist[w][d] + rank[r];
       sk[slot] = k[r];
       sv[slot] = v[r];
@@ -202,12 +237,17 @@ __global__ void __launch_bounds__(RS_THREADS)
   __syncthreads();
   for (int i = threadIdx.x; i < cnt; i += RS_THREADS) {
     const uint32_t kk = sk[i];
-    const unsigned d = (kk >> shift) & (RS_RADIX - 1);
+    const unsigned d = (kk >> shift) & (RADIX - 1);
     const unsigned dst = gofs[d] + (unsigned)i - dstart[d];
     kout[dst] = kk;
     vout[dst] = sv[i];
   }
 }
+
+// One radix pass with digits of BITS bits at `shift`.
+template <int BITS>
+static int radix_pass(gc_ctx *ctx, const uint32_t *kin, const uint32_t *vin, long long n, int shift, int ntiles,
+                      uint32_t *ko, uint32_t *vo);
 
 static int exclusive_scan(gc_ctx *ctx, unsigned *a, long long n) {
   const long long nt = (n + SC_TILE - 1) / SC_TILE;
@@ -219,12 +259,32 @@ static int exclusive_scan(gc_ctx *ctx, unsigned *a, long long n) {
   return GC_OK;
 }
 
+template <int BITS>
+static int radix_pass(gc_ctx *ctx, const uint32_t *kin, const uint32_t *vin, long long n, int shift, int ntiles,
+                      uint32_t *ko, uint32_t *vo) {
+  constexpr size_t smem = scatter_smem_bytes<BITS>();
+  static_assert(smem <= 227 * 1024, "scatter tile does not fit shared memory");
+  static int attr_device = -1;  // the opt-in above 48 KB, once per device
+  if (smem > 48 * 1024 && attr_device != ctx->device) {
+    GC_CUDA(ctx, cudaFuncSetAttribute(k_rs_scatter<BITS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_device = ctx->device;
+  }
+  gc_launch(ctx, GK_SORT, k_rs_hist<BITS>, dim3(ntiles), dim3(RS_THREADS), 0, kin, n, shift, ctx->hist, ntiles);
+  GC_LAUNCH_CHECK(ctx, "radix hist");
+  int s = exclusive_scan(ctx, ctx->hist, (long long)ntiles << BITS);
+  if (s) return s;
+  gc_launch(ctx, GK_SORT, k_rs_scatter<BITS>, dim3(ntiles), dim3(RS_THREADS), smem, kin, vin, n, shift, ctx->hist,
+            ntiles, ko, vo);
+  GC_LAUNCH_CHECK(ctx, "radix scatter");
+  return GC_OK;
+}
+
 // Key/value ping-pong buffers and digit histograms for n items (grown, never shrunk).
 static int ensure_sort_scratch(gc_ctx *ctx, int64_t n) {
   int s = gc_ensure_particle_scratch(ctx, (size_t)n);
   if (s) return s;
   const size_t ntiles = (ctx->pcap + RS_TILE - 1) / RS_TILE;  // sized for the scratch capacity
-  const size_t hn = ntiles * RS_RADIX;
+  const size_t hn = ntiles * RS_MAX_RADIX;
   if (ctx->hist_cap < hn) {
     GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     cudaFree(ctx->hist);
@@ -252,25 +312,34 @@ int gc_radix_sort_pairs(gc_ctx *ctx, const uint32_t *keys_in, const uint32_t *va
   int s = ensure_sort_scratch(ctx, n);
   if (s) return s;
   const int ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
-  const size_t hn = (size_t)ntiles * RS_RADIX;
   const uint32_t *kin = keys_in, *vin = vals_in;
   // ping-pong between (keys, vals) and (keys2, vals2); never write into the caller's input
   uint32_t *ka = ctx->keys, *va = ctx->vals, *kb = ctx->keys2, *vb = ctx->vals2;
-  int passes = (bits + RS_BITS - 1) / RS_BITS;
-  if (passes < 1) passes = 1;
+  // passes of at most RS_MAX_BITS bits, as even as possible (25 bits: 9 + 8 + 8)
+  if (bits < 1) bits = 1;
+  const int passes = (bits + RS_MAX_BITS - 1) / RS_MAX_BITS;
+  int shift = 0;
   for (int pss = 0; pss < passes; ++pss) {
-    const int shift = pss * RS_BITS;
+    const int w = (bits - shift + (passes - pss) - 1) / (passes - pss);
     uint32_t *ko = (pss & 1) ? kb : ka;
     uint32_t *vo = (pss & 1) ? vb : va;
     if (kin == ko) {  // input aliases this pass's output: use the other buffer
       ko = (ko == ka) ? kb : ka;
       vo = (vo == va) ? vb : va;
     }
-    gc_launch(ctx, GK_SORT, k_rs_hist, dim3(ntiles), dim3(RS_THREADS), 0, kin, (long long)n, shift, ctx->hist, ntiles);
-    GC_LAUNCH_CHECK(ctx, "radix hist");
-    if ((s = exclusive_scan(ctx, ctx->hist, (long long)hn))) return s;
-    gc_launch(ctx, GK_SORT, k_rs_scatter, dim3(ntiles), dim3(RS_THREADS), 0, kin, vin, (long long)n, shift, ctx->hist, ntiles, ko, vo);
-    GC_LAUNCH_CHECK(ctx, "radix scatter");
+    switch (w) {
+      case 1: s = radix_pass<1>(ctx, kin, vin, n, shift, ntiles, ko, vo); break;
+      case 2: s = radix_pass<2>(ctx, kin, vin, n, shift, ntiles, ko, vo); break;
+      case 3: s = radix_pass<3>(ctx, kin, vin, n, shift, ntiles, ko, vo); break;
+      case 4: s = radix_pass<4>(ctx, kin, vin, n, shift, ntiles, ko, vo); break;
+      case 5: s = radix_pass<5>(ctx, kin, vin, n, shift, ntiles, ko, vo); break;
+      case 6: s = radix_pass<6>(ctx, kin, vin, n, shift, ntiles, ko, vo); break;
+      case 7: s = radix_pass<7>(ctx, kin, vin, n, shift, ntiles, ko, vo); break;
+      case 8: s = radix_pass<8>(ctx, kin, vin, n, shift, ntiles, ko, vo); break;
+      default: s = radix_pass<9>(ctx, kin, vin, n, shift, ntiles, ko, vo); break;
+    }
+    if (s) return s;
+    shift += w;
     kin = ko;
     vin = vo;
   }
@@ -333,16 +402,40 @@ struct PermSet {
   int32_t *iout[2];
 };
 
+// Each thread takes PERM_U particles per round (PERM_U perm loads, then all
+// their gathers, then the stores), so that a thread keeps many independent
+// loads in flight instead of two dependent ones.
+#define PERM_U 4
 __global__ void __launch_bounds__(256)
     k_permute_set(PermSet s, const uint32_t *__restrict__ perm, long long n) {
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
-    const uint32_t q = perm[p];
+  const long long T = (long long)gridDim.x * blockDim.x;
+  for (long long p0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; p0 < n; p0 += PERM_U * T) {
+    uint32_t q[PERM_U];
+#pragma unroll
+    for (int u = 0; u < PERM_U; ++u) q[u] = p0 + u * T < n ? __ldg(perm + p0 + u * T) : 0u;
+    float fv[7][PERM_U];
+    int32_t iv[2][PERM_U];
 #pragma unroll
     for (int a = 0; a < 7; ++a)
-      if (s.fin[a]) s.fout[a][p] = __ldg(s.fin[a] + q);
+#pragma unroll
+      for (int u = 0; u < PERM_U; ++u)
+        if (s.fin[a] && p0 + u * T < n) fv[a][u] = __ldg(s.fin[a] + q[u]);
 #pragma unroll
     for (int a = 0; a < 2; ++a)
-      if (s.iin[a]) s.iout[a][p] = __ldg(s.iin[a] + q);
+#pragma unroll
+      for (int u = 0; u < PERM_U; ++u)
+        if (s.iin[a] && p0 + u * T < n) iv[a][u] = __ldg(s.iin[a] + q[u]);
+#pragma unroll
+    for (int u = 0; u < PERM_U; ++u) {
+      const long long p = p0 + u * T;
+      if (p >= n) break;
+#pragma unroll
+      for (int a = 0; a < 7; ++a)
+        if (s.fin[a]) s.fout[a][p] = fv[a][u];
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+        if (s.iin[a]) s.iout[a][p] = iv[a][u];
+    }
   }
 }
 
