@@ -88,6 +88,8 @@ def _parse(argv=None):
     ap.add_argument("--pre-sweeps", type=int, default=2, help="red-black sweeps before restriction (reference: 2)")
     ap.add_argument("--post-sweeps", type=int, default=2, help="red-black sweeps after prolongation (reference: 2)")
     ap.add_argument("--sort-every", type=int, default=20, help="steps between cell sorts of the particles")
+    ap.add_argument("--deposit-next", action="store_true",
+                    help="the particle pass also deposits the drifted positions for the next step")
     ap.add_argument("--sort-ahead", type=float, default=None,
                     help="sort by the cells predicted this many steps ahead (x + v * steps * dt); "
                          "default half the sort period")
@@ -350,7 +352,7 @@ def run_ours(args):
     def make_engine(mode=None, plain_f32=False):
         e = PMEngine(G, dx, grav=1.0, origin=cfg["origin"], tol=args.tol, max_cycles=20 if plain_f32 else 60,
                      fixed_point_bits=bits, sort_every=args.sort_every, sort_ahead=args.sort_ahead,
-                     grad_grid=bool(args.grad_grid),
+                     grad_grid=bool(args.grad_grid), deposit_next=args.deposit_next,
                      pre_sweeps=args.pre_sweeps, post_sweeps=args.post_sweeps, plain_f32=plain_f32)
         m = mode or args.warmstart
         e.set_warmstart(m, net=(net if net is not None else _load_net()) if m == "learned" else None)
