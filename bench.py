@@ -69,8 +69,8 @@ MG_KERNELS = ("smooth0", "update0", "resid0", "resid0e", "restrict", "smooth", "
 def _parse(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40,
-                    help="timed steps (default: two cell-sort periods, so the sorts are inside the timed region)")
+    ap.add_argument("--steps", type=int, default=100,
+                    help="timed steps (default: five cell-sort periods, so the sorts are inside the timed region)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--config", default="two_disk_100M")
