@@ -1524,7 +1524,7 @@ static int launch_coarse(gc_ctx *ctx, const gc_mg_params *p, bool up) {
 static int coarse_levels(gc_ctx *ctx, const gc_mg_params *p) {
   const int L = ctx->nlev;
   int st;
-  if (!(p->flags & GC_MG_NATURAL_LAYOUT) && ctx->tail > 1) {
+  if (!(p->flags & (GC_MG_NATURAL_LAYOUT | GC_MG_PHASE_LAUNCHES)) && ctx->tail > 1) {
     if ((st = launch_coarse(ctx, p, false))) return st;
     if (ctx->tail < L && (st = launch_tail(ctx, p))) return st;
     return launch_coarse(ctx, p, true);

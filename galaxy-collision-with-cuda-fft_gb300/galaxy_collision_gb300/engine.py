@@ -42,7 +42,7 @@ class PMEngine:
                  max_cycles: int = 50, pre_sweeps: int = 2, post_sweeps: int = 2, coarse_sweeps: int = 40,
                  fixed_point_bits: int = 52, sort_every: int = 20, grad_grid: bool = True, fixed_cycles: int = 0,
                  max_particles: int = 0, deposit_next: bool = False, plain_f32: bool = False,
-                 sort_ahead: float | None = None):
+                 sort_ahead: float | None = None, phase_launches: bool = False):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
         self.grav = float(grav)
@@ -57,6 +57,8 @@ class PMEngine:
         self.mg.tol = float(tol)
         if plain_f32:  # the all-FP32 method: stalls at the FP32 floor, runs to max_cycles
             self.mg.flags |= _native.GC_MG_PLAIN_F32
+        if phase_launches:  # coarse levels launched phase by phase (ensembles of small runs)
+            self.mg.flags |= _native.GC_MG_PHASE_LAUNCHES
         # fixed_cycles > 0: exactly that many V-cycles per solve and no host read in
         # the step (the residual stays on the device, see last_residual), which is
         # what lets a step be captured as a CUDA graph

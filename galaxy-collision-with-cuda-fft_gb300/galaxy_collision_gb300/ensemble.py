@@ -16,6 +16,9 @@ Workload (the batched-ensemble configuration): 64 two-disk collisions with
 particle counts log-uniform in [0.25M, 4M], 64^3 grids below 1M particles and
 128^3 otherwise, geometry randomised as in the training set. The comparison is
 the same runs advanced one after the other, each through its own step graph.
+The runs' coarse multigrid levels are launched phase by phase
+(GC_MG_PHASE_LAUNCHES): at 64^3 and 128^3 that is faster than the persistent
+cooperative kernels, alone and side by side.
 
 Command line::
 
@@ -48,7 +51,7 @@ class Ensemble:
     """Independent PM engines advanced together, one whole-step graph per run per step."""
 
     def __init__(self, n_runs: int = 64, seed: int = 5, tol: float = 1e-6, warmstart: str = "extrapolate",
-                 sort_every: int = 20, dt: float = DT, box: float = BOX, net=None):
+                 sort_every: int = 20, dt: float = DT, box: float = BOX, net=None, phase_launches: bool = True):
         members, rng = ensemble_members(n_runs, seed)
         self.dt = dt
         self.engines: list[PMEngine] = []
@@ -56,7 +59,7 @@ class Ensemble:
         for n, grid in members:
             icr = random_collision(rng, n, box / grid)
             e = PMEngine(grid, box / grid, grav=1.0, origin=(-box / 2.0,) * 3, tol=tol, sort_every=sort_every,
-                         fixed_point_bits=40)
+                         fixed_point_bits=40, phase_launches=phase_launches)
             e.set_warmstart(warmstart, net=net if warmstart == "learned" else None)
             e.load(icr.pos, icr.vel, icr.mass, icr.gid)
             self.engines.append(e)
@@ -111,11 +114,11 @@ class Ensemble:
 
 
 def run_comparison(n_runs: int = 64, steps: int = 300, seed: int = 5, one_by_one_steps: int | None = None,
-                   log=None) -> dict:
+                   log=None, phase_launches: bool = True) -> dict:
     """Aggregate particle-steps/s of the ensemble step and of the same runs
     advanced one after the other (each through its own step graph)."""
     t0 = time.time()
-    ens = Ensemble(n_runs, seed=seed)
+    ens = Ensemble(n_runs, seed=seed, phase_launches=phase_launches)
     if log:
         log(f"{n_runs} runs, {ens.particles:,} particles, IC {time.time() - t0:.0f}s")
     ens.prime()
@@ -163,12 +166,15 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--one-by-one-steps", type=int, default=None)
     ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--persistent-coarse", action="store_true",
+                    help="coarse multigrid levels by the persistent kernels instead of one launch per phase")
     args = ap.parse_args(argv)
     from galaxy_collision_gb300 import _build
 
     _build.build()
     res = run_comparison(args.runs, args.steps, args.seed, args.one_by_one_steps,
-                         log=lambda m: print(f"[ensemble] {m}", flush=True))
+                         log=lambda m: print(f"[ensemble] {m}", flush=True),
+                         phase_launches=not args.persistent_coarse)
     print(json.dumps(res), flush=True)
 
 

@@ -49,6 +49,7 @@ class MultigridPoissonSolver(PoissonSolver):
         plain_f32: bool = False,
         natural_layout: bool = False,
         boundary: str = "multipole",
+        phase_launches: bool = False,
     ):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
@@ -68,6 +69,9 @@ class MultigridPoissonSolver(PoissonSolver):
         # natural_layout: validation path, the finest correction in natural
         # layout through the generic level kernels (identical potentials)
         self.natural_layout = bool(natural_layout)
+        # phase_launches: the coarse levels by one launch per phase instead of
+        # the persistent kernels (identical potentials)
+        self.phase_launches = bool(phase_launches)
         if boundary not in ("multipole", "isolated"):
             raise ValueError(f"unknown boundary {boundary!r} (expected 'multipole' or 'isolated')")
         self.boundary = boundary
@@ -84,7 +88,8 @@ class MultigridPoissonSolver(PoissonSolver):
         p.min_cycles = self.min_cycles
         p.tol = self.tol
         p.flags = ((_native.GC_MG_PLAIN_F32 if self.plain_f32 else 0)
-                   | (_native.GC_MG_NATURAL_LAYOUT if self.natural_layout else 0))
+                   | (_native.GC_MG_NATURAL_LAYOUT if self.natural_layout else 0)
+                   | (_native.GC_MG_PHASE_LAUNCHES if self.phase_launches else 0))
         return p
 
     def solve(self, rho, phi, warm_start: bool = False) -> None:

@@ -72,6 +72,11 @@ enum gc_status_code {
  * warm_start, else zero. With faces from a free-space (lattice Green's function)
  * evaluation this is the isolated-boundary solve of James's method. */
 #define GC_MG_FACES_GIVEN 0x10
+/* gc_mg_params.flags: the coarse levels by one launch per phase instead of the
+ * two persistent cooperative launches: slower for one solve alone, but the
+ * launches of many small solves running at once on one GPU (an ensemble of
+ * runs on separate streams) can interleave. Same potentials bit for bit. */
+#define GC_MG_PHASE_LAUNCHES 0x20
 
 typedef struct gc_ctx gc_ctx;
 

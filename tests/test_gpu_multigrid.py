@@ -103,6 +103,16 @@ def test_split_layout_bitwise_equals_natural_layout(cuda, n, dx, plain):
     assert sa.last_stats["res_norm"] == pytest.approx(sb.last_stats["res_norm"], rel=1e-5)
 
 
+@pytest.mark.parametrize("n,dx", [(64, 1.0), (130, 0.25), (256, 0.25)])
+def test_phase_launches_bitwise_equal_persistent_coarse_levels(cuda, n, dx):
+    """The coarse levels launched phase by phase (GC_MG_PHASE_LAUNCHES) run the
+    persistent kernels' arithmetic: identical potentials."""
+    rho = gaussian_rho(n, dx, 3.0 * dx, 1.5, center=(0.45 * n * dx, 0.5 * n * dx, 0.6 * n * dx))
+    _, _, a = _solve(rho, dx, 1.0, n_cycles=3, tol=0.0)
+    _, _, b = _solve(rho, dx, 1.0, n_cycles=3, tol=0.0, phase_launches=True)
+    np.testing.assert_array_equal(a.to_numpy(), b.to_numpy())
+
+
 def test_plain_f32_stalls_at_the_fp32_floor(cuda):
     """The plain FP32 method (the reference's precision) cannot go below the
     FP32 floor: asked for 1e-6 it runs to its cycle cap with the residual near
