@@ -493,7 +493,7 @@ __device__ __forceinline__ bool grid_barrier(GridBar *gb, unsigned &target, unsi
 // reads a value that the phase writes (a half-sweep reads only the other
 // colour; the residual, restriction and prolongation write other arrays or
 // only the node itself), so deferring the stores changes nothing.
-#define PR 2
+#define PR 1  // (2 and 4 rows per round measured slower: more registers, fewer warps)
 #define SK 2
 __device__ __forceinline__ unsigned p_warp() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
 __device__ __forceinline__ unsigned p_nwarps() { return (gridDim.x * blockDim.x) >> 5; }
