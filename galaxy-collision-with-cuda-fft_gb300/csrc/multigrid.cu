@@ -1115,21 +1115,50 @@ __device__ void t_resid(const float *e, const float *b, float *r, const LevelGeo
   __syncthreads();
 }
 
+// 1-D transfer weights of a tail level pair (fine f, coarse cg), computed once
+// per launch into shared memory so that the restriction and prolongation loops
+// are table lookups (the far-face weights take a division): restriction weight
+// rw[3 I + a + 1] = restrict_w(I, a, f, cg); prolongation of fine index i:
+// coarse index pc[2 i], node count pc[2 i + 1], weights pw[2 i], pw[2 i + 1].
+#define TAIL_TAB 16  // indices 0 .. GC_TAIL_MAX_N - 2
+static_assert(GC_TAIL_MAX_N - 1 <= TAIL_TAB, "tail transfer tables too small");
+struct TailTab {
+  float rw[TAIL_TAB * 3];
+  float pw[TAIL_TAB * 2];
+  int pc[TAIL_TAB * 2];
+};
+
+__device__ void t_tables(TailTab &t, const LevelGeom &f, const LevelGeom &cg) {
+  for (int q = threadIdx.x; q < TAIL_TAB * 3; q += blockDim.x) {
+    const int I = q / 3, a = q % 3 - 1;
+    t.rw[q] = I >= 1 && I <= cg.J ? restrict_w(I, a, f, cg) : 0.0f;
+  }
+  for (int i = threadIdx.x; i < TAIL_TAB; i += blockDim.x) {
+    int c0 = 0, cnt = 0;
+    float w0 = 0.0f, w1 = 0.0f;
+    if (i >= 1 && i <= f.J) cnt = prolong_w(i, f, cg, c0, w0, w1);
+    t.pc[2 * i] = c0;
+    t.pc[2 * i + 1] = cnt;
+    t.pw[2 * i] = w0;
+    t.pw[2 * i + 1] = w1;
+  }
+}
+
 template <typename T>
-__device__ void t_restrict(const float *rf, const LevelGeom &f, T *bc, const LevelGeom &cg) {
+__device__ void t_restrict(const float *rf, const LevelGeom &f, T *bc, const LevelGeom &cg, const TailTab &tb) {
   const int J = cg.J, m = cg.n, n = f.n;
   const int K = (threadIdx.x & 15) + 1, Jj = ((threadIdx.x >> 4) & 15) + 1;
   if (K <= J && Jj <= J) {
     for (int I = (threadIdx.x >> 8) + 1; I <= J; I += 4) {
       float acc = 0.0f;
       for (int a = -1; a <= 1; ++a) {
-        const float wa = restrict_w(I, a, f, cg);
+        const float wa = tb.rw[3 * I + a + 1];
         if (wa == 0.0f) continue;
         for (int bb = -1; bb <= 1; ++bb) {
-          const float wb = restrict_w(Jj, bb, f, cg);
+          const float wb = tb.rw[3 * Jj + bb + 1];
           if (wb == 0.0f) continue;
           for (int c = -1; c <= 1; ++c) {
-            const float wc = restrict_w(K, c, f, cg);
+            const float wc = tb.rw[3 * K + c + 1];
             if (wc == 0.0f) continue;
             acc += wa * wb * wc * rf[((2 * I + a) * n + (2 * Jj + bb)) * n + (2 * K + c)];
           }
@@ -1142,16 +1171,15 @@ __device__ void t_restrict(const float *rf, const LevelGeom &f, T *bc, const Lev
 }
 
 template <typename T>
-__device__ void t_prolong(const T *ec, const LevelGeom &cg, float *ef, const LevelGeom &f) {
+__device__ void t_prolong(const T *ec, const LevelGeom &cg, float *ef, const LevelGeom &f, const TailTab &tb) {
   const int J = f.J, n = f.n, m = cg.n;
   const int k = (threadIdx.x & 15) + 1, j = ((threadIdx.x >> 4) & 15) + 1;
   if (k <= J && j <= J) {
+    const int cj = tb.pc[2 * j], nj = tb.pc[2 * j + 1], ck = tb.pc[2 * k], nk = tb.pc[2 * k + 1];
+    const float wj0 = tb.pw[2 * j], wj1 = tb.pw[2 * j + 1], wk0 = tb.pw[2 * k], wk1 = tb.pw[2 * k + 1];
     for (int i = (threadIdx.x >> 8) + 1; i <= J; i += 4) {
-      int ci, cj, ck;
-      float wi0, wi1, wj0, wj1, wk0, wk1;
-      const int ni = prolong_w(i, f, cg, ci, wi0, wi1);
-      const int nj = prolong_w(j, f, cg, cj, wj0, wj1);
-      const int nk = prolong_w(k, f, cg, ck, wk0, wk1);
+      const int ci = tb.pc[2 * i], ni = tb.pc[2 * i + 1];
+      const float wi0 = tb.pw[2 * i], wi1 = tb.pw[2 * i + 1];
       float val = 0.0f;
       for (int a = 0; a < ni; ++a)
         for (int bb = 0; bb < nj; ++bb)
@@ -1184,6 +1212,9 @@ __global__ void __launch_bounds__(1024) k_tail(const float *__restrict__ b_in, f
     }
     off = (off + 15) & ~(size_t)15;
   }
+  // transfer weights of every level pair (the first CTA barrier below orders them)
+  __shared__ TailTab tabs[GC_MAX_LEVELS];
+  for (int l = 0; l + 1 < d.nl; ++l) t_tables(tabs[l], d.g[l], d.g[l + 1]);
   const int n0 = d.g[0].n * d.g[0].n * d.g[0].n;
   if (d.nl == 1) {
     for (int i = threadIdx.x; i < n0; i += blockDim.x) {
@@ -1218,9 +1249,9 @@ __global__ void __launch_bounds__(1024) k_tail(const float *__restrict__ b_in, f
     t_smooth<float>(E[l], B[l], d.g[l], d.pre);
     t_resid(E[l], B[l], R[l], d.g[l]);
     if (l + 1 == d.nl - 1)
-      t_restrict<double>(R[l], d.g[l], B64, d.g[l + 1]);
+      t_restrict<double>(R[l], d.g[l], B64, d.g[l + 1], tabs[l]);
     else
-      t_restrict<float>(R[l], d.g[l], B[l + 1], d.g[l + 1]);
+      t_restrict<float>(R[l], d.g[l], B[l + 1], d.g[l + 1], tabs[l]);
   }
   {
     const LevelGeom &gc = d.g[d.nl - 1];
@@ -1230,9 +1261,9 @@ __global__ void __launch_bounds__(1024) k_tail(const float *__restrict__ b_in, f
   }
   for (int l = d.nl - 2; l >= 0; --l) {
     if (l + 1 == d.nl - 1)
-      t_prolong<double>(E64, d.g[l + 1], E[l], d.g[l]);
+      t_prolong<double>(E64, d.g[l + 1], E[l], d.g[l], tabs[l]);
     else
-      t_prolong<float>(E[l + 1], d.g[l + 1], E[l], d.g[l]);
+      t_prolong<float>(E[l + 1], d.g[l + 1], E[l], d.g[l], tabs[l]);
     t_smooth<float>(E[l], B[l], d.g[l], d.post);
   }
   for (int i = threadIdx.x; i < n0; i += blockDim.x) e_out[i] = E[0][i];
