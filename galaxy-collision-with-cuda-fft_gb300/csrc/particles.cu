@@ -252,6 +252,7 @@ __global__ void __launch_bounds__(256)
 #define DEP_TILE (256 * DEP_PER)
 #define DEP_BOX 8192
 #define DEP_WBOX (DEP_BOX / 8)  // nodes of one warp's box
+static_assert(DEP_WBOX <= 1024, "the box flush's reciprocal quotients are exact below 2^10 nodes");
 #define DEP_BIAS 0x4B400000u
 
 // Packed f32x2 arithmetic (two lanes of a 64-bit register, IEEE round to
@@ -624,13 +625,18 @@ __global__ void __launch_bounds__(256, 4)
     }
     if (use_box) {
       __syncwarp();
-      // the warp's box to the grid, one atomic per nonzero node; zeroed as read
+      // the warp's box to the grid, one atomic per nonzero node; zeroed as read.
+      // Node coordinates by correctly rounded reciprocals instead of integer
+      // divisions: for i < 2^10 the product (i + 1/2) * (1/nyz) is off by less
+      // than the distance to the next integer, so truncating it is the quotient.
       const int vol = nx * bx.nyz;
+      const float inv_nyz = __frcp_rn((float)bx.nyz), inv_nz = __frcp_rn((float)bx.nz);
       for (int i = lane; i < vol; i += 32) {
         const int v = wbox[i];
         if (v == 0) continue;
         wbox[i] = 0;
-        const int rx = i / bx.nyz, rem = i - rx * bx.nyz, ry = rem / bx.nz, rz = rem - ry * bx.nz;
+        const int rx = (int)(((float)i + 0.5f) * inv_nyz), rem = i - rx * bx.nyz;
+        const int ry = (int)(((float)rem + 0.5f) * inv_nz), rz = rem - ry * bx.nz;
         const int jx = bx.x0 + rx, jy = bx.y0 + ry, jz = bx.z0 + rz;
         if ((unsigned)jx < (unsigned)d.G && (unsigned)jy < (unsigned)d.G && (unsigned)jz < (unsigned)d.G)
           atomicAdd((unsigned long long *)(qg + ((size_t)jx * d.G + jy) * d.G + jz), (unsigned long long)(long long)v);
