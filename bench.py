@@ -87,6 +87,9 @@ def _parse(argv=None):
                          "extrapolation, or the extrapolation + the trained network's correction")
     ap.add_argument("--pre-sweeps", type=int, default=2, help="red-black sweeps before restriction (reference: 2)")
     ap.add_argument("--post-sweeps", type=int, default=2, help="red-black sweeps after prolongation (reference: 2)")
+    ap.add_argument("--coarse-level-sweeps", type=int, default=None,
+                    help="sweeps each way below the finest level: 1, or (default) the same as --pre/--post-sweeps "
+                         "as the reference")
     ap.add_argument("--sort-every", type=int, default=20, help="steps between cell sorts of the particles")
     ap.add_argument("--deposit-next", action="store_true",
                     help="the particle pass also deposits the drifted positions for the next step")
@@ -353,7 +356,9 @@ def run_ours(args):
         e = PMEngine(G, dx, grav=1.0, origin=cfg["origin"], tol=args.tol, max_cycles=20 if plain_f32 else 60,
                      fixed_point_bits=bits, sort_every=args.sort_every, sort_ahead=args.sort_ahead,
                      grad_grid=bool(args.grad_grid), deposit_next=args.deposit_next,
-                     pre_sweeps=args.pre_sweeps, post_sweeps=args.post_sweeps, plain_f32=plain_f32)
+                     pre_sweeps=args.pre_sweeps, post_sweeps=args.post_sweeps, plain_f32=plain_f32,
+                     # the plain FP32 chain is the reference's method: the same sweeps on every level
+                     coarse_level_sweeps=None if plain_f32 else args.coarse_level_sweeps)
         m = mode or args.warmstart
         e.set_warmstart(m, net=(net if net is not None else _load_net()) if m == "learned" else None)
         return e
@@ -419,6 +424,7 @@ def run_ours(args):
                         f"[{cfg['origin'][0]:g},{-cfg['origin'][0]:g}]^3, dt={dt}, seed {cfg['seed']}, "
                         f"multigrid to {args.tol:g} relative residual, int64 deposit quantum 2^-{bits} of the total",
             "warm_start": args.warmstart, "precision": args.precision, "sweeps": [args.pre_sweeps, args.post_sweeps],
+            "coarse_level_sweeps": None if args.precision == "plain_f32" else args.coarse_level_sweeps,
             "sort_every": args.sort_every,
             "sort_ahead": args.sort_every / 2.0 if args.sort_ahead is None else args.sort_ahead, "particles_per_gpu": n, "grid": G, "parallelism": f"replicas x{world}",
             "l2": "inputs larger than L2: 32 B/particle state = %.1f GB per GPU" % (n * 32 / 1e9),

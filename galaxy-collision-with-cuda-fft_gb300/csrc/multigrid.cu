@@ -1442,6 +1442,10 @@ static dim3 rb_grid(const LevelGeom &g) {
   return dim3(gc_blocks(nkk, RB_TX), gc_blocks(g.J, RB_TY), (unsigned)g.J);
 }
 static dim3 node_grid(const LevelGeom &g) { return dim3(gc_blocks(g.J, 32), gc_blocks(g.J, 8), (unsigned)g.J); }
+// Sweeps each way on the levels below the finest.
+static int coarse_pre(const gc_mg_params *p) { return (p->flags & GC_MG_COARSE_ONE_SWEEP) ? 1 : p->pre_sweeps; }
+static int coarse_post(const gc_mg_params *p) { return (p->flags & GC_MG_COARSE_ONE_SWEEP) ? 1 : p->post_sweeps; }
+
 static int launch_smooth(gc_ctx *ctx, int l, int sweeps) {
   const LevelGeom &g = ctx->lev[l];
   for (int s = 0; s < sweeps; ++s)
@@ -1455,8 +1459,8 @@ static int launch_tail(gc_ctx *ctx, const gc_mg_params *p) {
   TailDesc d;
   memset(&d, 0, sizeof(d));
   d.nl = ctx->nlev - ctx->tail;
-  d.pre = p->pre_sweeps;
-  d.post = p->post_sweeps;
+  d.pre = coarse_pre(p);
+  d.post = coarse_post(p);
   for (int l = 0; l < d.nl; ++l) d.g[l] = ctx->lev[ctx->tail + l];
   // The coarsest level has at most 3^3 unknowns: a few FP64 Gauss-Seidel sweeps
   // solve it far below the V-cycle's contraction (J = 1 is exact in one sweep).
@@ -1526,8 +1530,8 @@ static int launch_coarse(gc_ctx *ctx, const gc_mg_params *p, bool up) {
   memset(&d, 0, sizeof(d));
   d.l0 = 1;
   d.l1 = ctx->tail;
-  d.pre = p->pre_sweeps;
-  d.post = p->post_sweeps;
+  d.pre = coarse_pre(p);
+  d.post = coarse_post(p);
   d.budget = 100000000LL;  // ~50 ms of SM clocks; a barrier normally takes microseconds
   d.bar = reinterpret_cast<GridBar *>(ctx->dsmall + GC_S_GRIDBAR);
   d.status = ctx->dstatus;
@@ -1564,7 +1568,7 @@ static int coarse_levels(gc_ctx *ctx, const gc_mg_params *p) {
     const LevelGeom &g = ctx->lev[l];
     const size_t n3 = (size_t)g.n * g.n * g.n;
     GC_CUDA(ctx, cudaMemsetAsync(ctx->e[l], 0, n3 * sizeof(float), ctx->stream));
-    if ((st = launch_smooth(ctx, l, p->pre_sweeps))) return st;
+    if ((st = launch_smooth(ctx, l, coarse_pre(p)))) return st;
     gc_launch(ctx, GK_RESID, k_resid, dim3(node_grid(g)), dim3(dim3(32, 8)), 0, ctx->e[l], ctx->b[l], ctx->rc, g);
     gc_launch(ctx, GK_RESTRICT, k_restrict, dim3(node_grid(ctx->lev[l + 1])), dim3(dim3(32, 8)), 0, ctx->rc, g,
               ctx->b[l + 1], ctx->lev[l + 1]);
@@ -1577,7 +1581,7 @@ static int coarse_levels(gc_ctx *ctx, const gc_mg_params *p) {
     gc_launch(ctx, GK_PROLONG, k_prolong, dim3(node_grid(ctx->lev[l])), dim3(dim3(32, 8)), 0, ctx->e[l + 1],
               ctx->lev[l + 1], ctx->e[l], ctx->lev[l]);
     GC_LAUNCH_CHECK(ctx, "prolong");
-    if ((st = launch_smooth(ctx, l, p->post_sweeps))) return st;
+    if ((st = launch_smooth(ctx, l, coarse_post(p)))) return st;
   }
   return GC_OK;
 }

@@ -31,6 +31,7 @@ GC_MG_PLAIN_F32 = 0x4
 GC_MG_NATURAL_LAYOUT = 0x8
 GC_MG_FACES_GIVEN = 0x10
 GC_MG_PHASE_LAUNCHES = 0x20
+GC_MG_COARSE_ONE_SWEEP = 0x40
 GC_STEP_GRAD_GRID = 0x1
 GC_STEP_SOLVE_ONLY = 0x2
 GC_STEP_PUSH_ONLY = 0x4

@@ -42,7 +42,8 @@ class PMEngine:
                  max_cycles: int = 50, pre_sweeps: int = 2, post_sweeps: int = 2, coarse_sweeps: int = 40,
                  fixed_point_bits: int = 52, sort_every: int = 20, grad_grid: bool = True, fixed_cycles: int = 0,
                  max_particles: int = 0, deposit_next: bool = False, plain_f32: bool = False,
-                 sort_ahead: float | None = None, phase_launches: bool = False):
+                 sort_ahead: float | None = None, phase_launches: bool = False,
+                 coarse_level_sweeps: int | None = None):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
         self.grav = float(grav)
@@ -59,6 +60,13 @@ class PMEngine:
             self.mg.flags |= _native.GC_MG_PLAIN_F32
         if phase_launches:  # coarse levels launched phase by phase (ensembles of small runs)
             self.mg.flags |= _native.GC_MG_PHASE_LAUNCHES
+        # sweeps each way below the finest level: None (the default) for pre/post_sweeps
+        # on every level, as the reference; 1 for fewer latency-bound coarse phases at
+        # the price of a weaker cycle (about 0.2 per cycle instead of 0.1)
+        if coarse_level_sweeps is not None and int(coarse_level_sweeps) == 1:
+            self.mg.flags |= _native.GC_MG_COARSE_ONE_SWEEP
+        elif coarse_level_sweeps is not None and not (int(coarse_level_sweeps) == int(pre_sweeps) == int(post_sweeps)):
+            raise ValueError("coarse_level_sweeps must be 1, None, or equal to pre_sweeps and post_sweeps")
         # fixed_cycles > 0: exactly that many V-cycles per solve and no host read in
         # the step (the residual stays on the device, see last_residual), which is
         # what lets a step be captured as a CUDA graph

@@ -50,6 +50,7 @@ class MultigridPoissonSolver(PoissonSolver):
         natural_layout: bool = False,
         boundary: str = "multipole",
         phase_launches: bool = False,
+        coarse_level_sweeps: int | None = None,
     ):
         self.grid_size = int(grid_size)
         self.dx = float(dx)
@@ -72,6 +73,11 @@ class MultigridPoissonSolver(PoissonSolver):
         # phase_launches: the coarse levels by one launch per phase instead of
         # the persistent kernels (identical potentials)
         self.phase_launches = bool(phase_launches)
+        # coarse_level_sweeps=1: one sweep each way below the finest level (the
+        # engine's default); None keeps pre/post sweeps on every level, as the reference
+        if coarse_level_sweeps not in (None, 1):
+            raise ValueError("coarse_level_sweeps must be None or 1")
+        self.coarse_one_sweep = coarse_level_sweeps == 1
         if boundary not in ("multipole", "isolated"):
             raise ValueError(f"unknown boundary {boundary!r} (expected 'multipole' or 'isolated')")
         self.boundary = boundary
@@ -89,7 +95,8 @@ class MultigridPoissonSolver(PoissonSolver):
         p.tol = self.tol
         p.flags = ((_native.GC_MG_PLAIN_F32 if self.plain_f32 else 0)
                    | (_native.GC_MG_NATURAL_LAYOUT if self.natural_layout else 0)
-                   | (_native.GC_MG_PHASE_LAUNCHES if self.phase_launches else 0))
+                   | (_native.GC_MG_PHASE_LAUNCHES if self.phase_launches else 0)
+                   | (_native.GC_MG_COARSE_ONE_SWEEP if self.coarse_one_sweep else 0))
         return p
 
     def solve(self, rho, phi, warm_start: bool = False) -> None:

@@ -77,6 +77,11 @@ enum gc_status_code {
  * launches of many small solves running at once on one GPU (an ensemble of
  * runs on separate streams) can interleave. Same potentials bit for bit. */
 #define GC_MG_PHASE_LAUNCHES 0x20
+/* gc_mg_params.flags: every level below the finest relaxes with one red-black
+ * sweep before restriction and one after prolongation; the finest keeps
+ * pre_sweeps / post_sweeps. Fewer barrier-separated phases on the latency-bound
+ * coarse levels for a slightly weaker V-cycle; the stopping rule is unchanged. */
+#define GC_MG_COARSE_ONE_SWEEP 0x40
 
 typedef struct gc_ctx gc_ctx;
 

@@ -113,6 +113,24 @@ def test_phase_launches_bitwise_equal_persistent_coarse_levels(cuda, n, dx):
     np.testing.assert_array_equal(a.to_numpy(), b.to_numpy())
 
 
+@pytest.mark.parametrize("n,dx", [(64, 1.0), (130, 0.25)])
+def test_one_coarse_sweep_same_in_every_launch_path_and_converges(cuda, n, dx):
+    """GC_MG_COARSE_ONE_SWEEP (one sweep each way below the finest level): the
+    persistent, phase-by-phase and natural-layout paths give identical
+    potentials, and the weaker cycle still converges (within a third more cycles
+    than the full one from a cold start)."""
+    rho = gaussian_rho(n, dx, 3.0 * dx, 1.5, center=(0.45 * n * dx, 0.5 * n * dx, 0.6 * n * dx))
+    _, _, a = _solve(rho, dx, 1.0, n_cycles=3, tol=0.0, coarse_level_sweeps=1)
+    _, _, b = _solve(rho, dx, 1.0, n_cycles=3, tol=0.0, coarse_level_sweeps=1, phase_launches=True)
+    _, _, c = _solve(rho, dx, 1.0, n_cycles=3, tol=0.0, coarse_level_sweeps=1, natural_layout=True)
+    np.testing.assert_array_equal(a.to_numpy(), b.to_numpy())
+    np.testing.assert_array_equal(a.to_numpy(), c.to_numpy())
+    s1, _, _ = _solve(rho, dx, 1.0, n_cycles=30, tol=1e-9, coarse_level_sweeps=1)
+    s2, _, _ = _solve(rho, dx, 1.0, n_cycles=30, tol=1e-9)
+    assert s1.last_stats["converged"] and s2.last_stats["converged"]
+    assert s1.last_cycles <= (4 * s2.last_cycles) // 3 + 2, (s1.last_cycles, s2.last_cycles)
+
+
 def test_plain_f32_stalls_at_the_fp32_floor(cuda):
     """The plain FP32 method (the reference's precision) cannot go below the
     FP32 floor: asked for 1e-6 it runs to its cycle cap with the residual near
