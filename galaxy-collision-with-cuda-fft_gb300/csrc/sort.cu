@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(SC_THREADS) k_scan_apply(unsigned *__restrict_
 // and digits) place every item at its slot of the tile's digit-sorted order in
 // shared memory; the items are then written out from there, so consecutive
 // threads write consecutive addresses of one digit's output segment. Dynamic
-// shared memory: scatter_smem_bytes(BITS).
+// shared memory: scatter_smem_bytes<BITS>().
 template <int BITS>
 constexpr size_t scatter_smem_bytes() {
   return sizeof(unsigned) * ((size_t)RS_WARPS * (1 << BITS) + 2 * (1 << BITS) + RS_WARPS + 2 * RS_TILE);
