@@ -51,21 +51,44 @@ class Ensemble:
     """Independent PM engines advanced together, one whole-step graph per run per step."""
 
     def __init__(self, n_runs: int = 64, seed: int = 5, tol: float = 1e-6, warmstart: str = "extrapolate",
-                 sort_every: int = 20, dt: float = DT, box: float = BOX, net=None, phase_launches: bool = True):
+                 sort_every: int = 20, dt: float = DT, box: float = BOX, net=None, phase_launches: bool = True,
+                 tuned: bool = False):
         members, rng = ensemble_members(n_runs, seed)
         self.dt = dt
         self.engines: list[PMEngine] = []
         self.counts = []
-        for n, grid in members:
-            icr = random_collision(rng, n, box / grid)
-            e = PMEngine(grid, box / grid, grav=1.0, origin=(-box / 2.0,) * 3, tol=tol, sort_every=sort_every,
-                         fixed_point_bits=40, phase_launches=phase_launches)
+        ics = [random_collision(rng, n, box / grid) for n, grid in members]
+
+        def make(grid, **settings):
+            e = PMEngine(grid, box / grid, grav=1.0, origin=(-box / 2.0,) * 3, tol=tol, fixed_point_bits=40,
+                         **settings)
             e.set_warmstart(warmstart, net=net if warmstart == "learned" else None)
+            return e
+
+        # per (grid, particle-count bucket): the tuned settings (autotune.py), timed on
+        # the group's first run when the cache has none; otherwise the given ones
+        settings = {}
+        if tuned:
+            import torch
+
+            from galaxy_collision_gb300 import autotune
+
+            device = torch.cuda.get_device_name()
+            for (n, grid), icr in zip(members, ics):
+                k = (grid, autotune.bucket(n))
+                if k not in settings:
+                    settings[k] = autotune.settings_for(
+                        grid, n, lambda g=grid, **st: make(g, **st), (icr.pos, icr.vel, icr.mass, icr.gid), dt,
+                        device=device)
+        self.settings = []
+        for (n, grid), icr in zip(members, ics):
+            st = settings.get((grid, int(n).bit_length() - 1)) if tuned else None
+            st = st or {"phase_launches": phase_launches, "sort_every": sort_every}
+            e = make(grid, **st)
             e.load(icr.pos, icr.vel, icr.mass, icr.gid)
             self.engines.append(e)
             self.counts.append(n)
-        self.steps_since_sort = 0
-        self.sort_every = sort_every
+            self.settings.append(st)
 
     @property
     def particles(self) -> int:
@@ -81,20 +104,18 @@ class Ensemble:
             e.steps_since_sort = 0
             e.prepare_graphs(self.dt)
         torch.cuda.synchronize()
-        self.steps_since_sort = 0
         for e in self.engines:
             e.solve_counters(reset=True)
 
     def step(self) -> None:
-        """One KDK step of every run: the runs are sorted together every
-        sort_every steps (on the current stream), then every run's step graph is
-        replayed on its own stream after that, and the current stream waits for
-        all of them."""
+        """One KDK step of every run: the runs due for their cell sort are
+        sorted (on the current stream), then every run's step graph is replayed
+        on its own stream after that, and the current stream waits for all of
+        them."""
         main = torch.cuda.current_stream()
-        if self.sort_every > 0 and self.steps_since_sort >= self.sort_every:
-            for e in self.engines:
+        for e in self.engines:
+            if e.sort_every > 0 and e.steps_since_sort >= e.sort_every:
                 e.sort(self.dt)
-            self.steps_since_sort = 0
         ready = torch.cuda.Event()
         ready.record(main)
         streams = []
@@ -103,7 +124,6 @@ class Ensemble:
             streams.append(e.launch_graph(self.dt))
         for s in streams:
             main.wait_stream(s)
-        self.steps_since_sort += 1
 
     def counters(self, reset: bool = True) -> dict:
         """Solves, V-cycles and the largest relative residual over all runs since
@@ -114,11 +134,11 @@ class Ensemble:
 
 
 def run_comparison(n_runs: int = 64, steps: int = 300, seed: int = 5, one_by_one_steps: int | None = None,
-                   log=None, phase_launches: bool = True) -> dict:
+                   log=None, phase_launches: bool = True, tuned: bool = False) -> dict:
     """Aggregate particle-steps/s of the ensemble step and of the same runs
     advanced one after the other (each through its own step graph)."""
     t0 = time.time()
-    ens = Ensemble(n_runs, seed=seed, phase_launches=phase_launches)
+    ens = Ensemble(n_runs, seed=seed, phase_launches=phase_launches, tuned=tuned)
     if log:
         log(f"{n_runs} runs, {ens.particles:,} particles, IC {time.time() - t0:.0f}s")
     ens.prime()
@@ -168,13 +188,16 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=5)
     ap.add_argument("--persistent-coarse", action="store_true",
                     help="coarse multigrid levels by the persistent kernels instead of one launch per phase")
+    ap.add_argument("--autotune", action="store_true",
+                    help="per (grid, particle-count bucket) settings from the autotuner's JSON cache (tuned on "
+                         "first use)")
     args = ap.parse_args(argv)
     from galaxy_collision_gb300 import _build
 
     _build.build()
     res = run_comparison(args.runs, args.steps, args.seed, args.one_by_one_steps,
                          log=lambda m: print(f"[ensemble] {m}", flush=True),
-                         phase_launches=not args.persistent_coarse)
+                         phase_launches=not args.persistent_coarse, tuned=args.autotune)
     print(json.dumps(res), flush=True)
 
 

@@ -112,6 +112,30 @@ def test_ensemble_steps_every_run_like_its_own_graph(cuda):
         np.testing.assert_array_equal(ea.cur["vx"].cpu().numpy(), eb.cur["vx"].cpu().numpy())
 
 
+def test_autotuned_ensemble_runs_with_the_cached_settings(cuda, tmp_path, monkeypatch):
+    """The autotuner times every candidate on a group's first run, caches the
+    fastest per (device, grid, count bucket) in JSON, and the ensemble's runs
+    step with them; a second ensemble reads the cache without timing again."""
+    from galaxy_collision_gb300 import autotune, ensemble
+
+    path = tmp_path / "tune.json"
+    monkeypatch.setenv("GC_AUTOTUNE_CACHE", str(path))
+    a = ensemble.Ensemble(n_runs=2, seed=11, tuned=True)
+    entries = autotune.load(path)
+    assert entries and all(set(e["ms_per_step"]) == {autotune._label(c) for c in autotune.CANDIDATES}
+                           for e in entries.values())
+    for e, st in zip(a.engines, a.settings):
+        assert st in [dict(c) for c in autotune.CANDIDATES]
+        assert e.sort_every == st["sort_every"]
+    monkeypatch.setattr(autotune, "time_candidate", lambda *args, **kw: pytest.fail("re-timed"))
+    b = ensemble.Ensemble(n_runs=2, seed=11, tuned=True)
+    assert b.settings == a.settings
+    a.prime()
+    for _ in range(3):
+        a.step()
+    assert a.counters()["max_rel_residual"] < 1e-6
+
+
 def test_split_step_is_the_whole_step_and_refine_meets_tol(cuda):
     G, dt = 32, 0.05
     pos, vel, mass = _cluster(30000, G, 2)
