@@ -451,6 +451,13 @@ def run_ours(args):
                                           sorted(stats.items(), key=lambda kv: -kv[1][2])}
         line["kernel_share"] = {k: round(v[2] / tot, 4) for k, v in sorted(stats.items(), key=lambda kv: -kv[1][2])}
         line["roofline"] = _roofline(stats, n, G, hbm, _load_traffic())
+        # one re-sort of the current state (the sort period's), CUDA-event ms per kernel group
+        eng.ctx.profile_reset()
+        eng.ctx.profile(True)
+        eng.sort(dt)
+        sort_stats = eng.ctx.kernel_stats()
+        eng.ctx.profile(False)
+        line["cell_sort_ms"] = {k: round(v[2], 4) for k, v in sorted(sort_stats.items(), key=lambda kv: -kv[1][2])}
         poisson_ms = sum(v[2] for k, v in stats.items() if k in MG_KERNELS) / args.profile_steps
         line["poisson"]["ms_per_solve"] = round(poisson_ms, 4)
         line["poisson"]["warm_start"] = args.warmstart

@@ -434,7 +434,8 @@ int gc_gather_kick_drift(gc_ctx *ctx, const gc_particles *p, float dt, int mode,
                          int deposit_next, float *axo, float *ayo, float *azo, int *nparts_out, int *deposited);
 // dst = sum a*b in FP64 (async).
 int gc_dot_async(gc_ctx *ctx, const float *a, const float *b, size_t n, double *dst);
-// Stable LSD radix sort of (keys, vals) pairs on the low `bits` bits; results in
-// ctx->keys/ctx->vals after the call (inputs may alias them).
+// Stable LSD radix sort of (keys, vals) pairs on the low `bits` bits; the results
+// are in the context's key/value scratch (*keys_out, *vals_out; the inputs may be
+// one of its buffers). vals_in == NULL sorts the identity values 0 .. n-1.
 int gc_radix_sort_pairs(gc_ctx *ctx, const uint32_t *keys_in, const uint32_t *vals_in, int64_t n, int bits,
                         uint32_t **keys_out, uint32_t **vals_out);

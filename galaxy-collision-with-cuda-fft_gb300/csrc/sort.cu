@@ -4,7 +4,8 @@
 // linearised over the (G+1)^3 cells that can receive mass (-1 <= ix <= G-1).
 // Each radix pass is reduce-then-scan: per-tile digit histograms, one exclusive
 // scan of the digit-major histogram, then a stable scatter in which every warp
-// ranks its items round by round with match.any, so equal keys keep their input
+// ranks its items round by round (by runs of equal neighbours when a round's
+// digits are in order, else with match.any), so equal keys keep their input
 // order and the permutation is unique. Digits are up to 9 bits wide (the 25-bit
 // cell keys of a 256^3 grid take three passes), tiles 4096 items.
 #include "common.cuh"
@@ -20,7 +21,7 @@
 
 __global__ void __launch_bounds__(256)
     k_cell_keys(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z, long long n,
-                float dx, int G, uint32_t *__restrict__ keys, uint32_t *__restrict__ iota) {
+                float dx, int G, uint32_t *__restrict__ keys) {
   const uint32_t sentinel = (uint32_t)(G + 1) * (uint32_t)(G + 1) * (uint32_t)(G + 1);
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     CellPos c;
@@ -28,13 +29,18 @@ __global__ void __launch_bounds__(256)
     if (gc_cell_of(x[p], y[p], z[p], dx, G, c))
       key = ((uint32_t)(c.ix + 1) * (uint32_t)(G + 1) + (uint32_t)(c.iy + 1)) * (uint32_t)(G + 1) + (uint32_t)(c.iz + 1);
     keys[p] = key;
-    if (iota) iota[p] = (uint32_t)p;
   }
 }
 
+// The lanes 0 .. lane as a mask.
+__device__ __forceinline__ unsigned lanes_upto(int lane) { return 0xffffffffu >> (31 - lane); }
+
 // Digit histogram of each tile: hist[d * ntiles + tile], digits of BITS bits
-// at `shift`. The lanes of a warp that hold the same digit add their count
-// once (match.any), so that nearly sorted keys do not serialise on one counter.
+// at `shift`. A thread loads its 16 keys first (16 loads in flight); then, for
+// each group of 32 consecutive keys, every run of equal neighbouring digits
+// adds its length with one atomic from its first lane, so nearly sorted keys
+// do not serialise on one counter and random keys cost one atomic each (a
+// digit that recurs after another digit simply starts a second run).
 template <int BITS>
 __global__ void __launch_bounds__(RS_THREADS)
     k_rs_hist(const uint32_t *__restrict__ keys, long long n, int shift, unsigned *__restrict__ hist, int ntiles) {
@@ -44,14 +50,24 @@ __global__ void __launch_bounds__(RS_THREADS)
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const long long base = (long long)blockIdx.x * RS_TILE;
-  const unsigned lt = (1u << lane) - 1u;
-#pragma unroll 4
-  for (int t = threadIdx.x; t < RS_TILE; t += RS_THREADS) {
-    const long long p = base + t;
-    const bool ok = p < n;
-    const unsigned d = ok ? ((keys[p] >> shift) & (RADIX - 1)) : (unsigned)RADIX + lane;
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
-    if (ok && (peers & lt) == 0) atomicAdd(&cnt[d], (unsigned)__popc(peers));
+  uint32_t kk[RS_IPT];
+#pragma unroll
+  for (int j = 0; j < RS_IPT; ++j) {
+    const long long p = base + j * RS_THREADS + threadIdx.x;
+    kk[j] = p < n ? keys[p] : 0u;
+  }
+#pragma unroll
+  for (int j = 0; j < RS_IPT; ++j) {
+    // the valid lanes of a group are a prefix of it (the tile's tail)
+    const bool ok = base + j * RS_THREADS + threadIdx.x < n;
+    const unsigned d = (kk[j] >> shift) & (RADIX - 1);
+    const unsigned dprev = __shfl_up_sync(0xffffffffu, d, 1);
+    const bool head = ok && (lane == 0 || d != dprev);
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    const unsigned nvalid = __popc(__ballot_sync(0xffffffffu, ok));
+    const unsigned above = heads & ~lanes_upto(lane);
+    const int end = above ? __ffs(above) - 1 : (int)nvalid;  // one past the run
+    if (head) atomicAdd(&cnt[d], (unsigned)(end - lane));
   }
   __syncthreads();
   for (int d = threadIdx.x; d < RADIX; d += RS_THREADS) hist[(size_t)d * ntiles + blockIdx.x] = cnt[d];
@@ -139,13 +155,24 @@ __global__ void __launch_bounds__(SC_THREADS) k_scan_apply(unsigned *__restrict_
 // shared memory; the items are then written out from there, so consecutive
 // threads write consecutive addresses of one digit's output segment. Dynamic
 // shared memory: scatter_smem_bytes<BITS>().
+//
+// Ranking a round: when the 32 digits are non-decreasing across the lanes
+// (nearly sorted keys, most rounds), each digit is one run of neighbours, so
+// the run's first lane reads and advances its warp counter by the run length
+// and the others take their offset in the run; otherwise the lanes holding
+// the same digit are found with match.any. Both give every item the number of
+// items with its digit before it in (round, lane) order. The values are read
+// only when the items are placed (fewer live registers: four CTAs per SM for
+// the 8- and 9-bit digits of the cell keys, measured faster than three or two;
+// three for narrower digits, whose kernels would spill at four); vin == NULL
+// means the identity values (an item's index).
 template <int BITS>
 constexpr size_t scatter_smem_bytes() {
   return sizeof(unsigned) * ((size_t)RS_WARPS * (1 << BITS) + 2 * (1 << BITS) + RS_WARPS + 2 * RS_TILE);
 }
 
 template <int BITS>
-__global__ void __launch_bounds__(RS_THREADS)
+__global__ void __launch_bounds__(RS_THREADS, BITS >= 8 ? 4 : 3)
     k_rs_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, long long n, int shift,
                  const unsigned *__restrict__ hist, int ntiles, uint32_t *__restrict__ kout,
                  uint32_t *__restrict__ vout) {
@@ -163,27 +190,43 @@ __global__ void __launch_bounds__(RS_THREADS)
   const long long tile0 = (long long)blockIdx.x * RS_TILE;
   const int cnt = (int)(n - tile0 < RS_TILE ? n - tile0 : RS_TILE);
   const long long seg = tile0 + (long long)w * 32 * RS_IPT;
-  uint32_t k[RS_IPT], v[RS_IPT];
+  uint32_t k[RS_IPT];
   unsigned rank[RS_IPT];
   const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
   for (int r = 0; r < RS_IPT; ++r) {
     const long long p = seg + r * 32 + lane;
-    const bool ok = p < n;
-    k[r] = ok ? kin[p] : 0u;
-    v[r] = ok ? vin[p] : 0u;
+    k[r] = p < n ? kin[p] : 0u;
   }
 #pragma unroll
   for (int r = 0; r < RS_IPT; ++r) {
+    // the valid lanes of a round are a prefix of it (the tile's tail)
     const bool ok = seg + r * 32 + lane < n;
-    const unsigned d = ok ? ((k[r] >> shift) & (RADIX - 1)) : (unsigned)RADIX + lane;
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
-    unsigned old = 0;
-    if (ok) old = whist[w][d];
-    __syncwarp();
-    if (ok && (peers & lt) == 0) whist[w][d] = old + __popc(peers);
-    __syncwarp();
-    rank[r] = old + __popc(peers & lt);
+    const unsigned d = (k[r] >> shift) & (RADIX - 1);
+    const unsigned dprev = __shfl_up_sync(0xffffffffu, d, 1);
+    if (__all_sync(0xffffffffu, !ok || lane == 0 || dprev <= d)) {
+      const unsigned heads = __ballot_sync(0xffffffffu, ok && (lane == 0 || d != dprev));
+      const unsigned nvalid = __popc(__ballot_sync(0xffffffffu, ok));
+      const int hl = 31 - __clz(heads & lanes_upto(lane));  // the run's first lane (-1: no valid lane at all)
+      const unsigned above = heads & ~lanes_upto(lane);
+      const int end = above ? __ffs(above) - 1 : (int)nvalid;
+      unsigned old = 0;
+      if (ok && hl == lane) {
+        old = whist[w][d];
+        whist[w][d] = old + (unsigned)(end - lane);
+      }
+      __syncwarp();
+      rank[r] = __shfl_sync(0xffffffffu, old, hl & 31) + (unsigned)(lane - hl);
+    } else {
+      const unsigned dd = ok ? d : (unsigned)RADIX + lane;
+      const unsigned peers = __match_any_sync(0xffffffffu, dd);
+      unsigned old = 0;
+      if (ok) old = whist[w][d];
+      __syncwarp();
+      if (ok && (peers & lt) == 0) whist[w][d] = old + __popc(peers);
+      __syncwarp();
+      rank[r] = old + __popc(peers & lt);
+    }
   }
   __syncthreads();
   // per digit (thread t takes digits t*DPT .. t*DPT+DPT-1): exclusive prefix
@@ -231,7 +274,7 @@ __global__ void __launch_bounds__(RS_THREADS)
       const unsigned d = (k[r] >> shift) & (RADIX - 1);
       const unsigned slot = dstart[d] + whist[w][d] + rank[r];
       sk[slot] = k[r];
-      sv[slot] = v[r];
+      sv[slot] = vin ? vin[p] : (uint32_t)p;
     }
   }
   __syncthreads();
@@ -364,14 +407,9 @@ extern "C" int gc_cell_keys(gc_ctx *ctx, const float *x, const float *y, const f
              "grid too large for 32-bit cell keys");
   unsigned nb = gc_blocks(n, 256);
   if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
-  gc_launch(ctx, GK_KEYS, k_cell_keys, dim3(nb), dim3(256), 0, x, y, z, (long long)n, (float)ctx->dx, ctx->G, keys, nullptr);
+  gc_launch(ctx, GK_KEYS, k_cell_keys, dim3(nb), dim3(256), 0, x, y, z, (long long)n, (float)ctx->dx, ctx->G, keys);
   GC_LAUNCH_CHECK(ctx, "cell keys");
   return GC_OK;
-}
-
-__global__ void k_iota(uint32_t *__restrict__ a, long long n) {
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
-    a[p] = (uint32_t)p;
 }
 
 extern "C" int gc_sort_keys(gc_ctx *ctx, const uint32_t *keys, int64_t n, uint32_t *sorted_keys, uint32_t *perm) {
@@ -381,13 +419,9 @@ extern "C" int gc_sort_keys(gc_ctx *ctx, const uint32_t *keys, int64_t n, uint32
   GC_REQUIRE(ctx, keys && perm, "gc_sort_keys: NULL pointer");
   int s = gc_ensure_particle_scratch(ctx, (size_t)n);
   if (s) return s;
-  // values start as the identity in keys2's partner buffer
-  uint32_t *iota = ctx->vals2;
-  gc_launch(ctx, GK_KEYS, k_iota, dim3(gc_blocks(n, 256) > 4096 ? 4096 : gc_blocks(n, 256)), dim3(256), 0, iota, (long long)n);
-  GC_LAUNCH_CHECK(ctx, "iota");
   uint32_t *ko, *vo;
-  // full 32-bit keys: any caller key is sorted stably
-  if ((s = gc_radix_sort_pairs(ctx, keys, iota, n, 32, &ko, &vo))) return s;
+  // full 32-bit keys: any caller key is sorted stably; values: the identity
+  if ((s = gc_radix_sort_pairs(ctx, keys, nullptr, n, 32, &ko, &vo))) return s;
   if (sorted_keys) GC_CUDA(ctx, cudaMemcpyAsync(sorted_keys, ko, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->stream));
   GC_CUDA(ctx, cudaMemcpyAsync(perm, vo, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->stream));
   return GC_OK;
@@ -447,8 +481,7 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(256)
     k_cell_keys_ahead(const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
                       const float *__restrict__ vx, const float *__restrict__ vy, const float *__restrict__ vz,
-                      float tau, long long n, float dx, int G, uint32_t *__restrict__ keys,
-                      uint32_t *__restrict__ iota) {
+                      float tau, long long n, float dx, int G, uint32_t *__restrict__ keys) {
   const uint32_t g1 = (uint32_t)(G + 1), sentinel = g1 * g1 * g1;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     const float px = x[p], py = y[p], pz = z[p];
@@ -459,7 +492,6 @@ __global__ void __launch_bounds__(256)
         gc_cell_of(px, py, pz, dx, G, c))
       key = ((uint32_t)(c.ix + 1) * g1 + (uint32_t)(c.iy + 1)) * g1 + (uint32_t)(c.iz + 1);
     keys[p] = key;
-    iota[p] = (uint32_t)p;
   }
 }
 
@@ -483,13 +515,13 @@ extern "C" int gc_pm_sort_ahead(gc_ctx *ctx, const gc_particles *in, const gc_pa
   if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
   if (tau == 0.0f)
     gc_launch(ctx, GK_KEYS, k_cell_keys, dim3(nb), dim3(256), 0, in->x, in->y, in->z, (long long)n, (float)ctx->dx,
-              ctx->G, ctx->keys2, ctx->vals2);
+              ctx->G, ctx->keys2);
   else
     gc_launch(ctx, GK_KEYS, k_cell_keys_ahead, dim3(nb), dim3(256), 0, in->x, in->y, in->z, in->vx, in->vy, in->vz,
-              tau, (long long)n, (float)ctx->dx, ctx->G, ctx->keys2, ctx->vals2);
+              tau, (long long)n, (float)ctx->dx, ctx->G, ctx->keys2);
   GC_LAUNCH_CHECK(ctx, "cell keys");
   uint32_t *ko, *vo;
-  if ((s = gc_radix_sort_pairs(ctx, ctx->keys2, ctx->vals2, n, key_bits(ctx->G), &ko, &vo))) return s;
+  if ((s = gc_radix_sort_pairs(ctx, ctx->keys2, nullptr, n, key_bits(ctx->G), &ko, &vo))) return s;
   PermSet ps;
   const float *fin[7] = {in->x, in->y, in->z, in->vx, in->vy, in->vz, in->m};
   float *fout[7] = {out->x, out->y, out->z, out->vx, out->vy, out->vz, out->m};
@@ -687,7 +719,7 @@ extern "C" int gc_pm_export_range(gc_ctx *ctx, const gc_particles *p, const doub
 // instead of one per component, and no intermediate unsorted copy.
 __global__ void __launch_bounds__(256)
     k_cell_keys_aos(const float *__restrict__ pos, double ox, double oy, double oz, long long n, float dx, int G,
-                    uint32_t *__restrict__ keys, uint32_t *__restrict__ iota) {
+                    uint32_t *__restrict__ keys) {
   const uint32_t sentinel = (uint32_t)(G + 1) * (uint32_t)(G + 1) * (uint32_t)(G + 1);
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     const float x = (float)((double)pos[3 * p] - ox);
@@ -698,7 +730,6 @@ __global__ void __launch_bounds__(256)
     if (gc_cell_of(x, y, z, dx, G, c))
       key = ((uint32_t)(c.ix + 1) * (uint32_t)(G + 1) + (uint32_t)(c.iy + 1)) * (uint32_t)(G + 1) + (uint32_t)(c.iz + 1);
     keys[p] = key;
-    iota[p] = (uint32_t)p;
   }
 }
 
@@ -741,10 +772,10 @@ extern "C" int gc_pm_import_order(gc_ctx *ctx, const float *pos, const double or
   unsigned nb = gc_blocks(n, 256);
   if (nb > gc_sms() * 32u) nb = gc_sms() * 32u;
   gc_launch(ctx, GK_KEYS, k_cell_keys_aos, dim3(nb), dim3(256), 0, pos, origin[0], origin[1], origin[2], (long long)n,
-            (float)ctx->dx, ctx->G, ctx->keys2, ctx->vals2);
+            (float)ctx->dx, ctx->G, ctx->keys2);
   GC_LAUNCH_CHECK(ctx, "cell keys");
   uint32_t *ko, *vo;
-  if ((s = gc_radix_sort_pairs(ctx, ctx->keys2, ctx->vals2, n, key_bits(ctx->G), &ko, &vo))) return s;
+  if ((s = gc_radix_sort_pairs(ctx, ctx->keys2, nullptr, n, key_bits(ctx->G), &ko, &vo))) return s;
   ctx->import_perm = vo;
   ctx->import_n = n;
   return GC_OK;
