@@ -83,6 +83,51 @@ def test_sort_permutation_bit_exact(cuda, n):
     np.testing.assert_array_equal(sk.cpu().numpy().view(np.uint32), keys[ref])
 
 
+@pytest.mark.parametrize("n", [4097, 100003, 1000003])
+def test_sort_permutation_nearly_sorted_bit_exact(cuda, n):
+    """Nearly sorted keys (the periodic re-sort's case): most warp rounds have
+    their digits in lane order and are ranked by runs, the rest by match.any;
+    sorted, reversed and constant stretches and the tile tail included."""
+    from galaxy_collision_gb300.deposit import sort_keys
+
+    rng = np.random.default_rng(n + 11)
+    keys = np.sort(rng.integers(0, max(2, n // 8), size=n)).astype(np.uint32)  # runs of ~8 equal keys
+    moved = rng.random(n) < 0.05
+    keys[moved] += rng.choice([1, 17, 289, 70000], size=int(moved.sum())).astype(np.uint32)
+    q = n // 8
+    keys[q:2 * q] = keys[q:2 * q][::-1]  # descending stretch
+    keys[2 * q:3 * q] = keys[2 * q]  # one key
+    keys[-5:] = np.uint32(0xFFFFFFFF)  # top digits in the last, partial tile
+    kt = torch.from_numpy(keys.view(np.int32)).cuda()
+    sk, perm = sort_keys(kt, 16)
+    ref = pm.stable_sort_perm(keys)
+    np.testing.assert_array_equal(perm.cpu().numpy().view(np.uint32), ref)
+    np.testing.assert_array_equal(sk.cpu().numpy().view(np.uint32), keys[ref])
+
+
+def test_pm_resort_of_drifted_particles_at_256(cuda):
+    """The engine's re-sort at G = 256 (25-bit cell keys: 9 + 8 + 8 bit passes)
+    of particles that left cell order by drifting: the stable permutation."""
+    from galaxy_collision_gb300.engine import PMEngine
+
+    G, dx, n = 256, 0.25, 300001
+    rng = np.random.default_rng(21)
+    cells = np.sort(rng.integers(0, 64 ** 3, size=n))  # a 64^3 block of cells, in cell order
+    ijk = np.stack([cells // 4096, (cells // 64) % 64, cells % 64], axis=1) + 96
+    pos = ((ijk + rng.uniform(0.0, 1.0, size=(n, 3))) * dx).astype(np.float32)
+    pos += rng.normal(scale=0.15 * dx, size=pos.shape).astype(np.float32)  # drift
+    pos[:3] = [[-5.0, 1.0, 1.0], [np.nan, 2.0, 2.0], [30.0, 30.0, 70.0]]  # outside / non-finite / face
+    vel = np.zeros_like(pos)
+    mass = np.ones(n, np.float32)
+    eng = PMEngine(G, dx, sort_every=0)
+    eng.load(pos, vel, mass, None, sort=False)
+    eng.sort()
+    perm = pm.stable_sort_perm(pm.cell_keys(pos, dx, G))
+    cur = {k: v.cpu().numpy() for k, v in eng.cur.items() if not k.startswith("_")}
+    np.testing.assert_array_equal(cur["pid"], perm.astype(np.int32))
+    np.testing.assert_array_equal(cur["z"], pos[perm, 2])
+
+
 def test_pm_sort_permutes_all_arrays(cuda):
     from galaxy_collision_gb300.engine import PMEngine
 
